@@ -1,0 +1,255 @@
+"""CPU oracle (test infrastructure only).
+
+ctypes wrapper over ``oracle/_build/liboracle.so``, the C++ FP64
+restatement of Bolt.jl's algorithm for the perturbation solve, source
+grid, line-of-sight spectra and P_lin.  Only the test suite, the smoke
+check and the CPU-baseline leg of ``bench.py`` import this module; the
+product library never does.
+
+Reference correspondence (paths within Bolt.jl):
+  CosmoParams                  src/Bolt.jl:56-66
+  Background                   src/background.jl:104-128
+  RECFAST / IonizationHistory  src/ionization/recfast.jl:22-121, 446-536, 674-726
+  boltsolve / hierarchy!       src/perturbations.jl:25-33, 161-271
+  source_grid(_P)              src/spectra.jl:6-42
+  cltt / clte / clee           src/spectra.jl:49-160
+  plin                         src/spectra.jl:163-198
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lp = C.POINTER(C.c_long)
+
+
+class _Params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in
+                ("h", "Omega_r", "Omega_b", "Omega_c", "A", "n", "Y_p", "N_nu", "Sigma_m_nu")]
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.oracle_mass_natural.restype = C.c_double
+        L.oracle_km_s_Mpc_100.restype = C.c_double
+        L.oracle_cosmo_new.restype = C.c_void_p
+        L.oracle_cosmo_new.argtypes = [C.POINTER(_Params), C.c_double, C.c_double, C.c_double, C.c_int,
+                                       C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.oracle_cosmo_free.argtypes = [C.c_void_p]
+        L.oracle_cosmo_ngrid.argtypes = [C.c_void_p]
+        L.oracle_grid_nodes.argtypes = [C.c_void_p, _dp]
+        L.oracle_cosmo_scalars.argtypes = [C.c_void_p, _dp]
+        L.oracle_table_eval.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp]
+        L.oracle_table_coefs.argtypes = [C.c_void_p, C.c_int, _dp]
+        L.oracle_recfast_xe.argtypes = [C.POINTER(_Params), C.c_double, C.c_double, C.c_double, C.c_int,
+                                        C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        _dp, C.c_int, _dp]
+        L.oracle_rhs.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                 _dp, _dp, _dp]
+        L.oracle_jacobian.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.c_double, _dp]
+        L.oracle_initial_conditions.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int,
+                                                C.c_int, _dp]
+        L.oracle_boltsolve.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, C.c_double, _dp, C.c_int, _dp, _lp]
+        L.oracle_source_grid.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         C.c_double, C.c_double, _dp, _dp, _lp, C.c_int]
+        L.oracle_quadratic_k.argtypes = [C.c_double, C.c_double, C.c_int, _dp]
+        L.oracle_log10_k.argtypes = [C.c_double, C.c_double, C.c_int, _dp]
+        L.oracle_sph_bessel.argtypes = [C.c_int, C.c_double, _dp]
+        L.oracle_cl.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double,
+                                C.c_int, _dp, _dp, _dp, C.c_int]
+        L.oracle_plin.restype = C.c_double
+        L.oracle_plin.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                  C.c_double, C.c_double, _ip]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def mass_natural() -> float:
+    return lib().oracle_mass_natural()
+
+
+def km_s_Mpc_100() -> float:
+    return lib().oracle_km_s_Mpc_100()
+
+
+@dataclass
+class Params:
+    """CosmoParams (Bolt.jl:56-66); Sigma_m_nu in eV here, converted on use."""
+    h: float = 0.7
+    Omega_r: float = 5.0469e-5
+    Omega_b: float = 0.046
+    Omega_c: float = 0.224
+    A: float = 2.097e-9
+    n: float = 1.0
+    Y_p: float = 0.24
+    N_nu: float = 3.046
+    Sigma_m_nu_eV: float = 0.06
+
+    def c(self) -> _Params:
+        return _Params(self.h, self.Omega_r, self.Omega_b, self.Omega_c, self.A, self.n, self.Y_p,
+                       self.N_nu, self.Sigma_m_nu_eV * mass_natural())
+
+
+TABLES = ["H", "Hp", "Hpp", "eta", "etap", "etapp", "rho0M", "Xe", "tau", "taup", "taupp",
+          "g", "gp", "gpp", "Tmat", "csb2"]
+
+
+def state_len(lg, lnu, lmnu, nq):
+    return 2 * (lg + 1) + (lnu + 1) + (lmnu + 1) * nq + 5
+
+
+class Cosmo:
+    """Background + RECFAST IonizationHistory for one parameter set."""
+
+    def __init__(self, p: Params, x_grid=(-20.0, 0.01, 0.0), nq=15, OmegaG=None, Tnow=-1.0,
+                 recfast_tol=1e-8):
+        self.p = p
+        self._pc = p.c()
+        og = p.Omega_r if OmegaG is None else OmegaG
+        self.h = lib().oracle_cosmo_new(C.byref(self._pc), x_grid[0], x_grid[1], x_grid[2], nq,
+                                        p.Y_p, p.Omega_b, og, Tnow, recfast_tol)
+        if not self.h:
+            raise RuntimeError("oracle_cosmo_new failed")
+        self.nx = lib().oracle_cosmo_ngrid(self.h)
+        self.x = np.zeros(self.nx)
+        lib().oracle_grid_nodes(self.h, _d(self.x))
+        s = np.zeros(8)
+        lib().oracle_cosmo_scalars(self.h, _d(s))
+        (self.H0, self.eta0, self.rho_crit, self.Omega_Lambda, self.z_He_evo_start,
+         self.z_H_He_evo_start, self.tau0, self.Tnow) = s
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().oracle_cosmo_free(self.h)
+        except Exception:
+            pass
+
+    def table(self, name, x=None):
+        x = self.x if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(len(x))
+        lib().oracle_table_eval(self.h, TABLES.index(name), _d(x), len(x), _d(out))
+        return out
+
+    def coefs(self, name):
+        out = np.zeros(self.nx + 2)
+        lib().oracle_table_coefs(self.h, TABLES.index(name), _d(out))
+        return out
+
+    def rhs(self, k, u, x, lg=8, lnu=8, lmnu=10, nq=15):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        dx = np.zeros_like(u)
+        lib().oracle_rhs(self.h, k, lg, lnu, lmnu, nq, x, _d(u), _d(du), _d(dx))
+        return du, dx
+
+    def jacobian(self, k, x, lg=8, lnu=8, lmnu=10, nq=15):
+        N = state_len(lg, lnu, lmnu, nq)
+        J = np.zeros((N, N))
+        lib().oracle_jacobian(self.h, k, lg, lnu, lmnu, nq, x, _d(J))
+        return J
+
+    def initial_conditions(self, k, lg=8, lnu=8, lmnu=10, nq=15):
+        u = np.zeros(state_len(lg, lnu, lmnu, nq))
+        lib().oracle_initial_conditions(self.h, k, lg, lnu, lmnu, nq, _d(u))
+        return u
+
+    def boltsolve(self, k, xout, lg=8, lnu=8, lmnu=10, nq=15, reltol=1e-6, abstol=1e-6):
+        xout = np.ascontiguousarray(xout, dtype=np.float64)
+        N = state_len(lg, lnu, lmnu, nq)
+        u = np.zeros((len(xout), N))
+        st = np.zeros(3, dtype=np.int64)
+        rc = lib().oracle_boltsolve(self.h, k, lg, lnu, lmnu, nq, reltol, abstol, _d(xout), len(xout),
+                                    _d(u), st.ctypes.data_as(_lp))
+        if rc != 0:
+            raise RuntimeError(f"oracle_boltsolve status {rc}")
+        return u, st
+
+    def source_grid(self, k_grid, lg=8, lnu=8, lmnu=10, nq=15, reltol=1e-11, abstol=1e-6, nthreads=0):
+        k_grid = np.ascontiguousarray(k_grid, dtype=np.float64)
+        nk = len(k_grid)
+        ST = np.zeros((nk, self.nx))
+        SE = np.zeros((nk, self.nx))
+        steps = np.zeros(nk, dtype=np.int64)
+        rc = lib().oracle_source_grid(self.h, _d(k_grid), nk, lg, lnu, lmnu, nq, reltol, abstol, _d(ST),
+                                      _d(SE), steps.ctypes.data_as(_lp), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle_source_grid status {rc}")
+        return ST, SE, steps
+
+    def cl(self, ST, SE, k_grid, ells, kd=None, nthreads=0):
+        ells = np.ascontiguousarray(ells, dtype=np.int32)
+        k_grid = np.ascontiguousarray(k_grid, dtype=np.float64)
+        ST = np.ascontiguousarray(ST, dtype=np.float64)
+        SE = np.ascontiguousarray(SE, dtype=np.float64)
+        if kd is None:
+            kd = (0.01 * self.H0, 1000.0 * self.H0, 5000)
+        tt, te, ee = (np.zeros(len(ells)) for _ in range(3))
+        lib().oracle_cl(self.h, _d(ST), _d(SE), _d(k_grid), len(k_grid),
+                        ells.ctypes.data_as(_ip), len(ells), kd[0], kd[1], kd[2], _d(tt), _d(te), _d(ee),
+                        nthreads)
+        return tt, te, ee
+
+    def plin(self, k, nq=15, lg=50, lnu=50, lmnu=20, x=0.0, reltol=1e-5, abstol=1e-6):
+        st = C.c_int(0)
+        v = lib().oracle_plin(self.h, k, nq, lg, lnu, lmnu, x, reltol, abstol, C.byref(st))
+        if st.value != 0:
+            raise RuntimeError(f"oracle_plin status {st.value}")
+        return v
+
+
+def recfast_xe(p: Params, z, x_grid=(-20.0, 0.01, 0.0), nq=15, OmegaG=None, Tnow=-1.0, tol=1e-8):
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    out = np.zeros(len(z))
+    pc = p.c()
+    og = p.Omega_r if OmegaG is None else OmegaG
+    rc = lib().oracle_recfast_xe(C.byref(pc), x_grid[0], x_grid[1], x_grid[2], nq, p.Y_p, p.Omega_b, og,
+                                 Tnow, tol, _d(z), len(z), _d(out))
+    if rc != 0:
+        raise RuntimeError("oracle_recfast_xe failed")
+    return out
+
+
+def quadratic_k(kmin, kmax, nk):
+    out = np.zeros(nk)
+    lib().oracle_quadratic_k(kmin, kmax, nk, _d(out))
+    return out
+
+
+def log10_k(kmin, kmax, nk):
+    out = np.zeros(nk)
+    lib().oracle_log10_k(kmin, kmax, nk, _d(out))
+    return out
+
+
+def sph_bessel_all(L, x):
+    out = np.zeros(L + 1)
+    lib().oracle_sph_bessel(L, x, _d(out))
+    return out

@@ -1,0 +1,325 @@
+// Oracle (test infrastructure only): C entry points over the CPU
+// restatement, loaded by tests/ and by bench.py's CPU-baseline leg through
+// oracle/oracle.py.  Never linked into the product library.
+#include <omp.h>
+
+#include <cstdio>
+#include <memory>
+
+#include "oracle_perturb.hpp"
+
+using namespace orc;
+
+extern "C" {
+
+struct oracle_params {
+  double h, Omega_r, Omega_b, Omega_c, A, n, Y_p, N_nu, Sigma_m_nu;
+};
+
+struct OCosmo {
+  Cosmo C;
+  std::unique_ptr<Background> bg;
+  std::unique_ptr<Recfast> rf;
+  std::unique_ptr<Ionization> ih;
+};
+
+static Params to_params(const oracle_params* p) {
+  Params q;
+  q.h = p->h; q.Omega_r = p->Omega_r; q.Omega_b = p->Omega_b; q.Omega_c = p->Omega_c;
+  q.A = p->A; q.n = p->n; q.Y_p = p->Y_p; q.N_nu = p->N_nu; q.Sigma_m_nu = p->Sigma_m_nu;
+  return q;
+}
+
+double oracle_mass_natural() { return units().mass_natural; }
+double oracle_km_s_Mpc_100() { return units().km_s_Mpc_100; }
+
+// Background(par; x_grid, nq) + RECFAST(bg; Yp, OmegaB, OmegaG[, Tnow]) +
+// IonizationHistory(recfast, par, bg).  Tnow <= 0 derives it from OmegaG.
+void* oracle_cosmo_new(const oracle_params* p, double x_start, double x_step, double x_stop, int nq, double Yp,
+                       double OmegaB, double OmegaG, double Tnow, double recfast_tol) {
+  try {
+    OCosmo* o = new OCosmo();
+    o->C.par = to_params(p);
+    o->bg.reset(new Background(o->C.par, Grid::range(x_start, x_step, x_stop), nq));
+    o->rf.reset(new Recfast(o->bg.get(), Yp, OmegaB, OmegaG, Tnow, recfast_tol));
+    o->ih.reset(new Ionization(*o->rf, o->C.par, *o->bg));
+    o->C.bg = o->bg.get();
+    o->C.ih = o->ih.get();
+    return o;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_cosmo_new: %s\n", e.what());
+    return nullptr;
+  }
+}
+
+void oracle_cosmo_free(void* h) { delete static_cast<OCosmo*>(h); }
+
+int oracle_cosmo_ngrid(void* h) { return static_cast<OCosmo*>(h)->bg->xg.n; }
+
+void oracle_grid_nodes(void* h, double* out) {
+  const Grid& g = static_cast<OCosmo*>(h)->bg->xg;
+  for (int j = 0; j < g.n; ++j) out[j] = g.at(j);
+}
+
+// H0, eta0, rho_crit, Omega_Lambda, z_He_evo_start, z_H_He_evo_start, tau0, Tnow
+void oracle_cosmo_scalars(void* h, double* out) {
+  OCosmo* o = static_cast<OCosmo*>(h);
+  out[0] = o->bg->H0; out[1] = o->bg->eta0; out[2] = o->bg->rho_crit; out[3] = o->bg->Omega_Lambda;
+  out[4] = o->ih->z_He_evo_start; out[5] = o->ih->z_H_He_evo_start; out[6] = o->ih->tau0; out[7] = o->rf->Tnow;
+}
+
+static const Spline* table(OCosmo* o, int which) {
+  switch (which) {
+    case 0: return &o->bg->H;
+    case 1: return &o->bg->Hp;
+    case 2: return &o->bg->Hpp;
+    case 3: return &o->bg->eta;
+    case 4: return &o->bg->etap;
+    case 5: return &o->bg->etapp;
+    case 6: return &o->bg->rho0M;
+    case 7: return &o->ih->Xe;
+    case 8: return &o->ih->tau;
+    case 9: return &o->ih->taup;
+    case 10: return &o->ih->taupp;
+    case 11: return &o->ih->g;
+    case 12: return &o->ih->gp;
+    case 13: return &o->ih->gpp;
+    case 14: return &o->ih->Tmat;
+    case 15: return &o->ih->csb2;
+  }
+  return nullptr;
+}
+
+int oracle_table_eval(void* h, int which, const double* x, int n, double* out) {
+  const Spline* s = table(static_cast<OCosmo*>(h), which);
+  if (!s) return -1;
+  for (int i = 0; i < n; ++i) out[i] = (*s)(x[i]);
+  return 0;
+}
+
+int oracle_table_coefs(void* h, int which, double* out) {
+  const Spline* s = table(static_cast<OCosmo*>(h), which);
+  if (!s) return -1;
+  for (size_t i = 0; i < s->c.size(); ++i) out[i] = s->c[i];
+  return int(s->c.size());
+}
+
+// Xe_RECFAST(recfastsolve(RECFAST(bg; ...)), z) at the given redshifts
+// (recfast.jl:413-475), as the reference's RECFAST test calls it.
+int oracle_recfast_xe(const oracle_params* p, double x_start, double x_step, double x_stop, int nq, double Yp,
+                      double OmegaB, double OmegaG, double Tnow, double tol, const double* z, int nz, double* xe) {
+  try {
+    Params q = to_params(p);
+    Background bg(q, Grid::range(x_start, x_step, x_stop), nq);
+    Recfast rf(&bg, Yp, OmegaB, OmegaG, Tnow, tol);
+    std::vector<double> zs(z, z + nz);
+    RecfastHistory rh(&rf, zs);
+    for (int i = 0; i < nz; ++i) xe[i] = rh.Xe_RECFAST(z[i]);
+    return 0;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_recfast_xe: %s\n", e.what());
+    return -1;
+  }
+}
+
+void oracle_rhs(void* h, double k, int lg, int lnu, int lmnu, int nq, double x, const double* u, double* du,
+                double* dudx) {
+  OCosmo* o = static_cast<OCosmo*>(h);
+  Mode md(&o->C, k, lg, lnu, lmnu, nq);
+  std::vector<D1> d(md.N);
+  hierarchy_rhs<D1>(md, D1(x, 1.0), u, d.data());
+  for (int i = 0; i < md.N; ++i) { du[i] = d[i].v; if (dudx) dudx[i] = d[i].d; }
+}
+
+// Jacobian split J = L + sum_r U_r W_r^T as a dense N x N matrix (row-major).
+void oracle_jacobian(void* h, double k, int lg, int lnu, int lmnu, int nq, double x, double* J) {
+  OCosmo* o = static_cast<OCosmo*>(h);
+  Mode md(&o->C, k, lg, lnu, lmnu, nq);
+  JacSplit S;
+  jacobian_split(md, x, S);
+  int N = md.N;
+  std::fill(J, J + size_t(N) * N, 0.0);
+  for (auto& e : S.L) J[size_t(e.r) * N + e.c] += e.v;
+  for (int r = 0; r < 3; ++r)
+    for (int i = 0; i < N; ++i)
+      if (S.U[r][i] != 0.0)
+        for (int j = 0; j < N; ++j) J[size_t(i) * N + j] += S.U[r][i] * S.W[r][j];
+}
+
+void oracle_initial_conditions(void* h, double k, int lg, int lnu, int lmnu, int nq, double* u) {
+  OCosmo* o = static_cast<OCosmo*>(h);
+  Mode md(&o->C, k, lg, lnu, lmnu, nq);
+  initial_conditions(md, o->bg->xg.at(0), u);
+}
+
+// boltsolve (perturbations.jl:25-33) sampled at ascending xout: u_out[j*N + i]
+int oracle_boltsolve(void* h, double k, int lg, int lnu, int lmnu, int nq, double reltol, double abstol,
+                     const double* xout, int nx, double* u_out, long* stats) {
+  OCosmo* o = static_cast<OCosmo*>(h);
+  Mode md(&o->C, k, lg, lnu, lmnu, nq);
+  std::vector<double> xo(xout, xout + nx);
+  int N = md.N;
+  SolveStats s = solve_mode(md, reltol, abstol, xo, [&](int j, double, const double* y) {
+    std::copy(y, y + N, u_out + size_t(j) * N);
+  });
+  if (stats) { stats[0] = s.steps; stats[1] = s.rejects; stats[2] = s.rsa; }
+  return s.status;
+}
+
+// source_grid / source_grid_P (spectra.jl:6-42): S_T and S_E on every x-grid
+// node for every k; layout S[ik * nx + ix].
+int oracle_source_grid(void* h, const double* kg, int nk, int lg, int lnu, int lmnu, int nq, double reltol,
+                       double abstol, double* ST, double* SE, long* steps, int nthreads) {
+  OCosmo* o = static_cast<OCosmo*>(h);
+  const Grid& g = o->bg->xg;
+  int nx = g.n;
+  std::vector<double> xo(nx);
+  for (int j = 0; j < nx; ++j) xo[j] = g.at(j);
+  int worst = 0;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(max : worst)
+  for (int ik = 0; ik < nk; ++ik) {
+    Mode md(&o->C, kg[ik], lg, lnu, lmnu, nq);
+    std::vector<double> du(md.N);
+    SolveStats s = solve_mode(md, reltol, abstol, xo, [&](int j, double x, const double* y) {
+      hierarchy_rhs<double>(md, x, y, du.data());
+      double st, se;
+      source_functions(md, x, y, du.data(), st, se);
+      ST[size_t(ik) * nx + j] = st;
+      SE[size_t(ik) * nx + j] = se;
+    });
+    if (steps) steps[ik] = s.steps;
+    worst = std::max(worst, s.status);
+  }
+  return worst;
+}
+
+// quadratic_k (spectra.jl:60-63)
+void oracle_quadratic_k(double kmin, double kmax, int nk, double* out) {
+  for (int i = 1; i <= nk; ++i) {
+    double t = double(i) / double(nk);
+    out[i - 1] = kmin + (kmax - kmin) * (t * t);
+  }
+}
+
+// log10_k (spectra.jl:65-68)
+void oracle_log10_k(double kmin, double kmax, int nk, double* out) {
+  for (int i = 1; i <= nk; ++i)
+    out[i - 1] = std::pow(10.0, std::log10(kmin) + (std::log10(kmax / kmin)) * double(i - 1) / double(nk - 1));
+}
+
+void oracle_sph_bessel(int L, double x, double* out) { sph_bessel_all(L, x, out); }
+
+// cltt / clte / clee (spectra.jl:49-160) on a precomputed source grid.
+// The dense k grid is quadratic_k(kd_min, kd_max, nkd); the reference uses
+// (0.01 H0, 1000 H0, 5000).  Any of tt/te/ee may be null.
+int oracle_cl(void* h, const double* ST, const double* SE, const double* kg, int nk, const int* ells, int nell,
+              double kd_min, double kd_max, int nkd, double* tt, double* te, double* ee, int nthreads) {
+  OCosmo* o = static_cast<OCosmo*>(h);
+  const Background& bg = *o->bg;
+  const Params& par = o->C.par;
+  const Grid& g = bg.xg;
+  int nx = g.n;
+  std::vector<double> kd(nkd);
+  oracle_quadratic_k(kd_min, kd_max, nkd, kd.data());
+  double argmax = kd[nkd - 1] * bg.eta0;
+  double dg = argmax / 5000.0;
+  const int nb = 5001;
+  int Lmax = 0;
+  for (int i = 0; i < nell; ++i) Lmax = std::max(Lmax, ells[i]);
+  // j_l on the Bessel grid, all requested l
+  std::vector<double> jtab(size_t(nell) * nb);
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+  {
+    std::vector<double> all(Lmax + 1);
+#pragma omp for schedule(dynamic, 16)
+    for (int ib = 0; ib < nb; ++ib) {
+      double xb = ib * dg;
+      sph_bessel_all(Lmax, xb, all.data());
+      for (int i = 0; i < nell; ++i) jtab[size_t(i) * nb + ib] = all[ells[i]];
+    }
+  }
+  int xi = 0;
+  while (xi < nx && !(g.at(xi) > -8.0)) ++xi;
+  std::vector<double> yv(nx), dx(nx);
+  for (int i = xi; i < nx - 1; ++i) {
+    yv[i] = bg.eta0 - bg.eta(g.at(i));
+    dx[i] = g.at(i + 1) - g.at(i);
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int il = 0; il < nell; ++il) {
+    int l = ells[il];
+    std::vector<double> col(jtab.begin() + size_t(il) * nb, jtab.begin() + size_t(il + 1) * nb);
+    Spline bes(col, 0.0, dg);
+    double lfac = std::sqrt(double(int64_t(l + 2) * int64_t(l + 1) * int64_t(l) * int64_t(l - 1)));
+    double stt = 0.0, ste = 0.0, see = 0.0;
+    for (int m = 0; m < nkd - 1; ++m) {
+      double k = (kd[m] + kd[m + 1]) / 2.0;
+      double dk = kd[m + 1] - kd[m];
+      int j = 0;
+      if (k >= kg[nk - 1]) j = nk - 2;
+      else { while (j < nk - 2 && kg[j + 1] <= k) ++j; }
+      double w = (k - kg[j]) / (kg[j + 1] - kg[j]);
+      const double* sT0 = ST + size_t(j) * nx;
+      const double* sT1 = ST + size_t(j + 1) * nx;
+      const double* sE0 = SE ? SE + size_t(j) * nx : nullptr;
+      const double* sE1 = SE ? SE + size_t(j + 1) * nx : nullptr;
+      double th = 0.0, ep = 0.0;
+      for (int i = xi; i < nx - 1; ++i) {
+        double b = bes(k * yv[i]);
+        th += b * ((1.0 - w) * sT0[i] + w * sT1[i]) * dx[i];
+        if (sE0) ep += b * ((1.0 - w) * sE0[i] + w * sE1[i]) * dx[i];
+      }
+      ep *= lfac;
+      double Pp = par.A * std::pow(k / 0.05, par.n - 1.0);
+      stt += th * th * Pp * dk / k;
+      ste += th * ep * Pp * dk / k;
+      see += ep * ep * Pp * dk / k;
+    }
+    if (tt) tt[il] = 4.0 * M_PI * stt;
+    if (te) te[il] = 4.0 * M_PI * ste;
+    if (ee) ee[il] = 4.0 * M_PI * see;
+  }
+  return 0;
+}
+
+// plin (spectra.jl:163-198)
+double oracle_plin(void* h, double k, int nq, int lg, int lnu, int lmnu, double x, double reltol, double abstol,
+                   int* status) {
+  OCosmo* o = static_cast<OCosmo*>(h);
+  const Background& bg = *o->bg;
+  const Params& p = o->C.par;
+  Mode md(&o->C, k, lg, lnu, lmnu, nq);
+  std::vector<double> u(md.N);
+  std::vector<double> xo(1, x);
+  SolveStats s = solve_mode(md, reltol, abstol, xo, [&](int, double, const double* y) {
+    std::copy(y, y + md.N, u.begin());
+  });
+  if (status) *status = s.status;
+  double a = std::exp(x);
+  std::vector<double> M0(nq), M1(nq), M2(nq);
+  for (int i = 0; i < nq; ++i) { M0[i] = u[md.M(0, i)]; M1[i] = u[md.M(1, i)]; M2[i] = u[md.M(2, i)]; }
+  double rho, sig;
+  rho_sigma(md, a, M0.data(), M2.data(), rho, sig);
+  double r0 = bg.rho0M(x);
+  double Mrho = rho / r0;
+  double th = 0.0;
+  for (int i = 0; i < nq; ++i) th += md.Bq[i] * M1[i];
+  double Mth = k * th / r0;
+  double dcN = u[md.iPhi + 1], dbN = u[md.iPhi + 3], vcN = u[md.iPhi + 2], vbN = u[md.iPhi + 4];
+  double vmnuN = -Mth / k;
+  double Tg = std::pow(15.0 / (M_PI * M_PI) * bg.rho_crit * p.Omega_r, 0.25);
+  double nufac = (90.0 * ZETA3 / (11.0 * std::pow(M_PI, 4))) * (p.Omega_r * p.h * p.h / Tg) * std::pow(p.N_nu / 3.0, 0.75);
+  double Omega_nu = p.Sigma_m_nu * nufac / (p.h * p.h);
+  double Om = p.Omega_c + p.Omega_b + Omega_nu;
+  double Hc = bg.H(x);
+  double dc = dcN - 3.0 * Hc * vcN / k;
+  double db = dbN - 3.0 * Hc * vbN / k;
+  double dmnu = Mrho - 3.0 * Hc * vmnuN / k;
+  double dm = (p.Omega_c * dc + p.Omega_b * db + Omega_nu * dmnu) / Om;
+  double Pprim = p.A * std::pow(k / 0.05, p.n - 1.0);
+  return (2.0 * M_PI * M_PI / (k * k * k)) * dm * dm * Pprim;
+}
+
+}  // extern "C"
