@@ -1,0 +1,101 @@
+"""ctypes binding of libbolt_gb300.so (include/bolt_gb300.h).
+
+Loading fails loudly: there is no CPU fallback for the solver or the
+line-of-sight kernels.  Only ``bolt_host_tables`` and the unit helpers work
+without a GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_i32p = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+
+
+class BoltParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in
+                ("h", "Omega_r", "Omega_b", "Omega_c", "A", "n", "Y_p", "N_nu", "Sigma_m_nu")]
+
+
+class BoltGrid(C.Structure):
+    _fields_ = [("start", C.c_double), ("step", C.c_double), ("stop", C.c_double)]
+
+
+class BoltRecfast(C.Structure):
+    _fields_ = [("Yp", C.c_double), ("OmegaB", C.c_double), ("OmegaG", C.c_double), ("Tnow", C.c_double),
+                ("tol", C.c_double)]
+
+
+class BoltHier(C.Structure):
+    _fields_ = [("lg", C.c_int), ("lnu", C.c_int), ("lmnu", C.c_int), ("nq", C.c_int)]
+
+
+class BoltOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("warps_per_block", C.c_int), ("max_steps", C.c_longlong)]
+
+
+EXPORTS = {
+    "bolt_version": (C.c_int, []),
+    "bolt_mass_natural": (C.c_double, []),
+    "bolt_km_s_Mpc_100": (C.c_double, []),
+    "bolt_host_tables": (C.c_int, [C.POINTER(BoltParams), C.POINTER(BoltGrid), C.c_int, C.POINTER(BoltRecfast),
+                                   _dp, _dp, C.c_char_p, C.c_int]),
+    "bolt_ctx_create": (C.c_int, [C.POINTER(BoltOpts), C.POINTER(C.c_void_p)]),
+    "bolt_ctx_destroy": (None, [C.c_void_p]),
+    "bolt_last_error": (C.c_char_p, [C.c_void_p]),
+    "bolt_cosmo_build": (C.c_int, [C.c_void_p, C.POINTER(BoltParams), C.POINTER(BoltGrid), C.c_int,
+                                   C.POINTER(BoltRecfast), _ip]),
+    "bolt_cosmo_upload": (C.c_int, [C.c_void_p, C.POINTER(BoltParams), C.POINTER(BoltGrid), C.c_int, _dp, _dp,
+                                    _ip]),
+    "bolt_cosmo_info": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "bolt_cosmo_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
+    "bolt_cosmo_free": (C.c_int, [C.c_void_p, C.c_int]),
+    "bolt_boltsolve": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.POINTER(BoltHier), C.c_double, C.c_double,
+                                 _dp, C.c_int, _dp, _i32p]),
+    "bolt_source_grid": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.POINTER(BoltHier), C.c_double,
+                                   C.c_double, _dp, _dp, _i32p]),
+    "bolt_cl": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int, _ip, C.c_int, _dp, _dp, _dp]),
+    "bolt_cl_pipeline": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.POINTER(BoltHier), C.c_double,
+                                   C.c_double, _ip, C.c_int, _dp, _dp, _dp, _i32p]),
+    "bolt_plin": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.POINTER(BoltHier), C.c_double, C.c_double,
+                            C.c_double, _dp, _i32p]),
+    "bolt_last_stats": (C.c_int, [C.c_void_p, _i64p]),
+}
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Loads (and if needed builds) the in-tree library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path) or not _build.up_to_date():
+        if not build_if_missing:
+            raise ImportError(f"libbolt_gb300.so is missing at {path}; run the build first")
+        _build.build()
+    L = C.CDLL(path)
+    for name, (res, args) in EXPORTS.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def dptr(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def iptr(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def i32ptr(a):
+    return a.ctypes.data_as(_i32p) if a is not None else None

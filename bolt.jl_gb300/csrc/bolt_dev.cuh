@@ -1,0 +1,146 @@
+// Device-side data layout shared by the GB300 kernels.
+//
+// Per cosmology, HBM holds one CosmoDev record plus its spline tables.  The
+// four tables the Rosenbrock right-hand side reads at every stage
+// (conformal Hubble rate, conformal time, opacity tau', baryon sound speed)
+// are interleaved coefficient-by-coefficient (hot[j][4]) so one 32-byte
+// sector delivers all four coefficients of node j; the remaining tables are
+// stored one after another (cold[t][n+2]).
+#pragma once
+#include <cstdint>
+
+namespace bolt {
+
+enum ColdId {
+  C_H = 0, C_HP, C_HPP, C_ETA, C_TAU, C_TAUP, C_TAUPP, C_G, C_GP, C_GPP, C_CSB2, C_RHO0M, C_COUNT
+};
+
+struct CosmoDev {
+  // cosmological parameters (CosmoParams, Bolt.jl:56-66); Sigma_m_nu in Mpc^-1
+  double h, Omega_r, Omega_b, Omega_c, A, n_s, Y_p, N_nu, Sigma_m_nu;
+  // background scalars
+  double H0, eta0, rho_crit, eta_last;  // eta_last = bg.η(x_grid[end])
+  double Tnu, logqmin, logqmax;
+  double Omega_nu;  // massless-neutrino density 7(2/3)N_nu/8 (4/11)^(4/3) Omega_r (perturbations.jl:171)
+  // uniform x grid: x_j = x0 + j * hx, n nodes; inv_hx = 1 / hx
+  double x0, hx, inv_hx;
+  int n, nq;
+  const double* hot;   // [n + 2][4]: H, eta, tau', csb2
+  const double* cold;  // [C_COUNT][n + 2]
+  const double* qw;    // [nq] Gauss-Legendre weights (on [-1, 1])
+  const double* qx;    // [nq] Gauss-Legendre nodes
+};
+
+// One k-mode of one cosmology.
+struct ModeDev {
+  double k;
+  int cosmo;
+  int lg, lnu, lmnu, nq;
+  int flags;          // MODE_* bits
+  int nout;           // landing nodes
+  const double* xout; // ascending landing nodes (device)
+  double* src_T;      // [nout] source S_T at the landing nodes (MODE_SOURCES)
+  double* src_E;      // [nout] source S_E
+  double* traj;       // [nout][N] state at the landing nodes (MODE_TRAJ)
+  double* plin;       // [1] P_lin at the last node (MODE_PLIN)
+  int32_t* status;    // [1]
+  int64_t* counters;  // [2] accepted steps, rejected steps
+};
+
+enum ModeFlags { MODE_SOURCES = 1, MODE_TRAJ = 2, MODE_PLIN = 4 };
+
+enum StatusBits {
+  ST_OK = 0,
+  ST_MAXITERS = 1,
+  ST_DT_UNDERFLOW = 2,
+  ST_NONFINITE = 3,
+  ST_LU_FAIL = 4,
+  ST_BAD_INPUT = 5,
+  ST_RSA_FIRED = 256  // informational, OR-ed into the code
+};
+
+struct SolverCfg {
+  double reltol, abstol, h0;
+  long long max_steps;
+};
+
+// ---------------------------------------------------------------- duals ----
+struct dd {
+  double v, d;
+};
+__device__ __forceinline__ dd mk(double v, double d) { dd r; r.v = v; r.d = d; return r; }
+__device__ __forceinline__ dd operator+(dd a, dd b) { return mk(a.v + b.v, a.d + b.d); }
+__device__ __forceinline__ dd operator-(dd a, dd b) { return mk(a.v - b.v, a.d - b.d); }
+__device__ __forceinline__ dd operator-(dd a) { return mk(-a.v, -a.d); }
+__device__ __forceinline__ dd operator*(dd a, dd b) { return mk(a.v * b.v, fma(a.d, b.v, a.v * b.d)); }
+__device__ __forceinline__ dd operator*(dd a, double b) { return mk(a.v * b, a.d * b); }
+__device__ __forceinline__ dd operator*(double b, dd a) { return mk(a.v * b, a.d * b); }
+__device__ __forceinline__ dd operator+(dd a, double b) { return mk(a.v + b, a.d); }
+__device__ __forceinline__ dd operator+(double b, dd a) { return mk(a.v + b, a.d); }
+__device__ __forceinline__ dd operator-(dd a, double b) { return mk(a.v - b, a.d); }
+__device__ __forceinline__ dd operator-(double b, dd a) { return mk(b - a.v, -a.d); }
+__device__ __forceinline__ dd operator/(dd a, dd b) {
+  double q = a.v / b.v;
+  return mk(q, (a.d - q * b.d) / b.v);
+}
+__device__ __forceinline__ dd operator/(dd a, double b) { return mk(a.v / b, a.d / b); }
+__device__ __forceinline__ dd operator/(double a, dd b) {
+  double q = a / b.v;
+  return mk(q, -q * b.d / b.v);
+}
+__device__ __forceinline__ double vof(double a) { return a; }
+__device__ __forceinline__ double vof(dd a) { return a.v; }
+template <class T> __device__ __forceinline__ T cst(double v);
+template <> __device__ __forceinline__ double cst<double>(double v) { return v; }
+template <> __device__ __forceinline__ dd cst<dd>(double v) { return mk(v, 0.0); }
+__device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ dd dsqrt(dd a) { double s = sqrt(a.v); return mk(s, 0.5 * a.d / s); }
+__device__ __forceinline__ double dexp(double a) { return exp(a); }
+__device__ __forceinline__ dd dexp(dd a) { double e = exp(a.v); return mk(e, e * a.d); }
+
+// ------------------------------------------------------- spline evaluation
+// Cubic B-spline on the uniform grid with Interpolations.jl's OnGrid
+// indexing: interval i = clamp(floor(u), 0, n-2), t = u - i.
+struct SplW {
+  int i;
+  double w0, w1, w2, w3;     // values
+  double d0, d1, d2, d3;     // first derivative weights (per unit x)
+};
+
+__device__ __forceinline__ void spl_locate(const CosmoDev& c, double x, int& i, double& t) {
+  double u = (x - c.x0) * c.inv_hx;
+  double f = floor(u);
+  f = fmin(fmax(f, 0.0), double(c.n - 2));
+  i = int(f);
+  t = u - f;
+}
+
+__device__ __forceinline__ void spl_weights(const CosmoDev& c, double x, SplW& w, bool deriv) {
+  double t;
+  spl_locate(c, x, w.i, t);
+  double s = 1.0 - t, t2 = t * t, s2 = s * s;
+  const double sixth = 1.0 / 6.0;
+  w.w0 = s2 * s * sixth;
+  w.w3 = t2 * t * sixth;
+  w.w1 = (4.0 - 6.0 * t2 + 3.0 * t2 * t) * sixth;
+  w.w2 = 1.0 - w.w0 - w.w1 - w.w3;
+  if (deriv) {
+    double ih = c.inv_hx;
+    w.d0 = -0.5 * s2 * ih;
+    w.d3 = 0.5 * t2 * ih;
+    w.d1 = (-2.0 * t + 1.5 * t2) * ih;
+    w.d2 = -(w.d0 + w.d1 + w.d3);
+  }
+}
+
+__device__ __forceinline__ double spl_cold(const CosmoDev& c, int id, double x) {
+  const double* p = c.cold + (size_t)id * (c.n + 2);
+  double t;
+  int i;
+  spl_locate(c, x, i, t);
+  double s = 1.0 - t, t2 = t * t, s2 = s * s;
+  return (p[i] * s2 * s + p[i + 1] * (4.0 - 6.0 * t2 + 3.0 * t2 * t) + p[i + 2] * (4.0 - 6.0 * s2 + 3.0 * s2 * s) +
+          p[i + 3] * t2 * t) * (1.0 / 6.0);
+}
+
+}  // namespace bolt

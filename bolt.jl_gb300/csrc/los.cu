@@ -1,0 +1,296 @@
+// Line-of-sight projection: spherical Bessel tables, source resampling and
+// the C_l^TT / TE / EE reduction (Bolt.jl src/spectra.jl:49-160).
+//
+//   bessel_interpolator(l, kmax*eta0)  spectra.jl:49-58  -> jl_raw_kernel + jl_prefilter_kernel
+//   Tl / _Tl_integrand                 spectra.jl:70-82  -> los_cl_kernel (inner x loop)
+//   cltt / clte / clee                 spectra.jl:84-160 -> los_cl_kernel (k sum, fused)
+//
+// The reference tabulates j_l on 5001 uniform points of [0, kmax*eta0],
+// splines it (cubic B-spline, natural ends) and evaluates
+//   Delta_l(k) = sum_{x_i > -8} j_l(k (eta0 - eta(x_i))) S(x_i, k) dx_i
+// at the midpoints of a 5000-point quadratic k grid, with S bilinearly
+// interpolated from the source grid (exact in x at the nodes, linear in k,
+// linearly extrapolated outside the source k range).  All arithmetic is FP64.
+#include <cuda_runtime.h>
+
+#include "bolt_dev.cuh"
+
+namespace bolt {
+
+// ------------------------------------------------------------- j_l table ---
+// Debye exponent D = nu (alpha - tanh alpha), cosh alpha = nu / x (nu > x):
+// j_l(x) ~ exp(-D).
+__device__ __forceinline__ double debye_exponent(double nu, double x) {
+  double r = nu / x;
+  double al = log(r + sqrt(r * r - 1.0));
+  return nu * (al - sqrt(1.0 - 1.0 / (r * r)));
+}
+
+// One thread per Bessel-grid point x_b = ib * dg.  Miller's downward
+// recurrence f_{l-1} = (2l+1)/x f_l - f_{l+1} started past max(Lmax, x),
+// normalised with the sum rule sum_l (2l+1) j_l(x)^2 = 1 and signed by the
+// closed forms of j_0 / j_1.  Raw (unnormalised) values are stored for the
+// requested l; norm[ib] carries the normalisation into the prefilter.
+// Values below ~1e-250 (far below the turning point) are stored as 0.
+__global__ void jl_raw_kernel(int nb, const double* __restrict__ dgs, int Lmax, const int* __restrict__ slot_of_l,
+                              int nslots, double* __restrict__ raw, double* __restrict__ norm,
+                              int* __restrict__ flags) {
+  const int ib = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cz = blockIdx.y;
+  if (ib >= nb) return;
+  const double dg = dgs[cz];
+  double* R = raw + (size_t)cz * nslots * nb;
+  const double x = ib * dg;
+  if (x <= 1.4901161193847656e-8) {
+    for (int l = 0; l <= Lmax; ++l) {
+      int s = slot_of_l[l];
+      if (s >= 0) R[(size_t)s * nb + ib] = (l == 0) ? 1.0 : 0.0;
+    }
+    norm[(size_t)cz * nb + ib] = 1.0;
+    return;
+  }
+  int ls = max(Lmax, (int)ceil(x)) + 20 + (int)ceil(10.0 * cbrt(x));
+  // cut where j_l(x) < ~1e-250: smallest nu with D(nu) > 575
+  double nus = ls + 0.5;
+  if (debye_exponent(nus, x) > 575.0) {
+    double lo = fmax(x, 0.5) * 1.0000001, hi = nus;
+    if (debye_exponent(lo, x) > 575.0) lo = x * 1.0000001;
+    for (int it = 0; it < 60; ++it) {
+      double mid = 0.5 * (lo + hi);
+      if (debye_exponent(mid, x) > 575.0) hi = mid; else lo = mid;
+    }
+    ls = (int)ceil(hi);
+  }
+  // zero the requested l above the start
+  for (int l = ls + 1; l <= Lmax; ++l) {
+    int s = slot_of_l[l];
+    if (s >= 0) R[(size_t)s * nb + ib] = 0.0;
+  }
+  double seed = 1e-290;
+  {
+    double nu = ls + 0.5;
+    if (nu > x * 1.0000001) seed = fmax(1e-290, exp(-fmin(debye_exponent(nu, x), 660.0)));
+    else seed = 1.0;
+  }
+  const double ix = 1.0 / x;
+  double fp1 = 0.0, f = seed, sum = 0.0;
+  int resc_l = -1;
+  for (int l = ls; l >= 0; --l) {
+    if (l <= Lmax) {
+      int s = slot_of_l[l];
+      if (s >= 0) R[(size_t)s * nb + ib] = f;
+    }
+    sum = fma(2.0 * l + 1.0, f * f, sum);
+    if (l == 0) break;
+    double fm1 = fma((2.0 * l + 1.0) * ix, f, -fp1);
+    fp1 = f;
+    f = fm1;
+    if (fabs(f) > 1e150) {  // keep the recurrence in range (values above are tiny)
+      f *= 1e-150; fp1 *= 1e-150; sum *= 1e-300;
+      resc_l = l - 1;
+      flags[0] = 1;
+    }
+  }
+  // f now holds f_0 (unnormalised).  Sign from the larger closed form.
+  double s_ = sin(x), c_ = cos(x);
+  double j0 = s_ * ix, j1 = s_ * ix * ix - c_ * ix;
+  double sgn;
+  if (fabs(j0) >= fabs(j1)) sgn = (j0 >= 0) == (f >= 0) ? 1.0 : -1.0;
+  else {
+    // f_1 = fp1 at loop end
+    sgn = (j1 >= 0) == (fp1 >= 0) ? 1.0 : -1.0;
+  }
+  double nrm = sgn / sqrt(sum);
+  norm[(size_t)cz * nb + ib] = nrm;
+  if (resc_l >= 0) {
+    // values stored above the rescale point need the extra factor: they are
+    // below 1e-150 of the peak and are flushed to zero
+    for (int l = resc_l + 1; l <= min(Lmax, ls); ++l) {
+      int s = slot_of_l[l];
+      if (s >= 0) R[(size_t)s * nb + ib] = 0.0;
+    }
+  }
+}
+
+// Natural cubic B-spline prefilter along the Bessel grid, one thread per
+// (slot, cosmology).  w[r] = 1 / pivot of the constant (1, 4, 1) system.
+__global__ void jl_prefilter_kernel(int nb, int nslots, int ncz, const double* __restrict__ raw,
+                                    const double* __restrict__ norm, const double* __restrict__ w,
+                                    double* __restrict__ coef) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nslots * ncz) return;
+  int cz = t / nslots, s = t - cz * nslots;
+  const double* y = raw + ((size_t)cz * nslots + s) * nb;
+  const double* nr = norm + (size_t)cz * nb;
+  double* c = coef + ((size_t)cz * nslots + s) * (nb + 2);
+  const int n = nb, m = n - 2;
+  double y0 = y[0] * nr[0], yl = y[n - 1] * nr[n - 1];
+  c[1] = y0;
+  c[n] = yl;
+  // forward sweep of the (1, 4, 1) system for c[2..n-1] (right-hand side 6 y)
+  double prev = 6.0 * (y[1] * nr[1]) - y0;
+  c[2] = prev;
+  for (int r = 1; r < m; ++r) {
+    double v = 6.0 * (y[r + 1] * nr[r + 1]) - prev * w[r - 1];
+    c[r + 2] = v;
+    prev = v;
+  }
+  double xv = (c[n - 1] - yl) * w[m - 1];
+  c[n - 1] = xv;
+  for (int r = m - 2; r >= 0; --r) {
+    xv = (c[r + 2] - xv) * w[r];
+    c[r + 2] = xv;
+  }
+  c[0] = 2.0 * c[1] - c[2];
+  c[n + 1] = 2.0 * c[n] - c[n - 1];
+}
+
+// ------------------------------------------------------ dense source grid --
+// Sd[i][m] = S(x_{i0+i}, k_m) * dx_{i0+i} for the k midpoints k_m; the x
+// direction is exact at the nodes, the k direction linear with linear
+// extrapolation (spectra.jl:21).  ST/SE layout: [nk][nx].
+__global__ void sdense_kernel(int nx, int i0, int nrow, int nk, const double* __restrict__ kgrid,
+                              const double* __restrict__ ST, const double* __restrict__ SE, int nm,
+                              const double* __restrict__ kmid, const double* __restrict__ dxs,
+                              double* __restrict__ SdT, double* __restrict__ SdE) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y;
+  if (m >= nm || i >= nrow) return;
+  double k = kmid[m];
+  // interval search (k grid ascending)
+  int lo = 0, hi = nk - 1;
+  if (k >= kgrid[nk - 1]) lo = nk - 2;
+  else if (k < kgrid[0]) lo = 0;
+  else {
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (kgrid[mid] <= k) lo = mid; else hi = mid;
+    }
+    if (lo > nk - 2) lo = nk - 2;
+  }
+  double wk = (k - kgrid[lo]) / (kgrid[lo + 1] - kgrid[lo]);
+  int ix = i0 + i;
+  double dx = dxs[i];
+  double t0 = ST[(size_t)lo * nx + ix], t1 = ST[(size_t)(lo + 1) * nx + ix];
+  SdT[(size_t)i * nm + m] = ((1.0 - wk) * t0 + wk * t1) * dx;
+  if (SE) {
+    double e0 = SE[(size_t)lo * nx + ix], e1 = SE[(size_t)(lo + 1) * nx + ix];
+    SdE[(size_t)i * nm + m] = ((1.0 - wk) * e0 + wk * e1) * dx;
+  }
+}
+
+// ---------------------------------------------------------------- C_l -------
+// One block per (l slot, cosmology); the l's spline coefficients sit in
+// shared memory; each thread owns k midpoints and runs the x sum for them.
+// wts[m] = A (k_m/0.05)^(n-1) dk_m / k_m.  The block reduction is in a
+// fixed order so results are bitwise reproducible run to run.
+struct LosArgs {
+  int nb, nslots, nrow, nm;
+  const int* ells;          // [nslots]
+  const double* coef;       // [ncz][nslots][nb+2]
+  const double* inv_dg;     // [ncz]
+  const double* yv;         // [ncz][nrow]  eta0 - eta(x_i)
+  const double* kmid;       // [ncz][nm]
+  const double* wts;        // [ncz][nm]
+  const double* SdT;        // [ncz][nrow][nm]
+  const double* SdE;        // [ncz][nrow][nm] or null
+  double* tt;               // [ncz][nslots]
+  double* te;
+  double* ee;
+};
+
+__global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
+  extern __shared__ double sh[];
+  const int s = blockIdx.x, cz = blockIdx.y;
+  const int nb2 = a.nb + 2;
+  double* cs = sh;                 // nb + 2 coefficients
+  double* yl = sh + nb2;           // nrow scaled arguments
+  double* red = yl + a.nrow;       // 3 * blockDim
+  const double* src = a.coef + ((size_t)cz * a.nslots + s) * nb2;
+  for (int j = threadIdx.x; j < nb2; j += blockDim.x) cs[j] = src[j];
+  const double idg = a.inv_dg[cz];
+  for (int j = threadIdx.x; j < a.nrow; j += blockDim.x) yl[j] = a.yv[(size_t)cz * a.nrow + j] * idg;
+  __syncthreads();
+  const int l = a.ells[s];
+  const double lfac = sqrt(double((long long)(l + 2) * (l + 1) * (long long)l * (l - 1)));
+  const double* SdT = a.SdT + (size_t)cz * a.nrow * a.nm;
+  const double* SdE = a.SdE ? a.SdE + (size_t)cz * a.nrow * a.nm : nullptr;
+  const double* km = a.kmid + (size_t)cz * a.nm;
+  const double* wm = a.wts + (size_t)cz * a.nm;
+  const double umax = double(a.nb - 2);
+  double stt = 0.0, ste = 0.0, see = 0.0;
+  for (int m = threadIdx.x; m < a.nm; m += blockDim.x) {
+    const double k = km[m];
+    double th = 0.0, ep = 0.0;
+    for (int i = 0; i < a.nrow; ++i) {
+      double u = k * yl[i];
+      double f = floor(u);
+      f = fmin(f, umax);
+      int j = (int)f;
+      double t = u - f, sm = 1.0 - t, t2 = t * t, s2 = sm * sm;
+      double w0 = s2 * sm, w3 = t2 * t;
+      double w1 = 4.0 - 6.0 * t2 + 3.0 * w3;
+      double w2 = 4.0 - 6.0 * s2 + 3.0 * w0;
+      double jv = (cs[j] * w0 + cs[j + 1] * w1 + cs[j + 2] * w2 + cs[j + 3] * w3) * (1.0 / 6.0);
+      th = fma(jv, SdT[(size_t)i * a.nm + m], th);
+      if (SdE) ep = fma(jv, SdE[(size_t)i * a.nm + m], ep);
+    }
+    ep *= lfac;
+    double w = wm[m];
+    stt = fma(th * th, w, stt);
+    ste = fma(th * ep, w, ste);
+    see = fma(ep * ep, w, see);
+  }
+  red[threadIdx.x] = stt;
+  red[blockDim.x + threadIdx.x] = ste;
+  red[2 * blockDim.x + threadIdx.x] = see;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      red[threadIdx.x] += red[threadIdx.x + o];
+      red[blockDim.x + threadIdx.x] += red[blockDim.x + threadIdx.x + o];
+      red[2 * blockDim.x + threadIdx.x] += red[2 * blockDim.x + threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double fp = 4.0 * M_PI;
+    if (a.tt) a.tt[(size_t)cz * a.nslots + s] = fp * red[0];
+    if (a.te) a.te[(size_t)cz * a.nslots + s] = fp * red[blockDim.x];
+    if (a.ee) a.ee[(size_t)cz * a.nslots + s] = fp * red[2 * blockDim.x];
+  }
+}
+
+// ------------------------------------------------------------ launchers ----
+int launch_jl_raw(int nb, const double* d_dgs, int ncz, int Lmax, const int* d_slot_of_l, int nslots, double* d_raw,
+                  double* d_norm, int* d_flags, cudaStream_t st) {
+  dim3 g((nb + 127) / 128, ncz);
+  jl_raw_kernel<<<g, 128, 0, st>>>(nb, d_dgs, Lmax, d_slot_of_l, nslots, d_raw, d_norm, d_flags);
+  return cudaGetLastError();
+}
+
+int launch_jl_prefilter(int nb, int nslots, int ncz, const double* d_raw, const double* d_norm, const double* d_w,
+                        double* d_coef, cudaStream_t st) {
+  int n = nslots * ncz;
+  jl_prefilter_kernel<<<(n + 63) / 64, 64, 0, st>>>(nb, nslots, ncz, d_raw, d_norm, d_w, d_coef);
+  return cudaGetLastError();
+}
+
+int launch_sdense(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_ST, const double* d_SE, int nm,
+                  const double* d_kmid, const double* d_dx, double* d_SdT, double* d_SdE, cudaStream_t st) {
+  dim3 g((nm + 255) / 256, nrow);
+  sdense_kernel<<<g, 256, 0, st>>>(nx, i0, nrow, nk, d_kgrid, d_ST, d_SE, nm, d_kmid, d_dx, d_SdT, d_SdE);
+  return cudaGetLastError();
+}
+
+int launch_los_cl(const LosArgs& a, int ncz, cudaStream_t st) {
+  const int threads = 256;
+  size_t smem = (size_t(a.nb + 2) + a.nrow + 3 * threads) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(los_cl_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return e;
+  dim3 g(a.nslots, ncz);
+  los_cl_kernel<<<g, threads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace bolt

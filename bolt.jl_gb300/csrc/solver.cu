@@ -1,0 +1,947 @@
+// Persistent Rosenbrock (Rodas4) solver for the Newtonian-gauge Boltzmann
+// hierarchy, one warp per k-mode.
+//
+// Restates, on the GPU, boltsolve + hierarchy! + initial_conditions +
+// source_function(_P) + plin from Bolt.jl (src/perturbations.jl:25-33,
+// 161-271, 274-338, 343-404; src/spectra.jl:163-198).  The reference
+// integrates with OrdinaryDiffEq's KenCarp4; this kernel integrates the same
+// linear ODE u' = A(x) u with Rodas4 (Hairer & Wanner, RODAS coefficient
+// set 1), landing exactly on every output node.
+//
+// Linear algebra.  A(x) = L(x) + U(x) W(x)^T where L is block diagonal with
+// one tridiagonal chain per species (photon temperature with the baryon pair
+// (delta_b, v_b) hanging off Theta_1, photon polarization, massless
+// neutrinos, one chain per massive-neutrino momentum bin, the CDM pair and
+// Phi) and U W^T holds the three global couplings Phi', Psi and Pi.  Each
+// chain is eliminated from its highest multipole down to l = 0, so the
+// rank-3 border only touches the last few rows of every chain: a stage
+// solve is one forward sweep, a 3x3 capacitance solve on the chain tails,
+// and one back substitution -- O(N) FP64 work, one lane per chain.
+//
+// Memory.  The whole per-mode working set (state, six stage vectors, the
+// chain factors and the border tails) lives in shared memory; the only
+// global traffic is the spline tables (L2-resident, ~0.3 MB per cosmology)
+// and the outputs.  Warps pull modes from a device work queue so modes with
+// very different step counts balance across the 152 SMs.
+#include <cuda_runtime.h>
+
+#include "bolt_dev.cuh"
+
+namespace bolt {
+
+namespace rodas {
+__constant__ double kA[5][4] = {{1.544, 0, 0, 0},
+                                {0.9466785280815826, 0.2557011698983284, 0, 0},
+                                {3.314825187068521, 2.896124015972201, 0.9986419139977817, 0},
+                                {1.221224509226641, 6.019134481288629, 12.53708332932087, -0.687886036105895},
+                                {0, 0, 0, 0}};
+__constant__ double kC[6][5] = {{0, 0, 0, 0, 0},
+                                {-5.6688, 0, 0, 0, 0},
+                                {-2.430093356833875, -0.2063599157091915, 0, 0, 0},
+                                {-0.1073529058151375, -9.594562251023355, -20.47028614809616, 0, 0},
+                                {7.496443313967647, -10.24680431464352, -33.99990352819905, 11.7089089320616, 0},
+                                {8.083246795921522, -7.981132988064893, -31.52159432874371, 16.31930543123136,
+                                 -6.058818238834054}};
+__constant__ double kCx[6] = {0.0, 0.386, 0.21, 0.63, 1.0, 1.0};
+__constant__ double kD[6] = {0.25, -0.1043, 0.1035, -0.0362, 0.0, 0.0};
+constexpr double kGamma = 0.25;
+}  // namespace rodas
+
+constexpr int kTail = 5;   // tail slots per chain
+constexpr int kBorder = 3; // Phi', Psi, Pi
+
+struct Shared {
+  double *y, *yt, *fx, *K, *fl, *fi, *fc;
+  double *q, *df0, *Aq, *Bq, *qe, *eq, *qe_d, *eq_d;
+  double *Uf, *Wt, *cl1, *cl2, *misc;
+};
+
+__host__ __device__ inline int per_warp_doubles(int N, int nq, int Lmax) {
+  int nch = nq + 5;
+  return 12 * N + 8 * nq + 2 * nch * kTail * kBorder + 2 * (Lmax + 1) + 32;
+}
+
+struct Mode {
+  const CosmoDev* C;
+  double k;
+  int N, lg, lnu, lmnu, nq, iTp, iN, iM, iPhi, nch;
+};
+
+// The four interleaved hot tables at node j (H, eta, tau', csb2).
+struct HotCoef {
+  double x, y, z, w;
+};
+__device__ __forceinline__ void load_hot(const CosmoDev& C, int i, HotCoef& c0, HotCoef& c1, HotCoef& c2, HotCoef& c3) {
+  const double2* p = reinterpret_cast<const double2*>(C.hot + 4 * (size_t)i);
+  double2 a0 = __ldg(p), b0 = __ldg(p + 1), a1 = __ldg(p + 2), b1 = __ldg(p + 3);
+  double2 a2 = __ldg(p + 4), b2 = __ldg(p + 5), a3 = __ldg(p + 6), b3 = __ldg(p + 7);
+  c0.x = a0.x; c0.y = a0.y; c0.z = b0.x; c0.w = b0.y;
+  c1.x = a1.x; c1.y = a1.y; c1.z = b1.x; c1.w = b1.y;
+  c2.x = a2.x; c2.y = a2.y; c2.z = b2.x; c2.w = b2.y;
+  c3.x = a3.x; c3.y = a3.y; c3.z = b3.x; c3.w = b3.y;
+}
+
+// Stage scalars: everything in the right-hand side that depends on x only.
+template <class T>
+struct Scal {
+  T Hc, eta, tp, cs2, a, kH, iHe, R, cpsi, dphi, k2H2;
+};
+
+template <class T>
+__device__ __forceinline__ void stage_scalars(const Mode& m, double x, Scal<T>& s);
+
+template <>
+__device__ __forceinline__ void stage_scalars<double>(const Mode& m, double x, Scal<double>& s) {
+  const CosmoDev& C = *m.C;
+  SplW w;
+  spl_weights(C, x, w, false);
+  HotCoef c0, c1, c2, c3;
+  load_hot(C, w.i, c0, c1, c2, c3);
+  s.Hc = c0.x * w.w0 + c1.x * w.w1 + c2.x * w.w2 + c3.x * w.w3;
+  s.eta = c0.y * w.w0 + c1.y * w.w1 + c2.y * w.w2 + c3.y * w.w3;
+  s.tp = c0.z * w.w0 + c1.z * w.w1 + c2.z * w.w2 + c3.z * w.w3;
+  s.cs2 = c0.w * w.w0 + c1.w * w.w1 + c2.w * w.w2 + c3.w * w.w3;
+  s.a = exp(x);
+  double iH = 1.0 / s.Hc;
+  s.kH = m.k * iH;
+  s.iHe = iH / s.eta;
+  s.R = 4.0 * C.Omega_r / (3.0 * C.Omega_b * s.a);
+  s.cpsi = 12.0 * C.H0 * C.H0 / (m.k * m.k) / (s.a * s.a);
+  s.dphi = C.H0 * C.H0 * 0.5 * iH * iH;
+  s.k2H2 = m.k * m.k / 3.0 * iH * iH;
+}
+
+template <>
+__device__ __forceinline__ void stage_scalars<dd>(const Mode& m, double x, Scal<dd>& s) {
+  const CosmoDev& C = *m.C;
+  SplW w;
+  spl_weights(C, x, w, true);
+  HotCoef c0, c1, c2, c3;
+  load_hot(C, w.i, c0, c1, c2, c3);
+  s.Hc = mk(c0.x * w.w0 + c1.x * w.w1 + c2.x * w.w2 + c3.x * w.w3, c0.x * w.d0 + c1.x * w.d1 + c2.x * w.d2 + c3.x * w.d3);
+  s.eta = mk(c0.y * w.w0 + c1.y * w.w1 + c2.y * w.w2 + c3.y * w.w3, c0.y * w.d0 + c1.y * w.d1 + c2.y * w.d2 + c3.y * w.d3);
+  s.tp = mk(c0.z * w.w0 + c1.z * w.w1 + c2.z * w.w2 + c3.z * w.w3, c0.z * w.d0 + c1.z * w.d1 + c2.z * w.d2 + c3.z * w.d3);
+  s.cs2 = mk(c0.w * w.w0 + c1.w * w.w1 + c2.w * w.w2 + c3.w * w.w3, c0.w * w.d0 + c1.w * w.d1 + c2.w * w.d2 + c3.w * w.d3);
+  double ea = exp(x);
+  s.a = mk(ea, ea);
+  dd iH = 1.0 / s.Hc;
+  s.kH = m.k * iH;
+  s.iHe = iH / s.eta;
+  s.R = (4.0 * C.Omega_r / (3.0 * C.Omega_b)) / s.a;
+  s.cpsi = (12.0 * C.H0 * C.H0 / (m.k * m.k)) / (s.a * s.a);
+  s.dphi = (C.H0 * C.H0 * 0.5) * iH * iH;
+  s.k2H2 = (m.k * m.k / 3.0) * iH * iH;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Massive-neutrino energies q/eps and eps/q at scale factor a (lane q).
+template <class T>
+__device__ __forceinline__ void nu_energies(const Mode& m, const Shared& S, T a, int lane);
+template <>
+__device__ __forceinline__ void nu_energies<double>(const Mode& m, const Shared& S, double a, int lane) {
+  for (int q = lane; q < m.nq; q += 32) {
+    double am = a * m.C->Sigma_m_nu, qq = S.q[q];
+    double eps = sqrt(qq * qq + am * am);
+    S.qe[q] = qq / eps;
+    S.eq[q] = eps / qq;
+  }
+}
+template <>
+__device__ __forceinline__ void nu_energies<dd>(const Mode& m, const Shared& S, dd a, int lane) {
+  for (int q = lane; q < m.nq; q += 32) {
+    double am = a.v * m.C->Sigma_m_nu, qq = S.q[q];
+    double eps = sqrt(qq * qq + am * am);
+    double deps = am * am / eps;  // d eps / dx
+    S.qe[q] = qq / eps;
+    S.eq[q] = eps / qq;
+    S.qe_d[q] = -qq * deps / (eps * eps);
+    S.eq_d[q] = deps / qq;
+  }
+}
+
+template <class T> __device__ __forceinline__ T qe_of(const Shared& S, int q);
+template <> __device__ __forceinline__ double qe_of<double>(const Shared& S, int q) { return S.qe[q]; }
+template <> __device__ __forceinline__ dd qe_of<dd>(const Shared& S, int q) { return mk(S.qe[q], S.qe_d[q]); }
+template <class T> __device__ __forceinline__ T eq_of(const Shared& S, int q);
+template <> __device__ __forceinline__ double eq_of<double>(const Shared& S, int q) { return S.eq[q]; }
+template <> __device__ __forceinline__ dd eq_of<dd>(const Shared& S, int q) { return mk(S.eq[q], S.eq_d[q]); }
+
+template <class T> __device__ __forceinline__ void put(double* v, double* d, int i, T x);
+template <> __device__ __forceinline__ void put<double>(double* v, double*, int i, double x) { v[i] = x; }
+template <> __device__ __forceinline__ void put<dd>(double* v, double* d, int i, dd x) { v[i] = x.v; d[i] = x.d; }
+
+template <class T> __device__ __forceinline__ T warp_sum_t(T v);
+template <> __device__ __forceinline__ double warp_sum_t<double>(double v) { return warp_sum(v); }
+template <> __device__ __forceinline__ dd warp_sum_t<dd>(dd v) { return mk(warp_sum(v.v), warp_sum(v.d)); }
+
+// Metric potentials Psi and Phi' (perturbations.jl:182-194) from the state u.
+template <class T>
+__device__ __forceinline__ void metric(const Mode& m, const Shared& S, const Scal<T>& s, const double* u, int lane,
+                                       T& Psi, T& Phip, T* rhoM_out = nullptr) {
+  const CosmoDev& C = *m.C;
+  T rho = cst<T>(0.0), sig = cst<T>(0.0);
+  for (int q = lane; q < m.nq; q += 32) {
+    T qe = qe_of<T>(S, q), eq = eq_of<T>(S, q);
+    double qq = S.q[q];
+    // eps = q * eq ; q^2/eps = q * qe
+    rho = rho + (S.Aq[q] * qq) * eq * u[m.iM + q];
+    sig = sig + (S.Aq[q] * qq) * qe * u[m.iM + 2 * m.nq + q];
+  }
+  rho = warp_sum_t<T>(rho);
+  sig = warp_sum_t<T>(sig);
+  if (rhoM_out) *rhoM_out = rho;
+  const double Omega_nu = C.Omega_nu;
+  double Phi = u[m.iPhi];
+  Psi = -Phi - s.cpsi * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig * (0.25 / C.rho_crit));
+  T ia = 1.0 / s.a;
+  Phip = Psi - s.k2H2 * Phi +
+         s.dphi * ((C.Omega_c * u[m.iPhi + 1] + C.Omega_b * u[m.iPhi + 3]) * ia +
+                   (4.0 * C.Omega_r * u[0] + 4.0 * Omega_nu * u[m.iN] + rho * (1.0 / C.rho_crit)) * (ia * ia));
+}
+
+// hierarchy! (perturbations.jl:161-271): writes f into out (and df/dx into
+// out_d for T = dd).  Returns true when the radiation-streaming switch is on.
+template <class T>
+__device__ bool rhs_rows(const Mode& m, const Shared& S, double x, const double* u, double* out, double* out_d, int lane) {
+  Scal<T> s;
+  stage_scalars<T>(m, x, s);
+  nu_energies<T>(m, S, s.a, lane);
+  __syncwarp();
+  T Psi, Phip;
+  metric<T>(m, S, s, u, lane, Psi, Phip);
+  const CosmoDev& C = *m.C;
+  const int lg = m.lg, lnu = m.lnu, lmnu = m.lmnu, nq = m.nq;
+  const double* cl1 = S.cl1;
+  const double* cl2 = S.cl2;
+  bool rsa = (m.k * vof(s.eta) > 240.0) && (-vof(s.tp) * vof(s.Hc) / vof(s.eta) > 100.0);
+  double Pi = u[2] + u[m.iTp + 2] + u[m.iTp];
+  double vb = u[m.iPhi + 4];
+  if (rsa) {
+    for (int i = lane; i < m.iM; i += 32) put<T>(out, out_d, i, cst<T>(0.0));
+  } else {
+    // photon temperature
+    for (int l = lane; l <= lg; l += 32) {
+      T f;
+      if (l < lg) {
+        double lo = l > 0 ? u[l - 1] : 0.0;
+        f = s.kH * (cl1[l] * lo - cl2[l] * u[l + 1]);
+        if (l >= 1) f = f + s.tp * u[l];
+        if (l == 0) f = f - Phip;
+        if (l == 1) f = f + (1.0 / 3.0) * s.kH * Psi + s.tp * (vb / 3.0);
+        if (l == 2) f = f - s.tp * (Pi / 10.0);
+      } else {
+        f = s.kH * u[lg - 1] - ((lg + 1.0) * s.iHe - s.tp) * u[lg];
+      }
+      put<T>(out, out_d, l, f);
+    }
+    // photon polarization
+    const double* P = u + m.iTp;
+    for (int l = lane; l <= lg; l += 32) {
+      T f;
+      if (l < lg) {
+        double lo = l > 0 ? P[l - 1] : 0.0;
+        f = s.kH * (cl1[l] * lo - cl2[l] * P[l + 1]) + s.tp * P[l];
+        if (l == 0) f = f - s.tp * (Pi / 2.0);
+        if (l == 2) f = f - s.tp * (Pi / 10.0);
+      } else {
+        f = s.kH * P[lg - 1] - ((lg + 1.0) * s.iHe - s.tp) * P[lg];
+      }
+      put<T>(out, out_d, m.iTp + l, f);
+    }
+    // massless neutrinos
+    const double* Nn = u + m.iN;
+    for (int l = lane; l <= lnu; l += 32) {
+      T f;
+      if (l < lnu) {
+        double lo = l > 0 ? Nn[l - 1] : 0.0;
+        f = s.kH * (cl1[l] * lo - cl2[l] * Nn[l + 1]);
+        if (l == 0) f = f - Phip;
+        if (l == 1) f = f + (1.0 / 3.0) * s.kH * Psi;
+      } else {
+        f = s.kH * Nn[lnu - 1] - (lnu + 1.0) * s.iHe * Nn[lnu];
+      }
+      put<T>(out, out_d, m.iN + l, f);
+    }
+  }
+  // massive neutrinos (MB 57)
+  const double* Mm = u + m.iM;
+  const int nM = (lmnu + 1) * nq;
+  for (int j = lane; j < nM; j += 32) {
+    int l = j / nq, q = j - l * nq;
+    T qe = qe_of<T>(S, q);
+    T f;
+    if (l < lmnu) {
+      double lo = l > 0 ? Mm[j - nq] : 0.0;
+      f = (s.kH * qe) * (cl1[l] * lo - cl2[l] * Mm[j + nq]);
+      if (l == 0) f = f + Phip * S.df0[q];
+      if (l == 1) f = f - (1.0 / 3.0) * s.kH * eq_of<T>(S, q) * Psi * S.df0[q];
+    } else {
+      f = qe * s.kH * Mm[j - nq] - (lmnu + 1.0) * s.iHe * Mm[j];
+    }
+    put<T>(out, out_d, m.iM + j, f);
+  }
+  // metric and matter
+  if (lane < 5) {
+    int i = m.iPhi + lane;
+    T f;
+    double del = u[m.iPhi + 1], v = u[m.iPhi + 2], delb = u[m.iPhi + 3];
+    if (lane == 0) f = Phip;
+    else if (lane == 1) f = s.kH * v - 3.0 * Phip;
+    else if (lane == 2) f = -v - s.kH * Psi;
+    else if (lane == 3) f = s.kH * vb - 3.0 * Phip;
+    else f = -vb - s.kH * (Psi + s.cs2 * delb) + s.tp * s.R * (3.0 * u[1] + vb);
+    put<T>(out, out_d, i, f);
+  }
+  (void)C;
+  return rsa;
+}
+
+// ------------------------------------------------------------ factorize ----
+// Chains: 0 photon temperature (+ baryon pair), 1 polarization, 2 massless
+// neutrinos, 3..3+nq-1 massive-neutrino bins, 3+nq CDM pair, 4+nq Phi.
+// Tail slots per chain: [l=0, l=1, l=2, extra0, extra1]; chain 0 uses the
+// extras for (v_b, delta_b); the CDM chain uses slots (delta, v) = (0, 1);
+// Phi uses slot 0.
+__device__ __forceinline__ int tail_index(const Mode& m, int c, int slot) {
+  if (c == 0) {
+    if (slot < 3) return slot;
+    return slot == 3 ? m.iPhi + 4 : m.iPhi + 3;
+  }
+  if (c == 1) return m.iTp + slot;
+  if (c == 2) return m.iN + slot;
+  if (c < 3 + m.nq) return m.iM + slot * m.nq + (c - 3);
+  if (c == 3 + m.nq) return m.iPhi + 1 + slot;  // delta, v
+  return m.iPhi;
+}
+
+__device__ __forceinline__ int tail_slots(const Mode& m, int c) {
+  if (c == 0) return 5;
+  if (c < 3 + m.nq) return 3;
+  if (c == 3 + m.nq) return 2;
+  return 1;
+}
+
+// Factor M = I/(h gamma) - L chain by chain (lane c), build the border tails
+// and the 3x3 capacitance inverse.  Returns false on a zero or non-finite
+// pivot.
+__device__ bool factorize(const Mode& m, const Shared& S, double x, double hg, int lane) {
+  const CosmoDev& C = *m.C;
+  Scal<double> s;
+  stage_scalars<double>(m, x, s);
+  nu_energies<double>(m, S, s.a, lane);
+  __syncwarp();
+  const double ig = 1.0 / hg;
+  const double* cl1 = S.cl1;
+  const double* cl2 = S.cl2;
+  const double Omega_nu = C.Omega_nu;
+  bool ok = true;
+  double cap[9];
+  for (int r = 0; r < 9; ++r) cap[r] = 0.0;
+  for (int c = lane; c < m.nch; c += 32) {
+    double U[kTail][kBorder], Wv[kTail][kBorder];
+    for (int a = 0; a < kTail; ++a)
+      for (int b = 0; b < kBorder; ++b) { U[a][b] = 0.0; Wv[a][b] = 0.0; }
+    double lb = 0.0;  // Theta_1 <- v_b multiplier (chain 0)
+    if (c <= 2 || c < 3 + m.nq) {
+      // multipole chain
+      int L, base, stride;
+      double mu = 1.0, dtop;
+      bool photon = c <= 1;
+      if (c == 0) { L = m.lg; base = 0; stride = 1; }
+      else if (c == 1) { L = m.lg; base = m.iTp; stride = 1; }
+      else if (c == 2) { L = m.lnu; base = m.iN; stride = 1; }
+      else { L = m.lmnu; base = m.iM + (c - 3); stride = m.nq; mu = S.qe[c - 3]; }
+      double mkH = mu * s.kH;
+      dtop = -(L + 1.0) * s.iHe + (photon ? s.tp : 0.0);
+      // baryon pair first (chain 0): eliminate delta_b, then v_b
+      double piv_vb = 1.0, Mvb_T1 = 0.0;
+      if (c == 0) {
+        int idb = m.iPhi + 3, ivb = m.iPhi + 4;
+        double Mdb_vb = -s.kH;                         // M[db][vb]
+        double Mvb_db = s.kH * s.cs2;                  // M[vb][db]
+        double dvb = ig + 1.0 - s.tp * s.R;            // M[vb][vb]
+        Mvb_T1 = -3.0 * s.tp * s.R;                    // M[vb][Theta1]
+        double ipdb = hg;                              // 1 / ig
+        double l_vb = Mvb_db * ipdb;
+        piv_vb = dvb - l_vb * Mdb_vb;
+        double ipvb = 1.0 / piv_vb;
+        S.fl[ivb] = l_vb; S.fi[ivb] = ipvb; S.fc[ivb] = Mvb_T1 * ipvb;
+        S.fi[idb] = ipdb; S.fc[idb] = Mdb_vb * ipdb;
+        double MT1_vb = -s.tp / 3.0;                   // M[Theta1][vb]
+        lb = MT1_vb * ipvb;
+        S.fl[idb] = lb;
+        ok = ok && isfinite(ipvb) && piv_vb != 0.0;
+      }
+      // top element
+      double piv = ig - dtop, ipiv = 1.0 / piv;
+      double cprev = -mkH;  // M[L][L-1]
+      int iL = base + L * stride;
+      S.fl[iL] = 0.0; S.fi[iL] = ipiv; S.fc[iL] = cprev * ipiv;
+      ok = ok && isfinite(ipiv);
+      for (int l = L - 1; l >= 0; --l) {
+        int i = base + l * stride;
+        double a = mkH * cl2[l];             // M[l][l+1]
+        double lm = a * ipiv;
+        double dl = photon ? ((c == 0 && l == 0) ? 0.0 : s.tp) : 0.0;
+        double pv = ig - dl - lm * cprev;
+        if (c == 0 && l == 1) pv -= lb * Mvb_T1;
+        ipiv = 1.0 / pv;
+        double cl = l >= 1 ? -mkH * cl1[l] : 0.0;  // M[l][l-1]
+        S.fl[i] = lm; S.fi[i] = ipiv; S.fc[i] = cl * ipiv;
+        cprev = cl;
+        ok = ok && isfinite(ipiv) && pv != 0.0;
+      }
+      // border tails: U (coefficients of Phi', Psi, Pi) and W (gradients)
+      if (c == 0) {
+        U[0][0] = -1.0; U[1][1] = s.kH / 3.0; U[2][2] = -s.tp / 10.0; U[3][1] = -s.kH; U[4][0] = -3.0;
+        double ia = 1.0 / s.a;
+        Wv[0][0] = s.dphi * 4.0 * C.Omega_r * ia * ia;
+        Wv[2][1] = -s.cpsi * C.Omega_r; Wv[2][0] = Wv[2][1]; Wv[2][2] = 1.0;
+        Wv[4][0] = s.dphi * C.Omega_b * ia;
+      } else if (c == 1) {
+        U[0][2] = -s.tp / 2.0; U[2][2] = -s.tp / 10.0;
+        Wv[0][2] = 1.0; Wv[2][2] = 1.0;
+      } else if (c == 2) {
+        U[0][0] = -1.0; U[1][1] = s.kH / 3.0;
+        double ia = 1.0 / s.a;
+        Wv[0][0] = s.dphi * 4.0 * Omega_nu * ia * ia;
+        Wv[2][1] = -s.cpsi * Omega_nu; Wv[2][0] = Wv[2][1];
+      } else {
+        int q = c - 3;
+        U[0][0] = S.df0[q]; U[1][1] = -s.kH / 3.0 * S.eq[q] * S.df0[q];
+        double qq = S.q[q], ia = 1.0 / s.a;
+        Wv[0][0] = s.dphi * S.Aq[q] * qq * S.eq[q] * ia * ia / C.rho_crit;
+        Wv[2][1] = -s.cpsi * S.Aq[q] * qq * S.qe[q] * 0.25 / C.rho_crit; Wv[2][0] = Wv[2][1];
+      }
+    } else if (c == 3 + m.nq) {
+      // CDM pair: eliminate v then delta
+      int idl = m.iPhi + 1, iv = m.iPhi + 2;
+      double ipv = 1.0 / (ig + 1.0);
+      double l_d = -s.kH * ipv;  // M[delta][v] / piv_v
+      S.fl[iv] = 0.0; S.fi[iv] = ipv; S.fc[iv] = 0.0;
+      S.fl[idl] = l_d; S.fi[idl] = hg; S.fc[idl] = 0.0;
+      U[0][0] = -3.0; U[1][1] = -s.kH;
+      Wv[0][0] = s.dphi * C.Omega_c / s.a;
+    } else {
+      S.fl[m.iPhi] = 0.0; S.fi[m.iPhi] = hg; S.fc[m.iPhi] = 0.0;
+      U[0][0] = 1.0;
+      Wv[0][1] = -1.0; Wv[0][0] = -1.0 - s.k2H2;
+    }
+    // forward sweep of the U columns over the tail (U vanishes above l = 2)
+    double Uf[kTail][kBorder];
+    for (int b = 0; b < kBorder; ++b) {
+      if (c < 3 + m.nq) {
+        int i0 = tail_index(m, c, 0), i1 = tail_index(m, c, 1);
+        double u2 = U[2][b];
+        double u1 = U[1][b] - S.fl[i1] * u2;
+        if (c == 0) {
+          double udb = U[4][b];
+          double uvb = U[3][b] - S.fl[m.iPhi + 4] * udb;
+          u1 -= lb * uvb;
+          Uf[3][b] = uvb; Uf[4][b] = udb;
+        } else { Uf[3][b] = 0.0; Uf[4][b] = 0.0; }
+        double u0 = U[0][b] - S.fl[i0] * u1;
+        Uf[0][b] = u0; Uf[1][b] = u1; Uf[2][b] = u2;
+      } else if (c == 3 + m.nq) {
+        double uv = U[1][b];
+        double ud = U[0][b] - S.fl[m.iPhi + 1] * uv;
+        Uf[0][b] = ud; Uf[1][b] = uv; Uf[2][b] = Uf[3][b] = Uf[4][b] = 0.0;
+      } else {
+        Uf[0][b] = U[0][b]; Uf[1][b] = Uf[2][b] = Uf[3][b] = Uf[4][b] = 0.0;
+      }
+    }
+    // partial back substitution of each forward-swept column -> M^{-1} U at
+    // the tail; accumulate W^T M^{-1} U
+    for (int b = 0; b < kBorder; ++b) {
+      double xs[kTail];
+      if (c < 3 + m.nq) {
+        int i0 = tail_index(m, c, 0), i1 = tail_index(m, c, 1), i2 = tail_index(m, c, 2);
+        xs[0] = Uf[0][b] * S.fi[i0];
+        xs[1] = Uf[1][b] * S.fi[i1] - S.fc[i1] * xs[0];
+        xs[2] = Uf[2][b] * S.fi[i2] - S.fc[i2] * xs[1];
+        if (c == 0) {
+          int ivb = m.iPhi + 4, idb = m.iPhi + 3;
+          xs[3] = Uf[3][b] * S.fi[ivb] - S.fc[ivb] * xs[1];
+          xs[4] = Uf[4][b] * S.fi[idb] - S.fc[idb] * xs[3];
+        } else { xs[3] = xs[4] = 0.0; }
+      } else if (c == 3 + m.nq) {
+        xs[0] = Uf[0][b] * S.fi[m.iPhi + 1];
+        xs[1] = Uf[1][b] * S.fi[m.iPhi + 2];
+        xs[2] = xs[3] = xs[4] = 0.0;
+      } else {
+        xs[0] = Uf[0][b] * S.fi[m.iPhi];
+        xs[1] = xs[2] = xs[3] = xs[4] = 0.0;
+      }
+      for (int r = 0; r < kBorder; ++r) {
+        double acc = 0.0;
+        for (int a = 0; a < kTail; ++a) acc += Wv[a][r] * xs[a];
+        cap[r * 3 + b] += acc;
+      }
+    }
+    double* uf = S.Uf + c * kTail * kBorder;
+    double* wt = S.Wt + c * kTail * kBorder;
+    for (int a = 0; a < kTail; ++a)
+      for (int b = 0; b < kBorder; ++b) { uf[a * kBorder + b] = Uf[a][b]; wt[a * kBorder + b] = Wv[a][b]; }
+  }
+  for (int r = 0; r < 9; ++r) cap[r] = warp_sum(cap[r]);
+  ok = __all_sync(0xffffffffu, ok);
+  // C = I - W^T M^{-1} U ; store its inverse in misc[0..8]
+  double Cm[9];
+  for (int r = 0; r < 9; ++r) Cm[r] = ((r % 4) == 0 ? 1.0 : 0.0) - cap[r];
+  double det = Cm[0] * (Cm[4] * Cm[8] - Cm[5] * Cm[7]) - Cm[1] * (Cm[3] * Cm[8] - Cm[5] * Cm[6]) +
+               Cm[2] * (Cm[3] * Cm[7] - Cm[4] * Cm[6]);
+  double id = 1.0 / det;
+  if (lane == 0) {
+    S.misc[0] = (Cm[4] * Cm[8] - Cm[5] * Cm[7]) * id;
+    S.misc[1] = (Cm[2] * Cm[7] - Cm[1] * Cm[8]) * id;
+    S.misc[2] = (Cm[1] * Cm[5] - Cm[2] * Cm[4]) * id;
+    S.misc[3] = (Cm[5] * Cm[6] - Cm[3] * Cm[8]) * id;
+    S.misc[4] = (Cm[0] * Cm[8] - Cm[2] * Cm[6]) * id;
+    S.misc[5] = (Cm[2] * Cm[3] - Cm[0] * Cm[5]) * id;
+    S.misc[6] = (Cm[3] * Cm[7] - Cm[4] * Cm[6]) * id;
+    S.misc[7] = (Cm[1] * Cm[6] - Cm[0] * Cm[7]) * id;
+    S.misc[8] = (Cm[0] * Cm[4] - Cm[1] * Cm[3]) * id;
+  }
+  __syncwarp();
+  return ok && isfinite(id) && det != 0.0;
+}
+
+// In-place solve b <- (M - U W^T)^{-1} b.
+__device__ void wsolve(const Mode& m, const Shared& S, double* b, int lane) {
+  double t[kBorder] = {0.0, 0.0, 0.0};
+  double xt[kTail];
+  int c = lane;
+  bool active = c < m.nch;  // nch <= 32 is enforced on the host
+  if (active) {
+    if (c < 3 + m.nq) {
+      int L, base, stride;
+      if (c == 0) { L = m.lg; base = 0; stride = 1; }
+      else if (c == 1) { L = m.lg; base = m.iTp; stride = 1; }
+      else if (c == 2) { L = m.lnu; base = m.iN; stride = 1; }
+      else { L = m.lmnu; base = m.iM + (c - 3); stride = m.nq; }
+      double bvb = 0.0, bdb = 0.0;
+      if (c == 0) {
+        bdb = b[m.iPhi + 3];
+        bvb = b[m.iPhi + 4] - S.fl[m.iPhi + 4] * bdb;
+      }
+      double prev = b[base + L * stride];
+      for (int l = L - 1; l >= 0; --l) {
+        int i = base + l * stride;
+        double v = b[i] - S.fl[i] * prev;
+        if (c == 0 && l == 1) v -= S.fl[m.iPhi + 3] * bvb;  // lb * b'_vb
+        b[i] = v;
+        prev = v;
+      }
+      if (c == 0) { b[m.iPhi + 4] = bvb; b[m.iPhi + 3] = bdb; }
+    } else if (c == 3 + m.nq) {
+      b[m.iPhi + 1] -= S.fl[m.iPhi + 1] * b[m.iPhi + 2];
+    }
+    // partial back substitution on the tail
+    int ns = tail_slots(m, c);
+    if (c < 3 + m.nq) {
+      int i0 = tail_index(m, c, 0), i1 = tail_index(m, c, 1), i2 = tail_index(m, c, 2);
+      xt[0] = b[i0] * S.fi[i0];
+      xt[1] = b[i1] * S.fi[i1] - S.fc[i1] * xt[0];
+      xt[2] = b[i2] * S.fi[i2] - S.fc[i2] * xt[1];
+      if (c == 0) {
+        int ivb = m.iPhi + 4, idb = m.iPhi + 3;
+        xt[3] = b[ivb] * S.fi[ivb] - S.fc[ivb] * xt[1];
+        xt[4] = b[idb] * S.fi[idb] - S.fc[idb] * xt[3];
+      }
+    } else if (c == 3 + m.nq) {
+      xt[0] = b[m.iPhi + 1] * S.fi[m.iPhi + 1];
+      xt[1] = b[m.iPhi + 2] * S.fi[m.iPhi + 2];
+    } else {
+      xt[0] = b[m.iPhi] * S.fi[m.iPhi];
+    }
+    const double* wt = S.Wt + c * kTail * kBorder;
+    for (int a = 0; a < ns; ++a)
+      for (int r = 0; r < kBorder; ++r) t[r] += wt[a * kBorder + r] * xt[a];
+  }
+  for (int r = 0; r < kBorder; ++r) t[r] = warp_sum(t[r]);
+  double sv[kBorder];
+  for (int r = 0; r < kBorder; ++r) sv[r] = S.misc[r * 3 + 0] * t[0] + S.misc[r * 3 + 1] * t[1] + S.misc[r * 3 + 2] * t[2];
+  if (active) {
+    // correct the forward-swept tail by the swept border columns, then
+    // complete the back substitution
+    const double* uf = S.Uf + c * kTail * kBorder;
+    int ns = tail_slots(m, c);
+    for (int a = 0; a < ns; ++a) {
+      int i = tail_index(m, c, a);
+      b[i] += uf[a * kBorder + 0] * sv[0] + uf[a * kBorder + 1] * sv[1] + uf[a * kBorder + 2] * sv[2];
+    }
+    if (c < 3 + m.nq) {
+      int L, base, stride;
+      if (c == 0) { L = m.lg; base = 0; stride = 1; }
+      else if (c == 1) { L = m.lg; base = m.iTp; stride = 1; }
+      else if (c == 2) { L = m.lnu; base = m.iN; stride = 1; }
+      else { L = m.lmnu; base = m.iM + (c - 3); stride = m.nq; }
+      double xp = b[base] * S.fi[base];
+      b[base] = xp;
+      double x1 = 0.0;
+      for (int l = 1; l <= L; ++l) {
+        int i = base + l * stride;
+        double v = b[i] * S.fi[i] - S.fc[i] * xp;
+        b[i] = v;
+        if (l == 1) x1 = v;
+        xp = v;
+      }
+      if (c == 0) {
+        int ivb = m.iPhi + 4, idb = m.iPhi + 3;
+        double xvb = b[ivb] * S.fi[ivb] - S.fc[ivb] * x1;
+        b[ivb] = xvb;
+        b[idb] = b[idb] * S.fi[idb] - S.fc[idb] * xvb;
+      }
+    } else if (c == 3 + m.nq) {
+      b[m.iPhi + 1] = b[m.iPhi + 1] * S.fi[m.iPhi + 1];
+      b[m.iPhi + 2] = b[m.iPhi + 2] * S.fi[m.iPhi + 2];
+    } else {
+      b[m.iPhi] = b[m.iPhi] * S.fi[m.iPhi];
+    }
+  }
+  __syncwarp();
+}
+
+// ------------------------------------------------------------- outputs ----
+// source_function and source_function_P (perturbations.jl:343-404) at a
+// grid node, from u and du = hierarchy!(u).
+__device__ void emit_sources(const Mode& m, const Shared& S, double x, const double* u, const double* du, int lane,
+                             double* outT, double* outE) {
+  const CosmoDev& C = *m.C;
+  double a = exp(x);
+  double sig = 0.0, sigp = 0.0;
+  for (int q = lane; q < m.nq; q += 32) {
+    double am = a * C.Sigma_m_nu, qq = S.q[q];
+    double eps = sqrt(qq * qq + am * am);
+    double w = S.Aq[q] * qq * qq / eps;
+    sig += w * u[m.iM + 2 * m.nq + q];
+    sigp += w * du[m.iM + 2 * m.nq + q];
+  }
+  sig = warp_sum(sig);
+  sigp = warp_sum(sigp);
+  if (lane != 0) return;
+  double H0sq = C.H0 * C.H0, k = m.k;
+  double Hc = spl_cold(C, C_H, x), Hcp = spl_cold(C, C_HP, x), Hcpp = spl_cold(C, C_HPP, x);
+  double tau = spl_cold(C, C_TAU, x), tp = spl_cold(C, C_TAUP, x), tpp = spl_cold(C, C_TAUPP, x);
+  double g = spl_cold(C, C_G, x), gp = spl_cold(C, C_GP, x), gpp = spl_cold(C, C_GPP, x);
+  double eta = spl_cold(C, C_ETA, x);
+  const double Omega_nu = C.Omega_nu;
+  const double* Th = u;
+  const double* Tp = u + m.iTp;
+  const double* dTh = du;
+  const double* dTp = du + m.iTp;
+  double Phi = u[m.iPhi], Phip = du[m.iPhi], vb = u[m.iPhi + 4], vbp = du[m.iPhi + 4];
+  double c = 12.0 * H0sq / (k * k) / (a * a);
+  double Psi = -Phi - c * (C.Omega_r * Th[2] + Omega_nu * u[m.iN + 2] + sig / C.rho_crit / 4.0);
+  double Psip = -Phip - c * (C.Omega_r * (dTh[2] - 2.0 * Th[2]) + Omega_nu * (du[m.iN + 2] - 2.0 * u[m.iN + 2]) +
+                             (sigp - 2.0 * sig) / C.rho_crit / 4.0);
+  double Pi = Th[2] + Tp[2] + Tp[0];
+  double Pip = dTh[2] + dTp[2] + dTp[0];
+  double term1 = g * (Th[0] + Psi + Pi / 4.0) + exp(-tau) * (Psip - Phip);
+  double term2 = (-1.0 / k) * (Hcp * g * vb + Hc * gp * vb + Hc * g * vbp);
+  double Pipp = 2.0 * k / (5.0 * Hc) * (-Hcp / Hc * Th[1] + dTh[1]) + (3.0 / 10.0) * (tpp * Pi + tp * Pip) -
+                3.0 * k / (5.0 * Hc) * (-Hcp / Hc * (Th[3] + Tp[1] + Tp[3]) + (dTh[3] + dTp[1] + dTp[3]));
+  double term3 = (3.0 / (4.0 * k * k)) * ((Hcp * Hcp + Hc * Hcpp) * g * Pi + 3.0 * Hc * Hcp * (gp * Pi + g * Pip) +
+                                          Hc * Hc * (gpp * Pi + 2.0 * gp * Pip + g * Pipp));
+  *outT = term1 + term2 + term3;
+  double y = k * (C.eta_last - eta);
+  *outE = (3.0 / (4.0 * y * y)) * g * Pi;
+}
+
+// plin (spectra.jl:163-198) at the final node x.
+__device__ void emit_plin(const Mode& m, const Shared& S, double x, const double* u, int lane, double* out) {
+  const CosmoDev& C = *m.C;
+  double a = exp(x);
+  double rho = 0.0, th = 0.0;
+  for (int q = lane; q < m.nq; q += 32) {
+    double am = a * C.Sigma_m_nu, qq = S.q[q];
+    double eps = sqrt(qq * qq + am * am);
+    rho += S.Aq[q] * eps * u[m.iM + q];
+    th += S.Bq[q] * u[m.iM + m.nq + q];
+  }
+  rho = warp_sum(rho);
+  th = warp_sum(th);
+  if (lane != 0) return;
+  double k = m.k;
+  double r0 = spl_cold(C, C_RHO0M, x);
+  double Mrho = rho / r0, Mth = k * th / r0;
+  double dcN = u[m.iPhi + 1], vcN = u[m.iPhi + 2], dbN = u[m.iPhi + 3], vbN = u[m.iPhi + 4];
+  double vmnu = -Mth / k;
+  double Tg = pow(15.0 / (M_PI * M_PI) * C.rho_crit * C.Omega_r, 0.25);
+  double nufac = (90.0 * 1.2020569 / (11.0 * pow(M_PI, 4))) * (C.Omega_r * C.h * C.h / Tg) * pow(C.N_nu / 3.0, 0.75);
+  double Omega_nu = C.Sigma_m_nu * nufac / (C.h * C.h);
+  double Om = C.Omega_c + C.Omega_b + Omega_nu;
+  double Hc = spl_cold(C, C_H, x);
+  double dc = dcN - 3.0 * Hc * vcN / k, db = dbN - 3.0 * Hc * vbN / k, dn = Mrho - 3.0 * Hc * vmnu / k;
+  double dm = (C.Omega_c * dc + C.Omega_b * db + Omega_nu * dn) / Om;
+  double Pp = C.A * pow(k / 0.05, C.n_s - 1.0);
+  *out = (2.0 * M_PI * M_PI / (k * k * k)) * dm * dm * Pp;
+}
+
+// initial_conditions (perturbations.jl:274-338), lane 0 serial (once per mode).
+__device__ void initial_state(const Mode& m, const Shared& S, double xi, double* u, int lane) {
+  for (int i = lane; i < m.N; i += 32) u[i] = 0.0;
+  __syncwarp();
+  if (lane == 0) {
+    const CosmoDev& C = *m.C;
+    double k = m.k;
+    double Hc = spl_cold(C, C_H, xi), eta = spl_cold(C, C_ETA, xi), tp = spl_cold(C, C_TAUP, xi);
+    double ai = exp(xi);
+    double fnu = 1.0 / (1.0 + 1.0 / (7.0 * C.N_nu / 8.0 * pow(4.0 / 11.0, 4.0 / 3.0)));
+    double Phi = (4.0 * fnu + 10.0) / (4.0 * fnu + 15.0);
+    double Cc = -((15.0 + 4.0 * fnu) / (20.0 + 8.0 * fnu)) * Phi;
+    double* Th = u;
+    double* Tp = u + m.iTp;
+    double* Nn = u + m.iN;
+    Th[0] = -40.0 * Cc / (15.0 + 4.0 * fnu) / 4.0;
+    Th[1] = 10.0 * Cc / (15.0 + 4.0 * fnu) * (k * k * eta) / (3.0 * k);
+    Th[2] = -8.0 * k / (15.0 * Hc * tp) * Th[1];
+    Tp[0] = (5.0 / 4.0) * Th[2];
+    Tp[1] = -k / (4.0 * Hc * tp) * Th[2];
+    Tp[2] = (1.0 / 4.0) * Th[2];
+    for (int l = 3; l <= m.lg; ++l) {
+      Th[l] = -l / (2.0 * l + 1.0) * k / (Hc * tp) * Th[l - 1];
+      Tp[l] = -l / (2.0 * l + 1.0) * k / (Hc * tp) * Tp[l - 1];
+    }
+    double del = 3.0 * Th[0];
+    double v = -3.0 * k * Th[1];
+    Nn[0] = Th[0];
+    Nn[1] = Th[1];
+    Nn[2] = -(k * k * eta * eta) / 15.0 * 1.0 / (1.0 + 2.0 / 5.0 * fnu) * Phi / 2.0;
+    for (int l = 3; l <= m.lnu; ++l) Nn[l] = k / ((2.0 * l + 1.0) * Hc) * Nn[l - 1];
+    for (int q = 0; q < m.nq; ++q) {
+      double qq = S.q[q], am = ai * C.Sigma_m_nu;
+      double eps = sqrt(qq * qq + am * am), df0 = S.df0[q];
+      u[m.iM + q] = -Nn[0] * df0;
+      u[m.iM + m.nq + q] = -eps / qq * Nn[1] * df0;
+      u[m.iM + 2 * m.nq + q] = -Nn[2] * df0;
+      for (int l = 3; l <= m.lmnu; ++l)
+        u[m.iM + l * m.nq + q] = qq / eps * k / ((2.0 * l + 1.0) * Hc) * u[m.iM + (l - 1) * m.nq + q];
+    }
+    u[m.iPhi] = Phi;
+    u[m.iPhi + 1] = del;
+    u[m.iPhi + 2] = v;
+    u[m.iPhi + 3] = del;
+    u[m.iPhi + 4] = v;
+  }
+  __syncwarp();
+}
+
+// --------------------------------------------------------------- driver ----
+__device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const SolverCfg& cfg, double* base, int lane) {
+  Mode m;
+  m.C = cosmos + md.cosmo;
+  m.k = md.k;
+  m.lg = md.lg; m.lnu = md.lnu; m.lmnu = md.lmnu; m.nq = md.nq;
+  m.N = 2 * (m.lg + 1) + (m.lnu + 1) + (m.lmnu + 1) * m.nq + 5;
+  m.iTp = m.lg + 1;
+  m.iN = 2 * (m.lg + 1);
+  m.iM = m.iN + m.lnu + 1;
+  m.iPhi = m.iM + (m.lmnu + 1) * m.nq;
+  m.nch = m.nq + 5;
+  const CosmoDev& C = *m.C;
+  const int N = m.N;
+  int Lmax = max(m.lg, max(m.lnu, m.lmnu));
+  Shared S;
+  double* p = base;
+  S.y = p; p += N;
+  S.yt = p; p += N;
+  S.fx = p; p += N;
+  S.K = p; p += 6 * N;
+  S.fl = p; p += N;
+  S.fi = p; p += N;
+  S.fc = p; p += N;
+  S.q = p; p += m.nq;
+  S.df0 = p; p += m.nq;
+  S.Aq = p; p += m.nq;
+  S.Bq = p; p += m.nq;
+  S.qe = p; p += m.nq;
+  S.eq = p; p += m.nq;
+  S.qe_d = p; p += m.nq;
+  S.eq_d = p; p += m.nq;
+  S.Uf = p; p += m.nch * kTail * kBorder;
+  S.Wt = p; p += m.nch * kTail * kBorder;
+  S.cl1 = p; p += Lmax + 1;
+  S.cl2 = p; p += Lmax + 1;
+  S.misc = p;
+  // per-mode constants (perturbations.jl:164-166; background.jl:21-30)
+  for (int l = lane; l <= Lmax; l += 32) {
+    S.cl1[l] = double(l) / (2.0 * l + 1.0);
+    S.cl2[l] = (l + 1.0) / (2.0 * l + 1.0);
+  }
+  for (int q = lane; q < m.nq; q += 32) {
+    double xq = C.qx[q];
+    double lq = C.logqmin + (C.logqmax - C.logqmin) / 2.0 * (xq + 1.0);
+    double qq = pow(10.0, lq);
+    double dxdq = (1.0 + (-1.0 + 2.0 / (C.logqmax - C.logqmin) * ((1.0 + C.logqmin) - C.logqmin))) / (qq * log(10.0));
+    double f0 = 2.0 / pow(2.0 * M_PI, 3.0) / (exp(qq / C.Tnu) + 1.0);
+    S.q[q] = qq;
+    S.df0[q] = -qq / C.Tnu / (1.0 + exp(-qq / C.Tnu));
+    S.Aq[q] = 4.0 * M_PI * qq * qq * f0 / dxdq * C.qw[q];  // rho: Aq eps M0, sigma: Aq q^2/eps M2
+    S.Bq[q] = 4.0 * M_PI * qq * qq * qq * f0 / dxdq * C.qw[q];
+  }
+  __syncwarp();
+  double x = C.x0;
+  const double xend = md.xout[md.nout - 1];
+  initial_state(m, S, x, S.y, lane);
+  int status = ST_OK;
+  bool rsa_any = false;
+  long long nacc = 0, nrej = 0;
+  int jo = 0;
+  double h = cfg.h0;
+  const double rtol = cfg.reltol, atol = cfg.abstol;
+  while (jo < md.nout && md.xout[jo] < x) ++jo;  // nodes before the start are not produced
+  while (true) {
+    bool at_node = (jo < md.nout) && (md.xout[jo] == x);
+    if (x >= xend) {
+      // final node: outputs at x_end
+      if (at_node) {
+        if (md.flags & MODE_SOURCES) {
+          rhs_rows<double>(m, S, x, S.y, S.K, nullptr, lane);
+          __syncwarp();
+          emit_sources(m, S, x, S.y, S.K, lane, md.src_T + jo, md.src_E + jo);
+        }
+        if (md.flags & MODE_TRAJ)
+          for (int i = lane; i < N; i += 32) md.traj[(size_t)jo * N + i] = S.y[i];
+        ++jo;
+      }
+      if (md.flags & MODE_PLIN) emit_plin(m, S, x, S.y, lane, md.plin);
+      break;
+    }
+    double target = jo < md.nout ? md.xout[jo] : xend;
+    if (at_node) target = (jo + 1 < md.nout) ? md.xout[jo + 1] : xend;
+    bool landing = false;
+    double hs = h;
+    if (x + hs >= target - 1e-14 * fabs(target)) { hs = target - x; landing = true; }
+    if (!factorize(m, S, x, hs * rodas::kGamma, lane)) { status = ST_LU_FAIL; break; }
+    // stage 1: f and df/dx at (x, y)
+    bool r = rhs_rows<dd>(m, S, x, S.y, S.K, S.fx, lane);
+    rsa_any |= r;
+    __syncwarp();
+    if (at_node) {
+      if (md.flags & MODE_SOURCES) emit_sources(m, S, x, S.y, S.K, lane, md.src_T + jo, md.src_E + jo);
+      if (md.flags & MODE_TRAJ)
+        for (int i = lane; i < N; i += 32) md.traj[(size_t)jo * N + i] = S.y[i];
+      ++jo;
+      __syncwarp();
+    }
+    const double ih = 1.0 / hs;
+    double* K0 = S.K;
+    for (int i = lane; i < N; i += 32) K0[i] += hs * rodas::kD[0] * S.fx[i];
+    __syncwarp();
+    wsolve(m, S, K0, lane);
+    double xn = landing ? target : x + hs;
+    for (int st = 1; st < 6; ++st) {
+      double* Ks = S.K + st * N;
+      // stage state
+      if (st < 5) {
+        for (int i = lane; i < N; i += 32) {
+          double acc = S.y[i];
+          for (int j = 0; j < st; ++j) acc += rodas::kA[st - 1][j] * S.K[j * N + i];
+          S.yt[i] = acc;
+        }
+      } else {
+        for (int i = lane; i < N; i += 32) S.yt[i] += S.K[4 * N + i];
+      }
+      __syncwarp();
+      double xs = st >= 4 ? xn : x + rodas::kCx[st] * hs;
+      r = rhs_rows<double>(m, S, xs, S.yt, Ks, nullptr, lane);
+      rsa_any |= r;
+      __syncwarp();
+      double hd = hs * rodas::kD[st];
+      for (int i = lane; i < N; i += 32) {
+        double acc = Ks[i];
+        if (st < 4) acc += hd * S.fx[i];
+        double cs = 0.0;
+        for (int j = 0; j < st; ++j) cs += rodas::kC[st][j] * S.K[j * N + i];
+        Ks[i] = acc + ih * cs;
+      }
+      __syncwarp();
+      wsolve(m, S, Ks, lane);
+    }
+    // error estimate: the last stage increment
+    double en = 0.0;
+    bool fin = true;
+    const double* K5 = S.K + 5 * N;
+    for (int i = lane; i < N; i += 32) {
+      double yn = S.yt[i] + K5[i];
+      double sc = atol + rtol * fmax(fabs(S.y[i]), fabs(yn));
+      double e = K5[i] / sc;
+      en += e * e;
+      fin = fin && isfinite(yn);
+    }
+    en = sqrt(warp_sum(en) / N);
+    fin = __all_sync(0xffffffffu, fin);
+    if (!fin || !(en == en)) en = 1e10;
+    double fac = 0.9 * pow(fmax(en, 1e-12), -0.25);
+    fac = fmin(6.0, fmax(0.2, fac));
+    if (en <= 1.0) {
+      for (int i = lane; i < N; i += 32) S.y[i] = S.yt[i] + K5[i];
+      __syncwarp();
+      x = xn;
+      ++nacc;
+      double hp = hs * fac;
+      h = landing ? fmax(h, hp) : hp;
+    } else {
+      ++nrej;
+      if (at_node) --jo;  // re-emit after the retry (same x, same y)
+      h = hs * fmin(1.0, fac);
+      if (!(h >= 1e-14 * fmax(1.0, fabs(x)))) { status = fin ? ST_DT_UNDERFLOW : ST_NONFINITE; break; }
+    }
+    if (nacc + nrej > cfg.max_steps) { status = ST_MAXITERS; break; }
+  }
+  if (lane == 0) {
+    *md.status = status | (rsa_any ? ST_RSA_FIRED : 0);
+    if (md.counters) { md.counters[0] = nacc; md.counters[1] = nrej; }
+  }
+}
+
+__global__ void __launch_bounds__(256) rodas_kernel(const ModeDev* __restrict__ modes, int nmodes,
+                                                    const CosmoDev* __restrict__ cosmos, SolverCfg cfg,
+                                                    int* __restrict__ queue, int per_warp) {
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  double* base = smem + (size_t)w * per_warp;
+  while (true) {
+    int mi = 0;
+    if (lane == 0) mi = atomicAdd(queue, 1);
+    mi = __shfl_sync(0xffffffffu, mi, 0);
+    if (mi >= nmodes) break;
+    solve_one(modes[mi], cosmos, cfg, base, lane);
+    __syncwarp();
+  }
+}
+
+// Host launcher.  Returns a cudaError_t.
+int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
+                 int maxN, int maxnq, int maxL, int warps_per_block, cudaStream_t stream) {
+  int per_warp = per_warp_doubles(maxN, maxnq, maxL);
+  size_t smem = size_t(per_warp) * warps_per_block * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(rodas_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return e;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  int bps = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, rodas_kernel, 32 * warps_per_block, smem);
+  if (e != cudaSuccess) return e;
+  if (bps < 1) return cudaErrorInvalidConfiguration;
+  int want = (nmodes + warps_per_block - 1) / warps_per_block;
+  int grid = std::min(want, nsm * bps);
+  e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
+  if (e != cudaSuccess) return e;
+  rodas_kernel<<<grid, 32 * warps_per_block, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, per_warp);
+  return cudaGetLastError();
+}
+
+size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL) {
+  return size_t(per_warp_doubles(maxN, maxnq, maxL)) * sizeof(double);
+}
+
+}  // namespace bolt
