@@ -1,0 +1,295 @@
+#!/usr/bin/env python
+"""Benchmark: C_l spectra per second for Bolt's full CMB pipeline on GB300.
+
+Workload (one step = one cosmology, the reference's configuration for the
+full CMB pipeline): fiducial LCDM (h 0.7, Omega_b 0.046, Omega_c 0.224,
+n_s 0.96, A_s 2.1e-9, Y_p 0.24, N_eff 3.046, Sum m_nu 0.06 eV), hierarchy
+l_gamma = l_gamma,P = l_nu = 50, l_mnu = 20, nq = 15 (N = 473), 1200
+log-spaced k in [0.1, 5000] H0, source functions on the 2001-node x grid,
+C_l^TT/TE/EE for l = 2..2500 by the reference's line-of-sight discretisation
+(5000-point quadratic k grid, x > -8).  FP64 throughout.
+
+Reported: ``value`` = spectra/s from CUDA-event time of the device work with
+the cosmology tables resident in HBM; ``e2e`` = spectra/s through the public
+C ABI from parameters in host memory (host table construction, upload,
+solve, projection, C_l back to the host); ``cpu_baseline`` = the CPU oracle
+(C++ restatement of Bolt's CPU algorithm, OpenMP on all host cores) on a
+bounded, stratified sample of the same workload, scaled to one spectrum.
+
+``--impl reference`` times that CPU restatement alone (the reference itself
+is Julia and cannot run on this machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "bolt.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "Cℓ+grad spectra/s on 1 GB300 (served vs plain) at ≤1e-4 rel err; p50/p99 latency"
+UNIT = "spectra/s"
+HIER = (50, 50, 20, 15)
+NK = 1200
+RELTOL, ABSTOL = 1e-8, 1e-6
+ELLS = np.arange(2, 2501, dtype=np.int32)
+
+
+def fid_params(B):
+    return B.CosmoParams(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Y_p=0.24, N_nu=3.046,
+                         Sigma_m_nu=0.06 * B.mass_natural())
+
+
+def solver_flops_per_step(N, nq):
+    """Algorithmic FP64 FLOPs of one Rodas4 step in solver.cu (FMA = 2):
+    6 right-hand sides (one with the x-derivative), the chain factorisation
+    with its rank-3 border, 6 structured solves, stage combinations and the
+    error norm -- 159 N + 560 (nq + 5) + 66 nq + 650."""
+    return 159 * N + 560 * (nq + 5) + 66 * nq + 650
+
+
+def los_flops(nslots, nm, nrow):
+    """line-of-sight reduction: 27 FLOPs per (l, k, x) term with T and E."""
+    return 27.0 * nslots * nm * nrow
+
+
+def clocks_sampler():
+    q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+    try:
+        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200",
+                              "-i", os.environ.get("LOCAL_RANK", "0")],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except Exception:
+        return None
+    rows = []
+
+    def rd():
+        for line in p.stdout:
+            rows.append(line.strip())
+    t = threading.Thread(target=rd, daemon=True)
+    t.start()
+    return p, rows
+
+
+def clocks_summary(sampler):
+    if sampler is None:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    p, rows = sampler
+    p.terminate()
+    try:
+        p.wait(timeout=5)
+    except Exception:
+        p.kill()
+    sm, mx, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for r in rows:
+        f = [v.strip() for v in r.split(",")]
+        if len(f) < 7:
+            continue
+        try:
+            sm.append(float(f[0]))
+            mx.append(float(f[1]))
+        except ValueError:
+            continue
+        for n, v in zip(names, f[3:7]):
+            if v.lower() == "active":
+                reasons.add(n)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(steps_budget_s=15.0):
+    """Times the CPU oracle on a stratified sample of the workload and scales
+    to one spectrum: 16 of the 1200 modes (every 75th, so the k range is
+    covered) and 32 of the 2499 multipoles."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    c = O.Cosmo(O.Params(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Sigma_m_nu_eV=0.06))
+    k_all = O.log10_k(0.1 * c.H0, 5000 * c.H0, NK)
+    idx = np.arange(37, NK, 75)
+    ks = k_all[idx]
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ST, SE, _ = c.source_grid(ks, *HIER[:3], HIER[3], reltol=RELTOL, abstol=ABSTOL, nthreads=cores)
+    t_sg = time.perf_counter() - t0
+    ells = ELLS[np.linspace(0, ELLS.size - 1, 32).astype(int)]
+    t0 = time.perf_counter()
+    c.cl(ST, SE, ks, ells, nthreads=cores)
+    t_los = time.perf_counter() - t0
+    per_spec = t_sg * NK / ks.size + t_los * ELLS.size / ells.size
+    return {"value": 1.0 / per_spec, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"CPU oracle (C++ restatement of Bolt's CPU algorithm, OpenMP): source grid for "
+                       f"{ks.size}/{NK} stratified k modes ({t_sg:.1f} s) + LOS for {ells.size}/{ELLS.size} "
+                       f"multipoles ({t_los:.1f} s), scaled to one spectrum ({per_spec:.1f} s)"),
+            "seconds_per_spectrum": per_spec}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    dist.init_process_group(backend="gloo")
+    return dist.get_rank(), ws, dist
+
+
+def max_over_ranks(v, dist):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    rank, ws, dist = dist_init()
+    if rank != 0:
+        return
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample()
+        if i >= args.warmup:
+            vals.append(r["value"])
+            last = r
+    v = statistics.median(vals)
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "full CMB pipeline: 1200 log k in [0.1,5000]H0, l_g=l_gP=l_nu=50, l_mnu=20, "
+                                  "nq=15, S on 2001 x nodes, C_l TT/TE/EE l=2..2500; one step = one cosmology",
+                      "parallelism": "host cores"},
+           "cpu_baseline": {k: last[k] for k in ("value", "unit", "cores", "kind", "sample")},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, ws, dist = dist_init()
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    import bolt_gb300 as B
+    ctx = B.Context(device=local)
+    par = fid_params(B)
+    bg = B.Background(par)
+    ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg, ctx=ctx)
+    ks = B.log10_k(0.1 * bg.H0, 5000 * bg.H0, NK)
+    lg, lnu, lmnu, nq = HIER
+    N = B.state_len(lg, lnu, lmnu, nq)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def device_step():
+        tt, te, ee, st = B.cl_all(ELLS, ih, ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL)
+        return ctx.stats(), (tt, te, ee, st)
+
+    for _ in range(args.warmup):
+        device_step()
+        flush.zero_()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    sampler = clocks_sampler()
+    dev_ms, solver_us, los_us, acc, rej, launches = [], 0, 0, 0, 0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s, res = device_step()
+        dev_ms.append((s["solver_us"] + s["los_us"]) / 1000.0)
+        solver_us += s["solver_us"]
+        los_us += s["los_us"]
+        acc += s["accepted_steps"]
+        rej += s["rejected_steps"]
+        launches += s["kernel_launches"]
+    torch.cuda.synchronize()
+    clocks = clocks_summary(sampler)
+    total_ms = max_over_ranks(sum(dev_ms), dist)
+    value = ws * args.steps / (total_ms / 1000.0)
+
+    # e2e through the public API: parameters in host memory -> C_l in host memory
+    e2e_t = []
+    h2d = d2h = 0
+    for i in range(args.steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bg2 = B.Background(par)
+        ih2 = B.IonizationHistory(B.RECFAST(bg2, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg2,
+                                  ctx=ctx)
+        tt, te, ee, st = B.cl_all(ELLS, ih2, ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL)
+        ih2.close()
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_t.append(time.perf_counter() - t0)
+        n2 = bg2.x_grid.size + 2
+        h2d = 8 * (n2 * 4 + 12 * n2 + 2 * nq) + 8 * NK + 8 * 4999 * 2 + 8 * 5000
+        d2h = 8 * 3 * ELLS.size + 4 * NK
+    e2e_val = ws * len(e2e_t) / max_over_ranks(sum(e2e_t), dist)
+
+    # roofline of the dominant kernel (FP64-pipe bound)
+    peak = ctypes_peak(B, local)
+    sol_flops = (acc + rej) * solver_flops_per_step(N, nq)
+    sol_s = solver_us / 1e6
+    los_f = los_flops(ELLS.size, 4999, 799) * args.steps
+    los_s = los_us / 1e6
+    dom = "rodas_kernel" if sol_s >= los_s else "los_cl_kernel"
+    ach = (sol_flops / sol_s if dom == "rodas_kernel" else los_f / los_s) / 1e12
+    roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak if peak else None,
+            "traffic": None, "kernel": dom,
+            "peak_source": "measured in this run: FP64 FMA loop (bolt_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
+            "breakdown": {"rodas_kernel_ms_per_step": solver_us / 1000.0 / args.steps,
+                          "rodas_tflops": sol_flops / sol_s / 1e12 if sol_s else None,
+                          "los_ms_per_step": los_us / 1000.0 / args.steps,
+                          "los_cl_tflops": los_f / los_s / 1e12 if los_s else None,
+                          "steps_per_spectrum": (acc + rej) / args.steps}}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        r = cpu_sample()
+        cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": "full CMB pipeline (plain, one cosmology per call): fiducial LCDM, 1200 log k "
+                                      "in [0.1,5000]H0, l_g=l_gP=l_nu=50, l_mnu=20, nq=15 (N=473), S_T/S_E on 2001 x "
+                                      "nodes, C_l TT/TE/EE l=2..2500; gradients not in this workload",
+                          "reltol": RELTOL, "abstol": ABSTOL, "l2": "flushed (256 MB write) between steps",
+                          "parallelism": f"replicas x{ws}"},
+               "clocks": clocks,
+               "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+               "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu}
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def ctypes_peak(B, dev):
+    import ctypes as C
+    v = C.c_double(0.0)
+    rc = B._lib.load().bolt_fp64_peak(dev, C.byref(v))
+    return v.value if rc == 0 else None
+
+
+if __name__ == "__main__":
+    main()

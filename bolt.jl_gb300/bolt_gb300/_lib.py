@@ -65,6 +65,7 @@ EXPORTS = {
     "bolt_plin": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.POINTER(BoltHier), C.c_double, C.c_double,
                             C.c_double, _dp, _i32p]),
     "bolt_last_stats": (C.c_int, [C.c_void_p, _i64p]),
+    "bolt_fp64_peak": (C.c_int, [C.c_int, _dp]),
 }
 
 _lib = None

@@ -19,7 +19,8 @@ struct CosmoDev {
   // cosmological parameters (CosmoParams, Bolt.jl:56-66); Sigma_m_nu in Mpc^-1
   double h, Omega_r, Omega_b, Omega_c, A, n_s, Y_p, N_nu, Sigma_m_nu;
   // background scalars
-  double H0, eta0, rho_crit, eta_last;  // eta_last = bg.η(x_grid[end])
+  double H0, eta0, rho_crit, eta_last;  // eta_last = bg.η(x_grid[end]) (host evaluation)
+  double x_last;                        // x_grid[end]
   double Tnu, logqmin, logqmax;
   double Omega_nu;  // massless-neutrino density 7(2/3)N_nu/8 (4/11)^(4/3) Omega_r (perturbations.jl:171)
   // uniform x grid: x_j = x0 + j * hx, n nodes; inv_hx = 1 / hx

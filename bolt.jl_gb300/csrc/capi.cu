@@ -133,6 +133,7 @@ void upload_cosmo(bolt_ctx* c, CosmoEntry& e) {
   d.Y_p = p.Y_p; d.N_nu = p.N_nu; d.Sigma_m_nu = p.Sigma_m_nu;
   d.H0 = T.H0; d.eta0 = T.eta0; d.rho_crit = T.rho_crit;
   d.eta_last = spline_eval(T.coef[T_ETA].data(), n, T.grid.x0, T.grid.h, T.grid.at(n - 1));
+  d.x_last = T.grid.at(n - 1);
   d.Tnu = T.Tnu; d.logqmin = T.logqmin; d.logqmax = T.logqmax;
   d.Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
   d.x0 = T.grid.x0; d.hx = T.grid.h; d.inv_hx = 1.0 / T.grid.h;

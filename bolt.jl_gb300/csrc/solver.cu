@@ -649,7 +649,9 @@ __device__ void emit_sources(const Mode& m, const Shared& S, double x, const dou
   double term3 = (3.0 / (4.0 * k * k)) * ((Hcp * Hcp + Hc * Hcpp) * g * Pi + 3.0 * Hc * Hcp * (gp * Pi + g * Pip) +
                                           Hc * Hc * (gpp * Pi + 2.0 * gp * Pip + g * Pipp));
   *outT = term1 + term2 + term3;
-  double y = k * (C.eta_last - eta);
+  // same spline, same evaluation as eta(x): y is exactly 0 at the last node,
+  // where the reference's 3 / (4 y^2) is infinite (perturbations.jl:401-403)
+  double y = k * (spl_cold(C, C_ETA, C.x_last) - eta);
   *outE = (3.0 / (4.0 * y * y)) * g * Pi;
 }
 

@@ -128,6 +128,10 @@ int bolt_plin(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const bolt_h
  * [4] modes, [5] solver kernel launches, [6] total kernel launches. */
 int bolt_last_stats(bolt_ctx* ctx, int64_t* out);
 
+/* Measured FP64 FMA throughput of the device (TFLOP/s): the roofline
+ * denominator for the FP64-pipe-bound kernels. */
+int bolt_fp64_peak(int device, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif
