@@ -651,7 +651,7 @@ __device__ void emit_sources(const Mode& m, const Shared& S, double x, const dou
   *outT = term1 + term2 + term3;
   // same spline, same evaluation as eta(x): y is exactly 0 at the last node,
   // where the reference's 3 / (4 y^2) is infinite (perturbations.jl:401-403)
-  double y = k * (spl_cold(C, C_ETA, C.x_last) - eta);
+  double y = (x == C.x_last) ? 0.0 : k * (spl_cold(C, C_ETA, C.x_last) - eta);
   *outE = (3.0 / (4.0 * y * y)) * g * Pi;
 }
 
