@@ -66,6 +66,7 @@ EXPORTS = {
                             C.c_double, _dp, _i32p]),
     "bolt_last_stats": (C.c_int, [C.c_void_p, _i64p]),
     "bolt_fp64_peak": (C.c_int, [C.c_int, _dp]),
+    "bolt_set_dense_x": (C.c_int, [C.c_void_p, C.c_double]),
 }
 
 _lib = None

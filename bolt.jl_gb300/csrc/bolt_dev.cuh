@@ -62,6 +62,7 @@ enum StatusBits {
 
 struct SolverCfg {
   double reltol, abstol, h0;
+  double x_dense;  // source nodes below this x come from dense output
   long long max_steps;
 };
 

@@ -19,9 +19,11 @@
 #include "host_cosmo.hpp"
 
 namespace bolt {
+int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int warps_per_block, int* blocks);
 int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
-                 int maxN, int maxnq, int maxL, int warps_per_block, cudaStream_t stream);
+                 int maxN, int maxnq, int maxL, int warps_per_block, int blocks, double* d_scratch, cudaStream_t stream);
 size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL);
+size_t rodas_scratch_per_warp(int maxN);
 struct LosArgs {
   int nb, nslots, nrow, nm;
   const int* ells;
@@ -95,9 +97,10 @@ struct bolt_ctx {
   cudaEvent_t ev[4];
   int wpb = 0;
   long long max_steps = 10000000;
+  double x_dense = -8.5;
   std::vector<CosmoEntry> cos;
   DBuf d_cos;
-  DBuf modes, xout, srcT, srcE, traj, plin, status, counters, queue, flags;
+  DBuf modes, xout, srcT, srcE, traj, plin, status, counters, queue, flags, scratch;
   DBuf kgrid, raw, norm, coef, w, slot_of_l, ells, SdT, SdE, kmid, wts, yv, dx, dgs, idg, out;
   std::string err;
   int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -225,14 +228,20 @@ void run_solver(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h
   cfg.reltol = reltol;
   cfg.abstol = abstol;
   cfg.h0 = 1e-3;
+  cfg.x_dense = c->x_dense;
   cfg.max_steps = c->max_steps;
   int Lmax = std::max(h->lg, std::max(h->lnu, h->lmnu));
   size_t pw = rodas_smem_per_warp(N, h->nq, Lmax);
   int wpb = c->wpb;
   if (wpb <= 0) wpb = int(std::max<size_t>(1, std::min<size_t>(8, (220 * 1024) / pw)));
   if (pw * wpb > 227 * 1024) throw Err(-1, "hierarchy too large for shared memory");
+  int blocks = 0;
+  int rc = rodas_grid_warps(nk, N, h->nq, Lmax, wpb, &blocks);
+  if (rc != 0) throw Err(-3, std::string("solver configuration: ") + cudaGetErrorString(cudaError_t(-rc)));
+  double* d_scr = c->scratch.as<double>(size_t(blocks) * wpb * rodas_scratch_per_warp(N) / sizeof(double));
   ck(cudaEventRecord(c->ev[0], c->stream), "event");
-  int rc = launch_rodas(d_modes, nk, c->d_cos.as<CosmoDev>(c->cos.size()), cfg, d_queue, N, h->nq, Lmax, wpb, c->stream);
+  rc = launch_rodas(d_modes, nk, c->d_cos.as<CosmoDev>(c->cos.size()), cfg, d_queue, N, h->nq, Lmax, wpb, blocks,
+                    d_scr, c->stream);
   if (rc != 0) throw Err(-3, std::string("solver launch: ") + cudaGetErrorString(cudaError_t(rc)));
   ck(cudaEventRecord(c->ev[1], c->stream), "event");
   std::vector<int32_t> st(nk);
@@ -442,7 +451,7 @@ void bolt_ctx_destroy(bolt_ctx* c) {
   for (auto& e : c->cos)
     if (e.d_tab) cudaFree(e.d_tab);
   DBuf* bufs[] = {&c->d_cos, &c->modes, &c->xout, &c->srcT, &c->srcE, &c->traj, &c->plin, &c->status, &c->counters,
-                  &c->queue, &c->flags, &c->kgrid, &c->raw, &c->norm, &c->coef, &c->w, &c->slot_of_l, &c->ells,
+                  &c->queue, &c->flags, &c->scratch, &c->kgrid, &c->raw, &c->norm, &c->coef, &c->w, &c->slot_of_l, &c->ells,
                   &c->SdT, &c->SdE, &c->kmid, &c->wts, &c->yv, &c->dx, &c->dgs, &c->idg, &c->out};
   for (DBuf* b : bufs) b->release();
   for (int i = 0; i < 4; ++i) cudaEventDestroy(c->ev[i]);
@@ -627,6 +636,12 @@ int bolt_plin(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h, 
     ck(cudaMemcpyAsync(P, d_p, nk * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "P");
     ck(cudaStreamSynchronize(c->stream), "sync");
   });
+}
+
+int bolt_set_dense_x(bolt_ctx* c, double x) {
+  if (!c) return -1;
+  c->x_dense = x;
+  return 0;
 }
 
 int bolt_last_stats(bolt_ctx* c, int64_t* out) {

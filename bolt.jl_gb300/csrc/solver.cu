@@ -18,11 +18,19 @@
 // solve is one forward sweep, a 3x3 capacitance solve on the chain tails,
 // and one back substitution -- O(N) FP64 work, one lane per chain.
 //
-// Memory.  The whole per-mode working set (state, six stage vectors, the
-// chain factors and the border tails) lives in shared memory; the only
-// global traffic is the spline tables (L2-resident, ~0.3 MB per cosmology)
-// and the outputs.  Warps pull modes from a device work queue so modes with
-// very different step counts balance across the 152 SMs.
+// Memory.  Everything the serial chain sweeps and the right-hand side touch
+// (stage state, the vector being solved, the chain factors, border tails,
+// stage scalars) lives in shared memory; the state, the six stage increments
+// and the previous step for dense output live in a per-warp global slab that
+// stays L2-resident, so eight modes fit on an SM.  Warps pull modes from a
+// device work queue so modes with very different step counts balance across
+// the 152 SMs.
+//
+// Outputs.  Trajectory nodes and source nodes at x >= x_dense are landed on
+// exactly; source nodes below x_dense (before recombination, where the
+// line-of-sight integral never reads them) come from cubic Hermite dense
+// output between accepted steps, as the reference's KenCarp4 dense output
+// does for every node.
 #include <cuda_runtime.h>
 
 #include "bolt_dev.cuh"
@@ -50,16 +58,31 @@ constexpr double kGamma = 0.25;
 constexpr int kTail = 5;   // tail slots per chain
 constexpr int kBorder = 3; // Phi', Psi, Pi
 
+// Shared memory per warp (mode): the stage state yt and the vector being
+// solved b (both read at random by the chain sweeps and the right-hand
+// side), the chain factors, the border tails and the per-stage scalars.
+// The state y, the stage increments K_1..K_6, df/dx and the previous step
+// (for dense output) live in a per-warp global scratch slab that stays
+// resident in L2; they are only touched by row-parallel, coalesced loops.
+constexpr int kStages = 6;   // slots: 0..4 the distinct stage abscissae, 5 any other x
+constexpr int kScal = 12;    // scalars per slot
+
 struct Shared {
-  double *y, *yt, *fx, *K, *fl, *fi, *fc;
+  double *yt, *b, *fl, *fi, *fc;
   double *q, *df0, *Aq, *Bq, *qe, *eq, *qe_d, *eq_d;
-  double *Uf, *Wt, *cl1, *cl2, *misc;
+  double *Uf, *Wt, *cl1, *cl2, *sc, *sc_d, *misc;
+};
+
+struct Scratch {
+  double *y, *fx, *K, *yp, *fp;  // K: 6 x N
 };
 
 __host__ __device__ inline int per_warp_doubles(int N, int nq, int Lmax) {
   int nch = nq + 5;
-  return 12 * N + 8 * nq + 2 * nch * kTail * kBorder + 2 * (Lmax + 1) + 32;
+  return 5 * N + 4 * nq + 2 * kStages * nq + 2 * nq + 2 * nch * kTail * kBorder + 2 * (Lmax + 1) + kStages * kScal +
+         kScal + 32;
 }
+__host__ __device__ inline int scratch_per_warp(int N) { return 10 * N; }
 
 struct Mode {
   const CosmoDev* C;
@@ -87,50 +110,89 @@ struct Scal {
   T Hc, eta, tp, cs2, a, kH, iHe, R, cpsi, dphi, k2H2;
 };
 
-template <class T>
-__device__ __forceinline__ void stage_scalars(const Mode& m, double x, Scal<T>& s);
-
-template <>
-__device__ __forceinline__ void stage_scalars<double>(const Mode& m, double x, Scal<double>& s) {
-  const CosmoDev& C = *m.C;
-  SplW w;
-  spl_weights(C, x, w, false);
-  HotCoef c0, c1, c2, c3;
-  load_hot(C, w.i, c0, c1, c2, c3);
-  s.Hc = c0.x * w.w0 + c1.x * w.w1 + c2.x * w.w2 + c3.x * w.w3;
-  s.eta = c0.y * w.w0 + c1.y * w.w1 + c2.y * w.w2 + c3.y * w.w3;
-  s.tp = c0.z * w.w0 + c1.z * w.w1 + c2.z * w.w2 + c3.z * w.w3;
-  s.cs2 = c0.w * w.w0 + c1.w * w.w1 + c2.w * w.w2 + c3.w * w.w3;
-  s.a = exp(x);
-  double iH = 1.0 / s.Hc;
-  s.kH = m.k * iH;
-  s.iHe = iH / s.eta;
-  s.R = 4.0 * C.Omega_r / (3.0 * C.Omega_b * s.a);
-  s.cpsi = 12.0 * C.H0 * C.H0 / (m.k * m.k) / (s.a * s.a);
-  s.dphi = C.H0 * C.H0 * 0.5 * iH * iH;
-  s.k2H2 = m.k * m.k / 3.0 * iH * iH;
-}
-
-template <>
-__device__ __forceinline__ void stage_scalars<dd>(const Mode& m, double x, Scal<dd>& s) {
+// Scalars (and their x-derivatives) at x, one lane per abscissa, written to
+// shared-memory slot `slot`; derivatives are kept for slot 0 only.
+__device__ __forceinline__ void stage_scalars_to(const Mode& m, const Shared& S, double x, int slot) {
   const CosmoDev& C = *m.C;
   SplW w;
   spl_weights(C, x, w, true);
   HotCoef c0, c1, c2, c3;
   load_hot(C, w.i, c0, c1, c2, c3);
-  s.Hc = mk(c0.x * w.w0 + c1.x * w.w1 + c2.x * w.w2 + c3.x * w.w3, c0.x * w.d0 + c1.x * w.d1 + c2.x * w.d2 + c3.x * w.d3);
-  s.eta = mk(c0.y * w.w0 + c1.y * w.w1 + c2.y * w.w2 + c3.y * w.w3, c0.y * w.d0 + c1.y * w.d1 + c2.y * w.d2 + c3.y * w.d3);
-  s.tp = mk(c0.z * w.w0 + c1.z * w.w1 + c2.z * w.w2 + c3.z * w.w3, c0.z * w.d0 + c1.z * w.d1 + c2.z * w.d2 + c3.z * w.d3);
-  s.cs2 = mk(c0.w * w.w0 + c1.w * w.w1 + c2.w * w.w2 + c3.w * w.w3, c0.w * w.d0 + c1.w * w.d1 + c2.w * w.d2 + c3.w * w.d3);
+  dd Hc = mk(c0.x * w.w0 + c1.x * w.w1 + c2.x * w.w2 + c3.x * w.w3, c0.x * w.d0 + c1.x * w.d1 + c2.x * w.d2 + c3.x * w.d3);
+  dd eta = mk(c0.y * w.w0 + c1.y * w.w1 + c2.y * w.w2 + c3.y * w.w3, c0.y * w.d0 + c1.y * w.d1 + c2.y * w.d2 + c3.y * w.d3);
+  dd tp = mk(c0.z * w.w0 + c1.z * w.w1 + c2.z * w.w2 + c3.z * w.w3, c0.z * w.d0 + c1.z * w.d1 + c2.z * w.d2 + c3.z * w.d3);
+  dd cs2 = mk(c0.w * w.w0 + c1.w * w.w1 + c2.w * w.w2 + c3.w * w.w3, c0.w * w.d0 + c1.w * w.d1 + c2.w * w.d2 + c3.w * w.d3);
   double ea = exp(x);
-  s.a = mk(ea, ea);
-  dd iH = 1.0 / s.Hc;
-  s.kH = m.k * iH;
-  s.iHe = iH / s.eta;
-  s.R = (4.0 * C.Omega_r / (3.0 * C.Omega_b)) / s.a;
-  s.cpsi = (12.0 * C.H0 * C.H0 / (m.k * m.k)) / (s.a * s.a);
-  s.dphi = (C.H0 * C.H0 * 0.5) * iH * iH;
-  s.k2H2 = (m.k * m.k / 3.0) * iH * iH;
+  dd a = mk(ea, ea);
+  dd iH = 1.0 / Hc;
+  dd v[11];
+  v[0] = Hc; v[1] = eta; v[2] = tp; v[3] = cs2; v[4] = a;
+  v[5] = m.k * iH;
+  v[6] = iH / eta;
+  v[7] = (4.0 * C.Omega_r / (3.0 * C.Omega_b)) / a;
+  v[8] = (12.0 * C.H0 * C.H0 / (m.k * m.k)) / (a * a);
+  v[9] = (C.H0 * C.H0 * 0.5) * iH * iH;
+  v[10] = (m.k * m.k / 3.0) * iH * iH;
+  double* o = S.sc + slot * kScal;
+  for (int f = 0; f < 11; ++f) o[f] = v[f].v;
+  if (slot == 0)
+    for (int f = 0; f < 11; ++f) S.sc_d[f] = v[f].d;
+}
+
+// Massive-neutrino energies q/eps, eps/q for (slot, q) pairs spread over lanes.
+__device__ __forceinline__ void nu_energies_slots(const Mode& m, const Shared& S, int s0, int s1, int lane) {
+  const int nq = m.nq, tot = (s1 - s0) * nq;
+  for (int t = lane; t < tot; t += 32) {
+    int sl = s0 + t / nq, q = t - (t / nq) * nq;
+    double a = S.sc[sl * kScal + 4];
+    double am = a * m.C->Sigma_m_nu, qq = S.q[q];
+    double eps = sqrt(qq * qq + am * am);
+    S.qe[sl * nq + q] = qq / eps;
+    S.eq[sl * nq + q] = eps / qq;
+    if (sl == 0) {
+      double deps = am * am / eps;  // d eps / dx
+      S.qe_d[q] = -qq * deps / (eps * eps);
+      S.eq_d[q] = deps / qq;
+    }
+  }
+}
+
+// All stage abscissae of one step at once (slots 0..4: x, x + c2 h, x + c3 h,
+// x + c4 h, x_new), one lane per abscissa.
+__device__ __forceinline__ void prepare_stages(const Mode& m, const Shared& S, double x, double h, double xn, int lane) {
+  if (lane < 5) {
+    double xs = lane == 0 ? x : (lane == 4 ? xn : x + rodas::kCx[lane] * h);
+    stage_scalars_to(m, S, xs, lane);
+  }
+  __syncwarp();
+  nu_energies_slots(m, S, 0, 5, lane);
+  __syncwarp();
+}
+
+// One extra abscissa in slot 5 (dense-output and final nodes).
+__device__ __forceinline__ void prepare_other(const Mode& m, const Shared& S, double x, int lane) {
+  if (lane == 0) stage_scalars_to(m, S, x, 5);
+  __syncwarp();
+  nu_energies_slots(m, S, 5, 6, lane);
+  __syncwarp();
+}
+
+template <class T> __device__ __forceinline__ Scal<T> get_scal(const Shared& S, int slot);
+template <> __device__ __forceinline__ Scal<double> get_scal<double>(const Shared& S, int slot) {
+  const double* o = S.sc + slot * kScal;
+  Scal<double> s;
+  s.Hc = o[0]; s.eta = o[1]; s.tp = o[2]; s.cs2 = o[3]; s.a = o[4]; s.kH = o[5]; s.iHe = o[6]; s.R = o[7];
+  s.cpsi = o[8]; s.dphi = o[9]; s.k2H2 = o[10];
+  return s;
+}
+template <> __device__ __forceinline__ Scal<dd> get_scal<dd>(const Shared& S, int slot) {
+  const double* o = S.sc + slot * kScal;
+  const double* d = S.sc_d;
+  Scal<dd> s;
+  s.Hc = mk(o[0], d[0]); s.eta = mk(o[1], d[1]); s.tp = mk(o[2], d[2]); s.cs2 = mk(o[3], d[3]); s.a = mk(o[4], d[4]);
+  s.kH = mk(o[5], d[5]); s.iHe = mk(o[6], d[6]); s.R = mk(o[7], d[7]); s.cpsi = mk(o[8], d[8]);
+  s.dphi = mk(o[9], d[9]); s.k2H2 = mk(o[10], d[10]);
+  return s;
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -139,37 +201,12 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Massive-neutrino energies q/eps and eps/q at scale factor a (lane q).
-template <class T>
-__device__ __forceinline__ void nu_energies(const Mode& m, const Shared& S, T a, int lane);
-template <>
-__device__ __forceinline__ void nu_energies<double>(const Mode& m, const Shared& S, double a, int lane) {
-  for (int q = lane; q < m.nq; q += 32) {
-    double am = a * m.C->Sigma_m_nu, qq = S.q[q];
-    double eps = sqrt(qq * qq + am * am);
-    S.qe[q] = qq / eps;
-    S.eq[q] = eps / qq;
-  }
-}
-template <>
-__device__ __forceinline__ void nu_energies<dd>(const Mode& m, const Shared& S, dd a, int lane) {
-  for (int q = lane; q < m.nq; q += 32) {
-    double am = a.v * m.C->Sigma_m_nu, qq = S.q[q];
-    double eps = sqrt(qq * qq + am * am);
-    double deps = am * am / eps;  // d eps / dx
-    S.qe[q] = qq / eps;
-    S.eq[q] = eps / qq;
-    S.qe_d[q] = -qq * deps / (eps * eps);
-    S.eq_d[q] = deps / qq;
-  }
-}
-
-template <class T> __device__ __forceinline__ T qe_of(const Shared& S, int q);
-template <> __device__ __forceinline__ double qe_of<double>(const Shared& S, int q) { return S.qe[q]; }
-template <> __device__ __forceinline__ dd qe_of<dd>(const Shared& S, int q) { return mk(S.qe[q], S.qe_d[q]); }
-template <class T> __device__ __forceinline__ T eq_of(const Shared& S, int q);
-template <> __device__ __forceinline__ double eq_of<double>(const Shared& S, int q) { return S.eq[q]; }
-template <> __device__ __forceinline__ dd eq_of<dd>(const Shared& S, int q) { return mk(S.eq[q], S.eq_d[q]); }
+template <class T> __device__ __forceinline__ T qe_of(const Shared& S, int sl, int nq, int q);
+template <> __device__ __forceinline__ double qe_of<double>(const Shared& S, int sl, int nq, int q) { return S.qe[sl * nq + q]; }
+template <> __device__ __forceinline__ dd qe_of<dd>(const Shared& S, int sl, int nq, int q) { return mk(S.qe[q], S.qe_d[q]); }
+template <class T> __device__ __forceinline__ T eq_of(const Shared& S, int sl, int nq, int q);
+template <> __device__ __forceinline__ double eq_of<double>(const Shared& S, int sl, int nq, int q) { return S.eq[sl * nq + q]; }
+template <> __device__ __forceinline__ dd eq_of<dd>(const Shared& S, int sl, int nq, int q) { return mk(S.eq[q], S.eq_d[q]); }
 
 template <class T> __device__ __forceinline__ void put(double* v, double* d, int i, T x);
 template <> __device__ __forceinline__ void put<double>(double* v, double*, int i, double x) { v[i] = x; }
@@ -181,12 +218,12 @@ template <> __device__ __forceinline__ dd warp_sum_t<dd>(dd v) { return mk(warp_
 
 // Metric potentials Psi and Phi' (perturbations.jl:182-194) from the state u.
 template <class T>
-__device__ __forceinline__ void metric(const Mode& m, const Shared& S, const Scal<T>& s, const double* u, int lane,
-                                       T& Psi, T& Phip, T* rhoM_out = nullptr) {
+__device__ __forceinline__ void metric(const Mode& m, const Shared& S, int sl, const Scal<T>& s, const double* u,
+                                       int lane, T& Psi, T& Phip, T* rhoM_out = nullptr) {
   const CosmoDev& C = *m.C;
   T rho = cst<T>(0.0), sig = cst<T>(0.0);
   for (int q = lane; q < m.nq; q += 32) {
-    T qe = qe_of<T>(S, q), eq = eq_of<T>(S, q);
+    T qe = qe_of<T>(S, sl, m.nq, q), eq = eq_of<T>(S, sl, m.nq, q);
     double qq = S.q[q];
     // eps = q * eq ; q^2/eps = q * qe
     rho = rho + (S.Aq[q] * qq) * eq * u[m.iM + q];
@@ -207,13 +244,10 @@ __device__ __forceinline__ void metric(const Mode& m, const Shared& S, const Sca
 // hierarchy! (perturbations.jl:161-271): writes f into out (and df/dx into
 // out_d for T = dd).  Returns true when the radiation-streaming switch is on.
 template <class T>
-__device__ bool rhs_rows(const Mode& m, const Shared& S, double x, const double* u, double* out, double* out_d, int lane) {
-  Scal<T> s;
-  stage_scalars<T>(m, x, s);
-  nu_energies<T>(m, S, s.a, lane);
-  __syncwarp();
+__device__ bool rhs_rows(const Mode& m, const Shared& S, int sl, const double* u, double* out, double* out_d, int lane) {
+  const Scal<T> s = get_scal<T>(S, sl);
   T Psi, Phip;
-  metric<T>(m, S, s, u, lane, Psi, Phip);
+  metric<T>(m, S, sl, s, u, lane, Psi, Phip);
   const CosmoDev& C = *m.C;
   const int lg = m.lg, lnu = m.lnu, lmnu = m.lmnu, nq = m.nq;
   const double* cl1 = S.cl1;
@@ -273,13 +307,13 @@ __device__ bool rhs_rows(const Mode& m, const Shared& S, double x, const double*
   const int nM = (lmnu + 1) * nq;
   for (int j = lane; j < nM; j += 32) {
     int l = j / nq, q = j - l * nq;
-    T qe = qe_of<T>(S, q);
+    T qe = qe_of<T>(S, sl, nq, q);
     T f;
     if (l < lmnu) {
       double lo = l > 0 ? Mm[j - nq] : 0.0;
       f = (s.kH * qe) * (cl1[l] * lo - cl2[l] * Mm[j + nq]);
       if (l == 0) f = f + Phip * S.df0[q];
-      if (l == 1) f = f - (1.0 / 3.0) * s.kH * eq_of<T>(S, q) * Psi * S.df0[q];
+      if (l == 1) f = f - (1.0 / 3.0) * s.kH * eq_of<T>(S, sl, nq, q) * Psi * S.df0[q];
     } else {
       f = qe * s.kH * Mm[j - nq] - (lmnu + 1.0) * s.iHe * Mm[j];
     }
@@ -329,12 +363,9 @@ __device__ __forceinline__ int tail_slots(const Mode& m, int c) {
 // Factor M = I/(h gamma) - L chain by chain (lane c), build the border tails
 // and the 3x3 capacitance inverse.  Returns false on a zero or non-finite
 // pivot.
-__device__ bool factorize(const Mode& m, const Shared& S, double x, double hg, int lane) {
+__device__ bool factorize(const Mode& m, const Shared& S, double hg, int lane) {
   const CosmoDev& C = *m.C;
-  Scal<double> s;
-  stage_scalars<double>(m, x, s);
-  nu_energies<double>(m, S, s.a, lane);
-  __syncwarp();
+  const Scal<double> s = get_scal<double>(S, 0);
   const double ig = 1.0 / hg;
   const double* cl1 = S.cl1;
   const double* cl2 = S.cl2;
@@ -735,7 +766,18 @@ __device__ void initial_state(const Mode& m, const Shared& S, double xi, double*
 }
 
 // --------------------------------------------------------------- driver ----
-__device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const SolverCfg& cfg, double* base, int lane) {
+// Cubic Hermite interpolation on [x0, x1] from (y0, f0, y1, f1) into u.
+__device__ __forceinline__ void hermite(int N, double x0, double x1, double xq, const double* y0, const double* f0,
+                                        const double* y1, const double* f1, double* u, int lane) {
+  double hh = x1 - x0, t = (xq - x0) / hh, t2 = t * t, t3 = t2 * t;
+  double h00 = 2.0 * t3 - 3.0 * t2 + 1.0, h10 = (t3 - 2.0 * t2 + t) * hh, h01 = -2.0 * t3 + 3.0 * t2,
+         h11 = (t3 - t2) * hh;
+  for (int i = lane; i < N; i += 32) u[i] = h00 * y0[i] + h10 * f0[i] + h01 * y1[i] + h11 * f1[i];
+  __syncwarp();
+}
+
+__device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const SolverCfg& cfg, double* base,
+                          double* gscr, int lane) {
   Mode m;
   m.C = cosmos + md.cosmo;
   m.k = md.k;
@@ -747,36 +789,42 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   m.iPhi = m.iM + (m.lmnu + 1) * m.nq;
   m.nch = m.nq + 5;
   const CosmoDev& C = *m.C;
-  const int N = m.N;
+  const int N = m.N, nq = m.nq;
   int Lmax = max(m.lg, max(m.lnu, m.lmnu));
   Shared S;
   double* p = base;
-  S.y = p; p += N;
   S.yt = p; p += N;
-  S.fx = p; p += N;
-  S.K = p; p += 6 * N;
+  S.b = p; p += N;
   S.fl = p; p += N;
   S.fi = p; p += N;
   S.fc = p; p += N;
-  S.q = p; p += m.nq;
-  S.df0 = p; p += m.nq;
-  S.Aq = p; p += m.nq;
-  S.Bq = p; p += m.nq;
-  S.qe = p; p += m.nq;
-  S.eq = p; p += m.nq;
-  S.qe_d = p; p += m.nq;
-  S.eq_d = p; p += m.nq;
+  S.q = p; p += nq;
+  S.df0 = p; p += nq;
+  S.Aq = p; p += nq;
+  S.Bq = p; p += nq;
+  S.qe = p; p += kStages * nq;
+  S.eq = p; p += kStages * nq;
+  S.qe_d = p; p += nq;
+  S.eq_d = p; p += nq;
   S.Uf = p; p += m.nch * kTail * kBorder;
   S.Wt = p; p += m.nch * kTail * kBorder;
   S.cl1 = p; p += Lmax + 1;
   S.cl2 = p; p += Lmax + 1;
+  S.sc = p; p += kStages * kScal;
+  S.sc_d = p; p += kScal;
   S.misc = p;
+  Scratch G;
+  G.y = gscr;
+  G.fx = gscr + N;
+  G.K = gscr + 2 * N;
+  G.yp = gscr + 8 * N;
+  G.fp = gscr + 9 * N;
   // per-mode constants (perturbations.jl:164-166; background.jl:21-30)
   for (int l = lane; l <= Lmax; l += 32) {
     S.cl1[l] = double(l) / (2.0 * l + 1.0);
     S.cl2[l] = (l + 1.0) / (2.0 * l + 1.0);
   }
-  for (int q = lane; q < m.nq; q += 32) {
+  for (int q = lane; q < nq; q += 32) {
     double xq = C.qx[q];
     double lq = C.logqmin + (C.logqmax - C.logqmin) / 2.0 * (xq + 1.0);
     double qq = pow(10.0, lq);
@@ -790,90 +838,161 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   __syncwarp();
   double x = C.x0;
   const double xend = md.xout[md.nout - 1];
-  initial_state(m, S, x, S.y, lane);
+  initial_state(m, S, x, S.yt, lane);
+  for (int i = lane; i < N; i += 32) G.y[i] = S.yt[i];
+  __syncwarp();
   int status = ST_OK;
   bool rsa_any = false;
   long long nacc = 0, nrej = 0;
   int jo = 0;
+  while (jo < md.nout && md.xout[jo] < x) ++jo;
+  // nodes below x_dense are produced by dense output (sources only)
+  const bool dense_ok = (md.flags & MODE_SOURCES) && !(md.flags & MODE_TRAJ);
+  int jd = 0;
+  if (dense_ok)
+    while (jd < md.nout - 1 && md.xout[jd] < cfg.x_dense) ++jd;
   double h = cfg.h0;
   const double rtol = cfg.reltol, atol = cfg.abstol;
-  while (jo < md.nout && md.xout[jo] < x) ++jo;  // nodes before the start are not produced
+  double xprev = x;
+  bool have_prev = false;
+  double x_done = -1e300;  // last abscissa whose dense nodes were emitted
   while (true) {
     bool at_node = (jo < md.nout) && (md.xout[jo] == x);
     if (x >= xend) {
-      // final node: outputs at x_end
-      if (at_node) {
-        if (md.flags & MODE_SOURCES) {
-          rhs_rows<double>(m, S, x, S.y, S.K, nullptr, lane);
+      if (at_node || (dense_ok && have_prev && jo < md.nout)) {
+        prepare_other(m, S, x, lane);
+        double* Kf = G.K + N;
+        for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
+        __syncwarp();
+        rhs_rows<double>(m, S, 5, S.yt, Kf, nullptr, lane);
+        __syncwarp();
+        if (dense_ok && have_prev) {
+          // dense nodes strictly inside the last step
+          while (jo < md.nout && md.xout[jo] < x) {
+            double xq = md.xout[jo];
+            hermite(N, xprev, x, xq, G.yp, G.fp, G.y, Kf, S.yt, lane);
+            prepare_other(m, S, xq, lane);
+            rhs_rows<double>(m, S, 5, S.yt, G.K, nullptr, lane);
+            __syncwarp();
+            emit_sources(m, S, xq, S.yt, G.K, lane, md.src_T + jo, md.src_E + jo);
+            __syncwarp();
+            ++jo;
+          }
+          prepare_other(m, S, x, lane);
+          for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
           __syncwarp();
-          emit_sources(m, S, x, S.y, S.K, lane, md.src_T + jo, md.src_E + jo);
         }
-        if (md.flags & MODE_TRAJ)
-          for (int i = lane; i < N; i += 32) md.traj[(size_t)jo * N + i] = S.y[i];
-        ++jo;
+        if (jo < md.nout && md.xout[jo] == x) {
+          if (md.flags & MODE_SOURCES) emit_sources(m, S, x, S.yt, Kf, lane, md.src_T + jo, md.src_E + jo);
+          if (md.flags & MODE_TRAJ)
+            for (int i = lane; i < N; i += 32) md.traj[(size_t)jo * N + i] = G.y[i];
+          ++jo;
+        }
+        __syncwarp();
       }
-      if (md.flags & MODE_PLIN) emit_plin(m, S, x, S.y, lane, md.plin);
+      if (md.flags & MODE_PLIN) {
+        for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
+        __syncwarp();
+        emit_plin(m, S, x, S.yt, lane, md.plin);
+      }
       break;
     }
-    double target = jo < md.nout ? md.xout[jo] : xend;
-    if (at_node) target = (jo + 1 < md.nout) ? md.xout[jo + 1] : xend;
+    // next landing target: the next node at or above x_dense (or the end)
+    int jt = max(jo, jd);
+    if (at_node && jt == jo) ++jt;
+    double target = jt < md.nout ? md.xout[jt] : xend;
     bool landing = false;
     double hs = h;
     if (x + hs >= target - 1e-14 * fabs(target)) { hs = target - x; landing = true; }
-    if (!factorize(m, S, x, hs * rodas::kGamma, lane)) { status = ST_LU_FAIL; break; }
-    // stage 1: f and df/dx at (x, y)
-    bool r = rhs_rows<dd>(m, S, x, S.y, S.K, S.fx, lane);
+    const double xn = landing ? target : x + hs;
+    prepare_stages(m, S, x, hs, xn, lane);
+    if (!factorize(m, S, hs * rodas::kGamma, lane)) { status = ST_LU_FAIL; break; }
+    // stage 1: f and df/dx at (x, y) into K0 / fx
+    double* K0 = G.K;
+    for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
+    __syncwarp();
+    bool r = rhs_rows<dd>(m, S, 0, S.yt, S.b, G.fx, lane);
     rsa_any |= r;
     __syncwarp();
-    if (at_node) {
-      if (md.flags & MODE_SOURCES) emit_sources(m, S, x, S.y, S.K, lane, md.src_T + jo, md.src_E + jo);
-      if (md.flags & MODE_TRAJ)
-        for (int i = lane; i < N; i += 32) md.traj[(size_t)jo * N + i] = S.y[i];
-      ++jo;
+    if (x != x_done) {
+      // outputs that fall on this abscissa or inside the last accepted step
+      if (dense_ok && have_prev && jo < jd) {
+        for (int i = lane; i < N; i += 32) K0[i] = S.b[i];  // f at x, kept while interpolating
+        __syncwarp();
+        while (jo < md.nout && md.xout[jo] < x) {
+          double xq = md.xout[jo];
+          hermite(N, xprev, x, xq, G.yp, G.fp, G.y, K0, S.yt, lane);
+          prepare_other(m, S, xq, lane);
+          rhs_rows<double>(m, S, 5, S.yt, G.K + N, nullptr, lane);
+          __syncwarp();
+          emit_sources(m, S, xq, S.yt, G.K + N, lane, md.src_T + jo, md.src_E + jo);
+          __syncwarp();
+          ++jo;
+        }
+        for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
+        __syncwarp();
+      }
+      if (jo < md.nout && md.xout[jo] == x) {
+        if (md.flags & MODE_SOURCES) emit_sources(m, S, x, S.yt, S.b, lane, md.src_T + jo, md.src_E + jo);
+        if (md.flags & MODE_TRAJ)
+          for (int i = lane; i < N; i += 32) md.traj[(size_t)jo * N + i] = G.y[i];
+        ++jo;
+        __syncwarp();
+      }
+      if (dense_ok) {
+        for (int i = lane; i < N; i += 32) { G.yp[i] = G.y[i]; G.fp[i] = S.b[i]; }
+        xprev = x;
+        have_prev = true;
+      }
+      x_done = x;
       __syncwarp();
     }
     const double ih = 1.0 / hs;
-    double* K0 = S.K;
-    for (int i = lane; i < N; i += 32) K0[i] += hs * rodas::kD[0] * S.fx[i];
+    for (int i = lane; i < N; i += 32) S.b[i] += hs * rodas::kD[0] * G.fx[i];
     __syncwarp();
-    wsolve(m, S, K0, lane);
-    double xn = landing ? target : x + hs;
+    wsolve(m, S, S.b, lane);
+    for (int i = lane; i < N; i += 32) K0[i] = S.b[i];
+    __syncwarp();
     for (int st = 1; st < 6; ++st) {
-      double* Ks = S.K + st * N;
       // stage state
       if (st < 5) {
+#pragma unroll 2
         for (int i = lane; i < N; i += 32) {
-          double acc = S.y[i];
-          for (int j = 0; j < st; ++j) acc += rodas::kA[st - 1][j] * S.K[j * N + i];
+          double acc = G.y[i];
+          for (int j = 0; j < st; ++j) acc += rodas::kA[st - 1][j] * G.K[j * N + i];
           S.yt[i] = acc;
         }
       } else {
-        for (int i = lane; i < N; i += 32) S.yt[i] += S.K[4 * N + i];
+        for (int i = lane; i < N; i += 32) S.yt[i] += G.K[4 * N + i];
       }
       __syncwarp();
-      double xs = st >= 4 ? xn : x + rodas::kCx[st] * hs;
-      r = rhs_rows<double>(m, S, xs, S.yt, Ks, nullptr, lane);
+      const int sl = st < 4 ? st : 4;
+      r = rhs_rows<double>(m, S, sl, S.yt, S.b, nullptr, lane);
       rsa_any |= r;
       __syncwarp();
-      double hd = hs * rodas::kD[st];
+      const double hd = hs * rodas::kD[st];
+#pragma unroll 2
       for (int i = lane; i < N; i += 32) {
-        double acc = Ks[i];
-        if (st < 4) acc += hd * S.fx[i];
+        double acc = S.b[i];
+        if (st < 4) acc += hd * G.fx[i];
         double cs = 0.0;
-        for (int j = 0; j < st; ++j) cs += rodas::kC[st][j] * S.K[j * N + i];
-        Ks[i] = acc + ih * cs;
+        for (int j = 0; j < st; ++j) cs += rodas::kC[st][j] * G.K[j * N + i];
+        S.b[i] = acc + ih * cs;
       }
       __syncwarp();
-      wsolve(m, S, Ks, lane);
+      wsolve(m, S, S.b, lane);
+      if (st < 5) {
+        for (int i = lane; i < N; i += 32) G.K[st * N + i] = S.b[i];
+        __syncwarp();
+      }
     }
-    // error estimate: the last stage increment
+    // error estimate: the last stage increment (in b)
     double en = 0.0;
     bool fin = true;
-    const double* K5 = S.K + 5 * N;
     for (int i = lane; i < N; i += 32) {
-      double yn = S.yt[i] + K5[i];
-      double sc = atol + rtol * fmax(fabs(S.y[i]), fabs(yn));
-      double e = K5[i] / sc;
+      double yn = S.yt[i] + S.b[i];
+      double sc = atol + rtol * fmax(fabs(G.y[i]), fabs(yn));
+      double e = S.b[i] / sc;
       en += e * e;
       fin = fin && isfinite(yn);
     }
@@ -883,7 +1002,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     double fac = 0.9 * pow(fmax(en, 1e-12), -0.25);
     fac = fmin(6.0, fmax(0.2, fac));
     if (en <= 1.0) {
-      for (int i = lane; i < N; i += 32) S.y[i] = S.yt[i] + K5[i];
+      for (int i = lane; i < N; i += 32) G.y[i] = S.yt[i] + S.b[i];
       __syncwarp();
       x = xn;
       ++nacc;
@@ -891,7 +1010,6 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       h = landing ? fmax(h, hp) : hp;
     } else {
       ++nrej;
-      if (at_node) --jo;  // re-emit after the retry (same x, same y)
       h = hs * fmin(1.0, fac);
       if (!(h >= 1e-14 * fmax(1.0, fabs(x)))) { status = fin ? ST_DT_UNDERFLOW : ST_NONFINITE; break; }
     }
@@ -905,45 +1023,55 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
 
 __global__ void __launch_bounds__(256) rodas_kernel(const ModeDev* __restrict__ modes, int nmodes,
                                                     const CosmoDev* __restrict__ cosmos, SolverCfg cfg,
-                                                    int* __restrict__ queue, int per_warp) {
+                                                    int* __restrict__ queue, int per_warp, double* __restrict__ scratch,
+                                                    int scr_per_warp) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   double* base = smem + (size_t)w * per_warp;
+  double* gscr = scratch + ((size_t)blockIdx.x * (blockDim.x >> 5) + w) * scr_per_warp;
   while (true) {
     int mi = 0;
     if (lane == 0) mi = atomicAdd(queue, 1);
     mi = __shfl_sync(0xffffffffu, mi, 0);
     if (mi >= nmodes) break;
-    solve_one(modes[mi], cosmos, cfg, base, lane);
+    solve_one(modes[mi], cosmos, cfg, base, gscr, lane);
     __syncwarp();
   }
 }
 
-// Host launcher.  Returns a cudaError_t.
-int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
-                 int maxN, int maxnq, int maxL, int warps_per_block, cudaStream_t stream) {
+// Host launcher: grid size (in warps) for the scratch allocation.
+int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int warps_per_block, int* blocks) {
   int per_warp = per_warp_doubles(maxN, maxnq, maxL);
   size_t smem = size_t(per_warp) * warps_per_block * sizeof(double);
   cudaError_t e = cudaFuncSetAttribute(rodas_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e != cudaSuccess) return e;
+  if (e != cudaSuccess) return -int(e);
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int bps = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, rodas_kernel, 32 * warps_per_block, smem);
-  if (e != cudaSuccess) return e;
-  if (bps < 1) return cudaErrorInvalidConfiguration;
+  if (e != cudaSuccess) return -int(e);
+  if (bps < 1) return -int(cudaErrorInvalidConfiguration);
   int want = (nmodes + warps_per_block - 1) / warps_per_block;
-  int grid = std::min(want, nsm * bps);
-  e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
+  *blocks = std::min(want, nsm * bps);
+  return 0;
+}
+
+int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
+                 int maxN, int maxnq, int maxL, int warps_per_block, int blocks, double* d_scratch, cudaStream_t stream) {
+  int per_warp = per_warp_doubles(maxN, maxnq, maxL);
+  size_t smem = size_t(per_warp) * warps_per_block * sizeof(double);
+  cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  rodas_kernel<<<grid, 32 * warps_per_block, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, per_warp);
+  rodas_kernel<<<blocks, 32 * warps_per_block, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, per_warp,
+                                                                d_scratch, scratch_per_warp(maxN));
   return cudaGetLastError();
 }
 
 size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL) {
   return size_t(per_warp_doubles(maxN, maxnq, maxL)) * sizeof(double);
 }
+size_t rodas_scratch_per_warp(int maxN) { return size_t(scratch_per_warp(maxN)) * sizeof(double); }
 
 }  // namespace bolt

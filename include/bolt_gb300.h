@@ -123,6 +123,12 @@ int bolt_cl_pipeline(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const
 int bolt_plin(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const bolt_hier* hier, double x,
               double reltol, double abstol, double* P, int32_t* status);
 
+/* Source-grid nodes with x below x_dense (default -8.5, before
+ * recombination; the line-of-sight integral starts at x > -8) are produced by
+ * cubic Hermite dense output between accepted steps instead of landing the
+ * integrator on every node.  Pass -INFINITY to land on every node. */
+int bolt_set_dense_x(bolt_ctx* ctx, double x_dense);
+
 /* Counters of the last call: [0] accepted steps, [1] rejected steps,
  * [2] solver kernel microseconds, [3] LOS kernels microseconds,
  * [4] modes, [5] solver kernel launches, [6] total kernel launches. */
