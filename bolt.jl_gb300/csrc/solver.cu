@@ -899,11 +899,12 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     }
     // next landing target: the next node at or above x_dense (or the end)
     int jt = max(jo, jd);
-    if (at_node && jt == jo) ++jt;
+    while (jt < md.nout && md.xout[jt] <= x) ++jt;
     double target = jt < md.nout ? md.xout[jt] : xend;
     bool landing = false;
     double hs = h;
     if (x + hs >= target - 1e-14 * fabs(target)) { hs = target - x; landing = true; }
+    if (!(hs > 0.0)) { status = ST_DT_UNDERFLOW; break; }
     const double xn = landing ? target : x + hs;
     prepare_stages(m, S, x, hs, xn, lane);
     if (!factorize(m, S, hs * rodas::kGamma, lane)) { status = ST_LU_FAIL; break; }
