@@ -231,14 +231,13 @@ void run_solver(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h
   cfg.x_dense = c->x_dense;
   cfg.max_steps = c->max_steps;
   int Lmax = std::max(h->lg, std::max(h->lnu, h->lmnu));
-  size_t pw = rodas_smem_per_warp(N, h->nq, Lmax);
-  int wpb = c->wpb;
-  if (wpb <= 0) wpb = int(std::max<size_t>(1, std::min<size_t>(8, (220 * 1024) / pw)));
-  if (pw * wpb > 227 * 1024) throw Err(-1, "hierarchy too large for shared memory");
+  size_t pw = rodas_smem_per_warp(N, h->nq, Lmax);  // shared memory of one mode (one CTA)
+  if (pw > 227 * 1024) throw Err(-1, "hierarchy too large for shared memory");
+  int wpb = 0;
   int blocks = 0;
   int rc = rodas_grid_warps(nk, N, h->nq, Lmax, wpb, &blocks);
   if (rc != 0) throw Err(-3, std::string("solver configuration: ") + cudaGetErrorString(cudaError_t(-rc)));
-  double* d_scr = c->scratch.as<double>(size_t(blocks) * wpb * rodas_scratch_per_warp(N) / sizeof(double));
+  double* d_scr = c->scratch.as<double>(size_t(blocks) * rodas_scratch_per_warp(N) / sizeof(double));
   ck(cudaEventRecord(c->ev[0], c->stream), "event");
   rc = launch_rodas(d_modes, nk, c->d_cos.as<CosmoDev>(c->cos.size()), cfg, d_queue, N, h->nq, Lmax, wpb, blocks,
                     d_scr, c->stream);

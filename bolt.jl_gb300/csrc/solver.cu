@@ -139,10 +139,10 @@ __device__ __forceinline__ void stage_scalars_to(const Mode& m, const Shared& S,
     for (int f = 0; f < 11; ++f) S.sc_d[f] = v[f].d;
 }
 
-// Massive-neutrino energies q/eps, eps/q for (slot, q) pairs spread over lanes.
-__device__ __forceinline__ void nu_energies_slots(const Mode& m, const Shared& S, int s0, int s1, int lane) {
+// Massive-neutrino energies q/eps, eps/q for (slot, q) pairs spread over the CTA.
+__device__ __forceinline__ void nu_energies_slots(const Mode& m, const Shared& S, int s0, int s1, int tid, int nth) {
   const int nq = m.nq, tot = (s1 - s0) * nq;
-  for (int t = lane; t < tot; t += 32) {
+  for (int t = tid; t < tot; t += nth) {
     int sl = s0 + t / nq, q = t - (t / nq) * nq;
     double a = S.sc[sl * kScal + 4];
     double am = a * m.C->Sigma_m_nu, qq = S.q[q];
@@ -158,23 +158,24 @@ __device__ __forceinline__ void nu_energies_slots(const Mode& m, const Shared& S
 }
 
 // All stage abscissae of one step at once (slots 0..4: x, x + c2 h, x + c3 h,
-// x + c4 h, x_new), one lane per abscissa.
-__device__ __forceinline__ void prepare_stages(const Mode& m, const Shared& S, double x, double h, double xn, int lane) {
-  if (lane < 5) {
-    double xs = lane == 0 ? x : (lane == 4 ? xn : x + rodas::kCx[lane] * h);
-    stage_scalars_to(m, S, xs, lane);
+// x + c4 h, x_new), one thread per abscissa.
+__device__ __forceinline__ void prepare_stages(const Mode& m, const Shared& S, double x, double h, double xn, int tid,
+                                               int nth) {
+  if (tid < 5) {
+    double xs = tid == 0 ? x : (tid == 4 ? xn : x + rodas::kCx[tid] * h);
+    stage_scalars_to(m, S, xs, tid);
   }
-  __syncwarp();
-  nu_energies_slots(m, S, 0, 5, lane);
-  __syncwarp();
+  __syncthreads();
+  nu_energies_slots(m, S, 0, 5, tid, nth);
+  __syncthreads();
 }
 
 // One extra abscissa in slot 5 (dense-output and final nodes).
-__device__ __forceinline__ void prepare_other(const Mode& m, const Shared& S, double x, int lane) {
-  if (lane == 0) stage_scalars_to(m, S, x, 5);
-  __syncwarp();
-  nu_energies_slots(m, S, 5, 6, lane);
-  __syncwarp();
+__device__ __forceinline__ void prepare_other(const Mode& m, const Shared& S, double x, int tid, int nth) {
+  if (tid == 0) stage_scalars_to(m, S, x, 5);
+  __syncthreads();
+  nu_energies_slots(m, S, 5, 6, tid, nth);
+  __syncthreads();
 }
 
 template <class T> __device__ __forceinline__ Scal<T> get_scal(const Shared& S, int slot);
@@ -242,96 +243,87 @@ __device__ __forceinline__ void metric(const Mode& m, const Shared& S, int sl, c
 }
 
 // hierarchy! (perturbations.jl:161-271): writes f into out (and df/dx into
-// out_d for T = dd).  Returns true when the radiation-streaming switch is on.
+// out_d for T = dd), one row per thread over the whole CTA.  Every warp
+// forms the metric potentials itself (two nq-term sums), so no barrier is
+// needed before the rows.  Returns true when the radiation-streaming switch
+// is on.
 template <class T>
-__device__ bool rhs_rows(const Mode& m, const Shared& S, int sl, const double* u, double* out, double* out_d, int lane) {
+__device__ bool rhs_rows(const Mode& m, const Shared& S, int sl, const double* u, double* out, double* out_d, int tid,
+                         int nth) {
+  const int lane = tid & 31;
   const Scal<T> s = get_scal<T>(S, sl);
   T Psi, Phip;
   metric<T>(m, S, sl, s, u, lane, Psi, Phip);
-  const CosmoDev& C = *m.C;
   const int lg = m.lg, lnu = m.lnu, lmnu = m.lmnu, nq = m.nq;
   const double* cl1 = S.cl1;
   const double* cl2 = S.cl2;
-  bool rsa = (m.k * vof(s.eta) > 240.0) && (-vof(s.tp) * vof(s.Hc) / vof(s.eta) > 100.0);
-  double Pi = u[2] + u[m.iTp + 2] + u[m.iTp];
-  double vb = u[m.iPhi + 4];
-  if (rsa) {
-    for (int i = lane; i < m.iM; i += 32) put<T>(out, out_d, i, cst<T>(0.0));
-  } else {
-    // photon temperature
-    for (int l = lane; l <= lg; l += 32) {
-      T f;
-      if (l < lg) {
-        double lo = l > 0 ? u[l - 1] : 0.0;
-        f = s.kH * (cl1[l] * lo - cl2[l] * u[l + 1]);
-        if (l >= 1) f = f + s.tp * u[l];
-        if (l == 0) f = f - Phip;
-        if (l == 1) f = f + (1.0 / 3.0) * s.kH * Psi + s.tp * (vb / 3.0);
-        if (l == 2) f = f - s.tp * (Pi / 10.0);
-      } else {
-        f = s.kH * u[lg - 1] - ((lg + 1.0) * s.iHe - s.tp) * u[lg];
-      }
-      put<T>(out, out_d, l, f);
-    }
-    // photon polarization
-    const double* P = u + m.iTp;
-    for (int l = lane; l <= lg; l += 32) {
-      T f;
-      if (l < lg) {
-        double lo = l > 0 ? P[l - 1] : 0.0;
-        f = s.kH * (cl1[l] * lo - cl2[l] * P[l + 1]) + s.tp * P[l];
-        if (l == 0) f = f - s.tp * (Pi / 2.0);
-        if (l == 2) f = f - s.tp * (Pi / 10.0);
-      } else {
-        f = s.kH * P[lg - 1] - ((lg + 1.0) * s.iHe - s.tp) * P[lg];
-      }
-      put<T>(out, out_d, m.iTp + l, f);
-    }
-    // massless neutrinos
-    const double* Nn = u + m.iN;
-    for (int l = lane; l <= lnu; l += 32) {
-      T f;
-      if (l < lnu) {
-        double lo = l > 0 ? Nn[l - 1] : 0.0;
-        f = s.kH * (cl1[l] * lo - cl2[l] * Nn[l + 1]);
-        if (l == 0) f = f - Phip;
-        if (l == 1) f = f + (1.0 / 3.0) * s.kH * Psi;
-      } else {
-        f = s.kH * Nn[lnu - 1] - (lnu + 1.0) * s.iHe * Nn[lnu];
-      }
-      put<T>(out, out_d, m.iN + l, f);
-    }
-  }
-  // massive neutrinos (MB 57)
-  const double* Mm = u + m.iM;
-  const int nM = (lmnu + 1) * nq;
-  for (int j = lane; j < nM; j += 32) {
-    int l = j / nq, q = j - l * nq;
-    T qe = qe_of<T>(S, sl, nq, q);
+  const bool rsa = (m.k * vof(s.eta) > 240.0) && (-vof(s.tp) * vof(s.Hc) / vof(s.eta) > 100.0);
+  const double Pi = u[2] + u[m.iTp + 2] + u[m.iTp];
+  const double vb = u[m.iPhi + 4];
+  for (int i = tid; i < m.N; i += nth) {
     T f;
-    if (l < lmnu) {
-      double lo = l > 0 ? Mm[j - nq] : 0.0;
-      f = (s.kH * qe) * (cl1[l] * lo - cl2[l] * Mm[j + nq]);
-      if (l == 0) f = f + Phip * S.df0[q];
-      if (l == 1) f = f - (1.0 / 3.0) * s.kH * eq_of<T>(S, sl, nq, q) * Psi * S.df0[q];
-    } else {
-      f = qe * s.kH * Mm[j - nq] - (lmnu + 1.0) * s.iHe * Mm[j];
+    if (i < m.iM) {
+      if (rsa) {
+        f = cst<T>(0.0);
+      } else if (i < m.iTp) {  // photon temperature
+        const int l = i;
+        if (l < lg) {
+          double lo = l > 0 ? u[l - 1] : 0.0;
+          f = s.kH * (cl1[l] * lo - cl2[l] * u[l + 1]);
+          if (l >= 1) f = f + s.tp * u[l];
+          if (l == 0) f = f - Phip;
+          if (l == 1) f = f + (1.0 / 3.0) * s.kH * Psi + s.tp * (vb / 3.0);
+          if (l == 2) f = f - s.tp * (Pi / 10.0);
+        } else {
+          f = s.kH * u[lg - 1] - ((lg + 1.0) * s.iHe - s.tp) * u[lg];
+        }
+      } else if (i < m.iN) {  // photon polarization
+        const int l = i - m.iTp;
+        const double* P = u + m.iTp;
+        if (l < lg) {
+          double lo = l > 0 ? P[l - 1] : 0.0;
+          f = s.kH * (cl1[l] * lo - cl2[l] * P[l + 1]) + s.tp * P[l];
+          if (l == 0) f = f - s.tp * (Pi / 2.0);
+          if (l == 2) f = f - s.tp * (Pi / 10.0);
+        } else {
+          f = s.kH * P[lg - 1] - ((lg + 1.0) * s.iHe - s.tp) * P[lg];
+        }
+      } else {  // massless neutrinos
+        const int l = i - m.iN;
+        const double* Nn = u + m.iN;
+        if (l < lnu) {
+          double lo = l > 0 ? Nn[l - 1] : 0.0;
+          f = s.kH * (cl1[l] * lo - cl2[l] * Nn[l + 1]);
+          if (l == 0) f = f - Phip;
+          if (l == 1) f = f + (1.0 / 3.0) * s.kH * Psi;
+        } else {
+          f = s.kH * Nn[lnu - 1] - (lnu + 1.0) * s.iHe * Nn[lnu];
+        }
+      }
+    } else if (i < m.iPhi) {  // massive neutrinos (MB 57)
+      const int j = i - m.iM;
+      const int l = j / nq, q = j - l * nq;
+      const double* Mm = u + m.iM;
+      T qe = qe_of<T>(S, sl, nq, q);
+      if (l < lmnu) {
+        double lo = l > 0 ? Mm[j - nq] : 0.0;
+        f = (s.kH * qe) * (cl1[l] * lo - cl2[l] * Mm[j + nq]);
+        if (l == 0) f = f + Phip * S.df0[q];
+        if (l == 1) f = f - (1.0 / 3.0) * s.kH * eq_of<T>(S, sl, nq, q) * Psi * S.df0[q];
+      } else {
+        f = qe * s.kH * Mm[j - nq] - (lmnu + 1.0) * s.iHe * Mm[j];
+      }
+    } else {  // metric and matter
+      const int r = i - m.iPhi;
+      const double v = u[m.iPhi + 2], delb = u[m.iPhi + 3];
+      if (r == 0) f = Phip;
+      else if (r == 1) f = s.kH * v - 3.0 * Phip;
+      else if (r == 2) f = -v - s.kH * Psi;
+      else if (r == 3) f = s.kH * vb - 3.0 * Phip;
+      else f = -vb - s.kH * (Psi + s.cs2 * delb) + s.tp * s.R * (3.0 * u[1] + vb);
     }
-    put<T>(out, out_d, m.iM + j, f);
-  }
-  // metric and matter
-  if (lane < 5) {
-    int i = m.iPhi + lane;
-    T f;
-    double del = u[m.iPhi + 1], v = u[m.iPhi + 2], delb = u[m.iPhi + 3];
-    if (lane == 0) f = Phip;
-    else if (lane == 1) f = s.kH * v - 3.0 * Phip;
-    else if (lane == 2) f = -v - s.kH * Psi;
-    else if (lane == 3) f = s.kH * vb - 3.0 * Phip;
-    else f = -vb - s.kH * (Psi + s.cs2 * delb) + s.tp * s.R * (3.0 * u[1] + vb);
     put<T>(out, out_d, i, f);
   }
-  (void)C;
   return rsa;
 }
 
@@ -766,18 +758,42 @@ __device__ void initial_state(const Mode& m, const Shared& S, double xi, double*
 }
 
 // --------------------------------------------------------------- driver ----
+// One CTA (kWarpsPerMode warps) integrates one mode.  Row-parallel work (the
+// right-hand sides, the stage combinations, the error norm, dense output) is
+// spread over all threads, so a mode's FP64 work is issued from every SM
+// sub-partition; the serial chain sweeps (factorisation and solves) run in
+// warp 0 with one lane per chain.
+constexpr int kWarpsPerMode = 4;
+constexpr int kThreads = 32 * kWarpsPerMode;
+
 // Cubic Hermite interpolation on [x0, x1] from (y0, f0, y1, f1) into u.
 __device__ __forceinline__ void hermite(int N, double x0, double x1, double xq, const double* y0, const double* f0,
-                                        const double* y1, const double* f1, double* u, int lane) {
+                                        const double* y1, const double* f1, double* u, int tid, int nth) {
   double hh = x1 - x0, t = (xq - x0) / hh, t2 = t * t, t3 = t2 * t;
   double h00 = 2.0 * t3 - 3.0 * t2 + 1.0, h10 = (t3 - 2.0 * t2 + t) * hh, h01 = -2.0 * t3 + 3.0 * t2,
          h11 = (t3 - t2) * hh;
-  for (int i = lane; i < N; i += 32) u[i] = h00 * y0[i] + h10 * f0[i] + h01 * y1[i] + h11 * f1[i];
-  __syncwarp();
+  for (int i = tid; i < N; i += nth) u[i] = h00 * y0[i] + h10 * f0[i] + h01 * y1[i] + h11 * f1[i];
+  __syncthreads();
+}
+
+__device__ __forceinline__ void copy_vec(int N, const double* src, double* dst, int tid, int nth) {
+  for (int i = tid; i < N; i += nth) dst[i] = src[i];
+}
+
+// Block sum of one value per thread (red: >= kWarpsPerMode doubles of smem).
+__device__ __forceinline__ double block_sum(double v, double* red, int tid) {
+  v = warp_sum(v);
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < kWarpsPerMode; ++w) t += red[w];
+  __syncthreads();
+  return t;
 }
 
 __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const SolverCfg& cfg, double* base,
-                          double* gscr, int lane) {
+                          double* gscr, int tid) {
+  const int nth = kThreads, lane = tid & 31, warp = tid >> 5;
   Mode m;
   m.C = cosmos + md.cosmo;
   m.k = md.k;
@@ -812,7 +828,8 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   S.cl2 = p; p += Lmax + 1;
   S.sc = p; p += kStages * kScal;
   S.sc_d = p; p += kScal;
-  S.misc = p;
+  S.misc = p;                 // [0..8] capacitance inverse, [16..23] block reductions, [24] flags
+  double* red = S.misc + 16;
   Scratch G;
   G.y = gscr;
   G.fx = gscr + N;
@@ -820,11 +837,11 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   G.yp = gscr + 8 * N;
   G.fp = gscr + 9 * N;
   // per-mode constants (perturbations.jl:164-166; background.jl:21-30)
-  for (int l = lane; l <= Lmax; l += 32) {
+  for (int l = tid; l <= Lmax; l += nth) {
     S.cl1[l] = double(l) / (2.0 * l + 1.0);
     S.cl2[l] = (l + 1.0) / (2.0 * l + 1.0);
   }
-  for (int q = lane; q < nq; q += 32) {
+  for (int q = tid; q < nq; q += nth) {
     double xq = C.qx[q];
     double lq = C.logqmin + (C.logqmax - C.logqmin) / 2.0 * (xq + 1.0);
     double qq = pow(10.0, lq);
@@ -835,12 +852,13 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     S.Aq[q] = 4.0 * M_PI * qq * qq * f0 / dxdq * C.qw[q];  // rho: Aq eps M0, sigma: Aq q^2/eps M2
     S.Bq[q] = 4.0 * M_PI * qq * qq * qq * f0 / dxdq * C.qw[q];
   }
-  __syncwarp();
+  __syncthreads();
   double x = C.x0;
   const double xend = md.xout[md.nout - 1];
-  initial_state(m, S, x, S.yt, lane);
-  for (int i = lane; i < N; i += 32) G.y[i] = S.yt[i];
-  __syncwarp();
+  if (warp == 0) initial_state(m, S, x, S.yt, lane);
+  __syncthreads();
+  copy_vec(N, S.yt, G.y, tid, nth);
+  __syncthreads();
   int status = ST_OK;
   bool rsa_any = false;
   long long nacc = 0, nrej = 0;
@@ -855,49 +873,49 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   const double rtol = cfg.reltol, atol = cfg.abstol;
   double xprev = x;
   bool have_prev = false;
-  double x_done = -1e300;  // last abscissa whose dense nodes were emitted
+  double x_done = -1e300;  // last abscissa whose outputs were emitted
   while (true) {
-    bool at_node = (jo < md.nout) && (md.xout[jo] == x);
     if (x >= xend) {
-      if (at_node || (dense_ok && have_prev && jo < md.nout)) {
-        prepare_other(m, S, x, lane);
+      const bool pend = (jo < md.nout);
+      if (pend) {
+        prepare_other(m, S, x, tid, nth);
         double* Kf = G.K + N;
-        for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
-        __syncwarp();
-        rhs_rows<double>(m, S, 5, S.yt, Kf, nullptr, lane);
-        __syncwarp();
+        copy_vec(N, G.y, S.yt, tid, nth);
+        __syncthreads();
+        rhs_rows<double>(m, S, 5, S.yt, Kf, nullptr, tid, nth);
+        __syncthreads();
         if (dense_ok && have_prev) {
-          // dense nodes strictly inside the last step
           while (jo < md.nout && md.xout[jo] < x) {
             double xq = md.xout[jo];
-            hermite(N, xprev, x, xq, G.yp, G.fp, G.y, Kf, S.yt, lane);
-            prepare_other(m, S, xq, lane);
-            rhs_rows<double>(m, S, 5, S.yt, G.K, nullptr, lane);
-            __syncwarp();
-            emit_sources(m, S, xq, S.yt, G.K, lane, md.src_T + jo, md.src_E + jo);
-            __syncwarp();
+            hermite(N, xprev, x, xq, G.yp, G.fp, G.y, Kf, S.yt, tid, nth);
+            prepare_other(m, S, xq, tid, nth);
+            rhs_rows<double>(m, S, 5, S.yt, G.K, nullptr, tid, nth);
+            __syncthreads();
+            if (warp == 0) emit_sources(m, S, xq, S.yt, G.K, lane, md.src_T + jo, md.src_E + jo);
+            __syncthreads();
             ++jo;
           }
-          prepare_other(m, S, x, lane);
-          for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
-          __syncwarp();
+          prepare_other(m, S, x, tid, nth);
+          copy_vec(N, G.y, S.yt, tid, nth);
+          __syncthreads();
         }
         if (jo < md.nout && md.xout[jo] == x) {
-          if (md.flags & MODE_SOURCES) emit_sources(m, S, x, S.yt, Kf, lane, md.src_T + jo, md.src_E + jo);
+          if ((md.flags & MODE_SOURCES) && warp == 0)
+            emit_sources(m, S, x, S.yt, Kf, lane, md.src_T + jo, md.src_E + jo);
           if (md.flags & MODE_TRAJ)
-            for (int i = lane; i < N; i += 32) md.traj[(size_t)jo * N + i] = G.y[i];
+            for (int i = tid; i < N; i += nth) md.traj[(size_t)jo * N + i] = G.y[i];
           ++jo;
         }
-        __syncwarp();
+        __syncthreads();
       }
       if (md.flags & MODE_PLIN) {
-        for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
-        __syncwarp();
-        emit_plin(m, S, x, S.yt, lane, md.plin);
+        copy_vec(N, G.y, S.yt, tid, nth);
+        __syncthreads();
+        if (warp == 0) emit_plin(m, S, x, S.yt, lane, md.plin);
       }
       break;
     }
-    // next landing target: the next node at or above x_dense (or the end)
+    // next landing target: the first node at or above x_dense strictly past x
     int jt = max(jo, jd);
     while (jt < md.nout && md.xout[jt] <= x) ++jt;
     double target = jt < md.nout ? md.xout[jt] : xend;
@@ -906,105 +924,105 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     if (x + hs >= target - 1e-14 * fabs(target)) { hs = target - x; landing = true; }
     if (!(hs > 0.0)) { status = ST_DT_UNDERFLOW; break; }
     const double xn = landing ? target : x + hs;
-    prepare_stages(m, S, x, hs, xn, lane);
-    if (!factorize(m, S, hs * rodas::kGamma, lane)) { status = ST_LU_FAIL; break; }
-    // stage 1: f and df/dx at (x, y) into K0 / fx
-    double* K0 = G.K;
-    for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
-    __syncwarp();
-    bool r = rhs_rows<dd>(m, S, 0, S.yt, S.b, G.fx, lane);
+    prepare_stages(m, S, x, hs, xn, tid, nth);
+    if (warp == 0) {
+      bool ok = factorize(m, S, hs * rodas::kGamma, lane);
+      if (lane == 0) S.misc[24] = ok ? 1.0 : 0.0;
+    }
+    // stage 1: f and df/dx at (x, y) into b / fx
+    copy_vec(N, G.y, S.yt, tid, nth);
+    __syncthreads();
+    if (S.misc[24] == 0.0) { status = ST_LU_FAIL; break; }
+    bool r = rhs_rows<dd>(m, S, 0, S.yt, S.b, G.fx, tid, nth);
     rsa_any |= r;
-    __syncwarp();
+    __syncthreads();
+    double* K0 = G.K;
     if (x != x_done) {
       // outputs that fall on this abscissa or inside the last accepted step
       if (dense_ok && have_prev && jo < jd) {
-        for (int i = lane; i < N; i += 32) K0[i] = S.b[i];  // f at x, kept while interpolating
-        __syncwarp();
+        copy_vec(N, S.b, K0, tid, nth);  // f at x, kept while interpolating
+        __syncthreads();
         while (jo < md.nout && md.xout[jo] < x) {
           double xq = md.xout[jo];
-          hermite(N, xprev, x, xq, G.yp, G.fp, G.y, K0, S.yt, lane);
-          prepare_other(m, S, xq, lane);
-          rhs_rows<double>(m, S, 5, S.yt, G.K + N, nullptr, lane);
-          __syncwarp();
-          emit_sources(m, S, xq, S.yt, G.K + N, lane, md.src_T + jo, md.src_E + jo);
-          __syncwarp();
+          hermite(N, xprev, x, xq, G.yp, G.fp, G.y, K0, S.yt, tid, nth);
+          prepare_other(m, S, xq, tid, nth);
+          rhs_rows<double>(m, S, 5, S.yt, G.K + N, nullptr, tid, nth);
+          __syncthreads();
+          if (warp == 0) emit_sources(m, S, xq, S.yt, G.K + N, lane, md.src_T + jo, md.src_E + jo);
+          __syncthreads();
           ++jo;
         }
-        for (int i = lane; i < N; i += 32) S.yt[i] = G.y[i];
-        __syncwarp();
+        copy_vec(N, G.y, S.yt, tid, nth);
+        __syncthreads();
       }
       if (jo < md.nout && md.xout[jo] == x) {
-        if (md.flags & MODE_SOURCES) emit_sources(m, S, x, S.yt, S.b, lane, md.src_T + jo, md.src_E + jo);
+        if ((md.flags & MODE_SOURCES) && warp == 0)
+          emit_sources(m, S, x, S.yt, S.b, lane, md.src_T + jo, md.src_E + jo);
         if (md.flags & MODE_TRAJ)
-          for (int i = lane; i < N; i += 32) md.traj[(size_t)jo * N + i] = G.y[i];
+          for (int i = tid; i < N; i += nth) md.traj[(size_t)jo * N + i] = G.y[i];
         ++jo;
-        __syncwarp();
       }
       if (dense_ok) {
-        for (int i = lane; i < N; i += 32) { G.yp[i] = G.y[i]; G.fp[i] = S.b[i]; }
+        for (int i = tid; i < N; i += nth) { G.yp[i] = G.y[i]; G.fp[i] = S.b[i]; }
         xprev = x;
         have_prev = true;
       }
       x_done = x;
-      __syncwarp();
+      __syncthreads();
     }
     const double ih = 1.0 / hs;
-    for (int i = lane; i < N; i += 32) S.b[i] += hs * rodas::kD[0] * G.fx[i];
-    __syncwarp();
-    wsolve(m, S, S.b, lane);
-    for (int i = lane; i < N; i += 32) K0[i] = S.b[i];
-    __syncwarp();
+    for (int i = tid; i < N; i += nth) S.b[i] += hs * rodas::kD[0] * G.fx[i];
+    __syncthreads();
+    if (warp == 0) wsolve(m, S, S.b, lane);
+    __syncthreads();
+    copy_vec(N, S.b, K0, tid, nth);
     for (int st = 1; st < 6; ++st) {
       // stage state
       if (st < 5) {
-#pragma unroll 2
-        for (int i = lane; i < N; i += 32) {
+        for (int i = tid; i < N; i += nth) {
           double acc = G.y[i];
           for (int j = 0; j < st; ++j) acc += rodas::kA[st - 1][j] * G.K[j * N + i];
           S.yt[i] = acc;
         }
       } else {
-        for (int i = lane; i < N; i += 32) S.yt[i] += G.K[4 * N + i];
+        for (int i = tid; i < N; i += nth) S.yt[i] += G.K[4 * N + i];
       }
-      __syncwarp();
+      __syncthreads();
       const int sl = st < 4 ? st : 4;
-      r = rhs_rows<double>(m, S, sl, S.yt, S.b, nullptr, lane);
+      r = rhs_rows<double>(m, S, sl, S.yt, S.b, nullptr, tid, nth);
       rsa_any |= r;
-      __syncwarp();
+      // each thread combines the rows it produced (same row assignment)
       const double hd = hs * rodas::kD[st];
-#pragma unroll 2
-      for (int i = lane; i < N; i += 32) {
+      for (int i = tid; i < N; i += nth) {
         double acc = S.b[i];
         if (st < 4) acc += hd * G.fx[i];
         double cs = 0.0;
         for (int j = 0; j < st; ++j) cs += rodas::kC[st][j] * G.K[j * N + i];
         S.b[i] = acc + ih * cs;
       }
-      __syncwarp();
-      wsolve(m, S, S.b, lane);
-      if (st < 5) {
-        for (int i = lane; i < N; i += 32) G.K[st * N + i] = S.b[i];
-        __syncwarp();
-      }
+      __syncthreads();
+      if (warp == 0) wsolve(m, S, S.b, lane);
+      __syncthreads();
+      if (st < 5) copy_vec(N, S.b, G.K + st * N, tid, nth);
     }
     // error estimate: the last stage increment (in b)
     double en = 0.0;
     bool fin = true;
-    for (int i = lane; i < N; i += 32) {
+    for (int i = tid; i < N; i += nth) {
       double yn = S.yt[i] + S.b[i];
       double sc = atol + rtol * fmax(fabs(G.y[i]), fabs(yn));
       double e = S.b[i] / sc;
       en += e * e;
       fin = fin && isfinite(yn);
     }
-    en = sqrt(warp_sum(en) / N);
-    fin = __all_sync(0xffffffffu, fin);
+    en = sqrt(block_sum(en, red, tid) / N);
+    fin = __syncthreads_and(fin);
     if (!fin || !(en == en)) en = 1e10;
     double fac = 0.9 * pow(fmax(en, 1e-12), -0.25);
     fac = fmin(6.0, fmax(0.2, fac));
     if (en <= 1.0) {
-      for (int i = lane; i < N; i += 32) G.y[i] = S.yt[i] + S.b[i];
-      __syncwarp();
+      for (int i = tid; i < N; i += nth) G.y[i] = S.yt[i] + S.b[i];
+      __syncthreads();
       x = xn;
       ++nacc;
       double hp = hs * fac;
@@ -1016,57 +1034,58 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     }
     if (nacc + nrej > cfg.max_steps) { status = ST_MAXITERS; break; }
   }
-  if (lane == 0) {
+  if (tid == 0) {
     *md.status = status | (rsa_any ? ST_RSA_FIRED : 0);
     if (md.counters) { md.counters[0] = nacc; md.counters[1] = nrej; }
   }
 }
 
-__global__ void __launch_bounds__(256) rodas_kernel(const ModeDev* __restrict__ modes, int nmodes,
-                                                    const CosmoDev* __restrict__ cosmos, SolverCfg cfg,
-                                                    int* __restrict__ queue, int per_warp, double* __restrict__ scratch,
-                                                    int scr_per_warp) {
+// Persistent CTAs: the first wave takes modes blockIdx.x (modes arrive sorted
+// by decreasing cost, and consecutive blocks land on different SMs, so the
+// longest modes spread one per SM); later modes come from a device queue.
+__global__ void __launch_bounds__(kThreads) rodas_kernel(const ModeDev* __restrict__ modes, int nmodes,
+                                                         const CosmoDev* __restrict__ cosmos, SolverCfg cfg,
+                                                         int* __restrict__ queue, int per_mode,
+                                                         double* __restrict__ scratch, int scr_per_mode) {
   extern __shared__ double smem[];
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
-  double* base = smem + (size_t)w * per_warp;
-  double* gscr = scratch + ((size_t)blockIdx.x * (blockDim.x >> 5) + w) * scr_per_warp;
-  while (true) {
-    int mi = 0;
-    if (lane == 0) mi = atomicAdd(queue, 1);
-    mi = __shfl_sync(0xffffffffu, mi, 0);
-    if (mi >= nmodes) break;
-    solve_one(modes[mi], cosmos, cfg, base, gscr, lane);
-    __syncwarp();
+  __shared__ int s_mode;
+  const int tid = threadIdx.x;
+  double* gscr = scratch + (size_t)blockIdx.x * scr_per_mode;
+  int mi = blockIdx.x;
+  while (mi < nmodes) {
+    solve_one(modes[mi], cosmos, cfg, smem, gscr, tid);
+    __syncthreads();
+    if (tid == 0) s_mode = gridDim.x + atomicAdd(queue, 1);
+    __syncthreads();
+    mi = s_mode;
   }
 }
 
-// Host launcher: grid size (in warps) for the scratch allocation.
-int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int warps_per_block, int* blocks) {
-  int per_warp = per_warp_doubles(maxN, maxnq, maxL);
-  size_t smem = size_t(per_warp) * warps_per_block * sizeof(double);
+// Host helpers: CTAs to launch (one mode each at a time).
+int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int /*unused*/, int* blocks) {
+  int per_mode = per_warp_doubles(maxN, maxnq, maxL);
+  size_t smem = size_t(per_mode) * sizeof(double);
   cudaError_t e = cudaFuncSetAttribute(rodas_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return -int(e);
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int bps = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, rodas_kernel, 32 * warps_per_block, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, rodas_kernel, kThreads, smem);
   if (e != cudaSuccess) return -int(e);
   if (bps < 1) return -int(cudaErrorInvalidConfiguration);
-  int want = (nmodes + warps_per_block - 1) / warps_per_block;
-  *blocks = std::min(want, nsm * bps);
+  *blocks = std::min(nmodes, nsm * bps);
   return 0;
 }
 
 int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
-                 int maxN, int maxnq, int maxL, int warps_per_block, int blocks, double* d_scratch, cudaStream_t stream) {
-  int per_warp = per_warp_doubles(maxN, maxnq, maxL);
-  size_t smem = size_t(per_warp) * warps_per_block * sizeof(double);
+                 int maxN, int maxnq, int maxL, int /*unused*/, int blocks, double* d_scratch, cudaStream_t stream) {
+  int per_mode = per_warp_doubles(maxN, maxnq, maxL);
+  size_t smem = size_t(per_mode) * sizeof(double);
   cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  rodas_kernel<<<blocks, 32 * warps_per_block, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, per_warp,
-                                                                d_scratch, scratch_per_warp(maxN));
+  rodas_kernel<<<blocks, kThreads, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, per_mode, d_scratch,
+                                                   scratch_per_warp(maxN));
   return cudaGetLastError();
 }
 
@@ -1074,5 +1093,6 @@ size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL) {
   return size_t(per_warp_doubles(maxN, maxnq, maxL)) * sizeof(double);
 }
 size_t rodas_scratch_per_warp(int maxN) { return size_t(scratch_per_warp(maxN)) * sizeof(double); }
+int rodas_warps_per_mode() { return kWarpsPerMode; }
 
 }  // namespace bolt
