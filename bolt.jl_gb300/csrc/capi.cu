@@ -650,3 +650,12 @@ int bolt_last_stats(bolt_ctx* c, int64_t* out) {
 }
 
 }  // extern "C"
+
+#ifdef BOLT_PHASE_TIMERS
+namespace bolt {
+int rodas_phase_cycles(unsigned long long* out, bool reset);
+}
+extern "C" int bolt_debug_phase_cycles(unsigned long long* out, int reset) {
+  return bolt::rodas_phase_cycles(out, reset != 0);
+}
+#endif

@@ -758,6 +758,20 @@ __device__ void initial_state(const Mode& m, const Shared& S, double xi, double*
 }
 
 // --------------------------------------------------------------- driver ----
+// Optional per-phase cycle counters (compile with -DBOLT_PHASE_TIMERS): thread
+// 0 accumulates clock64() deltas between phase boundaries, which include the
+// barrier waits, i.e. the CTA's critical path per phase.
+#ifdef BOLT_PHASE_TIMERS
+__device__ unsigned long long g_phase_cycles[16];
+#define PT_DECL long long pt_last_ = clock64(); long long pt_acc_[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+#define PT(k) if (tid == 0) { long long n_ = clock64(); pt_acc_[k] += n_ - pt_last_; pt_last_ = n_; }
+#define PT_FLUSH if (tid == 0) for (int i_ = 0; i_ < 12; ++i_) atomicAdd(&g_phase_cycles[i_], (unsigned long long)pt_acc_[i_]);
+#else
+#define PT_DECL
+#define PT(k)
+#define PT_FLUSH
+#endif
+
 // One CTA (kWarpsPerMode warps) integrates one mode.  Row-parallel work (the
 // right-hand sides, the stage combinations, the error norm, dense output) is
 // spread over all threads, so a mode's FP64 work is issued from every SM
@@ -874,6 +888,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   double xprev = x;
   bool have_prev = false;
   double x_done = -1e300;  // last abscissa whose outputs were emitted
+  PT_DECL
   while (true) {
     if (x >= xend) {
       const bool pend = (jo < md.nout);
@@ -924,7 +939,9 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     if (x + hs >= target - 1e-14 * fabs(target)) { hs = target - x; landing = true; }
     if (!(hs > 0.0)) { status = ST_DT_UNDERFLOW; break; }
     const double xn = landing ? target : x + hs;
+    PT(9)
     prepare_stages(m, S, x, hs, xn, tid, nth);
+    PT(0)
     if (warp == 0) {
       bool ok = factorize(m, S, hs * rodas::kGamma, lane);
       if (lane == 0) S.misc[24] = ok ? 1.0 : 0.0;
@@ -933,9 +950,11 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     copy_vec(N, G.y, S.yt, tid, nth);
     __syncthreads();
     if (S.misc[24] == 0.0) { status = ST_LU_FAIL; break; }
+    PT(1)
     bool r = rhs_rows<dd>(m, S, 0, S.yt, S.b, G.fx, tid, nth);
     rsa_any |= r;
     __syncthreads();
+    PT(2)
     double* K0 = G.K;
     if (x != x_done) {
       // outputs that fall on this abscissa or inside the last accepted step
@@ -970,12 +989,14 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       x_done = x;
       __syncthreads();
     }
+    PT(3)
     const double ih = 1.0 / hs;
     for (int i = tid; i < N; i += nth) S.b[i] += hs * rodas::kD[0] * G.fx[i];
     __syncthreads();
     if (warp == 0) wsolve(m, S, S.b, lane);
     __syncthreads();
     copy_vec(N, S.b, K0, tid, nth);
+    PT(4)
     for (int st = 1; st < 6; ++st) {
       // stage state
       if (st < 5) {
@@ -988,6 +1009,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
         for (int i = tid; i < N; i += nth) S.yt[i] += G.K[4 * N + i];
       }
       __syncthreads();
+      PT(5)
       const int sl = st < 4 ? st : 4;
       r = rhs_rows<double>(m, S, sl, S.yt, S.b, nullptr, tid, nth);
       rsa_any |= r;
@@ -1001,9 +1023,11 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
         S.b[i] = acc + ih * cs;
       }
       __syncthreads();
+      PT(6)
       if (warp == 0) wsolve(m, S, S.b, lane);
       __syncthreads();
       if (st < 5) copy_vec(N, S.b, G.K + st * N, tid, nth);
+      PT(7)
     }
     // error estimate: the last stage increment (in b)
     double en = 0.0;
@@ -1033,7 +1057,9 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       if (!(h >= 1e-14 * fmax(1.0, fabs(x)))) { status = fin ? ST_DT_UNDERFLOW : ST_NONFINITE; break; }
     }
     if (nacc + nrej > cfg.max_steps) { status = ST_MAXITERS; break; }
+    PT(8)
   }
+  PT_FLUSH
   if (tid == 0) {
     *md.status = status | (rsa_any ? ST_RSA_FIRED : 0);
     if (md.counters) { md.counters[0] = nacc; md.counters[1] = nrej; }
@@ -1093,6 +1119,17 @@ size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL) {
   return size_t(per_warp_doubles(maxN, maxnq, maxL)) * sizeof(double);
 }
 size_t rodas_scratch_per_warp(int maxN) { return size_t(scratch_per_warp(maxN)) * sizeof(double); }
+
+#ifdef BOLT_PHASE_TIMERS
+int rodas_phase_cycles(unsigned long long* out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(unsigned long long) * 16);
+  if (reset) {
+    unsigned long long z[16] = {0};
+    cudaMemcpyToSymbol(g_phase_cycles, z, sizeof(z));
+  }
+  return int(e);
+}
+#endif
 int rodas_warps_per_mode() { return kWarpsPerMode; }
 
 }  // namespace bolt
