@@ -77,10 +77,13 @@ struct Scratch {
   double *y, *fx, *K, *yp, *fp;  // K: 6 x N
 };
 
+constexpr int kMiscDoubles = 32 + 9 * 32;        // capacitance, reductions, per-chain partials
+constexpr int kPackInts = 128 * 2 + 128 * 8 + 32 + 2;  // lane packing of the chains (chains.cuh)
+
 __host__ __device__ inline int per_warp_doubles(int N, int nq, int Lmax) {
   int nch = nq + 5;
   return 5 * N + 4 * nq + 2 * kStages * nq + 2 * nq + 2 * nch * kTail * kBorder + 2 * (Lmax + 1) + kStages * kScal +
-         kScal + 32;
+         kScal + kMiscDoubles + (kPackInts + 1) / 2;
 }
 __host__ __device__ inline int scratch_per_warp(int N) { return 10 * N; }
 
@@ -352,284 +355,6 @@ __device__ __forceinline__ int tail_slots(const Mode& m, int c) {
   return 1;
 }
 
-// Factor M = I/(h gamma) - L chain by chain (lane c), build the border tails
-// and the 3x3 capacitance inverse.  Returns false on a zero or non-finite
-// pivot.
-__device__ bool factorize(const Mode& m, const Shared& S, double hg, int lane) {
-  const CosmoDev& C = *m.C;
-  const Scal<double> s = get_scal<double>(S, 0);
-  const double ig = 1.0 / hg;
-  const double* cl1 = S.cl1;
-  const double* cl2 = S.cl2;
-  const double Omega_nu = C.Omega_nu;
-  bool ok = true;
-  double cap[9];
-  for (int r = 0; r < 9; ++r) cap[r] = 0.0;
-  for (int c = lane; c < m.nch; c += 32) {
-    double U[kTail][kBorder], Wv[kTail][kBorder];
-    for (int a = 0; a < kTail; ++a)
-      for (int b = 0; b < kBorder; ++b) { U[a][b] = 0.0; Wv[a][b] = 0.0; }
-    double lb = 0.0;  // Theta_1 <- v_b multiplier (chain 0)
-    if (c <= 2 || c < 3 + m.nq) {
-      // multipole chain
-      int L, base, stride;
-      double mu = 1.0, dtop;
-      bool photon = c <= 1;
-      if (c == 0) { L = m.lg; base = 0; stride = 1; }
-      else if (c == 1) { L = m.lg; base = m.iTp; stride = 1; }
-      else if (c == 2) { L = m.lnu; base = m.iN; stride = 1; }
-      else { L = m.lmnu; base = m.iM + (c - 3); stride = m.nq; mu = S.qe[c - 3]; }
-      double mkH = mu * s.kH;
-      dtop = -(L + 1.0) * s.iHe + (photon ? s.tp : 0.0);
-      // baryon pair first (chain 0): eliminate delta_b, then v_b
-      double piv_vb = 1.0, Mvb_T1 = 0.0;
-      if (c == 0) {
-        int idb = m.iPhi + 3, ivb = m.iPhi + 4;
-        double Mdb_vb = -s.kH;                         // M[db][vb]
-        double Mvb_db = s.kH * s.cs2;                  // M[vb][db]
-        double dvb = ig + 1.0 - s.tp * s.R;            // M[vb][vb]
-        Mvb_T1 = -3.0 * s.tp * s.R;                    // M[vb][Theta1]
-        double ipdb = hg;                              // 1 / ig
-        double l_vb = Mvb_db * ipdb;
-        piv_vb = dvb - l_vb * Mdb_vb;
-        double ipvb = 1.0 / piv_vb;
-        S.fl[ivb] = l_vb; S.fi[ivb] = ipvb; S.fc[ivb] = Mvb_T1 * ipvb;
-        S.fi[idb] = ipdb; S.fc[idb] = Mdb_vb * ipdb;
-        double MT1_vb = -s.tp / 3.0;                   // M[Theta1][vb]
-        lb = MT1_vb * ipvb;
-        S.fl[idb] = lb;
-        ok = ok && isfinite(ipvb) && piv_vb != 0.0;
-      }
-      // top element
-      double piv = ig - dtop, ipiv = 1.0 / piv;
-      double cprev = -mkH;  // M[L][L-1]
-      int iL = base + L * stride;
-      S.fl[iL] = 0.0; S.fi[iL] = ipiv; S.fc[iL] = cprev * ipiv;
-      ok = ok && isfinite(ipiv);
-      for (int l = L - 1; l >= 0; --l) {
-        int i = base + l * stride;
-        double a = mkH * cl2[l];             // M[l][l+1]
-        double lm = a * ipiv;
-        double dl = photon ? ((c == 0 && l == 0) ? 0.0 : s.tp) : 0.0;
-        double pv = ig - dl - lm * cprev;
-        if (c == 0 && l == 1) pv -= lb * Mvb_T1;
-        ipiv = 1.0 / pv;
-        double cl = l >= 1 ? -mkH * cl1[l] : 0.0;  // M[l][l-1]
-        S.fl[i] = lm; S.fi[i] = ipiv; S.fc[i] = cl * ipiv;
-        cprev = cl;
-        ok = ok && isfinite(ipiv) && pv != 0.0;
-      }
-      // border tails: U (coefficients of Phi', Psi, Pi) and W (gradients)
-      if (c == 0) {
-        U[0][0] = -1.0; U[1][1] = s.kH / 3.0; U[2][2] = -s.tp / 10.0; U[3][1] = -s.kH; U[4][0] = -3.0;
-        double ia = 1.0 / s.a;
-        Wv[0][0] = s.dphi * 4.0 * C.Omega_r * ia * ia;
-        Wv[2][1] = -s.cpsi * C.Omega_r; Wv[2][0] = Wv[2][1]; Wv[2][2] = 1.0;
-        Wv[4][0] = s.dphi * C.Omega_b * ia;
-      } else if (c == 1) {
-        U[0][2] = -s.tp / 2.0; U[2][2] = -s.tp / 10.0;
-        Wv[0][2] = 1.0; Wv[2][2] = 1.0;
-      } else if (c == 2) {
-        U[0][0] = -1.0; U[1][1] = s.kH / 3.0;
-        double ia = 1.0 / s.a;
-        Wv[0][0] = s.dphi * 4.0 * Omega_nu * ia * ia;
-        Wv[2][1] = -s.cpsi * Omega_nu; Wv[2][0] = Wv[2][1];
-      } else {
-        int q = c - 3;
-        U[0][0] = S.df0[q]; U[1][1] = -s.kH / 3.0 * S.eq[q] * S.df0[q];
-        double qq = S.q[q], ia = 1.0 / s.a;
-        Wv[0][0] = s.dphi * S.Aq[q] * qq * S.eq[q] * ia * ia / C.rho_crit;
-        Wv[2][1] = -s.cpsi * S.Aq[q] * qq * S.qe[q] * 0.25 / C.rho_crit; Wv[2][0] = Wv[2][1];
-      }
-    } else if (c == 3 + m.nq) {
-      // CDM pair: eliminate v then delta
-      int idl = m.iPhi + 1, iv = m.iPhi + 2;
-      double ipv = 1.0 / (ig + 1.0);
-      double l_d = -s.kH * ipv;  // M[delta][v] / piv_v
-      S.fl[iv] = 0.0; S.fi[iv] = ipv; S.fc[iv] = 0.0;
-      S.fl[idl] = l_d; S.fi[idl] = hg; S.fc[idl] = 0.0;
-      U[0][0] = -3.0; U[1][1] = -s.kH;
-      Wv[0][0] = s.dphi * C.Omega_c / s.a;
-    } else {
-      S.fl[m.iPhi] = 0.0; S.fi[m.iPhi] = hg; S.fc[m.iPhi] = 0.0;
-      U[0][0] = 1.0;
-      Wv[0][1] = -1.0; Wv[0][0] = -1.0 - s.k2H2;
-    }
-    // forward sweep of the U columns over the tail (U vanishes above l = 2)
-    double Uf[kTail][kBorder];
-    for (int b = 0; b < kBorder; ++b) {
-      if (c < 3 + m.nq) {
-        int i0 = tail_index(m, c, 0), i1 = tail_index(m, c, 1);
-        double u2 = U[2][b];
-        double u1 = U[1][b] - S.fl[i1] * u2;
-        if (c == 0) {
-          double udb = U[4][b];
-          double uvb = U[3][b] - S.fl[m.iPhi + 4] * udb;
-          u1 -= lb * uvb;
-          Uf[3][b] = uvb; Uf[4][b] = udb;
-        } else { Uf[3][b] = 0.0; Uf[4][b] = 0.0; }
-        double u0 = U[0][b] - S.fl[i0] * u1;
-        Uf[0][b] = u0; Uf[1][b] = u1; Uf[2][b] = u2;
-      } else if (c == 3 + m.nq) {
-        double uv = U[1][b];
-        double ud = U[0][b] - S.fl[m.iPhi + 1] * uv;
-        Uf[0][b] = ud; Uf[1][b] = uv; Uf[2][b] = Uf[3][b] = Uf[4][b] = 0.0;
-      } else {
-        Uf[0][b] = U[0][b]; Uf[1][b] = Uf[2][b] = Uf[3][b] = Uf[4][b] = 0.0;
-      }
-    }
-    // partial back substitution of each forward-swept column -> M^{-1} U at
-    // the tail; accumulate W^T M^{-1} U
-    for (int b = 0; b < kBorder; ++b) {
-      double xs[kTail];
-      if (c < 3 + m.nq) {
-        int i0 = tail_index(m, c, 0), i1 = tail_index(m, c, 1), i2 = tail_index(m, c, 2);
-        xs[0] = Uf[0][b] * S.fi[i0];
-        xs[1] = Uf[1][b] * S.fi[i1] - S.fc[i1] * xs[0];
-        xs[2] = Uf[2][b] * S.fi[i2] - S.fc[i2] * xs[1];
-        if (c == 0) {
-          int ivb = m.iPhi + 4, idb = m.iPhi + 3;
-          xs[3] = Uf[3][b] * S.fi[ivb] - S.fc[ivb] * xs[1];
-          xs[4] = Uf[4][b] * S.fi[idb] - S.fc[idb] * xs[3];
-        } else { xs[3] = xs[4] = 0.0; }
-      } else if (c == 3 + m.nq) {
-        xs[0] = Uf[0][b] * S.fi[m.iPhi + 1];
-        xs[1] = Uf[1][b] * S.fi[m.iPhi + 2];
-        xs[2] = xs[3] = xs[4] = 0.0;
-      } else {
-        xs[0] = Uf[0][b] * S.fi[m.iPhi];
-        xs[1] = xs[2] = xs[3] = xs[4] = 0.0;
-      }
-      for (int r = 0; r < kBorder; ++r) {
-        double acc = 0.0;
-        for (int a = 0; a < kTail; ++a) acc += Wv[a][r] * xs[a];
-        cap[r * 3 + b] += acc;
-      }
-    }
-    double* uf = S.Uf + c * kTail * kBorder;
-    double* wt = S.Wt + c * kTail * kBorder;
-    for (int a = 0; a < kTail; ++a)
-      for (int b = 0; b < kBorder; ++b) { uf[a * kBorder + b] = Uf[a][b]; wt[a * kBorder + b] = Wv[a][b]; }
-  }
-  for (int r = 0; r < 9; ++r) cap[r] = warp_sum(cap[r]);
-  ok = __all_sync(0xffffffffu, ok);
-  // C = I - W^T M^{-1} U ; store its inverse in misc[0..8]
-  double Cm[9];
-  for (int r = 0; r < 9; ++r) Cm[r] = ((r % 4) == 0 ? 1.0 : 0.0) - cap[r];
-  double det = Cm[0] * (Cm[4] * Cm[8] - Cm[5] * Cm[7]) - Cm[1] * (Cm[3] * Cm[8] - Cm[5] * Cm[6]) +
-               Cm[2] * (Cm[3] * Cm[7] - Cm[4] * Cm[6]);
-  double id = 1.0 / det;
-  if (lane == 0) {
-    S.misc[0] = (Cm[4] * Cm[8] - Cm[5] * Cm[7]) * id;
-    S.misc[1] = (Cm[2] * Cm[7] - Cm[1] * Cm[8]) * id;
-    S.misc[2] = (Cm[1] * Cm[5] - Cm[2] * Cm[4]) * id;
-    S.misc[3] = (Cm[5] * Cm[6] - Cm[3] * Cm[8]) * id;
-    S.misc[4] = (Cm[0] * Cm[8] - Cm[2] * Cm[6]) * id;
-    S.misc[5] = (Cm[2] * Cm[3] - Cm[0] * Cm[5]) * id;
-    S.misc[6] = (Cm[3] * Cm[7] - Cm[4] * Cm[6]) * id;
-    S.misc[7] = (Cm[1] * Cm[6] - Cm[0] * Cm[7]) * id;
-    S.misc[8] = (Cm[0] * Cm[4] - Cm[1] * Cm[3]) * id;
-  }
-  __syncwarp();
-  return ok && isfinite(id) && det != 0.0;
-}
-
-// In-place solve b <- (M - U W^T)^{-1} b.
-__device__ void wsolve(const Mode& m, const Shared& S, double* b, int lane) {
-  double t[kBorder] = {0.0, 0.0, 0.0};
-  double xt[kTail];
-  int c = lane;
-  bool active = c < m.nch;  // nch <= 32 is enforced on the host
-  if (active) {
-    if (c < 3 + m.nq) {
-      int L, base, stride;
-      if (c == 0) { L = m.lg; base = 0; stride = 1; }
-      else if (c == 1) { L = m.lg; base = m.iTp; stride = 1; }
-      else if (c == 2) { L = m.lnu; base = m.iN; stride = 1; }
-      else { L = m.lmnu; base = m.iM + (c - 3); stride = m.nq; }
-      double bvb = 0.0, bdb = 0.0;
-      if (c == 0) {
-        bdb = b[m.iPhi + 3];
-        bvb = b[m.iPhi + 4] - S.fl[m.iPhi + 4] * bdb;
-      }
-      double prev = b[base + L * stride];
-      for (int l = L - 1; l >= 0; --l) {
-        int i = base + l * stride;
-        double v = b[i] - S.fl[i] * prev;
-        if (c == 0 && l == 1) v -= S.fl[m.iPhi + 3] * bvb;  // lb * b'_vb
-        b[i] = v;
-        prev = v;
-      }
-      if (c == 0) { b[m.iPhi + 4] = bvb; b[m.iPhi + 3] = bdb; }
-    } else if (c == 3 + m.nq) {
-      b[m.iPhi + 1] -= S.fl[m.iPhi + 1] * b[m.iPhi + 2];
-    }
-    // partial back substitution on the tail
-    int ns = tail_slots(m, c);
-    if (c < 3 + m.nq) {
-      int i0 = tail_index(m, c, 0), i1 = tail_index(m, c, 1), i2 = tail_index(m, c, 2);
-      xt[0] = b[i0] * S.fi[i0];
-      xt[1] = b[i1] * S.fi[i1] - S.fc[i1] * xt[0];
-      xt[2] = b[i2] * S.fi[i2] - S.fc[i2] * xt[1];
-      if (c == 0) {
-        int ivb = m.iPhi + 4, idb = m.iPhi + 3;
-        xt[3] = b[ivb] * S.fi[ivb] - S.fc[ivb] * xt[1];
-        xt[4] = b[idb] * S.fi[idb] - S.fc[idb] * xt[3];
-      }
-    } else if (c == 3 + m.nq) {
-      xt[0] = b[m.iPhi + 1] * S.fi[m.iPhi + 1];
-      xt[1] = b[m.iPhi + 2] * S.fi[m.iPhi + 2];
-    } else {
-      xt[0] = b[m.iPhi] * S.fi[m.iPhi];
-    }
-    const double* wt = S.Wt + c * kTail * kBorder;
-    for (int a = 0; a < ns; ++a)
-      for (int r = 0; r < kBorder; ++r) t[r] += wt[a * kBorder + r] * xt[a];
-  }
-  for (int r = 0; r < kBorder; ++r) t[r] = warp_sum(t[r]);
-  double sv[kBorder];
-  for (int r = 0; r < kBorder; ++r) sv[r] = S.misc[r * 3 + 0] * t[0] + S.misc[r * 3 + 1] * t[1] + S.misc[r * 3 + 2] * t[2];
-  if (active) {
-    // correct the forward-swept tail by the swept border columns, then
-    // complete the back substitution
-    const double* uf = S.Uf + c * kTail * kBorder;
-    int ns = tail_slots(m, c);
-    for (int a = 0; a < ns; ++a) {
-      int i = tail_index(m, c, a);
-      b[i] += uf[a * kBorder + 0] * sv[0] + uf[a * kBorder + 1] * sv[1] + uf[a * kBorder + 2] * sv[2];
-    }
-    if (c < 3 + m.nq) {
-      int L, base, stride;
-      if (c == 0) { L = m.lg; base = 0; stride = 1; }
-      else if (c == 1) { L = m.lg; base = m.iTp; stride = 1; }
-      else if (c == 2) { L = m.lnu; base = m.iN; stride = 1; }
-      else { L = m.lmnu; base = m.iM + (c - 3); stride = m.nq; }
-      double xp = b[base] * S.fi[base];
-      b[base] = xp;
-      double x1 = 0.0;
-      for (int l = 1; l <= L; ++l) {
-        int i = base + l * stride;
-        double v = b[i] * S.fi[i] - S.fc[i] * xp;
-        b[i] = v;
-        if (l == 1) x1 = v;
-        xp = v;
-      }
-      if (c == 0) {
-        int ivb = m.iPhi + 4, idb = m.iPhi + 3;
-        double xvb = b[ivb] * S.fi[ivb] - S.fc[ivb] * x1;
-        b[ivb] = xvb;
-        b[idb] = b[idb] * S.fi[idb] - S.fc[idb] * xvb;
-      }
-    } else if (c == 3 + m.nq) {
-      b[m.iPhi + 1] = b[m.iPhi + 1] * S.fi[m.iPhi + 1];
-      b[m.iPhi + 2] = b[m.iPhi + 2] * S.fi[m.iPhi + 2];
-    } else {
-      b[m.iPhi] = b[m.iPhi] * S.fi[m.iPhi];
-    }
-  }
-  __syncwarp();
-}
-
 // ------------------------------------------------------------- outputs ----
 // source_function and source_function_P (perturbations.jl:343-404) at a
 // grid node, from u and du = hierarchy!(u).
@@ -757,6 +482,8 @@ __device__ void initial_state(const Mode& m, const Shared& S, double xi, double*
   __syncwarp();
 }
 
+#include "chains.cuh"
+
 // --------------------------------------------------------------- driver ----
 // Optional per-phase cycle counters (compile with -DBOLT_PHASE_TIMERS): thread
 // 0 accumulates clock64() deltas between phase boundaries, which include the
@@ -842,8 +569,18 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   S.cl2 = p; p += Lmax + 1;
   S.sc = p; p += kStages * kScal;
   S.sc_d = p; p += kScal;
-  S.misc = p;                 // [0..8] capacitance inverse, [16..23] block reductions, [24] flags
+  S.misc = p;                 // [0..8] capacitance inverse, [16..23] block reductions, [24] flags, [32..] partials
+  p += kMiscDoubles;
   double* red = S.misc + 16;
+  Pack PK;
+  {
+    int* ip = reinterpret_cast<int*>(p);
+    PK.seg = ip; ip += 128;
+    PK.chain = ip; ip += 128;
+    PK.idx = ip; ip += 128 * kEmax;
+    PK.owner = ip; ip += 32;
+    PK.E = ip;
+  }
   Scratch G;
   G.y = gscr;
   G.fx = gscr + N;
@@ -866,9 +603,14 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     S.Aq[q] = 4.0 * M_PI * qq * qq * f0 / dxdq * C.qw[q];  // rho: Aq eps M0, sigma: Aq q^2/eps M2
     S.Bq[q] = 4.0 * M_PI * qq * qq * qq * f0 / dxdq * C.qw[q];
   }
+  if (tid == 0) S.misc[25] = build_pack(m, PK, nth) ? 1.0 : 0.0;
   __syncthreads();
   double x = C.x0;
   const double xend = md.xout[md.nout - 1];
+  if (S.misc[25] == 0.0) {
+    if (tid == 0) { *md.status = ST_BAD_INPUT; if (md.counters) { md.counters[0] = 0; md.counters[1] = 0; } }
+    return;
+  }
   if (warp == 0) initial_state(m, S, x, S.yt, lane);
   __syncthreads();
   copy_vec(N, S.yt, G.y, tid, nth);
@@ -942,14 +684,11 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     PT(9)
     prepare_stages(m, S, x, hs, xn, tid, nth);
     PT(0)
-    if (warp == 0) {
-      bool ok = factorize(m, S, hs * rodas::kGamma, lane);
-      if (lane == 0) S.misc[24] = ok ? 1.0 : 0.0;
-    }
+    const bool fok = factorize_scan(m, S, PK, hs * rodas::kGamma, tid, nth);
     // stage 1: f and df/dx at (x, y) into b / fx
     copy_vec(N, G.y, S.yt, tid, nth);
     __syncthreads();
-    if (S.misc[24] == 0.0) { status = ST_LU_FAIL; break; }
+    if (!fok) { status = ST_LU_FAIL; break; }
     PT(1)
     bool r = rhs_rows<dd>(m, S, 0, S.yt, S.b, G.fx, tid, nth);
     rsa_any |= r;
@@ -993,8 +732,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     const double ih = 1.0 / hs;
     for (int i = tid; i < N; i += nth) S.b[i] += hs * rodas::kD[0] * G.fx[i];
     __syncthreads();
-    if (warp == 0) wsolve(m, S, S.b, lane);
-    __syncthreads();
+    wsolve_scan(m, S, PK, S.b, tid, nth);
     copy_vec(N, S.b, K0, tid, nth);
     PT(4)
     for (int st = 1; st < 6; ++st) {
@@ -1024,8 +762,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       }
       __syncthreads();
       PT(6)
-      if (warp == 0) wsolve(m, S, S.b, lane);
-      __syncthreads();
+      wsolve_scan(m, S, PK, S.b, tid, nth);
       if (st < 5) copy_vec(N, S.b, G.K + st * N, tid, nth);
       PT(7)
     }
