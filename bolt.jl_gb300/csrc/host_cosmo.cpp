@@ -639,3 +639,8 @@ void finish_uploaded_tables(CosmoTables& T) {
 }
 
 }  // namespace bolt
+
+namespace bolt {
+// Gauss-Legendre nodes and weights on [-1, 1] (FastGaussQuadrature.gausslegendre).
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) { gauss_legendre_nodes(n, x, w); }
+}  // namespace bolt

@@ -77,6 +77,9 @@ double units_mass_eV();
 // Builds Background + RECFAST + IonizationHistory.  Throws std::runtime_error.
 void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const RecfastOpts& r, CosmoTables& out);
 
+// Gauss-Legendre nodes and weights on [-1, 1].
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);
+
 // Builds the remaining slots (re-splined derivatives) from caller-provided
 // node values of the primary tables: H, eta, rho0M, Xe, tau, g, Tmat, csb2.
 void finish_uploaded_tables(CosmoTables& t);

@@ -134,6 +134,26 @@ int bolt_set_dense_x(bolt_ctx* ctx, double x_dense);
  * [4] modes, [5] solver kernel launches, [6] total kernel launches. */
 int bolt_last_stats(bolt_ctx* ctx, int64_t* out);
 
+/* Allocation-free source grid (no counterpart in the reference; added for
+ * callers that cannot allocate device memory themselves, e.g. code running
+ * under another framework's allocator or a host that forbids cudaMalloc after
+ * start-up).  Same solver as bolt_source_grid, no context: inputs are host
+ * arrays (parameters, the grid, nodes[8][n] and scalars[3] as for
+ * bolt_cosmo_upload, k[nk]); outputs are caller-owned DEVICE buffers
+ * d_S_T[nk][n], d_S_E[nk][n], d_status[nk], written asynchronously on
+ * `stream` (a cudaStream_t, NULL = legacy default stream).  All other device
+ * memory comes from one fixed, file-scope device array (~14 MB, held by every
+ * GPU that loads the library until exit): N <= 512, nk <= 2048, n <= 4097,
+ * nq <= 27; larger calls are rejected with an error.  No cudaMalloc or cudaFree
+ * is called.  The first call on a device looks up the array's address (make
+ * it before any stream capture); calls that overlap on the GPU share the
+ * array and race, so serialise them.  Returns 0, or a negative code with the
+ * message in errbuf. */
+int bolt_source_grid_static(const bolt_params* par, const bolt_grid* grid, int nq, const double* nodes,
+                            const double* scalars, const double* k, int nk, const bolt_hier* hier, double reltol,
+                            double abstol, double* d_S_T, double* d_S_E, int32_t* d_status, void* stream,
+                            char* errbuf, int errlen);
+
 /* Measured FP64 FMA throughput of the device (TFLOP/s): the roofline
  * denominator for the FP64-pipe-bound kernels. */
 int bolt_fp64_peak(int device, double* tflops);
