@@ -40,7 +40,7 @@ METRIC = "Cℓ+grad spectra/s on 1 GB300 (served vs plain) at ≤1e-4 rel err; p
 UNIT = "spectra/s"
 HIER = (50, 50, 20, 15)
 NK = 1200
-RELTOL, ABSTOL = 1e-8, 1e-6
+RELTOL, ABSTOL = 1e-8, 3e-7
 ELLS = np.arange(2, 2501, dtype=np.int32)
 
 
@@ -183,6 +183,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling captures)")
+    ap.add_argument("--nk", type=int, default=NK, help="source-grid wavenumbers (smaller cases for ncu captures)")
+    ap.add_argument("--kmax-h0", type=float, default=5000.0, help="largest source-grid wavenumber in units of H0")
+    ap.add_argument("--lmax", type=int, default=int(ELLS[-1]), help="largest multipole")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -196,13 +200,14 @@ def main():
     par = fid_params(B)
     bg = B.Background(par)
     ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg, ctx=ctx)
-    ks = B.log10_k(0.1 * bg.H0, 5000 * bg.H0, NK)
+    ks = B.log10_k(0.1 * bg.H0, args.kmax_h0 * bg.H0, args.nk)
+    ells = np.arange(2, args.lmax + 1, dtype=np.int32)
     lg, lnu, lmnu, nq = HIER
     N = B.state_len(lg, lnu, lmnu, nq)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def device_step():
-        tt, te, ee, st = B.cl_all(ELLS, ih, ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL)
+        tt, te, ee, st = B.cl_all(ells, ih, ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL)
         return ctx.stats(), (tt, te, ee, st)
 
     for _ in range(args.warmup):
@@ -231,27 +236,27 @@ def main():
     # e2e through the public API: parameters in host memory -> C_l in host memory
     e2e_t = []
     h2d = d2h = 0
-    for i in range(args.steps + 1):
+    for i in range(0 if args.no_e2e else args.steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         bg2 = B.Background(par)
         ih2 = B.IonizationHistory(B.RECFAST(bg2, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg2,
                                   ctx=ctx)
-        tt, te, ee, st = B.cl_all(ELLS, ih2, ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL)
+        tt, te, ee, st = B.cl_all(ells, ih2, ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL)
         ih2.close()
         torch.cuda.synchronize()
         if i > 0:
             e2e_t.append(time.perf_counter() - t0)
         n2 = bg2.x_grid.size + 2
-        h2d = 8 * (n2 * 4 + 12 * n2 + 2 * nq) + 8 * NK + 8 * 4999 * 2 + 8 * 5000
-        d2h = 8 * 3 * ELLS.size + 4 * NK
-    e2e_val = ws * len(e2e_t) / max_over_ranks(sum(e2e_t), dist)
+        h2d = 8 * (n2 * 4 + 12 * n2 + 2 * nq) + 8 * ks.size + 8 * 4999 * 2 + 8 * 5000
+        d2h = 8 * 3 * ells.size + 4 * ks.size
+    e2e_val = ws * len(e2e_t) / max_over_ranks(sum(e2e_t), dist) if e2e_t else None
 
     # roofline of the dominant kernel (FP64-pipe bound)
     peak = ctypes_peak(B, local)
     sol_flops = (acc + rej) * solver_flops_per_step(N, nq)
     sol_s = solver_us / 1e6
-    los_f = los_flops(ELLS.size, 4999, 799) * args.steps
+    los_f = los_flops(ells.size, 4999, 799) * args.steps
     los_s = los_us / 1e6
     dom = "rodas_kernel" if sol_s >= los_s else "los_cl_kernel"
     ach = (sol_flops / sol_s if dom == "rodas_kernel" else los_f / los_s) / 1e12
@@ -271,10 +276,15 @@ def main():
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-               "config": {"workload": "full CMB pipeline (plain, one cosmology per call): fiducial LCDM, 1200 log k "
-                                      "in [0.1,5000]H0, l_g=l_gP=l_nu=50, l_mnu=20, nq=15 (N=473), S_T/S_E on 2001 x "
-                                      "nodes, C_l TT/TE/EE l=2..2500; gradients not in this workload",
-                          "reltol": RELTOL, "abstol": ABSTOL, "l2": "flushed (256 MB write) between steps",
+               "config": {"workload": f"full CMB pipeline (plain, one cosmology per call): fiducial LCDM, {ks.size} "
+                                      f"log k in [0.1,{args.kmax_h0:g}]H0, l_g=l_gP=l_nu=50, l_mnu=20, nq=15 (N={N}), "
+                                      f"S_T/S_E on 2001 x nodes, C_l TT/TE/EE l=2..{args.lmax}; gradients not in this "
+                                      "workload",
+                          "reltol": RELTOL, "abstol": ABSTOL,
+                          "accuracy": "at reltol 1e-8 / abstol 3e-7 the oracle's C_l differ from its converged "
+                                      "(1e-11) solution by <= 3.5e-5 (EE), 7.5e-6 (TT), 3.4e-6 (TE) relative; the "
+                                      "GPU path matches the oracle at equal tolerances to 1e-10",
+                          "l2": "flushed (256 MB write) between steps",
                           "parallelism": f"replicas x{ws}"},
                "clocks": clocks,
                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
