@@ -39,6 +39,19 @@ class BoltOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("warps_per_block", C.c_int), ("max_steps", C.c_longlong)]
 
 
+class BoltRequest(C.Structure):
+    _fields_ = [("kind", C.c_int), ("grad", C.c_int), ("par", BoltParams), ("grid", BoltGrid), ("nq", C.c_int),
+                ("hier", BoltHier), ("reltol", C.c_double), ("abstol", C.c_double), ("k", _dp), ("nk", C.c_int),
+                ("plin_x", C.c_double), ("ells", _ip), ("nell", C.c_int), ("cl_want", C.c_int),
+                ("plin", _dp), ("dplin", _dp), ("tt", _dp), ("te", _dp), ("ee", _dp), ("dtt", _dp), ("dte", _dp),
+                ("dee", _dp), ("status", _i32p)]
+
+
+class BoltEngineCfg(C.Structure):
+    _fields_ = [("device", C.c_int), ("lanes", C.c_int), ("host_threads", C.c_int), ("max_batch", C.c_int),
+                ("mem_budget_gb", C.c_double), ("warps_per_mode", C.c_int), ("max_steps", C.c_longlong)]
+
+
 EXPORTS = {
     "bolt_version": (C.c_int, []),
     "bolt_mass_natural": (C.c_double, []),
@@ -70,6 +83,13 @@ EXPORTS = {
     "bolt_source_grid_static": (C.c_int, [C.POINTER(BoltParams), C.POINTER(BoltGrid), C.c_int, _dp, _dp, _dp,
                                           C.c_int, C.POINTER(BoltHier), C.c_double, C.c_double, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]),
+    "bolt_engine_create": (C.c_int, [C.POINTER(BoltEngineCfg), C.POINTER(C.c_void_p)]),
+    "bolt_engine_destroy": (None, [C.c_void_p]),
+    "bolt_engine_last_error": (C.c_char_p, [C.c_void_p]),
+    "bolt_engine_submit": (C.c_int, [C.c_void_p, C.POINTER(BoltRequest), _i64p]),
+    "bolt_engine_wait": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, _ip, _dp, C.c_char_p, C.c_int]),
+    "bolt_request_run": (C.c_int, [C.c_void_p, C.POINTER(BoltRequest), C.c_char_p, C.c_int]),
+    "bolt_engine_stats": (C.c_int, [C.c_void_p, _i64p]),
 }
 
 _lib = None

@@ -46,9 +46,14 @@ struct ModeDev {
   double* plin;       // [1] P_lin at the last node (MODE_PLIN)
   int32_t* status;    // [1]
   int64_t* counters;  // [2] accepted steps, rejected steps
+  double* rec;        // [rec_cap] end abscissae of the accepted steps (MODE_RECORD / MODE_REPLAY)
+  int rec_cap;
 };
 
-enum ModeFlags { MODE_SOURCES = 1, MODE_TRAJ = 2, MODE_PLIN = 4 };
+// MODE_RECORD stores the end abscissa of every accepted step; MODE_REPLAY
+// takes exactly those steps (no error control), so a mode of perturbed
+// parameters is integrated on the same discretisation as the recorded one.
+enum ModeFlags { MODE_SOURCES = 1, MODE_TRAJ = 2, MODE_PLIN = 4, MODE_RECORD = 8, MODE_REPLAY = 16 };
 
 enum StatusBits {
   ST_OK = 0,
@@ -57,13 +62,27 @@ enum StatusBits {
   ST_NONFINITE = 3,
   ST_LU_FAIL = 4,
   ST_BAD_INPUT = 5,
-  ST_RSA_FIRED = 256  // informational, OR-ed into the code
+  ST_REPLAY_SHORT = 6,   // MODE_REPLAY ran past the recorded steps
+  ST_RSA_FIRED = 256,    // informational, OR-ed into the code
+  ST_REC_OVERFLOW = 512  // MODE_RECORD: more accepted steps than rec_cap (record unusable)
 };
 
 struct SolverCfg {
   double reltol, abstol, h0;
   double x_dense;  // source nodes below this x come from dense output
   long long max_steps;
+};
+
+// Argument block of one solver launch captured as a graph kernel node.
+struct RodasNodeArgs {
+  const ModeDev* modes;
+  int nmodes;
+  const CosmoDev* cosmos;
+  SolverCfg cfg;
+  int* queue;
+  double* scratch;
+  int spm;
+  void* ptrs[7];
 };
 
 // ---------------------------------------------------------------- duals ----

@@ -23,6 +23,7 @@ int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int warps_per_bl
 int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
                  int maxN, int maxnq, int maxL, int warps_per_block, int blocks, double* d_scratch, cudaStream_t stream);
 size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL);
+size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm);
 size_t rodas_scratch_per_warp(int maxN);
 struct LosArgs {
   int nb, nslots, nrow, nm;
@@ -231,9 +232,9 @@ void run_solver(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h
   cfg.x_dense = c->x_dense;
   cfg.max_steps = c->max_steps;
   int Lmax = std::max(h->lg, std::max(h->lnu, h->lmnu));
-  size_t pw = rodas_smem_per_warp(N, h->nq, Lmax);  // shared memory of one mode (one CTA)
+  const int wpb = c->wpb;  // warps per mode (0: four)
+  size_t pw = rodas_smem_per_mode(N, h->nq, Lmax, wpb);  // shared memory of one mode (one CTA)
   if (pw > 227 * 1024) throw Err(-1, "hierarchy too large for shared memory");
-  int wpb = 0;
   int blocks = 0;
   int rc = rodas_grid_warps(nk, N, h->nq, Lmax, wpb, &blocks);
   if (rc != 0) throw Err(-3, std::string("solver configuration: ") + cudaGetErrorString(cudaError_t(-rc)));

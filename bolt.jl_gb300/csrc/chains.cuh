@@ -20,16 +20,17 @@
 // tail helpers it uses.
 #pragma once
 
-constexpr int kEmax = 6;
+constexpr int kLaneElems = 768;  // threads x elements-per-lane budget of every variant
 constexpr int kMaxChains = 32;
 
 // Packing of chains onto the CTA's lanes (shared memory, built per mode).
 struct Pack {
-  int* seg;      // [kThreads] segment start lane within the warp, -1 = idle lane
-  int* chain;    // [kThreads] chain id of the lane
-  int* idx;      // [kThreads][kEmax] state indices in elimination order, -1 = pad
+  int* seg;      // [threads] segment start lane within the warp, -1 = idle lane
+  int* chain;    // [threads] chain id of the lane
+  int* idx;      // [threads][em] state indices in elimination order, -1 = pad (at the end)
   int* owner;    // [kMaxChains] thread holding the chain's l = 0 element
   int* E;        // [1] elements per lane; E[1] = thread for the CDM pair + Phi
+  int em;        // largest elements per lane (kLaneElems / threads)
 };
 
 struct ChainDesc {
@@ -50,7 +51,7 @@ __device__ __forceinline__ ChainDesc chain_desc(const Mode& m, int c) {
 // one idle thread is kept for the CDM pair and Phi.
 __device__ bool build_pack(const Mode& m, const Pack& P, int nthreads) {
   const int nw = nthreads / 32, nc = 3 + m.nq;
-  for (int E = 2; E <= kEmax; ++E) {
+  for (int E = 2; E <= P.em; ++E) {
     int used[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int place[kMaxChains];
     bool ok = true;
@@ -70,7 +71,7 @@ __device__ bool build_pack(const Mode& m, const Pack& P, int nthreads) {
     for (int t = 0; t < nthreads; ++t) {
       P.seg[t] = -1;
       P.chain[t] = -1;
-      for (int e = 0; e < kEmax; ++e) P.idx[t * kEmax + e] = -1;
+      for (int e = 0; e < P.em; ++e) P.idx[t * P.em + e] = -1;
     }
     for (int c = 0; c < nc; ++c) {
       ChainDesc d = chain_desc(m, c);
@@ -81,7 +82,7 @@ __device__ bool build_pack(const Mode& m, const Pack& P, int nthreads) {
         P.chain[t] = c;
         for (int e = 0; e < E; ++e) {
           int j = g * E + e;
-          if (j < len) P.idx[t * kEmax + e] = d.base + (d.L - j) * d.stride;
+          if (j < len) P.idx[t * P.em + e] = d.base + (d.L - j) * d.stride;
         }
       }
       P.owner[c] = t0 + (len - 1) / E;
@@ -260,15 +261,16 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
   const int own_c = (tid == P.E[1]) ? 3 + m.nq : ((c >= 0 && P.owner[c] == tid) ? c : -1);
   const int own_c2 = (tid == P.E[1]) ? 4 + m.nq : -1;
   bool ok = true;
-  // ---- local Moebius products
-  double am[kEmax], bm[kEmax], lo_e[kEmax], up_e[kEmax];
+  const int* idx = P.idx + tid * P.em;
+  // ---- local Moebius products; the per-element factors wait in fl / fi
+  // (multipliers) and yt / b (couplings), which are free during the
+  // factorisation
   M2 loc = {1.0, 0.0, 0.0, 1.0};
   if (c >= 0) {
     ChainDesc cd = chain_desc(m, c);
-#pragma unroll
-    for (int e = 0; e < kEmax; ++e) {
-      int i = e < E ? P.idx[tid * kEmax + e] : -1;
-      if (i < 0) { am[e] = 0.0; bm[e] = 0.0; lo_e[e] = 0.0; up_e[e] = 0.0; continue; }
+    for (int e = 0; e < E; ++e) {
+      const int i = idx[e];
+      if (i < 0) break;
       int l = (i - cd.base) / cd.stride;
       ElemC ec = elem_coef(m, S, s, ig, c, l, cd.L);
       if (c == 0 && l == 1) {
@@ -278,11 +280,12 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
       }
       double p = ec.lo * ec.upPrev;  // 0 for the chain's first element
       double id = 1.0 / ec.d;
-      am[e] = -p * id;
-      bm[e] = id;
-      lo_e[e] = ec.lo;
-      up_e[e] = ec.up;
-      M2 t = {1.0, am[e], bm[e], 0.0};
+      double am = -p * id;
+      S.fl[i] = am;
+      S.fi[i] = id;
+      S.yt[i] = ec.lo;
+      S.b[i] = ec.up;
+      M2 t = {1.0, am, id, 0.0};
       loc = mmul(t, loc);
     }
   }
@@ -297,15 +300,15 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
   if (c >= 0) {
     double vn = ex.a, vm = ex.c;  // ex * (1, 0)
     double fi_prev = vm / vn;     // 0 at the chain's first element
-#pragma unroll
-    for (int e = 0; e < kEmax; ++e) {
-      int i = e < E ? P.idx[tid * kEmax + e] : -1;
+    for (int e = 0; e < E; ++e) {
+      const int i = idx[e];
       if (i < 0) break;
-      double n2 = fma(am[e], vm, vn), m2 = bm[e] * vn;
+      double am = S.fl[i], bm = S.fi[i], lo = S.yt[i], up = S.b[i];
+      double n2 = fma(am, vm, vn), m2 = bm * vn;
       double fi = m2 / n2;
       S.fi[i] = fi;
-      S.fl[i] = lo_e[e] * fi_prev;
-      S.fc[i] = up_e[e] * fi;
+      S.fl[i] = lo * fi_prev;
+      S.fc[i] = up * fi;
       ok = ok && isfinite(fi) && n2 != 0.0;
       fi_prev = fi;
       vn = n2;
@@ -361,24 +364,25 @@ __device__ void wsolve_scan(const Mode& m, const Shared& S, const Pack& P, doubl
   const int own_c = (tid == P.E[1]) ? 3 + m.nq : ((c >= 0 && P.owner[c] == tid) ? c : -1);
   const int own_c2 = (tid == P.E[1]) ? 4 + m.nq : -1;
   // ---- forward: b'_j = b_j - fl_j b'_{j-1}
-  double al[kEmax], be[kEmax];
+  const int* idx = P.idx + tid * P.em;
   double A = 1.0, B = 0.0;
+  int cnt = 0;  // valid elements of this lane
   if (c >= 0) {
-#pragma unroll
-    for (int e = 0; e < kEmax; ++e) {
-      int i = e < E ? P.idx[tid * kEmax + e] : -1;
-      if (i < 0) { al[e] = 1.0; be[e] = 0.0; continue; }
+    for (int e = 0; e < E; ++e) {
+      const int i = idx[e];
+      if (i < 0) break;
       double bi = b[i];
       if (c == 0 && i == 1) {  // Theta_1 <- baryon pair (eliminated first)
         double bdb = b[m.iPhi + 3];
         double bvb = b[m.iPhi + 4] - S.fl[m.iPhi + 4] * bdb;
         bi -= S.fl[m.iPhi + 3] * bvb;
         b[m.iPhi + 4] = bvb;
+        b[i] = bi;
       }
-      al[e] = -S.fl[i];
-      be[e] = bi;
-      A = al[e] * A;
-      B = fma(al[e], B, bi);
+      double al = -S.fl[i];
+      A = al * A;
+      B = fma(al, B, bi);
+      cnt = e + 1;
     }
   }
   for (int off = 1; off < 32; off <<= 1) {
@@ -387,15 +391,11 @@ __device__ void wsolve_scan(const Mode& m, const Shared& S, const Pack& P, doubl
   }
   double prev = __shfl_up_sync(0xffffffffu, B, 1);
   if (!(seg >= 0 && lane > seg)) prev = 0.0;
-  if (c >= 0) {
-#pragma unroll
-    for (int e = 0; e < kEmax; ++e) {
-      int i = e < E ? P.idx[tid * kEmax + e] : -1;
-      if (i < 0) break;
-      double v = fma(al[e], prev, be[e]);
-      b[i] = v;
-      prev = v;
-    }
+  for (int e = 0; e < cnt; ++e) {
+    const int i = idx[e];
+    double v = fma(-S.fl[i], prev, b[i]);
+    b[i] = v;
+    prev = v;
   }
   if (tid == P.E[1]) b[m.iPhi + 1] -= S.fl[m.iPhi + 1] * b[m.iPhi + 2];
   __syncthreads();
@@ -445,22 +445,13 @@ __device__ void wsolve_scan(const Mode& m, const Shared& S, const Pack& P, doubl
   }
   __syncthreads();
   // ---- backward: x_j = fi_j b'_j - fc_j x_{j+1} (reverse scan)
-  double ga[kEmax], de[kEmax];
   A = 1.0;
   B = 0.0;
-  int last = -1;
-  if (c >= 0) {
-#pragma unroll
-    for (int e = 0; e < kEmax; ++e) {
-      int i = e < E ? P.idx[tid * kEmax + e] : -1;
-      if (i < 0) { ga[e] = 0.0; de[e] = 1.0; continue; }
-      ga[e] = b[i] * S.fi[i];
-      de[e] = -S.fc[i];
-      last = e;
-    }
-#pragma unroll
-    for (int e = kEmax - 1; e >= 0; --e)
-      if (e <= last) { B = fma(de[e], B, ga[e]); A = de[e] * A; }
+  for (int e = cnt - 1; e >= 0; --e) {
+    const int i = idx[e];
+    double ga = b[i] * S.fi[i], de = -S.fc[i];
+    B = fma(de, B, ga);
+    A = de * A;
   }
   int segend = 31;
   {
@@ -476,20 +467,16 @@ __device__ void wsolve_scan(const Mode& m, const Shared& S, const Pack& P, doubl
   }
   double nxt = __shfl_down_sync(0xffffffffu, B, 1);
   if (!(seg >= 0 && lane < segend)) nxt = 0.0;
-  if (c >= 0) {
-#pragma unroll
-    for (int e = kEmax - 1; e >= 0; --e) {
-      if (e > last) continue;
-      int i = P.idx[tid * kEmax + e];
-      double v = fma(de[e], nxt, ga[e]);
-      b[i] = v;
-      nxt = v;
-      if (c == 0 && i == 1) {  // baryon pair after Theta_1
-        int ivb = m.iPhi + 4, idb = m.iPhi + 3;
-        double xvb = b[ivb] * S.fi[ivb] - S.fc[ivb] * v;
-        b[ivb] = xvb;
-        b[idb] = b[idb] * S.fi[idb] - S.fc[idb] * xvb;
-      }
+  for (int e = cnt - 1; e >= 0; --e) {
+    const int i = idx[e];
+    double v = fma(-S.fc[i], nxt, b[i] * S.fi[i]);
+    b[i] = v;
+    nxt = v;
+    if (c == 0 && i == 1) {  // baryon pair after Theta_1
+      int ivb = m.iPhi + 4, idb = m.iPhi + 3;
+      double xvb = b[ivb] * S.fi[ivb] - S.fc[ivb] * v;
+      b[ivb] = xvb;
+      b[idb] = b[idb] * S.fi[idb] - S.fc[idb] * xvb;
     }
   }
   if (tid == P.E[1]) {

@@ -1,0 +1,1163 @@
+// Batching and serving engine (include/bolt_gb300.h: bolt_engine_*,
+// bolt_request_run).
+//
+// A request is one cosmology with its own k grid, hierarchy and outputs:
+// P_lin(k) (Bolt.jl src/spectra.jl:163-198) or C_l (source_grid + cltt /
+// clte / clee, spectra.jl:6-160), optionally with the Jacobian with respect
+// to theta = (h, omega_b, omega_c, n, A, Sigma m_nu).
+//
+//   submit ──> host worker threads: Background + RECFAST tables
+//              (13 table sets for a gradient: the cosmology and theta ± d)
+//          ──> ready FIFO ──> scheduler thread: admits ready requests while
+//              the in-flight device footprint fits the budget, forms a batch
+//              and enqueues it on an idle lane (stream):
+//                upload ─ solver graph (all modes of all requests, one
+//                persistent launch) ─ solver graph (replay modes of the
+//                gradient sets) ─ line-of-sight kernels per request ─
+//                download ─ done event
+//          ──> on the done event: outputs, central differences, release.
+//
+// Lanes overlap on the device: the CTAs of a new batch fill the SMs that the
+// tail of the previous batch leaves idle, so requests that arrive while
+// others are on the GPU are admitted as memory and lanes free up.
+//
+// Gradients are central differences of the discrete pipeline with every
+// discretisation choice frozen: the perturbed modes replay the accepted
+// steps of the unperturbed mode (MODE_RECORD / MODE_REPLAY), RECFAST replays
+// its steps and switch redshifts (RecfastFreeze), and the k grids and the
+// Bessel grid are those of the unperturbed cosmology, as the reference's
+// ForwardDiff gradient holds them (spectra.jl:46-66, recfast.jl:451-456).
+// The pipeline is then a smooth function of theta, and the relative step
+// 1e-5 leaves truncation errors ~1e-10 and round-off ~1e-9 (relative).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/bolt_gb300.h"
+#include "bolt_dev.cuh"
+#include "host_cosmo.hpp"
+
+namespace bolt {
+int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, int* blocks);
+int rodas_node_params(int wpm, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg,
+                      int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch, RodasNodeArgs* args,
+                      cudaKernelNodeParams* p);
+size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm);
+size_t rodas_scratch_per_warp(int maxN);
+struct LosArgs {
+  int nb, nslots, nrow, nm;
+  const int* ells;
+  const double* coef;
+  const double* inv_dg;
+  const double* yv;
+  const double* kmid;
+  const double* wts;
+  const double* SdT;
+  const double* SdE;
+  double* tt;
+  double* te;
+  double* ee;
+};
+int launch_jl_raw(int nb, const double* d_dgs, int ncz, int Lmax, const int* d_slot_of_l, int nslots, double* d_raw,
+                  double* d_norm, int* d_flags, cudaStream_t st);
+int launch_jl_prefilter(int nb, int nslots, int ncz, const double* d_raw, const double* d_norm, const double* d_w,
+                        double* d_coef, cudaStream_t st);
+int launch_sdense(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_ST, const double* d_SE, int nm,
+                  const double* d_kmid, const double* d_dx, double* d_SdT, double* d_SdE, cudaStream_t st);
+int launch_los_cl(const LosArgs& a, int ncz, cudaStream_t st);
+void fill_cosmo_dev(const CosmoTables& T, double* d_tab, double* h_tab, CosmoDev& d);
+size_t cosmo_table_doubles(const CosmoTables& T);
+}  // namespace bolt
+
+using namespace bolt;
+
+namespace {
+
+constexpr int kTheta = 6;
+constexpr int kRecCap = 12288;      // recorded steps per mode (gradient requests)
+constexpr double kRelStep = 1e-5;   // central-difference step, relative to |theta_j|
+constexpr int kNb = 5001;           // Bessel grid points (spectra.jl:52)
+constexpr int kNkd = 5000;          // dense LOS k grid (spectra.jl:133)
+
+struct EngErr : std::runtime_error {
+  int code;
+  EngErr(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw EngErr(-3, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+double now_s(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+struct GrowDev {  // grow-only device buffer, resized only while its lane is idle
+  void* p = nullptr;
+  size_t cap = 0;
+  void* get(size_t bytes) {
+    if (bytes > cap) {
+      if (p) cudaFree(p);
+      p = nullptr;
+      cap = 0;
+      size_t want = std::max<size_t>(bytes + bytes / 4, 4096);
+      ck(cudaMalloc(&p, want), "cudaMalloc lane scratch");
+      cap = want;
+    }
+    return p;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+struct GrowHost {  // grow-only pinned host buffer
+  void* p = nullptr;
+  size_t cap = 0;
+  void* get(size_t bytes) {
+    if (bytes > cap) {
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+      cap = 0;
+      size_t want = std::max<size_t>(bytes + bytes / 4, 4096);
+      ck(cudaMallocHost(&p, want), "cudaMallocHost lane staging");
+      cap = want;
+    }
+    return p;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// theta = (h, omega_b, omega_c, n, A, Sigma m_nu [eV]) <-> CosmoParams.
+void theta_of(const CosmoParamsH& p, double* th) {
+  const double me = units_mass_eV();
+  th[0] = p.h;
+  th[1] = p.Omega_b * p.h * p.h;
+  th[2] = p.Omega_c * p.h * p.h;
+  th[3] = p.n;
+  th[4] = p.A;
+  th[5] = p.Sigma_m_nu / me;
+}
+CosmoParamsH params_of(const CosmoParamsH& base, const double* th) {
+  const double me = units_mass_eV();
+  CosmoParamsH p = base;
+  p.h = th[0];
+  p.Omega_b = th[1] / (th[0] * th[0]);
+  p.Omega_c = th[2] / (th[0] * th[0]);
+  p.n = th[3];
+  p.A = th[4];
+  p.Sigma_m_nu = th[5] * me;
+  return p;
+}
+
+struct Req {
+  int64_t ticket = 0;
+  bolt_request r{};
+  std::vector<double> k;
+  std::vector<int> ells;
+  GridSpec grid{};
+  int nsets = 1;
+  std::vector<CosmoParamsH> pars;  // [nsets]
+  double step[kTheta] = {0, 0, 0, 0, 0, 0};
+  bool one_sided[kTheta] = {false, false, false, false, false, false};
+  std::vector<CosmoTables> T;      // [nsets]
+  RecfastFreeze fz;
+  int tables_left = 0;
+  int state = 0;  // 0 building, 1 ready, 2 on the GPU, 3 done
+  int rc = 0;
+  std::string err;
+  double t[4] = {0, 0, 0, 0};
+  size_t bytes = 0;  // device footprint of the request in a batch
+  int N = 0;
+  // LOS (C_l): sorted unique multipoles
+  std::vector<int> uniq;
+  // offsets into the batch's device block and the lane's download area
+  size_t o_xout = 0, o_src = 0, o_plin = 0, o_stat = 0, o_cnt = 0, o_rec = 0, o_cl = 0, o_los = 0;
+  size_t h_stat = 0, h_plin = 0, h_cl = 0, h_cnt = 0;
+  int cos0 = 0;  // first CosmoDev index of the request in the batch
+  bool wantE = false;
+};
+
+struct Tuner {  // seconds per mode-step by batch-size bucket and warps per mode
+  double sps[48][3];
+  int n[48][3];
+  Tuner() {
+    for (int b = 0; b < 48; ++b)
+      for (int v = 0; v < 3; ++v) { sps[b][v] = 0.0; n[b][v] = 0; }
+  }
+  static int bucket(int nmodes) {
+    int b = 0;
+    while ((1 << (b + 1)) <= nmodes && b < 47) ++b;
+    return b;
+  }
+  static int vidx(int wpm) { return wpm == 1 ? 0 : (wpm == 2 ? 1 : 2); }
+  int pick(int nmodes, int nsm) const {
+    // candidates: only launches that fill the GPU benefit from the
+    // instruction-lean narrow variants
+    int cands[3] = {4, 0, 0}, nc = 1;
+    if (nmodes > 2 * nsm) cands[nc++] = 2;
+    if (nmodes > 4 * nsm) cands[nc++] = 1;
+    const int b = bucket(nmodes);
+    for (int i = 0; i < nc; ++i)
+      if (n[b][vidx(cands[i])] == 0) return cands[i];
+    int best = cands[0];
+    for (int i = 1; i < nc; ++i)
+      if (sps[b][vidx(cands[i])] < sps[b][vidx(best)]) best = cands[i];
+    return best;
+  }
+  void update(int nmodes, int wpm, double secs, double steps) {
+    if (!(steps > 0) || !(secs > 0)) return;
+    const int b = bucket(nmodes), v = vidx(wpm);
+    double x = secs / steps;
+    sps[b][v] = n[b][v] == 0 ? x : 0.7 * sps[b][v] + 0.3 * x;
+    ++n[b][v];
+  }
+};
+
+struct Graph {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t knode = nullptr;
+};
+
+struct Lane {
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // start, phase 1, phase 2, LOS, done
+  int* d_queue = nullptr;  // [2] work-queue counters of the two solver phases
+  Graph graph[3][2];       // [warps-per-mode variant][phase]
+  GrowDev scr, los_raw, los_norm, los_coef, los_SdT, los_SdE;
+  GrowHost up, down;
+  bool busy = false;
+  std::vector<Req*> batch;
+  void* d_block = nullptr;
+  size_t block_bytes = 0;
+  int wpm[2] = {4, 4};
+  int nmodes[2] = {0, 0};
+  int nlaunch = 0;
+  std::vector<int> los_flags_dummy;
+};
+
+}  // namespace
+
+struct bolt_engine {
+  bolt_engine_cfg cfg{};
+  int device = 0, nsm = 0;
+  std::chrono::steady_clock::time_point t0;
+  std::mutex mu;
+  std::condition_variable cv_sched, cv_done, cv_pool;
+  bool stop = false;
+  std::string err;
+  int64_t next_ticket = 1;
+  std::map<int64_t, std::unique_ptr<Req>> reqs;
+  std::deque<Req*> ready;
+  std::deque<std::function<void()>> tasks;
+  std::vector<std::thread> pool;
+  std::thread sched;
+  std::vector<Lane> lanes;
+  size_t inflight_bytes = 0;
+  size_t budget = 0;
+  Tuner tuner;
+  int64_t stats[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double* d_w = nullptr;  // Bessel prefilter pivots (constant)
+  int* d_flags = nullptr;
+};
+
+namespace {
+
+// --------------------------------------------------------------- validation
+void check_request(const bolt_request* q) {
+  if (!q) throw EngErr(-1, "request is null");
+  if (q->kind != BOLT_REQ_PLIN && q->kind != BOLT_REQ_CL) throw EngErr(-1, "request kind must be PLIN or CL");
+  const bolt_hier& h = q->hier;
+  if (h.lg < 3 || h.lnu < 3 || h.lmnu < 3) throw EngErr(-1, "hierarchy truncations must be >= 3");
+  if (h.nq < 1 || h.nq > 27) throw EngErr(-1, "nq must be in 1..27");
+  if (h.lg > 1000 || h.lnu > 1000 || h.lmnu > 1000) throw EngErr(-1, "hierarchy truncation too large");
+  if (q->nq != h.nq) throw EngErr(-1, "hierarchy nq must equal the Background nq");
+  if (!(q->reltol > 0) || !(q->abstol > 0)) throw EngErr(-1, "tolerances must be positive");
+  if (!q->k || q->nk < 1) throw EngErr(-1, "no wavenumbers");
+  if (q->nk > 1000000) throw EngErr(-1, "too many wavenumbers");
+  for (int i = 0; i < q->nk; ++i) {
+    if (!(q->k[i] > 0) || !std::isfinite(q->k[i])) throw EngErr(-1, "wavenumbers must be positive and finite");
+    if (i > 0 && !(q->k[i] > q->k[i - 1])) throw EngErr(-1, "wavenumbers must be strictly ascending");
+  }
+  const bolt_params& p = q->par;
+  if (!(p.h > 0) || !(p.Omega_b > 0) || !(p.Omega_c >= 0) || !(p.Omega_r > 0) || !(p.A > 0) || !(p.N_nu > 0) ||
+      !(p.Sigma_m_nu >= 0) || !std::isfinite(p.n))
+    throw EngErr(-1, "invalid cosmological parameters");
+  if (!(q->grid.step > 0) || !(q->grid.stop > q->grid.start)) throw EngErr(-1, "invalid x grid");
+  if (q->kind == BOLT_REQ_PLIN) {
+    if (!q->plin) throw EngErr(-1, "plin output is null");
+    if (q->grad && !q->dplin) throw EngErr(-1, "dplin output is null");
+    if (!(q->plin_x > q->grid.start) || !(q->plin_x <= q->grid.stop)) throw EngErr(-1, "plin_x outside the x grid");
+  } else {
+    if (q->nk < 2) throw EngErr(-1, "C_l needs at least two source-grid wavenumbers");
+    if (!q->ells || q->nell < 1) throw EngErr(-1, "no multipoles");
+    for (int i = 0; i < q->nell; ++i)
+      if (q->ells[i] < 2 || q->ells[i] > 20000) throw EngErr(-1, "multipoles must be in 2..20000");
+    const int w = q->cl_want;
+    if (w <= 0 || w > 7) throw EngErr(-1, "cl_want must name TT, TE and/or EE");
+    if (((w & BOLT_CL_TT) && !q->tt) || ((w & BOLT_CL_TE) && !q->te) || ((w & BOLT_CL_EE) && !q->ee))
+      throw EngErr(-1, "C_l output is null");
+    if (q->grad && (((w & BOLT_CL_TT) && !q->dtt) || ((w & BOLT_CL_TE) && !q->dte) || ((w & BOLT_CL_EE) && !q->dee)))
+      throw EngErr(-1, "C_l gradient output is null");
+  }
+}
+
+// ------------------------------------------------------------ host tables
+void build_set(Req* r, int s) {
+  RecfastOpts ro;
+  const CosmoParamsH& p = r->pars[s];
+  ro.Yp = p.Y_p;
+  ro.OmegaB = p.Omega_b;
+  ro.OmegaG = p.Omega_r;
+  ro.Tnow = -1.0;
+  ro.tol = 1e-8;
+  build_cosmo_tables(p, r->grid, r->r.nq, ro, r->T[s], r->nsets > 1 ? &r->fz : nullptr);
+}
+
+size_t align_up(size_t v) { return (v + 255) & ~size_t(255); }
+
+// Device footprint of a request inside a batch (its share of the batch block).
+void layout_request(Req* r, size_t& off) {
+  const int nk = r->r.nk, n = r->grid.n, ns = r->nsets;
+  const size_t tabd = cosmo_table_doubles(r->T[0]);
+  size_t start = off;
+  off = align_up(off + size_t(ns) * tabd * 8);  // tables of every set
+  r->o_xout = off;
+  off = align_up(off + size_t(r->r.kind == BOLT_REQ_CL ? n : 1) * 8);
+  r->o_stat = off;
+  off = align_up(off + size_t(ns) * nk * 4);
+  r->o_cnt = off;
+  off = align_up(off + size_t(ns) * nk * 16);
+  r->o_rec = off;
+  if (r->nsets > 1) off = align_up(off + size_t(nk) * kRecCap * 8);
+  if (r->r.kind == BOLT_REQ_CL) {
+    r->o_src = off;
+    off = align_up(off + size_t(ns) * nk * n * 8 * (r->wantE ? 2 : 1));
+    r->o_cl = off;
+    off = align_up(off + size_t(ns) * 3 * r->uniq.size() * 8);
+    r->o_los = off;  // k grid, kmid, dx, slots, ells, inv_dg, per-set wts and y
+    const int nm = kNkd - 1;
+    off = align_up(off + size_t(nk + nm + n + 8) * 8 + size_t(r->uniq.back() + 1 + r->uniq.size()) * 4 +
+                   size_t(ns) * (nm + n) * 8 + 1024);
+  } else {
+    r->o_plin = off;
+    off = align_up(off + size_t(ns) * nk * 8);
+  }
+  r->bytes = off - start;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ engine
+namespace {
+
+void pool_worker(bolt_engine* E) {
+  cudaSetDevice(E->device);
+  std::unique_lock<std::mutex> lk(E->mu);
+  while (true) {
+    E->cv_pool.wait(lk, [&] { return E->stop || !E->tasks.empty(); });
+    if (E->tasks.empty()) {
+      if (E->stop) return;
+      continue;
+    }
+    auto f = std::move(E->tasks.front());
+    E->tasks.pop_front();
+    lk.unlock();
+    f();
+    lk.lock();
+  }
+}
+
+// Called with the lock held when a table set of r finished (ok or not).
+void set_done(bolt_engine* E, Req* r, int s, const std::string& err) {
+  if (!err.empty() && r->rc == 0) {
+    r->rc = -1;
+    r->err = "table construction: " + err;
+  }
+  if (s == 0 && r->rc == 0 && r->nsets > 1) {
+    for (int j = 1; j < r->nsets; ++j)
+      E->tasks.push_back([E, r, j] {
+        std::string e;
+        try { build_set(r, j); } catch (const std::exception& x) { e = x.what(); }
+        std::lock_guard<std::mutex> g(E->mu);
+        set_done(E, r, j, e);
+      });
+    E->cv_pool.notify_all();
+  }
+  if (s == 0 && r->rc != 0) r->tables_left = 1;  // skip the perturbed sets
+  if (--r->tables_left == 0) {
+    r->t[1] = now_s(E->t0);
+    if (r->rc != 0) {
+      r->state = 3;
+      r->t[3] = r->t[1];
+      E->cv_done.notify_all();
+    } else {
+      r->state = 1;
+      E->ready.push_back(r);
+      E->cv_sched.notify_all();
+    }
+  }
+}
+
+Graph& lane_graph(bolt_engine* E, Lane& L, int wpm, int phase, const cudaKernelNodeParams& kp) {
+  const int v = wpm == 1 ? 0 : (wpm == 2 ? 1 : 2);
+  Graph& G = L.graph[v][phase];
+  if (!G.exec) {
+    ck(cudaGraphCreate(&G.g, 0), "cudaGraphCreate");
+    cudaMemsetParams mp;
+    std::memset(&mp, 0, sizeof(mp));
+    mp.dst = L.d_queue + phase;
+    mp.value = 0;
+    mp.elementSize = 4;
+    mp.width = 1;
+    mp.height = 1;
+    mp.pitch = 0;
+    cudaGraphNode_t mnode;
+    ck(cudaGraphAddMemsetNode(&mnode, G.g, nullptr, 0, &mp), "cudaGraphAddMemsetNode");
+    ck(cudaGraphAddKernelNode(&G.knode, G.g, &mnode, 1, &kp), "cudaGraphAddKernelNode");
+    ck(cudaGraphInstantiate(&G.exec, G.g, 0), "cudaGraphInstantiate");
+  } else {
+    ck(cudaGraphExecKernelNodeSetParams(G.exec, G.knode, &kp), "cudaGraphExecKernelNodeSetParams");
+  }
+  (void)E;
+  return G;
+}
+
+// Enqueues one batch on an idle lane.  Runs without the engine lock.  Every
+// lane buffer is sized before the first enqueue (a reallocation later would
+// free memory that enqueued work still uses).
+void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
+  cudaStream_t st = L.st;
+  // ---- device layout of the batch block (inputs and outputs)
+  size_t off = 0;
+  int ncos = 0, m1 = 0, m2 = 0, maxN = 0, maxnq = 1, maxL = 3;
+  size_t max_sd = 0;
+  int max_slots = 0;
+  bool anyE = false;
+  for (Req* r : batch) {
+    layout_request(r, off);
+    r->cos0 = ncos;
+    ncos += r->nsets;
+    m1 += r->r.nk;
+    m2 += (r->nsets - 1) * r->r.nk;
+    maxN = std::max(maxN, r->N);
+    maxnq = std::max(maxnq, r->r.hier.nq);
+    maxL = std::max(maxL, std::max(r->r.hier.lg, std::max(r->r.hier.lnu, r->r.hier.lmnu)));
+    if (r->r.kind == BOLT_REQ_CL) {
+      max_slots = std::max(max_slots, int(r->uniq.size()));
+      int n = r->grid.n, i0 = 0;
+      while (i0 < n && !(r->grid.at(i0) > -8.0)) ++i0;
+      max_sd = std::max(max_sd, size_t(std::max(n - 1 - i0, 1)) * (kNkd - 1));
+      anyE |= r->wantE;
+    }
+  }
+  const size_t o_cos = off;
+  off = align_up(off + size_t(ncos) * sizeof(CosmoDev));
+  const size_t o_modes = off;
+  off = align_up(off + size_t(m1 + m2) * sizeof(ModeDev));
+  const size_t total = off;
+  // ---- solver configurations of both phases (autotuned) and lane buffers
+  int wpm[2] = {4, 4}, blocks[2] = {0, 0};
+  const int nph = m2 > 0 ? 2 : 1;
+  const int nmodes[2] = {m1, m2};
+  for (int ph = 0; ph < nph; ++ph) {
+    int w = E->cfg.warps_per_mode;
+    if (w != 1 && w != 2 && w != 4) {
+      std::lock_guard<std::mutex> g(E->mu);
+      w = E->tuner.pick(nmodes[ph], E->nsm);
+    }
+    int rc = rodas_grid_warps(nmodes[ph], maxN, maxnq, maxL, w, &blocks[ph]);
+    if (rc != 0) throw EngErr(-3, std::string("solver configuration: ") + cudaGetErrorString(cudaError_t(-rc)));
+    wpm[ph] = w;
+  }
+  double* d_scr = static_cast<double*>(
+      L.scr.get(size_t(std::max(blocks[0], blocks[1])) * rodas_scratch_per_warp(maxN)));
+  double *raw = nullptr, *norm = nullptr, *coef = nullptr, *SdT = nullptr, *SdE = nullptr;
+  if (max_slots > 0) {
+    raw = static_cast<double*>(L.los_raw.get(size_t(max_slots) * kNb * 8));
+    norm = static_cast<double*>(L.los_norm.get(size_t(kNb) * 8));
+    coef = static_cast<double*>(L.los_coef.get(size_t(max_slots) * (kNb + 2) * 8));
+    SdT = static_cast<double*>(L.los_SdT.get(max_sd * 8));
+    if (anyE) SdE = static_cast<double*>(L.los_SdE.get(max_sd * 8));
+  }
+  // ---- host staging (pinned, compact): input segments only
+  struct Seg {
+    size_t dev, host, bytes;
+  };
+  std::vector<Seg> segs;
+  size_t hoff = 0;
+  auto seg = [&](size_t dev_off, size_t bytes) {
+    segs.push_back({dev_off, hoff, bytes});
+    hoff = align_up(hoff + bytes);
+    return segs.size() - 1;
+  };
+  std::vector<size_t> seg_tab(batch.size()), seg_x(batch.size()), seg_los(batch.size());
+  size_t req_start = 0;
+  std::vector<size_t> starts(batch.size());
+  for (size_t b = 0; b < batch.size(); ++b) {
+    Req* r = batch[b];
+    starts[b] = req_start;
+    seg_tab[b] = seg(req_start, size_t(r->nsets) * cosmo_table_doubles(r->T[0]) * 8);
+    seg_x[b] = seg(r->o_xout, size_t(r->r.kind == BOLT_REQ_CL ? r->grid.n : 1) * 8);
+    if (r->r.kind == BOLT_REQ_CL) {
+      const int nm = kNkd - 1, n = r->grid.n, ns = int(r->uniq.size());
+      size_t head = align_up(size_t(r->r.nk + nm + n + 8) * 8 + size_t(r->uniq.back() + 1 + ns) * 4);
+      seg_los[b] = seg(r->o_los, head + size_t(r->nsets) * (nm + n) * 8);
+    }
+    req_start += r->bytes;
+  }
+  const size_t seg_cos = seg(o_cos, size_t(ncos) * sizeof(CosmoDev));
+  const size_t seg_modes = seg(o_modes, size_t(m1 + m2) * sizeof(ModeDev));
+  char* up = static_cast<char*>(L.up.get(std::max<size_t>(hoff, 8)));
+  // downloads: status + counters + results per request
+  size_t doff = 0;
+  for (Req* r : batch) {
+    const int nk = r->r.nk, ns = r->nsets;
+    r->h_stat = doff;
+    doff = align_up(doff + size_t(ns) * nk * 4);
+    r->h_cnt = doff;
+    doff = align_up(doff + size_t(ns) * nk * 16);
+    if (r->r.kind == BOLT_REQ_CL) {
+      r->h_cl = doff;
+      doff = align_up(doff + size_t(ns) * 3 * r->uniq.size() * 8);
+    } else {
+      r->h_plin = doff;
+      doff = align_up(doff + size_t(ns) * nk * 8);
+    }
+  }
+  char* down = static_cast<char*>(L.down.get(std::max<size_t>(doff, 8)));
+  ck(cudaMallocAsync(&L.d_block, total, st), "cudaMallocAsync batch");
+  char* dev = static_cast<char*>(L.d_block);
+  // ---- host images: tables, x nodes, modes
+  std::vector<CosmoDev> cos(ncos);
+  std::vector<ModeDev> modes, modes2;
+  modes.reserve(m1);
+  modes2.reserve(m2);
+  for (size_t b = 0; b < batch.size(); ++b) {
+    Req* r = batch[b];
+    const int nk = r->r.nk, ns = r->nsets, n = r->grid.n;
+    const size_t tabd = cosmo_table_doubles(r->T[0]);
+    for (int s = 0; s < ns; ++s) {
+      double* h_tab = reinterpret_cast<double*>(up + segs[seg_tab[b]].host + size_t(s) * tabd * 8);
+      double* d_tab = reinterpret_cast<double*>(dev + starts[b] + size_t(s) * tabd * 8);
+      fill_cosmo_dev(r->T[s], d_tab, h_tab, cos[r->cos0 + s]);
+    }
+    double* hx = reinterpret_cast<double*>(up + segs[seg_x[b]].host);
+    const double* dx = reinterpret_cast<const double*>(dev + r->o_xout);
+    int nout;
+    if (r->r.kind == BOLT_REQ_CL) {
+      for (int j = 0; j < n; ++j) hx[j] = r->grid.at(j);
+      nout = n;
+    } else {
+      hx[0] = r->r.plin_x;
+      nout = 1;
+    }
+    int32_t* dstat = reinterpret_cast<int32_t*>(dev + r->o_stat);
+    int64_t* dcnt = reinterpret_cast<int64_t*>(dev + r->o_cnt);
+    double* drec = reinterpret_cast<double*>(dev + r->o_rec);
+    for (int s = 0; s < ns; ++s)
+      for (int i = 0; i < nk; ++i) {
+        ModeDev m;
+        std::memset(&m, 0, sizeof(m));
+        m.k = r->k[i];
+        m.cosmo = r->cos0 + s;
+        m.lg = r->r.hier.lg; m.lnu = r->r.hier.lnu; m.lmnu = r->r.hier.lmnu; m.nq = r->r.hier.nq;
+        m.nout = nout;
+        m.xout = dx;
+        if (r->r.kind == BOLT_REQ_CL) {
+          double* src = reinterpret_cast<double*>(dev + r->o_src);
+          m.flags = MODE_SOURCES;
+          m.src_T = src + (size_t(s) * nk + i) * n;
+          m.src_E = r->wantE ? src + size_t(ns) * nk * n + (size_t(s) * nk + i) * n : nullptr;
+        } else {
+          m.flags = MODE_PLIN;
+          m.plin = reinterpret_cast<double*>(dev + r->o_plin) + size_t(s) * nk + i;
+        }
+        m.status = dstat + size_t(s) * nk + i;
+        m.counters = dcnt + 2 * (size_t(s) * nk + i);
+        if (ns > 1) {
+          m.flags |= s == 0 ? MODE_RECORD : MODE_REPLAY;
+          m.rec = drec + size_t(i) * kRecCap;
+          m.rec_cap = kRecCap;
+        }
+        if (s == 0) modes.push_back(m);
+        else modes2.push_back(m);
+      }
+  }
+  // longest modes first: the cost grows with k and with the state length
+  auto cost_order = [](std::vector<ModeDev>& v) {
+    std::stable_sort(v.begin(), v.end(), [](const ModeDev& a, const ModeDev& b) {
+      double ca = a.k * (2 * (a.lg + 1) + (a.lnu + 1) + (a.lmnu + 1) * a.nq);
+      double cb = b.k * (2 * (b.lg + 1) + (b.lnu + 1) + (b.lmnu + 1) * b.nq);
+      return ca > cb;
+    });
+  };
+  cost_order(modes);
+  cost_order(modes2);
+  std::memcpy(up + segs[seg_cos].host, cos.data(), cos.size() * sizeof(CosmoDev));
+  std::memcpy(up + segs[seg_modes].host, modes.data(), modes.size() * sizeof(ModeDev));
+  if (!modes2.empty())
+    std::memcpy(up + segs[seg_modes].host + modes.size() * sizeof(ModeDev), modes2.data(),
+                modes2.size() * sizeof(ModeDev));
+  // ---- LOS inputs per C_l request (grids frozen to the unperturbed set)
+  struct LosPlan {
+    Req* r;
+    int i0, nrow, nm, ns, Lmax;
+    size_t head;
+  };
+  std::vector<LosPlan> plans;
+  for (size_t b = 0; b < batch.size(); ++b) {
+    Req* r = batch[b];
+    if (r->r.kind != BOLT_REQ_CL) continue;
+    const CosmoTables& T0 = r->T[0];
+    const GridSpec& g = r->grid;
+    const int n = g.n, nm = kNkd - 1, ns = int(r->uniq.size());
+    int i0 = 0;
+    while (i0 < n && !(g.at(i0) > -8.0)) ++i0;
+    const int nrow = n - 1 - i0;
+    char* lb = up + segs[seg_los[b]].host;
+    double* kg = reinterpret_cast<double*>(lb);
+    double* kmid = kg + r->r.nk;
+    double* dxs = kmid + nm;
+    double* misc = dxs + n;  // [0] Bessel grid step, [1] its inverse
+    int* slot = reinterpret_cast<int*>(misc + 8);
+    int* ells = slot + (r->uniq.back() + 1);
+    const size_t head = align_up(size_t(r->r.nk + nm + n + 8) * 8 + size_t(r->uniq.back() + 1 + ns) * 4);
+    double* per = reinterpret_cast<double*>(lb + head);
+    std::copy(r->k.begin(), r->k.end(), kg);
+    std::vector<double> kd(kNkd), dk(nm);
+    for (int i = 1; i <= kNkd; ++i) {  // quadratic_k(0.01 H0, 1000 H0, 5000), spectra.jl:60-63,133
+      double t = double(i) / double(kNkd);
+      kd[i - 1] = 0.01 * T0.H0 + (1000.0 * T0.H0 - 0.01 * T0.H0) * (t * t);
+    }
+    for (int m = 0; m < nm; ++m) {
+      kmid[m] = (kd[m] + kd[m + 1]) / 2.0;
+      dk[m] = kd[m + 1] - kd[m];
+    }
+    for (int i = 0; i < nrow; ++i) dxs[i] = g.at(i0 + i + 1) - g.at(i0 + i);
+    misc[0] = kd[kNkd - 1] * T0.eta0 / 5000.0;  // bessel_interpolator grid (spectra.jl:49-58)
+    misc[1] = 1.0 / misc[0];
+    for (int l = 0; l <= r->uniq.back(); ++l) slot[l] = -1;
+    for (int q = 0; q < ns; ++q) {
+      slot[r->uniq[q]] = q;
+      ells[q] = r->uniq[q];
+    }
+    for (int s = 0; s < r->nsets; ++s) {
+      const CosmoTables& T = r->T[s];
+      double* wts = per + size_t(s) * (nm + n);
+      double* yv = wts + nm;
+      for (int m = 0; m < nm; ++m) wts[m] = T.par.A * std::pow(kmid[m] / 0.05, T.par.n - 1.0) * dk[m] / kmid[m];
+      for (int i = 0; i < nrow; ++i) yv[i] = T.eta0 - spline_eval(T.coef[T_ETA].data(), n, g.x0, g.h, g.at(i0 + i));
+    }
+    plans.push_back({r, i0, nrow, nm, ns, r->uniq.back(), head});
+  }
+  // ---- enqueue
+  int launches = 0;
+  ck(cudaEventRecord(L.ev[0], st), "event");
+  for (const Seg& sg : segs)
+    if (sg.bytes) ck(cudaMemcpyAsync(dev + sg.dev, up + sg.host, sg.bytes, cudaMemcpyHostToDevice, st), "upload");
+  const ModeDev* d_modes = reinterpret_cast<const ModeDev*>(dev + o_modes);
+  const CosmoDev* d_cos = reinterpret_cast<const CosmoDev*>(dev + o_cos);
+  SolverCfg cfg;
+  cfg.reltol = batch[0]->r.reltol;  // a batch groups requests of equal tolerances
+  cfg.abstol = batch[0]->r.abstol;
+  cfg.h0 = 1e-3;
+  cfg.x_dense = -8.5;
+  cfg.max_steps = E->cfg.max_steps > 0 ? E->cfg.max_steps : 10000000;
+  for (int ph = 0; ph < nph; ++ph) {
+    RodasNodeArgs args;
+    cudaKernelNodeParams kp;
+    rodas_node_params(wpm[ph], d_modes + (ph ? m1 : 0), nmodes[ph], d_cos, cfg, L.d_queue + ph, maxN, maxnq, maxL,
+                      blocks[ph], d_scr, &args, &kp);
+    Graph& G = lane_graph(E, L, wpm[ph], ph, kp);
+    ck(cudaGraphLaunch(G.exec, st), "cudaGraphLaunch");
+    L.wpm[ph] = wpm[ph];
+    L.nmodes[ph] = nmodes[ph];
+    ++launches;
+    ck(cudaEventRecord(L.ev[1 + ph], st), "event");
+  }
+  if (nph == 1) {
+    L.nmodes[1] = 0;
+    ck(cudaEventRecord(L.ev[2], st), "event");
+  }
+  for (auto& P : plans) {
+    Req* r = P.r;
+    const int n = r->grid.n, nk = r->r.nk;
+    char* lb = dev + r->o_los;
+    const double* kg = reinterpret_cast<const double*>(lb);
+    const double* kmid = kg + nk;
+    const double* dxs = kmid + P.nm;
+    const double* misc = dxs + n;
+    const int* slot = reinterpret_cast<const int*>(misc + 8);
+    const int* ells = slot + (P.Lmax + 1);
+    const double* per = reinterpret_cast<const double*>(lb + P.head);
+    int rc = launch_jl_raw(kNb, misc, 1, P.Lmax, slot, P.ns, raw, norm, E->d_flags, st);
+    if (rc == 0) rc = launch_jl_prefilter(kNb, P.ns, 1, raw, norm, E->d_w, coef, st);
+    if (rc != 0) throw EngErr(-3, std::string("Bessel tables: ") + cudaGetErrorString(cudaError_t(rc)));
+    launches += 2;
+    const double* src = reinterpret_cast<const double*>(dev + r->o_src);
+    double* cl = reinterpret_cast<double*>(dev + r->o_cl);
+    for (int s = 0; s < r->nsets; ++s) {
+      const double* ST = src + size_t(s) * nk * n;
+      const double* SE = r->wantE ? src + size_t(r->nsets) * nk * n + size_t(s) * nk * n : nullptr;
+      rc = launch_sdense(n, P.i0, P.nrow, nk, kg, ST, SE, P.nm, kmid, dxs, SdT, SE ? SdE : nullptr, st);
+      if (rc != 0) throw EngErr(-3, std::string("source resampling: ") + cudaGetErrorString(cudaError_t(rc)));
+      const double* wts = per + size_t(s) * (P.nm + n);
+      LosArgs a;
+      a.nb = kNb; a.nslots = P.ns; a.nrow = P.nrow; a.nm = P.nm;
+      a.ells = ells; a.coef = coef; a.inv_dg = misc + 1; a.yv = wts + P.nm; a.kmid = kmid; a.wts = wts;
+      a.SdT = SdT; a.SdE = SE ? SdE : nullptr;
+      double* out = cl + size_t(s) * 3 * P.ns;
+      a.tt = out; a.te = SE ? out + P.ns : nullptr; a.ee = SE ? out + 2 * P.ns : nullptr;
+      rc = launch_los_cl(a, 1, st);
+      if (rc != 0) throw EngErr(-3, std::string("line of sight: ") + cudaGetErrorString(cudaError_t(rc)));
+      launches += 2;
+    }
+  }
+  ck(cudaEventRecord(L.ev[3], st), "event");
+  for (Req* r : batch) {
+    const int nk = r->r.nk, ns = r->nsets;
+    ck(cudaMemcpyAsync(down + r->h_stat, dev + r->o_stat, size_t(ns) * nk * 4, cudaMemcpyDeviceToHost, st), "status");
+    ck(cudaMemcpyAsync(down + r->h_cnt, dev + r->o_cnt, size_t(ns) * nk * 16, cudaMemcpyDeviceToHost, st), "counters");
+    if (r->r.kind == BOLT_REQ_CL)
+      ck(cudaMemcpyAsync(down + r->h_cl, dev + r->o_cl, size_t(ns) * 3 * r->uniq.size() * 8, cudaMemcpyDeviceToHost,
+                         st), "C_l");
+    else
+      ck(cudaMemcpyAsync(down + r->h_plin, dev + r->o_plin, size_t(ns) * nk * 8, cudaMemcpyDeviceToHost, st), "P_lin");
+  }
+  ck(cudaFreeAsync(L.d_block, st), "cudaFreeAsync batch");
+  L.d_block = nullptr;
+  ck(cudaEventRecord(L.ev[4], st), "event");
+  L.nlaunch = launches;
+}
+
+// Outputs of one request from the lane's download area (lock held).
+void finalize_request(bolt_engine* E, Lane& L, Req* r) {
+  const char* down = static_cast<const char*>(L.down.p);
+  const int nk = r->r.nk, ns = r->nsets;
+  const int32_t* st = reinterpret_cast<const int32_t*>(down + r->h_stat);
+  if (r->r.status) std::copy(st, st + nk, r->r.status);
+  for (int s = 0; s < ns && r->rc == 0; ++s)
+    for (int i = 0; i < nk; ++i) {
+      int v = st[size_t(s) * nk + i];
+      if ((v & 0xFF) != 0 || (s == 0 && ns > 1 && (v & ST_REC_OVERFLOW))) {
+        r->rc = -4;
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "mode k=%.6g (parameter set %d) ended with status %d", r->k[i], s, v);
+        r->err = buf;
+        break;
+      }
+    }
+  auto deriv = [&](const double* f, size_t stride, int j, size_t i) -> double {
+    const double h = r->step[j];
+    const double fa = f[size_t(1 + 2 * j) * stride + i], fb = f[size_t(2 + 2 * j) * stride + i];
+    if (r->one_sided[j]) {  // sets: +h, +2h
+      return (-3.0 * f[i] + 4.0 * fa - fb) / (2.0 * h);
+    }
+    return (fa - fb) / (2.0 * h);
+  };
+  if (r->r.kind == BOLT_REQ_PLIN) {
+    const double* P = reinterpret_cast<const double*>(down + r->h_plin);
+    std::copy(P, P + nk, r->r.plin);
+    if (ns > 1)
+      for (int j = 0; j < kTheta; ++j)
+        for (int i = 0; i < nk; ++i) r->r.dplin[size_t(j) * nk + i] = deriv(P, nk, j, i);
+  } else {
+    const double* cl = reinterpret_cast<const double*>(down + r->h_cl);
+    const int nsl = int(r->uniq.size());
+    const size_t stride = size_t(3) * nsl;
+    double* outs[3] = {r->r.tt, r->r.te, r->r.ee};
+    double* douts[3] = {r->r.dtt, r->r.dte, r->r.dee};
+    const int bits[3] = {BOLT_CL_TT, BOLT_CL_TE, BOLT_CL_EE};
+    for (int q = 0; q < 3; ++q) {
+      if (!(r->r.cl_want & bits[q])) continue;
+      for (int e = 0; e < r->r.nell; ++e) {
+        int sl = int(std::lower_bound(r->uniq.begin(), r->uniq.end(), r->ells[e]) - r->uniq.begin());
+        outs[q][e] = cl[size_t(q) * nsl + sl];
+        if (ns > 1)
+          for (int j = 0; j < kTheta; ++j) douts[q][size_t(j) * r->r.nell + e] = deriv(cl, stride, j, size_t(q) * nsl + sl);
+      }
+    }
+  }
+  (void)E;
+}
+
+void finish_lane(bolt_engine* E, Lane& L) {
+  float ms1 = 0, ms2 = 0, ms3 = 0;
+  cudaEventElapsedTime(&ms1, L.ev[0], L.ev[1]);
+  cudaEventElapsedTime(&ms2, L.ev[1], L.ev[2]);
+  cudaEventElapsedTime(&ms3, L.ev[2], L.ev[3]);
+  const char* down = static_cast<const char*>(L.down.p);
+  double steps[2] = {0, 0};
+  int64_t modes = 0;
+  for (Req* r : L.batch) {
+    const int64_t* cnt = reinterpret_cast<const int64_t*>(down + r->h_cnt);
+    for (int s = 0; s < r->nsets; ++s)
+      for (int i = 0; i < r->r.nk; ++i) {
+        size_t q = 2 * (size_t(s) * r->r.nk + i);
+        steps[s == 0 ? 0 : 1] += double(cnt[q] + cnt[q + 1]);
+      }
+    modes += int64_t(r->nsets) * r->r.nk;
+  }
+  E->tuner.update(L.nmodes[0], L.wpm[0], ms1 * 1e-3, steps[0]);
+  if (L.nmodes[1] > 0) E->tuner.update(L.nmodes[1], L.wpm[1], ms2 * 1e-3, steps[1]);
+  const double t = now_s(E->t0);
+  for (Req* r : L.batch) {
+    finalize_request(E, L, r);
+    r->state = 3;
+    r->t[3] = t;
+    E->inflight_bytes -= r->bytes;
+  }
+  E->stats[0] += 1;
+  E->stats[1] += int64_t(L.batch.size());
+  E->stats[2] += modes;
+  E->stats[3] += int64_t((ms1 + ms2) * 1000.0);
+  E->stats[4] += int64_t(ms3 * 1000.0);
+  E->stats[5] += int64_t(steps[0] + steps[1]);
+  E->stats[6] += L.nlaunch;
+  E->stats[7] += L.nmodes[1] > 0 ? 2 : 1;
+  E->stats[8 + (L.wpm[0] == 1 ? 0 : (L.wpm[0] == 2 ? 1 : 2))] += 1;
+  L.batch.clear();
+  L.busy = false;
+  E->cv_done.notify_all();
+}
+
+void fail_batch(bolt_engine* E, Lane& L, const std::string& msg, int code) {
+  const double t = now_s(E->t0);
+  for (Req* r : L.batch) {
+    if (r->rc == 0) { r->rc = code; r->err = msg; }
+    r->state = 3;
+    r->t[3] = t;
+    E->inflight_bytes -= r->bytes;
+  }
+  L.batch.clear();
+  L.busy = false;
+  E->cv_done.notify_all();
+}
+
+void scheduler(bolt_engine* E) {
+  cudaSetDevice(E->device);
+  std::unique_lock<std::mutex> lk(E->mu);
+  while (true) {
+    // completions
+    bool any_busy = false;
+    for (Lane& L : E->lanes) {
+      if (!L.busy) continue;
+      cudaError_t q = cudaEventQuery(L.ev[4]);
+      if (q == cudaSuccess) finish_lane(E, L);
+      else if (q != cudaErrorNotReady) fail_batch(E, L, std::string("device error: ") + cudaGetErrorString(q), -3);
+      else any_busy = true;
+    }
+    if (E->stop && !any_busy) break;
+    // new batches on idle lanes
+    if (!E->stop) {
+      for (Lane& L : E->lanes) {
+        if (L.busy || E->ready.empty()) continue;
+        std::vector<Req*> batch;
+        size_t bytes = 0;
+        const int maxb = E->cfg.max_batch > 0 ? E->cfg.max_batch : 1 << 30;
+        const double rt = E->ready.front()->r.reltol, at = E->ready.front()->r.abstol;
+        for (auto it = E->ready.begin(); it != E->ready.end() && int(batch.size()) < maxb;) {
+          Req* r = *it;
+          if (r->r.reltol != rt || r->r.abstol != at) { ++it; continue; }
+          size_t off = 0;
+          layout_request(r, off);
+          if (r->bytes > E->budget) {
+            r->rc = -5;
+            r->err = "request exceeds the device memory budget";
+            r->state = 3;
+            r->t[3] = now_s(E->t0);
+            it = E->ready.erase(it);
+            E->cv_done.notify_all();
+            continue;
+          }
+          if (E->inflight_bytes + bytes + r->bytes > E->budget) break;  // FIFO admission
+          bytes += r->bytes;
+          batch.push_back(r);
+          it = E->ready.erase(it);
+        }
+        if (batch.empty()) continue;
+        E->inflight_bytes += bytes;
+        const double t = now_s(E->t0);
+        for (Req* r : batch) { r->state = 2; r->t[2] = t; }
+        L.busy = true;
+        L.batch = batch;
+        lk.unlock();
+        std::string msg;
+        try {
+          launch_batch(E, L, L.batch);
+        } catch (const std::exception& x) {
+          msg = x.what();
+        }
+        lk.lock();
+        if (!msg.empty()) {
+          if (L.d_block) { cudaStreamSynchronize(L.st); cudaFree(L.d_block); L.d_block = nullptr; }
+          fail_batch(E, L, msg, -3);
+        }
+      }
+    }
+    E->cv_sched.wait_for(lk, std::chrono::microseconds(200));
+  }
+}
+
+}  // namespace
+
+namespace bolt {
+// Per-cosmology device table image (capi.cu's upload layout): hot[n+2][4],
+// cold[C_COUNT][n+2], GL nodes and weights.
+size_t cosmo_table_doubles(const CosmoTables& T) {
+  const size_t n2 = size_t(T.grid.n) + 2;
+  return n2 * 4 + size_t(C_COUNT) * n2 + 2 * size_t(T.nq);
+}
+
+void fill_cosmo_dev(const CosmoTables& T, double* d_tab, double* h, CosmoDev& d) {
+  const int n = T.grid.n, n2 = n + 2, nq = T.nq;
+  const int hot_ids[4] = {T_H, T_ETA, T_TAUP, T_CSB2};
+  for (int j = 0; j < n2; ++j)
+    for (int t = 0; t < 4; ++t) h[size_t(j) * 4 + t] = T.coef[hot_ids[t]][j];
+  const int cold_ids[C_COUNT] = {T_H, T_HP, T_HPP, T_ETA, T_TAU, T_TAUP, T_TAUPP, T_G, T_GP, T_GPP, T_CSB2, T_RHO0M};
+  double* cold = h + size_t(n2) * 4;
+  for (int t = 0; t < C_COUNT; ++t) std::copy(T.coef[cold_ids[t]].begin(), T.coef[cold_ids[t]].end(), cold + size_t(t) * n2);
+  double* qx = cold + size_t(C_COUNT) * n2;
+  std::copy(T.quad_pts.begin(), T.quad_pts.end(), qx);
+  std::copy(T.quad_wts.begin(), T.quad_wts.end(), qx + nq);
+  const CosmoParamsH& p = T.par;
+  d.h = p.h; d.Omega_r = p.Omega_r; d.Omega_b = p.Omega_b; d.Omega_c = p.Omega_c; d.A = p.A; d.n_s = p.n;
+  d.Y_p = p.Y_p; d.N_nu = p.N_nu; d.Sigma_m_nu = p.Sigma_m_nu;
+  d.H0 = T.H0; d.eta0 = T.eta0; d.rho_crit = T.rho_crit;
+  d.eta_last = spline_eval(T.coef[T_ETA].data(), n, T.grid.x0, T.grid.h, T.grid.at(n - 1));
+  d.x_last = T.grid.at(n - 1);
+  d.Tnu = T.Tnu; d.logqmin = T.logqmin; d.logqmax = T.logqmax;
+  d.Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
+  d.x0 = T.grid.x0; d.hx = T.grid.h; d.inv_hx = 1.0 / T.grid.h;
+  d.n = n; d.nq = nq;
+  d.hot = d_tab;
+  d.cold = d_tab + size_t(n2) * 4;
+  d.qx = d.cold + size_t(C_COUNT) * n2;
+  d.qw = d.qx + nq;
+}
+}  // namespace bolt
+
+// ------------------------------------------------------------------- C ABI
+extern "C" {
+
+int bolt_engine_create(const bolt_engine_cfg* cfg, bolt_engine** out) {
+  if (!out) return -1;
+  *out = nullptr;
+  std::unique_ptr<bolt_engine> E(new bolt_engine());
+  if (cfg) E->cfg = *cfg;
+  E->device = E->cfg.device;
+  if (E->cfg.lanes <= 0) E->cfg.lanes = 2;
+  if (E->cfg.lanes > 8) E->cfg.lanes = 8;
+  if (E->cfg.max_steps <= 0) E->cfg.max_steps = 10000000;
+  E->budget = size_t((E->cfg.mem_budget_gb > 0 ? E->cfg.mem_budget_gb : 150.0) * 1073741824.0);
+  E->t0 = std::chrono::steady_clock::now();
+  try {
+    ck(cudaSetDevice(E->device), "cudaSetDevice");
+    ck(cudaDeviceGetAttribute(&E->nsm, cudaDevAttrMultiProcessorCount, E->device), "device attribute");
+    cudaMemPool_t pool;
+    ck(cudaDeviceGetDefaultMemPool(&pool, E->device), "memory pool");
+    uint64_t thr = ~uint64_t(0);
+    ck(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr), "memory pool threshold");
+    E->lanes.resize(E->cfg.lanes);
+    for (Lane& L : E->lanes) {
+      ck(cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking), "stream");
+      for (auto& e : L.ev) ck(cudaEventCreate(&e), "event");
+      ck(cudaMalloc(&L.d_queue, 2 * sizeof(int)), "queue");
+    }
+    // Bessel prefilter pivots of the constant (1, 4, 1) system (natural ends)
+    std::vector<double> w(kNb - 2);
+    w[0] = 0.25;
+    for (int r = 1; r < kNb - 2; ++r) w[r] = 1.0 / (4.0 - w[r - 1]);
+    ck(cudaMalloc(&E->d_w, w.size() * sizeof(double)), "pivots");
+    ck(cudaMemcpy(E->d_w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice), "pivots");
+    ck(cudaMalloc(&E->d_flags, sizeof(int)), "flags");
+    ck(cudaMemset(E->d_flags, 0, sizeof(int)), "flags");
+  } catch (const std::exception& x) {
+    for (Lane& L : E->lanes) {
+      if (L.st) cudaStreamDestroy(L.st);
+      for (auto& e : L.ev) if (e) cudaEventDestroy(e);
+      if (L.d_queue) cudaFree(L.d_queue);
+    }
+    return -3;
+  }
+  int nt = E->cfg.host_threads > 0 ? E->cfg.host_threads : int(std::thread::hardware_concurrency());
+  nt = std::max(1, std::min(nt, 64));
+  bolt_engine* raw = E.get();
+  for (int i = 0; i < nt; ++i) E->pool.emplace_back(pool_worker, raw);
+  E->sched = std::thread(scheduler, raw);
+  *out = E.release();
+  return 0;
+}
+
+void bolt_engine_destroy(bolt_engine* E) {
+  if (!E) return;
+  {
+    std::lock_guard<std::mutex> g(E->mu);
+    E->stop = true;
+  }
+  E->cv_pool.notify_all();
+  E->cv_sched.notify_all();
+  for (auto& t : E->pool) t.join();
+  E->sched.join();
+  cudaSetDevice(E->device);
+  for (Lane& L : E->lanes) {
+    cudaStreamSynchronize(L.st);
+    for (auto& row : L.graph)
+      for (auto& G : row) {
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        if (G.g) cudaGraphDestroy(G.g);
+      }
+    L.scr.release(); L.los_raw.release(); L.los_norm.release(); L.los_coef.release(); L.los_SdT.release();
+    L.los_SdE.release(); L.up.release(); L.down.release();
+    cudaFree(L.d_queue);
+    for (auto& e : L.ev) cudaEventDestroy(e);
+    cudaStreamDestroy(L.st);
+  }
+  cudaFree(E->d_w);
+  cudaFree(E->d_flags);
+  delete E;
+}
+
+const char* bolt_engine_last_error(const bolt_engine* E) { return E ? E->err.c_str() : "null engine"; }
+
+int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
+  if (!E || !ticket) return -1;
+  std::unique_ptr<Req> r(new Req());
+  try {
+    check_request(q);
+    r->r = *q;
+    r->k.assign(q->k, q->k + q->nk);
+    r->r.k = r->k.data();
+    if (q->kind == BOLT_REQ_CL) {
+      r->ells.assign(q->ells, q->ells + q->nell);
+      r->r.ells = r->ells.data();
+      r->uniq = r->ells;
+      std::sort(r->uniq.begin(), r->uniq.end());
+      r->uniq.erase(std::unique(r->uniq.begin(), r->uniq.end()), r->uniq.end());
+      r->wantE = (q->cl_want & (BOLT_CL_TE | BOLT_CL_EE)) != 0;
+    } else {
+      r->r.ells = nullptr;
+      r->r.nell = 0;
+    }
+    r->grid = make_grid(q->grid.start, q->grid.step, q->grid.stop);
+    if (r->grid.n < 4 || r->grid.n > 100000) throw EngErr(-1, "x grid needs 4..100000 nodes");
+    if (q->kind == BOLT_REQ_CL && !(r->grid.at(r->grid.n - 1) > -8.0)) throw EngErr(-1, "x grid does not reach x > -8");
+    const bolt_hier& h = q->hier;
+    r->N = 2 * (h.lg + 1) + (h.lnu + 1) + (h.lmnu + 1) * h.nq + 5;
+    const size_t smem = rodas_smem_per_mode(r->N, h.nq, std::max(h.lg, std::max(h.lnu, h.lmnu)), 4);
+    if (smem > 227 * 1024) throw EngErr(-1, "hierarchy too large for shared memory");
+    CosmoParamsH base{q->par.h, q->par.Omega_r, q->par.Omega_b, q->par.Omega_c, q->par.A, q->par.n, q->par.Y_p,
+                      q->par.N_nu, q->par.Sigma_m_nu};
+    r->pars.push_back(base);
+    if (q->grad) {
+      r->nsets = 1 + 2 * kTheta;
+      double th[kTheta];
+      theta_of(base, th);
+      for (int j = 0; j < kTheta; ++j) {
+        double hstep = kRelStep * std::max(std::fabs(th[j]), j == 5 ? 0.1 : 1e-30);
+        r->step[j] = hstep;
+        r->one_sided[j] = (j == 5 && th[j] < 2.0 * hstep);
+        double a[kTheta], b[kTheta];
+        std::copy(th, th + kTheta, a);
+        std::copy(th, th + kTheta, b);
+        if (r->one_sided[j]) { a[j] += hstep; b[j] += 2.0 * hstep; }
+        else { a[j] += hstep; b[j] -= hstep; }
+        r->pars.push_back(params_of(base, a));
+        r->pars.push_back(params_of(base, b));
+      }
+    }
+    r->T.resize(r->nsets);
+    r->tables_left = r->nsets;
+  } catch (const EngErr& x) {
+    std::lock_guard<std::mutex> g(E->mu);
+    E->err = x.what();
+    return x.code;
+  } catch (const std::exception& x) {
+    std::lock_guard<std::mutex> g(E->mu);
+    E->err = x.what();
+    return -1;
+  }
+  std::lock_guard<std::mutex> g(E->mu);
+  if (E->stop) { E->err = "engine is shutting down"; return -6; }
+  r->ticket = E->next_ticket++;
+  r->t[0] = now_s(E->t0);
+  Req* rp = r.get();
+  E->reqs[r->ticket] = std::move(r);
+  E->tasks.push_back([E, rp] {
+    std::string e;
+    try { build_set(rp, 0); } catch (const std::exception& x) { e = x.what(); }
+    std::lock_guard<std::mutex> g2(E->mu);
+    set_done(E, rp, 0, e);
+  });
+  E->cv_pool.notify_one();
+  *ticket = rp->ticket;
+  return 0;
+}
+
+int bolt_engine_wait(bolt_engine* E, int64_t ticket, double timeout_s, int* rc_out, double* times_out, char* errbuf,
+                     int errlen) {
+  if (!E) return -1;
+  std::unique_lock<std::mutex> lk(E->mu);
+  auto it = E->reqs.find(ticket);
+  if (it == E->reqs.end()) { E->err = "unknown ticket"; return -2; }
+  Req* r = it->second.get();
+  auto pred = [&] { return r->state == 3; };
+  if (timeout_s < 0) E->cv_done.wait(lk, pred);
+  else if (!E->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) return 0;
+  if (rc_out) *rc_out = r->rc;
+  if (times_out) std::copy(r->t, r->t + 4, times_out);
+  if (errbuf && errlen > 0) {
+    std::strncpy(errbuf, r->err.c_str(), size_t(errlen) - 1);
+    errbuf[errlen - 1] = 0;
+  }
+  E->reqs.erase(it);
+  return 1;
+}
+
+int bolt_request_run(bolt_engine* E, const bolt_request* q, char* errbuf, int errlen) {
+  int64_t t = 0;
+  int rc = bolt_engine_submit(E, q, &t);
+  if (rc != 0) {
+    if (errbuf && errlen > 0) {
+      std::lock_guard<std::mutex> g(E->mu);
+      std::strncpy(errbuf, E->err.c_str(), size_t(errlen) - 1);
+      errbuf[errlen - 1] = 0;
+    }
+    return rc;
+  }
+  int out = 0;
+  rc = bolt_engine_wait(E, t, -1.0, &out, nullptr, errbuf, errlen);
+  return rc == 1 ? out : rc;
+}
+
+int bolt_engine_stats(bolt_engine* E, int64_t* out) {
+  if (!E || !out) return -1;
+  std::lock_guard<std::mutex> g(E->mu);
+  std::copy(E->stats, E->stats + 11, out);
+  return 0;
+}
+
+}  // extern "C"

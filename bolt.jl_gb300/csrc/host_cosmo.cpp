@@ -235,8 +235,11 @@ struct Traj {
 
 typedef std::function<void(double, const double*, double*)> OdeFn;
 
+// replay: if non-null, the accepted abscissae of an earlier run (replay[0]
+// == t0); the same steps are taken without error control, so the result is
+// a smooth function of the right-hand side's parameters.
 Traj tsit5_integrate(const OdeFn& fn, int dim, const double* y0, double t0, double t1, double rtol, double atol,
-                     std::vector<double> land) {
+                     std::vector<double> land, const std::vector<double>* replay = nullptr) {
   const double C[7] = {0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0};
   const double A[7][6] = {
       {0, 0, 0, 0, 0, 0},
@@ -261,6 +264,29 @@ Traj tsit5_integrate(const OdeFn& fn, int dim, const double* y0, double t0, doub
   tr.y.insert(tr.y.end(), y.begin(), y.end());
   tr.f.insert(tr.f.end(), K.begin(), K.begin() + dim);
   double t = t0, hnext = std::fabs(t1 - t0) * 1e-6;
+  if (replay) {
+    if (replay->empty() || (*replay)[0] != t0) throw std::runtime_error("RECFAST replay does not start at t0");
+    for (size_t i = 1; i < replay->size(); ++i) {
+      const double tn = (*replay)[i], h = tn - t;
+      for (int s = 1; s < 7; ++s) {
+        for (int d = 0; d < dim; ++d) {
+          double acc = 0.0;
+          for (int j = 0; j < s; ++j) acc += A[s][j] * K[j * dim + d];
+          tmp[d] = y[d] + h * acc;
+        }
+        double ts = s >= 5 ? tn : t + C[s] * h;
+        if (s == 6) std::copy(tmp.begin(), tmp.end(), yn.begin());
+        fn(ts, tmp.data(), &K[s * dim]);
+      }
+      t = tn;
+      y = yn;
+      std::copy(K.begin() + 6 * dim, K.begin() + 7 * dim, K.begin());
+      tr.t.push_back(t);
+      tr.y.insert(tr.y.end(), y.begin(), y.end());
+      tr.f.insert(tr.f.end(), K.begin(), K.begin() + dim);
+    }
+    return tr;
+  }
   size_t li = 0;
   long guard = 0;
   while (li < land.size()) {
@@ -469,7 +495,9 @@ double bracket_root(const std::function<double(double)>& f, double a, double b) 
 
 }  // namespace
 
-void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const RecfastOpts& ro, CosmoTables& T) {
+void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const RecfastOpts& ro, CosmoTables& T,
+                        RecfastFreeze* fz) {
+  const bool replay = fz && fz->have;
   if (g.n < 4) throw std::runtime_error("x grid needs at least 4 nodes");
   if (nq < 1) throw std::runtime_error("nq must be positive");
   if (!(p.h > 0) || !(p.Omega_b > 0) || !(p.Omega_r > 0) || !(p.N_nu > 0) || p.Sigma_m_nu < 0 || !(p.A > 0))
@@ -506,8 +534,10 @@ void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const 
   rf.init(&bg, &sH, &sHp, ro);
   T.Tnow = rf.Tnow;
   const double zini = 10000.0, zfin = 0.0, zre_ini = 50.0;
-  double zHe = bracket_root([&](double z) { return (rf.xtot_He1_saha(z) - 1.0) / rf.fHe - 0.99; }, std::min(zini, 3500.0), zfin);
-  double zHH = bracket_root([&](double z) { return rf.xH_saha(z) - 0.985; }, zHe, zfin);
+  double zHe = replay ? fz->zHe
+                      : bracket_root([&](double z) { return (rf.xtot_He1_saha(z) - 1.0) / rf.fHe - 0.99; },
+                                     std::min(zini, 3500.0), zfin);
+  double zHH = replay ? fz->zHH : bracket_root([&](double z) { return rf.xH_saha(z) - 0.985; }, zHe, zfin);
   T.z_He_evo_start = zHe;
   T.z_H_He_evo_start = zHH;
   std::vector<double> zland;
@@ -523,12 +553,12 @@ void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const 
         du[0] = d[1];
         du[1] = d[2];
       },
-      2, y2, zHe, zHH, rf.tol, 1e-6, zland);
+      2, y2, zHe, zHH, rf.tol, 1e-6, zland, replay ? &fz->tHe : nullptr);
   double y3[3] = {rf.xH_saha(zHH), He.last()[0], He.last()[1]};
   std::vector<double> land3 = zland;
   land3.push_back(zre_ini);
   Traj HHe = tsit5_integrate([&](double z, const double* u, double* du) { rf.rhs(z, u, du); }, 3, y3, zHH, zfin, rf.tol,
-                             1e-6, land3);
+                             1e-6, land3, replay ? &fz->tHHe : nullptr);
   auto xe_recfast = [&](double z) -> double {  // recfast.jl:413-433
     if (z > 8000.) return 1 + 2 * rf.fHe;
     if (z > 5000.) {
@@ -561,7 +591,15 @@ void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const 
         double Hz = sH(std::log(a)) / a / sec_per_nat(), Trad = rf.Tnow * (1 + z);
         du[0] = rf.CT * std::pow(Trad, 4) * xr / (1 + xr + rf.fHe) * (u[0] - Trad) / (Hz * (1 + z)) + 2 * u[0] / (1 + z);
       },
-      1, &T50, zre_ini, zfin, rf.tol, 1e-6, zland);
+      1, &T50, zre_ini, zfin, rf.tol, 1e-6, zland, replay ? &fz->tRe : nullptr);
+  if (fz && !replay) {
+    fz->zHe = zHe;
+    fz->zHH = zHH;
+    fz->tHe = He.t;
+    fz->tHHe = HHe.t;
+    fz->tRe = Re.t;
+    fz->have = true;
+  }
 
   // --- node values (recfast.jl:689-708)
   double xini = std::log(1.0 / (zini + 1.0));

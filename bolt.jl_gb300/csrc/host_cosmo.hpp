@@ -74,8 +74,22 @@ double spline_deriv2(const double* c, int n, double x0, double h, double x);
 double units_km_s_Mpc_100();
 double units_mass_eV();
 
+// The discretisation choices of one RECFAST run: the two Saha switch
+// redshifts (root finds) and the accepted abscissae of its three Tsit5
+// integrations.  Replaying them makes the tables a smooth function of the
+// parameters, for derivatives by central differences; the switch redshifts
+// are held fixed as the reference's ForwardDiff gradient does
+// (recfast.jl:451-456, assume_nondual).
+struct RecfastFreeze {
+  bool have = false;
+  double zHe = 0.0, zHH = 0.0;
+  std::vector<double> tHe, tHHe, tRe;
+};
+
 // Builds Background + RECFAST + IonizationHistory.  Throws std::runtime_error.
-void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const RecfastOpts& r, CosmoTables& out);
+// freeze: null, or recorded into when empty, or replayed when filled.
+void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const RecfastOpts& r, CosmoTables& out,
+                        RecfastFreeze* freeze = nullptr);
 
 // Gauss-Legendre nodes and weights on [-1, 1].
 void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);

@@ -199,17 +199,46 @@ struct LosArgs {
   double* ee;
 };
 
+constexpr double kSkipRel = 1e-14;
+
 __global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
   extern __shared__ double sh[];
   const int s = blockIdx.x, cz = blockIdx.y;
   const int nb2 = a.nb + 2;
   double* cs = sh;                 // nb + 2 coefficients
   double* yl = sh + nb2;           // nrow scaled arguments
-  double* red = yl + a.nrow;       // 3 * blockDim
   const double* src = a.coef + ((size_t)cz * a.nslots + s) * nb2;
   for (int j = threadIdx.x; j < nb2; j += blockDim.x) cs[j] = src[j];
   const double idg = a.inv_dg[cz];
   for (int j = threadIdx.x; j < a.nrow; j += blockDim.x) yl[j] = a.yv[(size_t)cz * a.nrow + j] * idg;
+  // Below its turning point j_l is negligible: find the first coefficient
+  // above kSkipRel of the largest; terms whose four coefficients all lie
+  // below it change C_l by less than ~kSkipRel relative and are skipped.
+  double cmax = 0.0;
+  for (int j = threadIdx.x; j < nb2; j += blockDim.x) cmax = fmax(cmax, fabs(cs[j]));
+  double* red = yl + a.nrow;  // 3 * blockDim
+  red[threadIdx.x] = cmax;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  const double thr = kSkipRel * red[0];
+  int jfirst = nb2;
+  for (int j = threadIdx.x; j < nb2; j += blockDim.x)
+    if (fabs(cs[j]) > thr) { jfirst = j; break; }
+  __syncthreads();
+  reinterpret_cast<int*>(red)[threadIdx.x] = jfirst;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      int* ir = reinterpret_cast<int*>(red);
+      ir[threadIdx.x] = min(ir[threadIdx.x], ir[threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  // keep a term when floor(u) + 3 >= jfirst, i.e. u >= ulo
+  const double ulo = double(reinterpret_cast<int*>(red)[0] - 3);
   __syncthreads();
   const int l = a.ells[s];
   const double lfac = sqrt(double((long long)(l + 2) * (l + 1) * (long long)l * (l - 1)));
@@ -222,7 +251,17 @@ __global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
   for (int m = threadIdx.x; m < a.nm; m += blockDim.x) {
     const double k = km[m];
     double th = 0.0, ep = 0.0;
-    for (int i = 0; i < a.nrow; ++i) {
+    // u = k yl[i] decreases with i: the kept terms are i < iend
+    int iend = 0;
+    if (k * yl[0] >= ulo) {
+      int lo = 0, hi = a.nrow;  // k yl[lo] >= ulo, k yl[hi] < ulo (hi = nrow: none)
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (k * yl[mid] >= ulo) lo = mid; else hi = mid;
+      }
+      iend = hi;
+    }
+    for (int i = 0; i < iend; ++i) {
       double u = k * yl[i];
       double f = floor(u);
       f = fmin(f, umax);

@@ -77,13 +77,16 @@ struct Scratch {
   double *y, *fx, *K, *yp, *fp;  // K: 6 x N
 };
 
-constexpr int kMiscDoubles = 32 + 9 * 32;        // capacitance, reductions, per-chain partials
-constexpr int kPackInts = 128 * 2 + 128 * 8 + 32 + 2;  // lane packing of the chains (chains.cuh)
+constexpr int kMiscDoubles = 32 + 9 * 32;  // capacitance, reductions, per-chain partials
 
-__host__ __device__ inline int per_warp_doubles(int N, int nq, int Lmax) {
+// Lane packing of the chains (chains.cuh): seg + chain per thread, the
+// element lists (768 ints for every variant), owners and two counters.
+__host__ __device__ inline int pack_ints(int threads) { return 2 * threads + 768 + 32 + 2; }
+
+__host__ __device__ inline int per_mode_doubles(int N, int nq, int Lmax, int threads) {
   int nch = nq + 5;
   return 5 * N + 4 * nq + 2 * kStages * nq + 2 * nq + 2 * nch * kTail * kBorder + 2 * (Lmax + 1) + kStages * kScal +
-         kScal + kMiscDoubles + (kPackInts + 1) / 2;
+         kScal + kMiscDoubles + (pack_ints(threads) + 1) / 2;
 }
 __host__ __device__ inline int scratch_per_warp(int N) { return 10 * N; }
 
@@ -399,8 +402,10 @@ __device__ void emit_sources(const Mode& m, const Shared& S, double x, const dou
   *outT = term1 + term2 + term3;
   // same spline, same evaluation as eta(x): y is exactly 0 at the last node,
   // where the reference's 3 / (4 y^2) is infinite (perturbations.jl:401-403)
-  double y = (x == C.x_last) ? 0.0 : k * (spl_cold(C, C_ETA, C.x_last) - eta);
-  *outE = (3.0 / (4.0 * y * y)) * g * Pi;
+  if (outE) {  // null when the caller wants S_T only
+    double y = (x == C.x_last) ? 0.0 : k * (spl_cold(C, C_ETA, C.x_last) - eta);
+    *outE = (3.0 / (4.0 * y * y)) * g * Pi;
+  }
 }
 
 // plin (spectra.jl:163-198) at the final node x.
@@ -499,13 +504,14 @@ __device__ unsigned long long g_phase_cycles[16];
 #define PT_FLUSH
 #endif
 
-// One CTA (kWarpsPerMode warps) integrates one mode.  Row-parallel work (the
+// One CTA of WPM warps integrates one mode.  Row-parallel work (the
 // right-hand sides, the stage combinations, the error norm, dense output) is
-// spread over all threads, so a mode's FP64 work is issued from every SM
-// sub-partition; the serial chain sweeps (factorisation and solves) run in
-// warp 0 with one lane per chain.
-constexpr int kWarpsPerMode = 4;
-constexpr int kThreads = 32 * kWarpsPerMode;
+// spread over all threads; the chain recurrences run as segmented scans over
+// all lanes (chains.cuh).  WPM = 4 spreads a mode's FP64 work over the four
+// SM sub-partitions (lowest latency per step); WPM = 1 issues the fewest
+// FP64 instructions per step (no per-warp duplicated scalar work, longer
+// per-lane scans) and fits more modes on an SM (highest throughput when
+// many modes are in flight).
 
 // Cubic Hermite interpolation on [x0, x1] from (y0, f0, y1, f1) into u.
 __device__ __forceinline__ void hermite(int N, double x0, double x1, double xq, const double* y0, const double* f0,
@@ -521,20 +527,24 @@ __device__ __forceinline__ void copy_vec(int N, const double* src, double* dst, 
   for (int i = tid; i < N; i += nth) dst[i] = src[i];
 }
 
-// Block sum of one value per thread (red: >= kWarpsPerMode doubles of smem).
+// Block sum of one value per thread (red: >= WPM doubles of smem).
+template <int WPM>
 __device__ __forceinline__ double block_sum(double v, double* red, int tid) {
   v = warp_sum(v);
+  if (WPM == 1) return v;
   if ((tid & 31) == 0) red[tid >> 5] = v;
   __syncthreads();
   double t = 0.0;
-  for (int w = 0; w < kWarpsPerMode; ++w) t += red[w];
+  for (int w = 0; w < WPM; ++w) t += red[w];
   __syncthreads();
   return t;
 }
 
+template <int WPM>
 __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const SolverCfg& cfg, double* base,
                           double* gscr, int tid) {
-  const int nth = kThreads, lane = tid & 31, warp = tid >> 5;
+  constexpr int nth = 32 * WPM;
+  const int lane = tid & 31, warp = tid >> 5;
   Mode m;
   m.C = cosmos + md.cosmo;
   m.k = md.k;
@@ -575,11 +585,12 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   Pack PK;
   {
     int* ip = reinterpret_cast<int*>(p);
-    PK.seg = ip; ip += 128;
-    PK.chain = ip; ip += 128;
-    PK.idx = ip; ip += 128 * kEmax;
+    PK.seg = ip; ip += nth;
+    PK.chain = ip; ip += nth;
+    PK.idx = ip; ip += kLaneElems;
     PK.owner = ip; ip += 32;
     PK.E = ip;
+    PK.em = kLaneElems / nth;
   }
   Scratch G;
   G.y = gscr;
@@ -627,6 +638,8 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     while (jd < md.nout - 1 && md.xout[jd] < cfg.x_dense) ++jd;
   double h = cfg.h0;
   const double rtol = cfg.reltol, atol = cfg.abstol;
+  const bool record = (md.flags & MODE_RECORD) != 0, replay = (md.flags & MODE_REPLAY) != 0;
+  bool rec_over = false;
   double xprev = x;
   bool have_prev = false;
   double x_done = -1e300;  // last abscissa whose outputs were emitted
@@ -648,7 +661,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
             prepare_other(m, S, xq, tid, nth);
             rhs_rows<double>(m, S, 5, S.yt, G.K, nullptr, tid, nth);
             __syncthreads();
-            if (warp == 0) emit_sources(m, S, xq, S.yt, G.K, lane, md.src_T + jo, md.src_E + jo);
+            if (warp == 0) emit_sources(m, S, xq, S.yt, G.K, lane, md.src_T + jo, md.src_E ? md.src_E + jo : nullptr);
             __syncthreads();
             ++jo;
           }
@@ -658,7 +671,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
         }
         if (jo < md.nout && md.xout[jo] == x) {
           if ((md.flags & MODE_SOURCES) && warp == 0)
-            emit_sources(m, S, x, S.yt, Kf, lane, md.src_T + jo, md.src_E + jo);
+            emit_sources(m, S, x, S.yt, Kf, lane, md.src_T + jo, md.src_E ? md.src_E + jo : nullptr);
           if (md.flags & MODE_TRAJ)
             for (int i = tid; i < N; i += nth) md.traj[(size_t)jo * N + i] = G.y[i];
           ++jo;
@@ -679,8 +692,14 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     bool landing = false;
     double hs = h;
     if (x + hs >= target - 1e-14 * fabs(target)) { hs = target - x; landing = true; }
+    double xn = landing ? target : x + hs;
+    if (replay) {
+      if (nacc >= md.rec_cap) { status = ST_REPLAY_SHORT; break; }
+      xn = md.rec[nacc];
+      hs = xn - x;
+      landing = (xn == target);
+    }
     if (!(hs > 0.0)) { status = ST_DT_UNDERFLOW; break; }
-    const double xn = landing ? target : x + hs;
     PT(9)
     prepare_stages(m, S, x, hs, xn, tid, nth);
     PT(0)
@@ -706,7 +725,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
           prepare_other(m, S, xq, tid, nth);
           rhs_rows<double>(m, S, 5, S.yt, G.K + N, nullptr, tid, nth);
           __syncthreads();
-          if (warp == 0) emit_sources(m, S, xq, S.yt, G.K + N, lane, md.src_T + jo, md.src_E + jo);
+          if (warp == 0) emit_sources(m, S, xq, S.yt, G.K + N, lane, md.src_T + jo, md.src_E ? md.src_E + jo : nullptr);
           __syncthreads();
           ++jo;
         }
@@ -715,7 +734,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       }
       if (jo < md.nout && md.xout[jo] == x) {
         if ((md.flags & MODE_SOURCES) && warp == 0)
-          emit_sources(m, S, x, S.yt, S.b, lane, md.src_T + jo, md.src_E + jo);
+          emit_sources(m, S, x, S.yt, S.b, lane, md.src_T + jo, md.src_E ? md.src_E + jo : nullptr);
         if (md.flags & MODE_TRAJ)
           for (int i = tid; i < N; i += nth) md.traj[(size_t)jo * N + i] = G.y[i];
         ++jo;
@@ -776,13 +795,21 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       en += e * e;
       fin = fin && isfinite(yn);
     }
-    en = sqrt(block_sum(en, red, tid) / N);
+    en = sqrt(block_sum<WPM>(en, red, tid) / N);
     fin = __syncthreads_and(fin);
     if (!fin || !(en == en)) en = 1e10;
+    if (replay) {
+      if (!fin) { status = ST_NONFINITE; break; }
+      en = 0.0;
+    }
     double fac = 0.9 * pow(fmax(en, 1e-12), -0.25);
     fac = fmin(6.0, fmax(0.2, fac));
     if (en <= 1.0) {
       for (int i = tid; i < N; i += nth) G.y[i] = S.yt[i] + S.b[i];
+      if (record && tid == 0) {
+        if (nacc < md.rec_cap) md.rec[nacc] = xn;
+        else rec_over = true;
+      }
       __syncthreads();
       x = xn;
       ++nacc;
@@ -798,7 +825,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   }
   PT_FLUSH
   if (tid == 0) {
-    *md.status = status | (rsa_any ? ST_RSA_FIRED : 0);
+    *md.status = status | (rsa_any ? ST_RSA_FIRED : 0) | (rec_over ? ST_REC_OVERFLOW : 0);
     if (md.counters) { md.counters[0] = nacc; md.counters[1] = nrej; }
   }
 }
@@ -806,17 +833,18 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
 // Persistent CTAs: the first wave takes modes blockIdx.x (modes arrive sorted
 // by decreasing cost, and consecutive blocks land on different SMs, so the
 // longest modes spread one per SM); later modes come from a device queue.
-__global__ void __launch_bounds__(kThreads) rodas_kernel(const ModeDev* __restrict__ modes, int nmodes,
+template <int WPM>
+__global__ void __launch_bounds__(32 * WPM) rodas_kernel(const ModeDev* __restrict__ modes, int nmodes,
                                                          const CosmoDev* __restrict__ cosmos, SolverCfg cfg,
-                                                         int* __restrict__ queue, int per_mode,
-                                                         double* __restrict__ scratch, int scr_per_mode) {
+                                                         int* __restrict__ queue, double* __restrict__ scratch,
+                                                         int scr_per_mode) {
   extern __shared__ double smem[];
   __shared__ int s_mode;
   const int tid = threadIdx.x;
   double* gscr = scratch + (size_t)blockIdx.x * scr_per_mode;
   int mi = blockIdx.x;
   while (mi < nmodes) {
-    solve_one(modes[mi], cosmos, cfg, smem, gscr, tid);
+    solve_one<WPM>(modes[mi], cosmos, cfg, smem, gscr, tid);
     __syncthreads();
     if (tid == 0) s_mode = gridDim.x + atomicAdd(queue, 1);
     __syncthreads();
@@ -824,37 +852,84 @@ __global__ void __launch_bounds__(kThreads) rodas_kernel(const ModeDev* __restri
   }
 }
 
-// Host helpers: CTAs to launch (one mode each at a time).
-int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int /*unused*/, int* blocks) {
-  int per_mode = per_warp_doubles(maxN, maxnq, maxL);
-  size_t smem = size_t(per_mode) * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(rodas_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+namespace {
+template <int WPM>
+int grid_for(int nmodes, size_t smem, int* blocks) {
+  cudaError_t e = cudaFuncSetAttribute(rodas_kernel<WPM>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return -int(e);
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int bps = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, rodas_kernel, kThreads, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, rodas_kernel<WPM>, 32 * WPM, smem);
   if (e != cudaSuccess) return -int(e);
   if (bps < 1) return -int(cudaErrorInvalidConfiguration);
   *blocks = std::min(nmodes, nsm * bps);
   return 0;
 }
+int norm_wpm(int wpm) { return (wpm == 1 || wpm == 2) ? wpm : 4; }
+}  // namespace
+
+// Host helpers.  wpm: warps per mode (1, 2 or 4; anything else means 4).
+// Writes the number of persistent CTAs to launch (one mode each at a time).
+int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, int* blocks) {
+  wpm = norm_wpm(wpm);
+  size_t smem = size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * wpm)) * sizeof(double);
+  if (wpm == 1) return grid_for<1>(nmodes, smem, blocks);
+  if (wpm == 2) return grid_for<2>(nmodes, smem, blocks);
+  return grid_for<4>(nmodes, smem, blocks);
+}
 
 int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
-                 int maxN, int maxnq, int maxL, int /*unused*/, int blocks, double* d_scratch, cudaStream_t stream) {
-  int per_mode = per_warp_doubles(maxN, maxnq, maxL);
-  size_t smem = size_t(per_mode) * sizeof(double);
+                 int maxN, int maxnq, int maxL, int wpm, int blocks, double* d_scratch, cudaStream_t stream) {
+  wpm = norm_wpm(wpm);
+  size_t smem = size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * wpm)) * sizeof(double);
   cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  rodas_kernel<<<blocks, kThreads, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, per_mode, d_scratch,
-                                                   scratch_per_warp(maxN));
+  const int spm = scratch_per_warp(maxN);
+  if (wpm == 1)
+    rodas_kernel<1><<<blocks, 32, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+  else if (wpm == 2)
+    rodas_kernel<2><<<blocks, 64, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+  else
+    rodas_kernel<4><<<blocks, 128, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
   return cudaGetLastError();
 }
 
-size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL) {
-  return size_t(per_warp_doubles(maxN, maxnq, maxL)) * sizeof(double);
+// Kernel-node description of one solver launch, for CUDA graphs whose
+// node parameters are updated per batch.  args must stay alive until the
+// node parameters have been set (the values are copied then).
+int rodas_node_params(int wpm, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg,
+                      int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch, RodasNodeArgs* args,
+                      cudaKernelNodeParams* p) {
+  wpm = norm_wpm(wpm);
+  args->modes = d_modes;
+  args->nmodes = nmodes;
+  args->cosmos = d_cosmos;
+  args->cfg = cfg;
+  args->queue = d_queue;
+  args->scratch = d_scratch;
+  args->spm = scratch_per_warp(maxN);
+  args->ptrs[0] = &args->modes;
+  args->ptrs[1] = &args->nmodes;
+  args->ptrs[2] = &args->cosmos;
+  args->ptrs[3] = &args->cfg;
+  args->ptrs[4] = &args->queue;
+  args->ptrs[5] = &args->scratch;
+  args->ptrs[6] = &args->spm;
+  p->func = wpm == 1 ? (void*)rodas_kernel<1> : (wpm == 2 ? (void*)rodas_kernel<2> : (void*)rodas_kernel<4>);
+  p->gridDim = dim3(blocks);
+  p->blockDim = dim3(32 * wpm);
+  p->sharedMemBytes = unsigned(size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * wpm)) * sizeof(double));
+  p->kernelParams = args->ptrs;
+  p->extra = nullptr;
+  return 0;
 }
+
+size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm) {
+  return size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * norm_wpm(wpm))) * sizeof(double);
+}
+size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL) { return rodas_smem_per_mode(maxN, maxnq, maxL, 4); }
 size_t rodas_scratch_per_warp(int maxN) { return size_t(scratch_per_warp(maxN)) * sizeof(double); }
 
 #ifdef BOLT_PHASE_TIMERS
@@ -867,6 +942,5 @@ int rodas_phase_cycles(unsigned long long* out, bool reset) {
   return int(e);
 }
 #endif
-int rodas_warps_per_mode() { return kWarpsPerMode; }
 
 }  // namespace bolt

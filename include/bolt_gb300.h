@@ -158,6 +158,99 @@ int bolt_source_grid_static(const bolt_params* par, const bolt_grid* grid, int n
  * denominator for the FP64-pipe-bound kernels. */
 int bolt_fp64_peak(int device, double* tflops);
 
+/* ------------------------------------------------------------------------
+ * Batched and served requests (the serving side of plin / cltt / clte /
+ * clee, with gradients for the rrule of the Julia binding).
+ *
+ * A request is one cosmology with its own k grid, hierarchy, tolerances and
+ * outputs: P_lin(k) at x (plin, spectra.jl:163-198) or C_l^TT/TE/EE for its
+ * multipoles (source_grid + cltt/clte/clee, spectra.jl:6-160; source grid
+ * on the request's k grid, dense k grid quadratic_k(0.01 H0, 1000 H0, 5000)).
+ * Background and RECFAST are built on the host (worker threads) from the
+ * parameters (RECFAST's Yp/OmegaB/OmegaG from the parameters, tol 1e-8).
+ *
+ * Gradients (grad = 1) are with respect to
+ *   theta = (h, omega_b = Omega_b h^2, omega_c = Omega_c h^2, n, A, Sigma m_nu [eV])
+ * with Omega_r, Y_p and N_nu held fixed: d/dtheta of the discrete pipeline
+ * by central differences (relative step 1e-5; one-sided at Sigma m_nu ~ 0)
+ * with every discretisation choice frozen -- the perturbed modes replay the
+ * accepted steps of the unperturbed solve, RECFAST replays its steps and
+ * switch redshifts, and the k grids and the Bessel grid stay those of the
+ * unperturbed cosmology (the reference's assume_nondual points,
+ * spectra.jl:46-66, recfast.jl:451-456).  Layout d*[6][n].
+ *
+ * Output arrays are caller-owned host memory that must stay valid (and
+ * untouched) until the request has completed.
+ * ---------------------------------------------------------------------- */
+enum { BOLT_REQ_PLIN = 1, BOLT_REQ_CL = 2 };
+enum { BOLT_CL_TT = 1, BOLT_CL_TE = 2, BOLT_CL_EE = 4 };
+
+typedef struct {
+  int kind;              /* BOLT_REQ_PLIN or BOLT_REQ_CL */
+  int grad;              /* 1: also the Jacobian with respect to theta */
+  bolt_params par;
+  bolt_grid grid;        /* Background x grid (e.g. -20:0.01:0) */
+  int nq;                /* massive-neutrino momentum bins (Background nq) */
+  bolt_hier hier;        /* hier.nq must equal nq */
+  double reltol, abstol;
+  const double* k;       /* [nk] ascending wavenumbers, Mpc^-1 (copied at submit) */
+  int nk;
+  double plin_x;         /* BOLT_REQ_PLIN: x at which P_lin is evaluated */
+  const int* ells;       /* BOLT_REQ_CL: [nell] multipoles (copied at submit) */
+  int nell;
+  int cl_want;           /* BOLT_CL_* bits */
+  /* outputs */
+  double* plin;          /* [nk] */
+  double* dplin;         /* [6][nk] (grad) */
+  double *tt, *te, *ee;  /* [nell] each, per cl_want */
+  double *dtt, *dte, *dee; /* [6][nell] each (grad), per cl_want */
+  int32_t* status;       /* [nk] status of the unperturbed modes, or NULL */
+} bolt_request;
+
+typedef struct {
+  int device;
+  int lanes;             /* batches in flight on separate streams (0 = 2) */
+  int host_threads;      /* table-building threads (0 = hardware threads) */
+  int max_batch;         /* requests per batch (0 = unlimited; 1 = one request per batch) */
+  double mem_budget_gb;  /* device memory admitted to in-flight requests (0 = 150) */
+  int warps_per_mode;    /* 0 = autotune per batch size, else 1, 2 or 4 */
+  long long max_steps;   /* per mode (0 = 10^7) */
+} bolt_engine_cfg;
+
+typedef struct bolt_engine bolt_engine;
+
+/* Creates an engine bound to one GPU: a scheduler thread forms batches from
+ * the requests whose tables are ready (admitted while the in-flight device
+ * footprint stays within the budget), runs every k-mode of a batch in one
+ * persistent solver launch (a CUDA graph whose kernel node is updated per
+ * batch; warps per mode autotuned by batch size), then the line-of-sight
+ * projections, on one of `lanes` streams, so a batch starts while earlier
+ * ones are still on the GPU. */
+int bolt_engine_create(const bolt_engine_cfg* cfg, bolt_engine** out);
+void bolt_engine_destroy(bolt_engine* eng);
+const char* bolt_engine_last_error(const bolt_engine* eng);
+
+/* Queues a request (validated and copied; outputs written on completion).
+ * Returns 0 and a ticket, or a negative code (message in last_error). */
+int bolt_engine_submit(bolt_engine* eng, const bolt_request* req, int64_t* ticket);
+
+/* Waits up to timeout_s (< 0: forever) for a ticket.  Returns 1 when done
+ * (the ticket is then released; rc_out = 0 or the request's negative error
+ * code, message in errbuf), 0 on timeout, negative on an unknown ticket.
+ * times_out (optional, seconds since engine creation): [0] submitted,
+ * [1] tables ready, [2] batch launched, [3] completed. */
+int bolt_engine_wait(bolt_engine* eng, int64_t ticket, double timeout_s, int* rc_out, double* times_out,
+                     char* errbuf, int errlen);
+
+/* One request, alone: submit + wait (the one-request-per-call path). */
+int bolt_request_run(bolt_engine* eng, const bolt_request* req, char* errbuf, int errlen);
+
+/* Engine counters: [0] batches, [1] requests completed, [2] modes solved,
+ * [3] solver microseconds (sum over batches), [4] LOS microseconds,
+ * [5] accepted + rejected steps, [6] kernel launches, [7] graph launches,
+ * [8..10] batches run with 1 / 2 / 4 warps per mode. */
+int bolt_engine_stats(bolt_engine* eng, int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -80,6 +80,12 @@ def lib():
         L.oracle_sph_bessel.argtypes = [C.c_int, C.c_double, _dp]
         L.oracle_cl.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double,
                                 C.c_int, _dp, _dp, _dp, C.c_int]
+        L.oracle_cl_frozen.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, _ip, C.c_int, C.c_double,
+                                       C.c_double, C.c_int, C.c_double, _dp, _dp, _dp, C.c_int]
+        L.oracle_cosmo_new_atol.restype = C.c_void_p
+        L.oracle_cosmo_new_atol.argtypes = [C.POINTER(_Params), C.c_double, C.c_double, C.c_double, C.c_int,
+                                            C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                            C.c_double]
         L.oracle_plin.restype = C.c_double
         L.oracle_plin.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                   C.c_double, C.c_double, _ip]
@@ -129,12 +135,16 @@ class Cosmo:
     """Background + RECFAST IonizationHistory for one parameter set."""
 
     def __init__(self, p: Params, x_grid=(-20.0, 0.01, 0.0), nq=15, OmegaG=None, Tnow=-1.0,
-                 recfast_tol=1e-8):
+                 recfast_tol=1e-8, recfast_atol=None):
         self.p = p
         self._pc = p.c()
         og = p.Omega_r if OmegaG is None else OmegaG
-        self.h = lib().oracle_cosmo_new(C.byref(self._pc), x_grid[0], x_grid[1], x_grid[2], nq,
-                                        p.Y_p, p.Omega_b, og, Tnow, recfast_tol)
+        if recfast_atol is None:
+            self.h = lib().oracle_cosmo_new(C.byref(self._pc), x_grid[0], x_grid[1], x_grid[2], nq,
+                                            p.Y_p, p.Omega_b, og, Tnow, recfast_tol)
+        else:
+            self.h = lib().oracle_cosmo_new_atol(C.byref(self._pc), x_grid[0], x_grid[1], x_grid[2], nq,
+                                                 p.Y_p, p.Omega_b, og, Tnow, recfast_tol, recfast_atol)
         if not self.h:
             raise RuntimeError("oracle_cosmo_new failed")
         self.nx = lib().oracle_cosmo_ngrid(self.h)
@@ -204,7 +214,7 @@ class Cosmo:
             raise RuntimeError(f"oracle_source_grid status {rc}")
         return ST, SE, steps
 
-    def cl(self, ST, SE, k_grid, ells, kd=None, nthreads=0):
+    def cl(self, ST, SE, k_grid, ells, kd=None, nthreads=0, bessel_argmax=None):
         ells = np.ascontiguousarray(ells, dtype=np.int32)
         k_grid = np.ascontiguousarray(k_grid, dtype=np.float64)
         ST = np.ascontiguousarray(ST, dtype=np.float64)
@@ -212,9 +222,9 @@ class Cosmo:
         if kd is None:
             kd = (0.01 * self.H0, 1000.0 * self.H0, 5000)
         tt, te, ee = (np.zeros(len(ells)) for _ in range(3))
-        lib().oracle_cl(self.h, _d(ST), _d(SE), _d(k_grid), len(k_grid),
-                        ells.ctypes.data_as(_ip), len(ells), kd[0], kd[1], kd[2], _d(tt), _d(te), _d(ee),
-                        nthreads)
+        lib().oracle_cl_frozen(self.h, _d(ST), _d(SE), _d(k_grid), len(k_grid), ells.ctypes.data_as(_ip),
+                               len(ells), kd[0], kd[1], kd[2], -1.0 if bessel_argmax is None else bessel_argmax,
+                               _d(tt), _d(te), _d(ee), nthreads)
         return tt, te, ee
 
     def plin(self, k, nq=15, lg=50, lnu=50, lmnu=20, x=0.0, reltol=1e-5, abstol=1e-6):

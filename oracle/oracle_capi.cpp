@@ -52,6 +52,26 @@ void* oracle_cosmo_new(const oracle_params* p, double x_start, double x_step, do
   }
 }
 
+// As oracle_cosmo_new with RECFAST's absolute tolerance set too (tight
+// tables for finite-difference gradient checks).
+void* oracle_cosmo_new_atol(const oracle_params* p, double x_start, double x_step, double x_stop, int nq, double Yp,
+                            double OmegaB, double OmegaG, double Tnow, double recfast_tol, double recfast_atol) {
+  try {
+    OCosmo* o = new OCosmo();
+    o->C.par = to_params(p);
+    o->bg.reset(new Background(o->C.par, Grid::range(x_start, x_step, x_stop), nq));
+    o->rf.reset(new Recfast(o->bg.get(), Yp, OmegaB, OmegaG, Tnow, recfast_tol));
+    o->rf->atol = recfast_atol;
+    o->ih.reset(new Ionization(*o->rf, o->C.par, *o->bg));
+    o->C.bg = o->bg.get();
+    o->C.ih = o->ih.get();
+    return o;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_cosmo_new_atol: %s\n", e.what());
+    return nullptr;
+  }
+}
+
 void oracle_cosmo_free(void* h) { delete static_cast<OCosmo*>(h); }
 
 int oracle_cosmo_ngrid(void* h) { return static_cast<OCosmo*>(h)->bg->xg.n; }
@@ -194,6 +214,15 @@ int oracle_source_grid(void* h, const double* kg, int nk, int lg, int lnu, int l
   return worst;
 }
 
+int oracle_cl_frozen(void* h, const double* ST, const double* SE, const double* kg, int nk, const int* ells, int nell,
+                     double kd_min, double kd_max, int nkd, double argmax_in, double* tt, double* te, double* ee,
+                     int nthreads);
+
+int oracle_cl(void* h, const double* ST, const double* SE, const double* kg, int nk, const int* ells, int nell,
+              double kd_min, double kd_max, int nkd, double* tt, double* te, double* ee, int nthreads) {
+  return oracle_cl_frozen(h, ST, SE, kg, nk, ells, nell, kd_min, kd_max, nkd, -1.0, tt, te, ee, nthreads);
+}
+
 // quadratic_k (spectra.jl:60-63)
 void oracle_quadratic_k(double kmin, double kmax, int nk, double* out) {
   for (int i = 1; i <= nk; ++i) {
@@ -213,8 +242,12 @@ void oracle_sph_bessel(int L, double x, double* out) { sph_bessel_all(L, x, out)
 // cltt / clte / clee (spectra.jl:49-160) on a precomputed source grid.
 // The dense k grid is quadratic_k(kd_min, kd_max, nkd); the reference uses
 // (0.01 H0, 1000 H0, 5000).  Any of tt/te/ee may be null.
-int oracle_cl(void* h, const double* ST, const double* SE, const double* kg, int nk, const int* ells, int nell,
-              double kd_min, double kd_max, int nkd, double* tt, double* te, double* ee, int nthreads) {
+// argmax_in > 0 fixes the Bessel grid's upper end (spectra.jl:49-52 with the
+// argument held constant, as assume_nondual does under ForwardDiff); <= 0
+// takes kd_max * eta0 of this cosmology.
+int oracle_cl_frozen(void* h, const double* ST, const double* SE, const double* kg, int nk, const int* ells, int nell,
+                     double kd_min, double kd_max, int nkd, double argmax_in, double* tt, double* te, double* ee,
+                     int nthreads) {
   OCosmo* o = static_cast<OCosmo*>(h);
   const Background& bg = *o->bg;
   const Params& par = o->C.par;
@@ -222,7 +255,7 @@ int oracle_cl(void* h, const double* ST, const double* SE, const double* kg, int
   int nx = g.n;
   std::vector<double> kd(nkd);
   oracle_quadratic_k(kd_min, kd_max, nkd, kd.data());
-  double argmax = kd[nkd - 1] * bg.eta0;
+  double argmax = argmax_in > 0 ? argmax_in : kd[nkd - 1] * bg.eta0;
   double dg = argmax / 5000.0;
   const int nb = 5001;
   int Lmax = 0;

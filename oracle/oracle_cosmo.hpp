@@ -126,6 +126,7 @@ struct Recfast {
   double H_frac = 1e-3;
   int Hswitch = 1, Heswitch = 6;
   double Yp, OmegaB, HO, OmegaG, Tnow, mu_H, mu_T, fHe, Nnow, fu, b_He = 0.86, tol = 1e-8;
+  double atol = 1e-6;  // OrdinaryDiffEq's default abstol in recfast.jl's solves
 
   // Tnow < 0 means "derive from OmegaG and the background" (recfast.jl:108)
   Recfast(const Background* b, double Yp_, double OmegaB_, double OmegaG_, double Tnow_ = -1.0,
@@ -337,13 +338,13 @@ struct RecfastHistory {
       du[0] = d[1];
       du[1] = d[2];
     };
-    sol_He = tsit5(fHe, 2, y2, z_He_evo_start, z_H_He_evo_start, r->tol, 1e-6, zout);
+    sol_He = tsit5(fHe, 2, y2, z_He_evo_start, z_H_He_evo_start, r->tol, r->atol, zout);
     double z3 = z_H_He_evo_start;
     double y3[3] = {r->x_H0_H_Saha(z3), sol_He.y[sol_He.y.size() - 2], sol_He.y[sol_He.y.size() - 1]};
     Rhs fH = [this](double z, const double* u, double* du) { r->ion(u, z, du); };
     std::vector<double> stops3 = zout;
     stops3.push_back(zre_ini);
-    sol_H_He = tsit5(fH, 3, y3, z3, zfinal, r->tol, 1e-6, stops3);
+    sol_H_He = tsit5(fH, 3, y3, z3, zfinal, r->tol, r->atol, stops3);
     double T50 = Tmat_RECFAST(zre_ini);
     Rhs fR = [this](double z, const double* u, double* du) {
       double x_reio = reionization_Xe(z);
@@ -353,7 +354,7 @@ struct RecfastHistory {
       du[0] = r->CT * std::pow(Trad, 4) * x_reio / (1 + x_reio + r->fHe) * (u[0] - Trad) / (Hz * (1 + z)) +
               2 * u[0] / (1 + z);
     };
-    sol_reio = tsit5(fR, 1, &T50, zre_ini, zfinal, r->tol, 1e-6, zout);
+    sol_reio = tsit5(fR, 1, &T50, zre_ini, zfinal, r->tol, r->atol, zout);
   }
   // recfast.jl:413-433
   double Xe_RECFAST(double z) const {

@@ -1,0 +1,167 @@
+"""The batching / serving engine (bolt_engine_*) against the drop-in entry
+points and the oracle.
+
+* A C_l request and a P_lin request give the drop-in results
+  (bolt_cl_pipeline, bolt_plin on the same host-built tables).
+* Requests give the same result alone (one request per batch) and in a mix
+  submitted together (batched, several lanes in flight).
+* Gradients (central differences of the frozen-step pipeline) agree with
+  central finite differences of the oracle (tight tolerances, the k grids and
+  the Bessel grid of the unperturbed cosmology held fixed as the reference's
+  assume_nondual does) within 1e-3.
+"""
+import numpy as np
+import pytest
+
+import bolt_gb300 as B
+
+pytestmark = pytest.mark.gpu
+
+HIER = (20, 20, 10, 15)
+
+
+def _par(h=0.7, wb=0.02254, wc=0.10976, n=0.96, A=2.1e-9, mnu=0.06):
+    return B.params_of(B.CosmoParams(), [h, wb, wc, n, A, mnu])
+
+
+def _ks(par, nk=60, kmax_h0=600.0):
+    H0 = par.h * B.km_s_Mpc_100()
+    return B.log10_k(0.1 * H0, kmax_h0 * H0, nk)
+
+
+def _dropin_cl(par, ks, ells):
+    bg = B.Background(par)
+    ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg)
+    tt, te, ee, st = B.cl_all(ells, ih, ks, *HIER, reltol=1e-8, abstol=3e-7)
+    ih.close()
+    return tt, te, ee
+
+
+def _rel(a, b):
+    return np.max(np.abs(np.asarray(a) - np.asarray(b))) / np.max(np.abs(b))
+
+
+def test_cl_request_matches_dropin():
+    par = _par()
+    ks = _ks(par)
+    ells = np.arange(2, 801, 7, dtype=np.int32)
+    with B.Engine(lanes=1) as eng:
+        r = eng.run(B.Request("cl", par, ks, hier=HIER, ells=ells, cl=("tt", "te", "ee")))
+    assert r.rc == 0, r.err
+    tt, te, ee = _dropin_cl(par, ks, ells)
+    assert _rel(r.cl["tt"], tt) < 1e-9
+    assert _rel(r.cl["te"], te) < 1e-9
+    assert _rel(r.cl["ee"], ee) < 1e-9
+
+
+def test_plin_request_matches_dropin():
+    par = _par(h=0.68, mnu=0.1)
+    H0 = par.h * B.km_s_Mpc_100()
+    ks = B.log10_k(1e-4 * par.h, 1.0 * par.h, 40)
+    with B.Engine(lanes=1) as eng:
+        r = eng.run(B.Request("plin", par, ks, hier=HIER))
+    assert r.rc == 0, r.err
+    bg = B.Background(par)
+    ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg)
+    P = B.plin(ks, par, bg, ih, n_q=15, lg=HIER[0], lnu=HIER[1], lmnu=HIER[2], reltol=1e-8, abstol=3e-7)
+    ih.close()
+    assert _rel(r.plin, P) < 1e-9
+    del H0
+
+
+def _mix():
+    rng = np.random.default_rng(7)
+    reqs = []
+    for i in range(6):
+        par = _par(h=rng.uniform(0.62, 0.78), wb=rng.uniform(0.019, 0.025), wc=rng.uniform(0.10, 0.14),
+                   n=rng.uniform(0.92, 1.0), A=np.exp(rng.uniform(2.9, 3.2)) / 1e10, mnu=rng.uniform(0.0, 0.3))
+        if i % 2 == 0:
+            ells = np.arange(2, 400, 11, dtype=np.int32)
+            reqs.append(B.Request("cl", par, _ks(par, nk=int(rng.integers(40, 80))), hier=HIER, ells=ells,
+                                  cl=("tt", "ee")))
+        else:
+            ks = B.log10_k(1e-4 * par.h, par.h, int(rng.integers(20, 50)))
+            reqs.append(B.Request("plin", par, ks, hier=HIER))
+    return reqs
+
+
+def test_alone_equals_mixed():
+    reqs = _mix()
+    with B.Engine(lanes=1, max_batch=1) as eng:
+        alone = [eng.run(q) for q in reqs]
+    with B.Engine(lanes=3) as eng:
+        tickets = [eng.submit(q) for q in reqs]
+        mixed = [eng.wait(t) for t in tickets]
+        st = eng.stats()
+    assert st["requests"] == len(reqs)
+    for q, a, m in zip(reqs, alone, mixed):
+        assert a.rc == 0 and m.rc == 0, (a.err, m.err)
+        if q.kind == "plin":
+            assert _rel(m.plin, a.plin) < 1e-9
+        else:
+            for c in q.cl:
+                assert _rel(m.cl[c], a.cl[c]) < 1e-9
+
+
+def _oracle_cl_fd(par, ks, ells, rel_step, j):
+    """Central difference of the oracle's C_l^TT in theta_j, frozen grids."""
+    import oracle as O
+    th = B.theta_of(par)
+    H0 = par.h * B.km_s_Mpc_100()
+    kd = (0.01 * H0, 1000.0 * H0, 5000)
+    c0 = O.Cosmo(O.Params(h=par.h, Omega_b=par.Omega_b, Omega_c=par.Omega_c, n=par.n, A=par.A,
+                          Sigma_m_nu_eV=th[5]))
+    argmax = kd[1] * c0.eta0
+    out = []
+    for sgn in (1.0, -1.0):
+        t = th.copy()
+        t[j] += sgn * rel_step * abs(th[j])
+        p = B.params_of(par, t)
+        c = O.Cosmo(O.Params(h=p.h, Omega_b=p.Omega_b, Omega_c=p.Omega_c, n=p.n, A=p.A, Sigma_m_nu_eV=t[5]),
+                    recfast_tol=1e-11, recfast_atol=1e-12)
+        ST, SE, _ = c.source_grid(ks, *HIER, reltol=1e-10, abstol=1e-10)
+        tt, _, _ = c.cl(ST, SE, ks, ells, kd=kd, bessel_argmax=argmax)
+        out.append(tt)
+    return (out[0] - out[1]) / (2 * rel_step * abs(th[j]))
+
+
+@pytest.mark.slow
+def test_cl_gradient_vs_oracle_fd():
+    par = _par()
+    ks = _ks(par, nk=40, kmax_h0=300.0)
+    ells = np.array([2, 10, 40, 120, 250], dtype=np.int32)
+    with B.Engine(lanes=1) as eng:
+        r = eng.run(B.Request("cl", par, ks, hier=HIER, ells=ells, cl=("tt",), grad=True))
+    assert r.rc == 0, r.err
+    d = r.dcl["tt"]
+    # A enters linearly: dC/dA = C/A
+    assert _rel(d[4], r.cl["tt"] / par.A) < 1e-7
+    for j in range(6):
+        fd3 = _oracle_cl_fd(par, ks, ells, 1e-3, j)
+        fd4 = _oracle_cl_fd(par, ks, ells, 1e-4, j)
+        scale = np.max(np.abs(fd3))
+        assert np.max(np.abs(fd3 - fd4)) < 1e-3 * scale, (B.THETA_NAMES[j], fd3, fd4)  # oracle FD converged
+        assert np.max(np.abs(d[j] - fd4)) < 1e-3 * scale, (B.THETA_NAMES[j], d[j], fd4)
+
+
+@pytest.mark.slow
+def test_plin_gradient_vs_oracle_fd():
+    import oracle as O
+    par = _par(mnu=0.12)
+    ks = B.log10_k(1e-3 * par.h, 0.5 * par.h, 6)
+    with B.Engine(lanes=1) as eng:
+        r = eng.run(B.Request("plin", par, ks, hier=HIER, grad=True))
+    assert r.rc == 0, r.err
+    th = B.theta_of(par)
+    for j in range(6):
+        vals = []
+        for sgn in (1.0, -1.0):
+            t = th.copy()
+            t[j] += sgn * 1e-4 * abs(th[j])
+            p = B.params_of(par, t)
+            c = O.Cosmo(O.Params(h=p.h, Omega_b=p.Omega_b, Omega_c=p.Omega_c, n=p.n, A=p.A, Sigma_m_nu_eV=t[5]),
+                        recfast_tol=1e-11, recfast_atol=1e-12)
+            vals.append(np.array([c.plin(k, lg=HIER[0], lnu=HIER[1], lmnu=HIER[2], reltol=1e-10, abstol=1e-10)
+                                  for k in ks]))
+        fd = (vals[0] - vals[1]) / (2e-4 * abs(th[j]))
+        assert np.max(np.abs(r.dplin[j] - fd)) < 1e-3 * np.max(np.abs(fd)), (B.THETA_NAMES[j], r.dplin[j], fd)
