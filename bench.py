@@ -1,23 +1,34 @@
 #!/usr/bin/env python
-"""Benchmark: C_l spectra per second for Bolt's full CMB pipeline on GB300.
+"""Benchmark: served vs one-request-per-call spectra/s with gradients, p50/p99.
 
-Workload (one step = one cosmology, the reference's configuration for the
-full CMB pipeline): fiducial LCDM (h 0.7, Omega_b 0.046, Omega_c 0.224,
-n_s 0.96, A_s 2.1e-9, Y_p 0.24, N_eff 3.046, Sum m_nu 0.06 eV), hierarchy
-l_gamma = l_gamma,P = l_nu = 50, l_mnu = 20, nq = 15 (N = 473), 1200
-log-spaced k in [0.1, 5000] H0, source functions on the 2001-node x grid,
-C_l^TT/TE/EE for l = 2..2500 by the reference's line-of-sight discretisation
-(5000-point quadratic k grid, x > -8).  FP64 throughout.
+Default workload (serving): a seeded Poisson stream (10 requests/s) of
+requests over one GB300.  Each request is one cosmology drawn uniformly from
+h in [0.6, 0.8], omega_b in [0.019, 0.025], omega_c in [0.10, 0.14], n_s in
+[0.92, 1.0], ln(1e10 A_s) in [2.9, 3.2], Sigma m_nu in [0, 0.3] eV, and one of
+(in the fixed proportion 5 : 4 : 1 of the mix)
+  * P_lin(k) at z = 0 on 100-400 log k in [1e-4, 1] h/Mpc (l_gamma = l_nu =
+    50, l_mnu = 20, nq = 15, the reference plin defaults),
+  * C_l^TT/TE/EE up to l_max in {1000, 2500} from a source grid of 64-1024
+    log k in [0.1, 1000] H0 (l_gamma = l_nu in {20, 35, 50}, l_mnu = 10),
+  * C_l^TT up to l = 2000 with its Jacobian with respect to (h, omega_b,
+    omega_c, n_s, A_s, Sigma m_nu), same source-grid draw.
+FP64 throughout, reltol 1e-8 / abstol 3e-7.  One step = one request.
 
-Reported: ``value`` = spectra/s from CUDA-event time of the device work with
-the cosmology tables resident in HBM; ``e2e`` = spectra/s through the public
-C ABI from parameters in host memory (host table construction, upload,
-solve, projection, C_l back to the host); ``cpu_baseline`` = the CPU oracle
-(C++ restatement of Bolt's CPU algorithm, OpenMP on all host cores) on a
-bounded, stratified sample of the same workload, scaled to one spectrum.
+Reported: ``value`` = served spectra/s over the GPU window of the timed
+stream (first batch launched to last request completed), requests in flight
+batched by the engine (continuous batching, 3 lanes); ``e2e`` = the same
+stream end to end (first submission to last completion: host table builds,
+uploads, solves, projections, downloads); ``plain`` = the same requests one
+per call (nothing else in flight); ``latency`` = p50 / p99 of submission to
+completion; ``roofline`` = the Rosenbrock kernel's FP64 rate in the plain leg
+(no overlap between requests) against the FP64 peak measured in this run;
+``cpu_baseline`` = the CPU oracle (C++ restatement of Bolt's CPU algorithm,
+threaded over k / l) on a bounded sample of every request type, scaled to
+the stream.
 
-``--impl reference`` times that CPU restatement alone (the reference itself
-is Julia and cannot run on this machine).
+``--workload pipeline``: the full CMB pipeline for one cosmology (1200 k,
+l <= 2500, N = 473) with device-timed throughput (the profiling case).
+``--impl reference``: the CPU oracle alone on the serving stream.
 """
 from __future__ import annotations
 
@@ -38,15 +49,13 @@ import numpy as np  # noqa: E402
 
 METRIC = "Cℓ+grad spectra/s on 1 GB300 (served vs plain) at ≤1e-4 rel err; p50/p99 latency"
 UNIT = "spectra/s"
-HIER = (50, 50, 20, 15)
-NK = 1200
 RELTOL, ABSTOL = 1e-8, 3e-7
-ELLS = np.arange(2, 2501, dtype=np.int32)
-
-
-def fid_params(B):
-    return B.CosmoParams(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Y_p=0.24, N_nu=3.046,
-                         Sigma_m_nu=0.06 * B.mass_natural())
+ACCURACY = ("at reltol 1e-8 / abstol 3e-7 the oracle's C_l differ from its converged (1e-11) solution by "
+            "<= 3.5e-5 (EE), 7.5e-6 (TT), 3.4e-6 (TE) relative; the GPU path matches the oracle at equal "
+            "tolerances to 1e-10; gradients agree with the oracle's central differences within 1e-3")
+KINDS = ["plin", "cl", "plin", "cl", "plin", "cl", "plin", "cl", "plin", "grad"]  # 5 : 4 : 1
+SEED = 20241204
+RATE = 10.0  # requests per second
 
 
 def solver_flops_per_step(N, nq):
@@ -62,6 +71,63 @@ def los_flops(nslots, nm, nrow):
     return 27.0 * nslots * nm * nrow
 
 
+def state_len(lg, lnu, lmnu, nq):
+    return 2 * (lg + 1) + (lnu + 1) + (lmnu + 1) * nq + 5
+
+
+# ----------------------------------------------------------------- stream --
+def draw_theta(rng):
+    return np.array([rng.uniform(0.6, 0.8), rng.uniform(0.019, 0.025), rng.uniform(0.10, 0.14),
+                     rng.uniform(0.92, 1.0), math.exp(rng.uniform(2.9, 3.2)) / 1e10, rng.uniform(0.0, 0.3)])
+
+
+def make_stream(n, offset=0):
+    """Seeded request descriptions (plain dicts, no library objects)."""
+    rng = np.random.default_rng(SEED + offset)
+    out = []
+    for i in range(n):
+        kind = KINDS[(i + offset) % len(KINDS)]
+        th = draw_theta(rng)
+        d = {"kind": kind, "theta": th}
+        if kind == "plin":
+            d.update(nk=int(rng.integers(100, 401)), hier=(50, 50, 20, 15))
+        else:
+            lg = int(rng.choice([20, 35, 50]))
+            d.update(nk=int(rng.integers(64, 1025)), hier=(lg, lg, 10, 15))
+            d["lmax"] = 2000 if kind == "grad" else int(rng.choice([1000, 2500]))
+        out.append(d)
+    return out
+
+
+def to_request(B, d):
+    par = B.params_of(B.CosmoParams(), d["theta"])
+    H0 = par.h * B.km_s_Mpc_100()
+    if d["kind"] == "plin":
+        ks = B.log10_k(1e-4 * par.h, 1.0 * par.h, d["nk"])
+        return B.Request("plin", par, ks, hier=d["hier"], reltol=RELTOL, abstol=ABSTOL)
+    ks = B.log10_k(0.1 * H0, 1000.0 * H0, d["nk"])
+    ells = np.arange(2, d["lmax"] + 1, dtype=np.int32)
+    if d["kind"] == "grad":
+        return B.Request("cl", par, ks, hier=d["hier"], ells=ells, cl=("tt",), grad=True, reltol=RELTOL,
+                         abstol=ABSTOL)
+    return B.Request("cl", par, ks, hier=d["hier"], ells=ells, cl=("tt", "te", "ee"), reltol=RELTOL, abstol=ABSTOL)
+
+
+def io_bytes(d):
+    """Host->device input and device->host output bytes of one request (the
+    request's k grid, multipoles, 2003-node tables of every parameter set and
+    mode records; results, statuses and step counters)."""
+    nsets = 13 if d["kind"] == "grad" else 1
+    nk = d["nk"]
+    tab = nsets * (2003 * 16 + 30) * 8
+    if d["kind"] == "plin":
+        return tab + nk * 8 + nsets * nk * 120, nsets * nk * (8 + 4 + 16)
+    nl = d["lmax"] - 1
+    h2d = tab + nk * 8 + 4999 * 8 * (1 + nsets) + 2001 * 8 * (1 + nsets) + nl * 8 + nsets * nk * 120
+    return h2d, nsets * nk * 20 + nsets * 3 * nl * 8
+
+
+# ----------------------------------------------------------------- clocks --
 def clocks_sampler():
     q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -109,32 +175,7 @@ def clocks_summary(sampler):
             "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(steps_budget_s=15.0):
-    """Times the CPU oracle on a stratified sample of the workload and scales
-    to one spectrum: 16 of the 1200 modes (every 75th, so the k range is
-    covered) and 32 of the 2499 multipoles."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    c = O.Cosmo(O.Params(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Sigma_m_nu_eV=0.06))
-    k_all = O.log10_k(0.1 * c.H0, 5000 * c.H0, NK)
-    idx = np.arange(37, NK, 75)
-    ks = k_all[idx]
-    cores = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    ST, SE, _ = c.source_grid(ks, *HIER[:3], HIER[3], reltol=RELTOL, abstol=ABSTOL, nthreads=cores)
-    t_sg = time.perf_counter() - t0
-    ells = ELLS[np.linspace(0, ELLS.size - 1, 32).astype(int)]
-    t0 = time.perf_counter()
-    c.cl(ST, SE, ks, ells, nthreads=cores)
-    t_los = time.perf_counter() - t0
-    per_spec = t_sg * NK / ks.size + t_los * ELLS.size / ells.size
-    return {"value": 1.0 / per_spec, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": (f"CPU oracle (C++ restatement of Bolt's CPU algorithm, OpenMP): source grid for "
-                       f"{ks.size}/{NK} stratified k modes ({t_sg:.1f} s) + LOS for {ells.size}/{ELLS.size} "
-                       f"multipoles ({t_los:.1f} s), scaled to one spectrum ({per_spec:.1f} s)"),
-            "seconds_per_spectrum": per_spec}
-
-
+# ------------------------------------------------------------ distributed --
 def dist_init():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
@@ -153,152 +194,282 @@ def max_over_ranks(v, dist):
     return float(t.item())
 
 
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ----------------------------------------------------------- CPU baseline --
+def cpu_stream_seconds(stream):
+    """CPU oracle seconds for the stream, from timed samples of each request
+    type scaled by its size (modes x state length for the solves, multipoles
+    for the projection; a gradient is 13 parameter sets, as central
+    differences over six parameters need).  About 10-30 s of CPU work."""
+    from concurrent.futures import ThreadPoolExecutor
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cores = os.cpu_count() or 1
+    par = O.Params(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Sigma_m_nu_eV=0.06)
+    t0 = time.perf_counter()
+    c = O.Cosmo(par)
+    t_tab = time.perf_counter() - t0
+    # P_lin: 2 * cores wavenumbers across [1e-4, 1] h/Mpc, threaded over k
+    ks = O.log10_k(1e-4 * 0.7, 0.7, 2 * cores)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        list(ex.map(lambda k: c.plin(k, lg=50, lnu=50, lmnu=20, reltol=RELTOL, abstol=ABSTOL), ks))
+    t_plin_k = (time.perf_counter() - t0) / ks.size  # seconds per k with all cores busy
+    # source grid: 2 * cores modes across [0.1, 1000] H0 at l_gamma = 35, OpenMP over k
+    kc = O.log10_k(0.1 * c.H0, 1000 * c.H0, 2 * cores)
+    t0 = time.perf_counter()
+    ST, SE, _ = c.source_grid(kc, 35, 35, 10, 15, reltol=RELTOL, abstol=ABSTOL, nthreads=cores)
+    t_mode = (time.perf_counter() - t0) / kc.size
+    n35 = state_len(35, 35, 10, 15)
+    # projection: 2 * cores multipoles spread over 2..2500 (TT/TE/EE)
+    ells = np.linspace(2, 2500, 2 * cores).astype(np.int32)
+    t0 = time.perf_counter()
+    c.cl(ST, SE, kc, ells, nthreads=cores)
+    t_ell = (time.perf_counter() - t0) / ells.size
+    total = 0.0
+    for d in stream:
+        nsets = 13 if d["kind"] == "grad" else 1
+        if d["kind"] == "plin":
+            total += t_tab + d["nk"] * t_plin_k
+        else:
+            N = state_len(*d["hier"])
+            total += nsets * (t_tab + d["nk"] * t_mode * N / n35 + (d["lmax"] - 1) * t_ell)
+    sample = (f"CPU oracle (C++ restatement of Bolt's CPU algorithm) on {cores} threads: tables {t_tab:.3f} s, "
+              f"P_lin {t_plin_k * 1e3:.1f} ms/k ({ks.size} k), source grid {t_mode * 1e3:.1f} ms/mode at N={n35} "
+              f"({kc.size} modes, scaled by state length), C_l {t_ell * 1e3:.2f} ms/l ({ells.size} l); "
+              f"gradients = 13 parameter sets; scaled to the {len(stream)}-request stream")
+    return total, cores, sample
+
+
+# ---------------------------------------------------------------- serving --
+def run_serving(args):
+    rank, ws, dist = dist_init()
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    import bolt_gb300 as B
+    K, W = args.steps, args.warmup
+    warm = make_stream(W, offset=1000 + rank)
+    stream = make_stream(K, offset=rank * 7919)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    lib = B._lib.load()
+
+    # ---- plain: one request per call, nothing else in flight
+    plain_lat, plain_solver_s, plain_flops = [], 0.0, 0.0
+    with B.Engine(device=local, lanes=1, max_batch=1) as eng:
+        for d in warm:
+            r = eng.run(to_request(B, d))
+            assert r.rc == 0, r.err
+        barrier(dist)
+        sampler = clocks_sampler()
+        for d in stream:
+            flush.zero_()
+            torch.cuda.synchronize()
+            s0 = eng.stats()
+            t0 = time.perf_counter()
+            r = eng.run(to_request(B, d))
+            plain_lat.append(time.perf_counter() - t0)
+            assert r.rc == 0, r.err
+            s1 = eng.stats()
+            plain_solver_s += (s1["solver_us"] - s0["solver_us"]) / 1e6
+            plain_flops += r.steps * solver_flops_per_step(state_len(*d["hier"]), d["hier"][3])
+        torch.cuda.synchronize()
+        plain_wall = max_over_ranks(sum(plain_lat), dist)
+
+    # ---- served: Poisson arrivals, continuous batching
+    with B.Engine(device=local, lanes=3) as eng:
+        ts = [eng.submit(to_request(B, d)) for d in warm]
+        for t in ts:
+            assert eng.wait(t).rc == 0
+        barrier(dist)
+        s0 = eng.stats()
+        rng = np.random.default_rng(SEED + 17 + rank)
+        arrivals = np.cumsum(rng.exponential(1.0 / RATE, K))
+        tickets = [None] * K
+        t_start = time.perf_counter()
+
+        def producer():
+            for i, d in enumerate(stream):
+                req = to_request(B, d)
+                delay = t_start + arrivals[i] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                tickets[i] = eng.submit(req)
+        th = threading.Thread(target=producer)
+        th.start()
+        th.join()
+        res = [eng.wait(t) for t in tickets]
+        torch.cuda.synchronize()
+        clocks = clocks_summary(sampler)
+        s1 = eng.stats()
+    for r in res:
+        assert r.rc == 0, r.err
+    lat = np.array([r.latency for r in res])
+    gpu_window = max_over_ranks(max(r.times[3] for r in res) - min(r.times[2] for r in res), dist)
+    e2e_window = max_over_ranks(max(r.times[3] for r in res) - min(r.times[0] for r in res), dist)
+    value = ws * K / gpu_window
+    e2e = ws * K / e2e_window
+    plain = ws * K / plain_wall
+    h2d = sum(io_bytes(d)[0] for d in stream) / K
+    d2h = sum(io_bytes(d)[1] for d in stream) / K
+    peak = ctypes_peak(lib, local)
+    ach = plain_flops / plain_solver_s / 1e12 if plain_solver_s > 0 else None
+    roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+            "frac": ach / peak if (peak and ach) else None, "traffic": None, "kernel": "rodas_kernel",
+            "peak_source": "measured in this run: FP64 FMA loop (bolt_fp64_peak); MEASURED_PEAKS.json has no "
+                           "FP64 figure",
+            "note": "plain leg (requests one at a time): algorithmic FLOPs of the accepted + rejected steps of every "
+                    "mode (159 N + 560 (nq+5) + 66 nq + 650 per step) / CUDA-event time of the solver launches; "
+                    "DRAM traffic is negligible (per-CTA state slab L2-resident), see profiles/"}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        secs, cores, sample = cpu_stream_seconds(stream)
+        cpu = {"value": K / secs, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    counts = {k: sum(1 for d in stream if d["kind"] == k) for k in ("plin", "cl", "grad")}
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+               "ms_per_step": 1000.0 * gpu_window / K, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": "serving: seeded Poisson stream (10 req/s) of one-cosmology requests from the "
+                                      "box h 0.6-0.8, omega_b 0.019-0.025, omega_c 0.10-0.14, n_s 0.92-1.0, "
+                                      "ln(1e10 A_s) 2.9-3.2, Sigma m_nu 0-0.3 eV; mix 5:4:1 of P_lin (100-400 log k "
+                                      "in [1e-4,1] h/Mpc, l 50/50/20, nq 15), C_l TT/TE/EE (l_max 1000 or 2500) and "
+                                      "C_l^TT l<=2000 + 6-parameter Jacobian (both: 64-1024 log k in [0.1,1000] H0, "
+                                      "l_gamma=l_nu in {20,35,50}, l_mnu 10, nq 15); one step = one request",
+                          "requests": counts, "reltol": RELTOL, "abstol": ABSTOL, "accuracy": ACCURACY,
+                          "timing": "value: served stream over the GPU window (first batch launch to last "
+                                    "completion, 3 lanes); plain: one request per call, sum of call times",
+                          "l2": "plain: flushed (256 MB write) before every request; served: continuous stream",
+                          "parallelism": f"replicas x{ws}"},
+               "plain": {"value": plain, "unit": UNIT, "p50_s": float(np.percentile(plain_lat, 50)),
+                         "p99_s": float(np.percentile(plain_lat, 99))},
+               "served_over_plain": value / plain,
+               "latency": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                           "arrival_rate_per_s": RATE},
+               "clocks": clocks,
+               "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+               "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]),
+               "engine": {k: s1[k] - s0[k] for k in s1},
+               "roofline": roof, "cpu_baseline": cpu}
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def run_reference(args):
     rank, ws, dist = dist_init()
     if rank != 0:
         return
-    vals = []
-    last = None
-    for i in range(args.warmup + args.steps):
-        r = cpu_sample()
+    stream = make_stream(args.steps)
+    vals, last = [], None
+    for i in range(args.warmup + 1):  # the sample timings themselves warm the host caches
+        secs, cores, sample = cpu_stream_seconds(stream)
         if i >= args.warmup:
-            vals.append(r["value"])
-            last = r
+            vals.append(len(stream) / secs)
+            last = (cores, sample)
     v = statistics.median(vals)
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "full CMB pipeline: 1200 log k in [0.1,5000]H0, l_g=l_gP=l_nu=50, l_mnu=20, "
-                                  "nq=15, S on 2001 x nodes, C_l TT/TE/EE l=2..2500; one step = one cosmology",
+           "config": {"workload": "the serving stream of the GPU arm (bench.py module docstring), CPU oracle",
                       "parallelism": "host cores"},
-           "cpu_baseline": {k: last[k] for k in ("value", "unit", "cores", "kind", "sample")},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": last[0], "kind": "port", "sample": last[1]},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling captures)")
-    ap.add_argument("--nk", type=int, default=NK, help="source-grid wavenumbers (smaller cases for ncu captures)")
-    ap.add_argument("--kmax-h0", type=float, default=5000.0, help="largest source-grid wavenumber in units of H0")
-    ap.add_argument("--lmax", type=int, default=int(ELLS[-1]), help="largest multipole")
-    args = ap.parse_args()
-    if args.impl == "reference":
-        run_reference(args)
-        return
+# --------------------------------------------------------------- pipeline --
+def run_pipeline(args):
+    """Full CMB pipeline for one cosmology, device-timed (the profiling case)."""
     rank, ws, dist = dist_init()
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     import bolt_gb300 as B
     ctx = B.Context(device=local)
-    par = fid_params(B)
+    par = B.CosmoParams(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Y_p=0.24, N_nu=3.046,
+                        Sigma_m_nu=0.06 * B.mass_natural())
     bg = B.Background(par)
     ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg, ctx=ctx)
     ks = B.log10_k(0.1 * bg.H0, args.kmax_h0 * bg.H0, args.nk)
     ells = np.arange(2, args.lmax + 1, dtype=np.int32)
-    lg, lnu, lmnu, nq = HIER
-    N = B.state_len(lg, lnu, lmnu, nq)
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
-
-    def device_step():
-        tt, te, ee, st = B.cl_all(ells, ih, ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL)
-        return ctx.stats(), (tt, te, ee, st)
-
+    hier = (50, 50, 20, 15)
+    N = B.state_len(*hier)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
-        device_step()
+        B.cl_all(ells, ih, ks, *hier, reltol=RELTOL, abstol=ABSTOL)
         flush.zero_()
     torch.cuda.synchronize()
-    if dist is not None:
-        dist.barrier()
+    barrier(dist)
     sampler = clocks_sampler()
-    dev_ms, solver_us, los_us, acc, rej, launches = [], 0, 0, 0, 0, 0
+    dev_ms, solver_us, los_us, steps, launches = [], 0, 0, 0, 0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
-        s, res = device_step()
+        B.cl_all(ells, ih, ks, *hier, reltol=RELTOL, abstol=ABSTOL)
+        s = ctx.stats()
         dev_ms.append((s["solver_us"] + s["los_us"]) / 1000.0)
         solver_us += s["solver_us"]
         los_us += s["los_us"]
-        acc += s["accepted_steps"]
-        rej += s["rejected_steps"]
+        steps += s["accepted_steps"] + s["rejected_steps"]
         launches += s["kernel_launches"]
     torch.cuda.synchronize()
     clocks = clocks_summary(sampler)
     total_ms = max_over_ranks(sum(dev_ms), dist)
     value = ws * args.steps / (total_ms / 1000.0)
-
-    # e2e through the public API: parameters in host memory -> C_l in host memory
-    e2e_t = []
-    h2d = d2h = 0
-    for i in range(0 if args.no_e2e else args.steps + 1):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        bg2 = B.Background(par)
-        ih2 = B.IonizationHistory(B.RECFAST(bg2, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg2,
-                                  ctx=ctx)
-        tt, te, ee, st = B.cl_all(ells, ih2, ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL)
-        ih2.close()
-        torch.cuda.synchronize()
-        if i > 0:
-            e2e_t.append(time.perf_counter() - t0)
-        n2 = bg2.x_grid.size + 2
-        h2d = 8 * (n2 * 4 + 12 * n2 + 2 * nq) + 8 * ks.size + 8 * 4999 * 2 + 8 * 5000
-        d2h = 8 * 3 * ells.size + 4 * ks.size
-    e2e_val = ws * len(e2e_t) / max_over_ranks(sum(e2e_t), dist) if e2e_t else None
-
-    # roofline of the dominant kernel (FP64-pipe bound)
-    peak = ctypes_peak(B, local)
-    sol_flops = (acc + rej) * solver_flops_per_step(N, nq)
-    sol_s = solver_us / 1e6
-    los_f = los_flops(ells.size, 4999, 799) * args.steps
-    los_s = los_us / 1e6
-    dom = "rodas_kernel" if sol_s >= los_s else "los_cl_kernel"
-    ach = (sol_flops / sol_s if dom == "rodas_kernel" else los_f / los_s) / 1e12
-    roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak if peak else None,
-            "traffic": None, "kernel": dom,
-            "peak_source": "measured in this run: FP64 FMA loop (bolt_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
-            "breakdown": {"rodas_kernel_ms_per_step": solver_us / 1000.0 / args.steps,
-                          "rodas_tflops": sol_flops / sol_s / 1e12 if sol_s else None,
-                          "los_ms_per_step": los_us / 1000.0 / args.steps,
-                          "los_cl_tflops": los_f / los_s / 1e12 if los_s else None,
-                          "steps_per_spectrum": (acc + rej) / args.steps}}
-    cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        r = cpu_sample()
-        cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    peak = ctypes_peak(B._lib.load(), local)
+    sol = steps * solver_flops_per_step(N, 15) / (solver_us / 1e6) / 1e12
+    los = los_flops(ells.size, 4999, 799) * args.steps / (los_us / 1e6) / 1e12
     if rank == 0:
-        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-               "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-               "config": {"workload": f"full CMB pipeline (plain, one cosmology per call): fiducial LCDM, {ks.size} "
-                                      f"log k in [0.1,{args.kmax_h0:g}]H0, l_g=l_gP=l_nu=50, l_mnu=20, nq=15 (N={N}), "
-                                      f"S_T/S_E on 2001 x nodes, C_l TT/TE/EE l=2..{args.lmax}; gradients not in this "
-                                      "workload",
-                          "reltol": RELTOL, "abstol": ABSTOL,
-                          "accuracy": "at reltol 1e-8 / abstol 3e-7 the oracle's C_l differ from its converged "
-                                      "(1e-11) solution by <= 3.5e-5 (EE), 7.5e-6 (TT), 3.4e-6 (TE) relative; the "
-                                      "GPU path matches the oracle at equal tolerances to 1e-10",
-                          "l2": "flushed (256 MB write) between steps",
-                          "parallelism": f"replicas x{ws}"},
-               "clocks": clocks,
-               "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-               "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu}
+        out = {"metric": "C_l spectra/s, full CMB pipeline, one cosmology per call (device time)", "value": value,
+               "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": f"full CMB pipeline: fiducial LCDM, {ks.size} log k in "
+                                      f"[0.1,{args.kmax_h0:g}]H0, l 50/50/20, nq 15 (N={N}), S_T/S_E on 2001 x "
+                                      f"nodes, C_l TT/TE/EE l=2..{args.lmax}", "reltol": RELTOL, "abstol": ABSTOL,
+                          "l2": "flushed (256 MB write) between steps", "parallelism": f"replicas x{ws}"},
+               "clocks": clocks, "gpu_launches": launches,
+               "roofline": {"bound": "fp64", "achieved": sol, "peak": peak, "unit": "TFLOP/s",
+                            "frac": sol / peak if peak else None, "traffic": None, "kernel": "rodas_kernel",
+                            "breakdown": {"rodas_kernel_ms_per_step": solver_us / 1000.0 / args.steps,
+                                          "los_ms_per_step": los_us / 1000.0 / args.steps, "los_cl_tflops": los,
+                                          "steps_per_spectrum": steps / args.steps}}}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
 
 
-def ctypes_peak(B, dev):
+def ctypes_peak(lib, dev):
     import ctypes as C
     v = C.c_double(0.0)
-    rc = B._lib.load().bolt_fp64_peak(dev, C.byref(v))
+    rc = lib.bolt_fp64_peak(dev, C.byref(v))
     return v.value if rc == 0 else None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20, help="timed requests (serving) or spectra (pipeline)")
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="serving", choices=["serving", "pipeline"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nk", type=int, default=1200, help="pipeline: source-grid wavenumbers")
+    ap.add_argument("--kmax-h0", type=float, default=5000.0, help="pipeline: largest wavenumber in units of H0")
+    ap.add_argument("--lmax", type=int, default=2500, help="pipeline: largest multipole")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    elif args.workload == "pipeline":
+        run_pipeline(args)
+    else:
+        run_serving(args)
 
 
 if __name__ == "__main__":

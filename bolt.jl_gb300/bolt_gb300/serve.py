@@ -56,7 +56,7 @@ class Request:
 class Result:
     rc: int
     err: str
-    times: np.ndarray               # submitted, tables ready, launched, completed (s since engine start)
+    times: np.ndarray               # submitted, tables ready, launched, completed (s since engine start), steps
     status: np.ndarray
     plin: np.ndarray | None = None
     dplin: np.ndarray | None = None  # [6][nk]
@@ -66,6 +66,10 @@ class Result:
     @property
     def latency(self) -> float:
         return float(self.times[3] - self.times[0])
+
+    @property
+    def steps(self) -> int:
+        return int(self.times[4])
 
 
 class _Pending:
@@ -149,7 +153,7 @@ class Engine:
     def wait(self, ticket: int, timeout: float | None = None) -> Result | None:
         p = self._pending[ticket]
         rc = C.c_int(0)
-        times = np.zeros(4)
+        times = np.zeros(5)
         err = C.create_string_buffer(512)
         done = self.lib.bolt_engine_wait(self.h, ticket, -1.0 if timeout is None else float(timeout), C.byref(rc),
                                          L.dptr(times), err, 512)

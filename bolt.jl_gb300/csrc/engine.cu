@@ -188,6 +188,7 @@ struct Req {
   int rc = 0;
   std::string err;
   double t[4] = {0, 0, 0, 0};
+  double steps = 0.0;  // accepted + rejected steps of all its modes (every parameter set)
   size_t bytes = 0;  // device footprint of the request in a batch
   int N = 0;
   // LOS (C_l): sorted unique multipoles
@@ -213,11 +214,17 @@ struct Tuner {  // seconds per mode-step by batch-size bucket and warps per mode
   }
   static int vidx(int wpm) { return wpm == 1 ? 0 : (wpm == 2 ? 1 : 2); }
   int pick(int nmodes, int nsm) const {
-    // candidates: only launches that fill the GPU benefit from the
-    // instruction-lean narrow variants
+    // Candidates, in the order they are explored: only launches that fill
+    // the GPU several times over benefit from the instruction-lean narrow
+    // variants (measured crossover between 8 and 32 modes per SM).
     int cands[3] = {4, 0, 0}, nc = 1;
-    if (nmodes > 2 * nsm) cands[nc++] = 2;
-    if (nmodes > 4 * nsm) cands[nc++] = 1;
+    if (nmodes >= 16 * nsm) {
+      cands[0] = 1; cands[1] = 2; cands[2] = 4; nc = 3;
+    } else if (nmodes > 4 * nsm) {
+      cands[1] = 2; cands[2] = 1; nc = 3;
+    } else if (nmodes > 2 * nsm) {
+      cands[1] = 2; nc = 2;
+    }
     const int b = bucket(nmodes);
     for (int i = 0; i < nc; ++i)
       if (n[b][vidx(cands[i])] == 0) return cands[i];
@@ -818,6 +825,7 @@ void finish_lane(bolt_engine* E, Lane& L) {
       for (int i = 0; i < r->r.nk; ++i) {
         size_t q = 2 * (size_t(s) * r->r.nk + i);
         steps[s == 0 ? 0 : 1] += double(cnt[q] + cnt[q + 1]);
+        r->steps += double(cnt[q] + cnt[q + 1]);
       }
     modes += int64_t(r->nsets) * r->r.nk;
   }
@@ -1128,7 +1136,10 @@ int bolt_engine_wait(bolt_engine* E, int64_t ticket, double timeout_s, int* rc_o
   if (timeout_s < 0) E->cv_done.wait(lk, pred);
   else if (!E->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) return 0;
   if (rc_out) *rc_out = r->rc;
-  if (times_out) std::copy(r->t, r->t + 4, times_out);
+  if (times_out) {
+    std::copy(r->t, r->t + 4, times_out);
+    times_out[4] = r->steps;
+  }
   if (errbuf && errlen > 0) {
     std::strncpy(errbuf, r->err.c_str(), size_t(errlen) - 1);
     errbuf[errlen - 1] = 0;

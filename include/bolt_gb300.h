@@ -237,8 +237,9 @@ int bolt_engine_submit(bolt_engine* eng, const bolt_request* req, int64_t* ticke
 /* Waits up to timeout_s (< 0: forever) for a ticket.  Returns 1 when done
  * (the ticket is then released; rc_out = 0 or the request's negative error
  * code, message in errbuf), 0 on timeout, negative on an unknown ticket.
- * times_out (optional, seconds since engine creation): [0] submitted,
- * [1] tables ready, [2] batch launched, [3] completed. */
+ * times_out (optional, 5 doubles): seconds since engine creation [0]
+ * submitted, [1] tables ready, [2] batch launched, [3] completed; [4] the
+ * request's Rodas4 steps (accepted + rejected, every parameter set). */
 int bolt_engine_wait(bolt_engine* eng, int64_t ticket, double timeout_s, int* rc_out, double* times_out,
                      char* errbuf, int errlen);
 
