@@ -97,7 +97,7 @@ struct bolt_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[4];
   int wpb = 0;
-  long long max_steps = 10000000;
+  long long max_steps = 100000;  // OrdinaryDiffEq's default maxiters
   double x_dense = -8.5;
   std::vector<CosmoEntry> cos;
   DBuf d_cos;

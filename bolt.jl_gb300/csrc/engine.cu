@@ -692,7 +692,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   cfg.abstol = batch[0]->r.abstol;
   cfg.h0 = 1e-3;
   cfg.x_dense = -8.5;
-  cfg.max_steps = E->cfg.max_steps > 0 ? E->cfg.max_steps : 10000000;
+  cfg.max_steps = E->cfg.max_steps > 0 ? E->cfg.max_steps : 100000;
   for (int ph = 0; ph < nph; ++ph) {
     RodasNodeArgs args;
     cudaKernelNodeParams kp;
@@ -979,7 +979,7 @@ int bolt_engine_create(const bolt_engine_cfg* cfg, bolt_engine** out) {
   E->device = E->cfg.device;
   if (E->cfg.lanes <= 0) E->cfg.lanes = 2;
   if (E->cfg.lanes > 8) E->cfg.lanes = 8;
-  if (E->cfg.max_steps <= 0) E->cfg.max_steps = 10000000;
+  if (E->cfg.max_steps <= 0) E->cfg.max_steps = 100000;  // OrdinaryDiffEq's default maxiters
   E->budget = size_t((E->cfg.mem_budget_gb > 0 ? E->cfg.mem_budget_gb : 150.0) * 1073741824.0);
   E->t0 = std::chrono::steady_clock::now();
   try {

@@ -48,7 +48,7 @@ typedef struct {
 typedef struct {
   int device;          /* CUDA device ordinal */
   int warps_per_block; /* solver CTA size in warps (0 = autotune) */
-  long long max_steps; /* per mode (0 = 10^7) */
+  long long max_steps; /* per mode (0 = 10^5, OrdinaryDiffEq's default maxiters) */
 } bolt_opts;
 
 /* Table slots for bolt_cosmo_table (nodes on the x grid). */
@@ -214,7 +214,7 @@ typedef struct {
   int max_batch;         /* requests per batch (0 = unlimited; 1 = one request per batch) */
   double mem_budget_gb;  /* device memory admitted to in-flight requests (0 = 150) */
   int warps_per_mode;    /* 0 = autotune per batch size, else 1, 2 or 4 */
-  long long max_steps;   /* per mode (0 = 10^7) */
+  long long max_steps;   /* per mode (0 = 10^5, OrdinaryDiffEq's default maxiters) */
 } bolt_engine_cfg;
 
 typedef struct bolt_engine bolt_engine;
