@@ -390,7 +390,7 @@ def run_pipeline(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     import bolt_gb300 as B
-    ctx = B.Context(device=local)
+    ctx = B.Context(device=local, warps_per_block=args.warps_per_mode)
     par = B.CosmoParams(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Y_p=0.24, N_nu=3.046,
                         Sigma_m_nu=0.06 * B.mass_natural())
     bg = B.Background(par)
@@ -462,6 +462,7 @@ def main():
     ap.add_argument("--nk", type=int, default=1200, help="pipeline: source-grid wavenumbers")
     ap.add_argument("--kmax-h0", type=float, default=5000.0, help="pipeline: largest wavenumber in units of H0")
     ap.add_argument("--lmax", type=int, default=2500, help="pipeline: largest multipole")
+    ap.add_argument("--warps-per-mode", type=int, default=0, help="pipeline: solver warps per mode (0: four)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
