@@ -58,6 +58,8 @@ EXPORTS = {
     "bolt_km_s_Mpc_100": (C.c_double, []),
     "bolt_host_tables": (C.c_int, [C.POINTER(BoltParams), C.POINTER(BoltGrid), C.c_int, C.POINTER(BoltRecfast),
                                    _dp, _dp, C.c_char_p, C.c_int]),
+    "bolt_host_tables_frozen": (C.c_int, [C.POINTER(BoltParams), C.POINTER(BoltParams), C.POINTER(BoltGrid), C.c_int,
+                                          C.POINTER(BoltRecfast), C.POINTER(BoltRecfast), _dp, C.c_char_p, C.c_int]),
     "bolt_ctx_create": (C.c_int, [C.POINTER(BoltOpts), C.POINTER(C.c_void_p)]),
     "bolt_ctx_destroy": (None, [C.c_void_p]),
     "bolt_last_error": (C.c_char_p, [C.c_void_p]),

@@ -421,6 +421,31 @@ int bolt_host_tables(const bolt_params* par, const bolt_grid* grid, int nq, cons
   }
 }
 
+int bolt_host_tables_frozen(const bolt_params* base, const bolt_params* par, const bolt_grid* grid, int nq,
+                            const bolt_recfast* rf_base, const bolt_recfast* rf, double* nodes, char* errbuf,
+                            int errlen) {
+  try {
+    if (!base || !par || !grid || !rf_base || !rf || !nodes) throw Err(-1, "null argument");
+    if (!(grid->step > 0) || !(grid->stop > grid->start)) throw Err(-1, "bad x grid");
+    const GridSpec g = make_grid(grid->start, grid->step, grid->stop);
+    RecfastFreeze fz;
+    CosmoTables T0, T;
+    RecfastOpts r0{rf_base->Yp, rf_base->OmegaB, rf_base->OmegaG, rf_base->Tnow, rf_base->tol > 0 ? rf_base->tol : 1e-8};
+    build_cosmo_tables(to_h(base), g, nq, r0, T0, &fz);  // records
+    RecfastOpts ro{rf->Yp, rf->OmegaB, rf->OmegaG, rf->Tnow, rf->tol > 0 ? rf->tol : 1e-8};
+    build_cosmo_tables(to_h(par), g, nq, ro, T, &fz);    // replays
+    const int n = T.grid.n;
+    for (int t = 0; t < T_COUNT; ++t) std::copy(T.nodes[t].begin(), T.nodes[t].end(), nodes + size_t(t) * n);
+    return 0;
+  } catch (const Err& e) {
+    if (errbuf && errlen > 0) { std::snprintf(errbuf, errlen, "%s", e.what()); }
+    return e.code;
+  } catch (const std::exception& e) {
+    if (errbuf && errlen > 0) { std::snprintf(errbuf, errlen, "%s", e.what()); }
+    return -4;
+  }
+}
+
 int bolt_ctx_create(const bolt_opts* opts, bolt_ctx** out) {
   if (!out) return -1;
   *out = nullptr;

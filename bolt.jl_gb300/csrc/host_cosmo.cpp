@@ -210,9 +210,20 @@ struct Bg {
 
 // ---------------------------------------------------------------- Tsit5
 // Tsitouras 5(4) with landing on requested points; Hermite dense output.
+// Which side of each state-dependent switch of the RECFAST right-hand side
+// every stage evaluation of the accepted steps took (one byte per
+// evaluation); replayed, perturbed runs take the same sides, as a
+// ForwardDiff derivative follows the branch of the unperturbed run.
+struct BranchLog {
+  std::vector<uint8_t>* bits = nullptr;
+  size_t pos = 0;
+  bool replay = false;
+};
+
 struct Traj {
   int dim = 0;
   std::vector<double> t, y, f;
+  std::vector<double> h;  // signed size of each accepted step
   void eval(double tq, double* out) const {
     size_t n = t.size();
     bool up = t.back() > t.front();
@@ -235,11 +246,13 @@ struct Traj {
 
 typedef std::function<void(double, const double*, double*)> OdeFn;
 
-// replay: if non-null, the accepted abscissae of an earlier run (replay[0]
-// == t0); the same steps are taken without error control, so the result is
-// a smooth function of the right-hand side's parameters.
+// replay / replay_h: if non-null, the accepted abscissae (replay[0] == t0)
+// and step sizes of an earlier run; the same steps are taken without error
+// control, so the result is a smooth function of the right-hand side's
+// parameters, and bitwise the earlier run's for the same right-hand side.
 Traj tsit5_integrate(const OdeFn& fn, int dim, const double* y0, double t0, double t1, double rtol, double atol,
-                     std::vector<double> land, const std::vector<double>* replay = nullptr) {
+                     std::vector<double> land, const std::vector<double>* replay = nullptr,
+                     const std::vector<double>* replay_h = nullptr, BranchLog* blog = nullptr) {
   const double C[7] = {0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0};
   const double A[7][6] = {
       {0, 0, 0, 0, 0, 0},
@@ -265,9 +278,10 @@ Traj tsit5_integrate(const OdeFn& fn, int dim, const double* y0, double t0, doub
   tr.f.insert(tr.f.end(), K.begin(), K.begin() + dim);
   double t = t0, hnext = std::fabs(t1 - t0) * 1e-6;
   if (replay) {
-    if (replay->empty() || (*replay)[0] != t0) throw std::runtime_error("RECFAST replay does not start at t0");
+    if (replay->empty() || (*replay)[0] != t0 || !replay_h || replay_h->size() + 1 != replay->size())
+      throw std::runtime_error("RECFAST replay does not match this integration");
     for (size_t i = 1; i < replay->size(); ++i) {
-      const double tn = (*replay)[i], h = tn - t;
+      const double tn = (*replay)[i], h = (*replay_h)[i - 1];
       for (int s = 1; s < 7; ++s) {
         for (int d = 0; d < dim; ++d) {
           double acc = 0.0;
@@ -290,6 +304,7 @@ Traj tsit5_integrate(const OdeFn& fn, int dim, const double* y0, double t0, doub
   size_t li = 0;
   long guard = 0;
   while (li < land.size()) {
+    const size_t mark = (blog && blog->bits && !blog->replay) ? blog->bits->size() : 0;
     double rem = (land[li] - t) * dir;
     bool hit = hnext >= rem * (1.0 - 1e-12);
     double hs = hit ? rem : hnext, h = hs * dir;
@@ -317,6 +332,7 @@ Traj tsit5_integrate(const OdeFn& fn, int dim, const double* y0, double t0, doub
     double fac = std::min(10.0, std::max(0.2, 0.9 * std::pow(std::max(err, 1e-10), -0.2)));
     if (err <= 1.0) {
       t = hit ? land[li] : t + h;
+      tr.h.push_back(h);
       y = yn;
       std::copy(K.begin() + 6 * dim, K.begin() + 7 * dim, K.begin());
       tr.t.push_back(t);
@@ -326,6 +342,7 @@ Traj tsit5_integrate(const OdeFn& fn, int dim, const double* y0, double t0, doub
       else hnext = hs * fac;
     } else {
       hnext = hs * std::min(1.0, fac);
+      if (blog && blog->bits && !blog->replay) blog->bits->resize(mark);  // forget the rejected attempt
     }
     if (++guard > 20000000) throw std::runtime_error("RECFAST integration did not finish");
   }
@@ -382,14 +399,40 @@ struct Rf {
   double saha(double z, double CBx) const {
     return std::exp(1.5 * std::log(CR * Tnow / (1 + z)) - CBx / (Tnow * (1 + z))) / Nnow;
   }
-  double xH_saha(double z) const { double r = saha(z, CB1); return 0.5 * (std::sqrt(r * r + 4 * r) - r); }
+  // The Saha roots (recfast.jl:396-411) 0.5 (sqrt(b^2 + 4c) - b) are
+  // evaluated as 2c / (sqrt(b^2 + 4c) + b) when b > 0: the same number
+  // without the cancellation that leaves ~1e-6 of rounding noise when
+  // r ~ 1e10 (early times), noise a central difference would amplify.
+  static double quad_root(double b, double c) {
+    double s = std::sqrt(b * b + 4.0 * c);
+    return b > 0.0 ? 2.0 * c / (s + b) : 0.5 * (s - b);
+  }
+  double xH_saha(double z) const { double r = saha(z, CB1); return quad_root(r, r); }
   double xtot_He1_saha(double z) const {
     double r = 4.0 * saha(z, CB1_He1);
-    return 0.5 * (std::sqrt((r - 1) * (r - 1) + 4 * (1 + fHe) * r) - (r - 1));
+    return quad_root(r - 1, (1 + fHe) * r);
   }
   // recfast.jl:156-310
+  mutable BranchLog* blog = nullptr;
+
   void rhs(double z, const double* y, double* f) const {
     double xH = y[0], xHe = y[1], Tm = y[2], x = xH + fHe * xHe;
+    uint8_t br = uint8_t((xHe < 5e-9 || xHe > 0.98) ? 1 : 0) | uint8_t(xH < 0.9999999 ? 2 : 0) |
+                 uint8_t(xH > 0.99999 ? 4 : 0) | uint8_t(xH > 0.99 ? 8 : 0) | uint8_t(xH > 0.985 ? 16 : 0) |
+                 uint8_t(xHe < 1e-15 ? 32 : 0);
+    {  // the temperature equation's switch (recfast.jl:293-307)
+      double tTh0 = (1.0 / (CT * std::pow(Tnow * (1.0 + z), 4))) * (1 + x + fHe) / x;
+      double tH0 = 2.0 / (3.0 * HO * std::pow(1.0 + z, 1.5));
+      if (tTh0 < H_frac * tH0) br |= 64;
+    }
+    if (blog && blog->bits) {
+      if (blog->replay) {
+        if (blog->pos >= blog->bits->size()) throw std::runtime_error("RECFAST branch replay ran out");
+        br = (*blog->bits)[blog->pos++];
+      } else {
+        blog->bits->push_back(br);
+      }
+    }
     double zp = 1.0 + z, n = Nnow * zp * zp * zp, nHe = fHe * n, Trad = Tnow * zp;
     double a = 1.0 / zp, xa = std::log(a);
     double Hz = (*H)(xa) / a / sec_per_nat();
@@ -404,7 +447,7 @@ struct Rf {
     double K = CK / Hz * (1.0 + AG1 * std::exp(-std::pow((lz - zG1) / wG1, 2)) + AG2 * std::exp(-std::pow((lz - zG2) / wG2, 2)));
     double Rdtr = atr / (s0 * std::pow(1 + s0, 1 - btr)) / std::pow(1 + s1, 1 + btr);
     double Rutr = Rdtr * std::exp(-h_P * C * L_He2St_ion / (k_B * Tm)) * std::pow(CR * Tm, 1.5) * (4.0 / 3.0);
-    int flag = (xHe < 5e-9 || xHe > 0.98) ? 0 : Heswitch;
+    int flag = (br & 1) ? 0 : Heswitch;
     double KHe, Cft = 0.0;
     if (flag == 0) {
       KHe = CK_He / Hz;
@@ -412,7 +455,7 @@ struct Rf {
       double tauS = A2P_s * CK_He * 3 * nHe * (1 - xHe) / Hz;
       double pS = (1 - std::exp(-tauS)) / tauS;
       KHe = 1.0 / (A2P_s * pS * 3 * nHe * (1 - xHe));
-      if ((flag == 2 || flag >= 5) && xH < 0.9999999) {
+      if ((flag == 2 || flag >= 5) && (br & 2)) {
         double Dop = C * L_He_2p * std::sqrt(2 * k_B * Tm / (m_H * not4 * C * C));
         double g2 = 3 * A2P_s * fHe * (1 - xHe) * C * C / (std::sqrt(M_PI) * sigma_He_2Ps * 8 * M_PI * Dop * (1 - xH)) /
                     std::pow(C * L_He_2p, 2);
@@ -423,7 +466,7 @@ struct Rf {
         double tauT = A2P_t * nHe * (1. - xHe) * 3 / (8 * M_PI * Hz * std::pow(L_He_2Pt, 3));
         double pT = (1 - std::exp(-tauT)) / tauT;
         double CLPSt = h_P * C * (L_He_2Pt - L_He_2St) / k_B;
-        if (flag == 3 || flag == 5 || xH > 0.99999) {
+        if (flag == 3 || flag == 5 || (br & 4)) {
           Cft = A2P_t * pT * std::exp(-CLPSt / Tm);
         } else {
           double Dop = C * L_He_2Pt * std::sqrt(2 * k_B * Tm / (m_H * not4 * C * C));
@@ -438,20 +481,20 @@ struct Rf {
     double tTh = (1.0 / (CT * std::pow(Trad, 4))) * (1 + x + fHe) / x;
     double tH = 2.0 / (3.0 * HO * std::pow(zp, 1.5));
     double f1;
-    if (xH > 0.99) f1 = 0.0;
-    else if (xH > 0.985) f1 = (x * xH * n * Rdown - Rup * (1 - xH) * std::exp(-CL / Tm)) / (Hz * zp);
+    if (br & 8) f1 = 0.0;
+    else if (br & 16) f1 = (x * xH * n * Rdown - Rup * (1 - xH) * std::exp(-CL / Tm)) / (Hz * zp);
     else
       f1 = ((x * xH * n * Rdown - Rup * (1.0 - xH) * std::exp(-CL / Tm)) * (1.0 + K * Lambda * n * (1.0 - xH))) /
            (Hz * zp * (1.0 / fu + K * Lambda * n * (1.0 - xH) / fu + K * Rup * n * (1.0 - xH)));
     double f2 = 0.0;
-    if (!(xHe < 1e-15)) {
+    if (!(br & 32)) {
       f2 = ((x * xHe * n * RdHe - RuHe * (1 - xHe) * std::exp(-CL_He / Tm)) * (1 + KHe * Lambda_He * nHe * (1 - xHe) * HeB)) /
            (Hz * zp * (1 + KHe * (Lambda_He + RuHe) * nHe * (1 - xHe) * HeB));
       if (flag >= 3)
         f2 += (x * xHe * n * Rdtr - (1 - xHe) * 3 * Rutr * std::exp(-h_P * C * L_He_2St / (k_B * Tm))) * Cft / (Hz * zp);
     }
     double f3;
-    if (tTh < H_frac * tH) {
+    if (br & 64) {
       double eps = Hz * (1 + x + fHe) / (CT * std::pow(Trad, 3) * x);
       f3 = Tnow + eps * ((1 + fHe) / (1 + fHe + x)) * ((f1 + fHe * f2) / x) - eps * dHdz / Hz + 3 * eps / zp;
     } else {
@@ -545,7 +588,15 @@ void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const 
     double z = 1.0 / std::exp(g.at(j)) - 1.0;
     if (z < zini) zland.push_back(z);
   }
+  BranchLog logHe, logHHe;
+  if (fz) {
+    logHe.bits = &fz->bHe;
+    logHHe.bits = &fz->bHHe;
+    logHe.replay = logHHe.replay = replay;
+    if (!replay) { fz->bHe.clear(); fz->bHHe.clear(); }
+  }
   double y2[2] = {(rf.xtot_He1_saha(zHe) - 1.0) / rf.fHe, rf.Tnow * (1 + zHe)};
+  rf.blog = fz ? &logHe : nullptr;
   Traj He = tsit5_integrate(
       [&](double z, const double* u, double* du) {
         double yy[3] = {rf.xH_saha(z), u[0], u[1]}, d[3];
@@ -553,17 +604,21 @@ void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const 
         du[0] = d[1];
         du[1] = d[2];
       },
-      2, y2, zHe, zHH, rf.tol, 1e-6, zland, replay ? &fz->tHe : nullptr);
+      2, y2, zHe, zHH, rf.tol, 1e-6, zland, replay ? &fz->tHe : nullptr, replay ? &fz->hHe : nullptr,
+      fz ? &logHe : nullptr);
+  rf.blog = fz ? &logHHe : nullptr;
   double y3[3] = {rf.xH_saha(zHH), He.last()[0], He.last()[1]};
   std::vector<double> land3 = zland;
   land3.push_back(zre_ini);
   Traj HHe = tsit5_integrate([&](double z, const double* u, double* du) { rf.rhs(z, u, du); }, 3, y3, zHH, zfin, rf.tol,
-                             1e-6, land3, replay ? &fz->tHHe : nullptr);
+                             1e-6, land3, replay ? &fz->tHHe : nullptr, replay ? &fz->hHHe : nullptr,
+                             fz ? &logHHe : nullptr);
+  rf.blog = nullptr;
   auto xe_recfast = [&](double z) -> double {  // recfast.jl:413-433
     if (z > 8000.) return 1 + 2 * rf.fHe;
     if (z > 5000.) {
       double r = rf.saha(z, rf.CB1_He2);
-      return 0.5 * (std::sqrt(std::pow(r - 1 - rf.fHe, 2) + 4 * (1 + 2 * rf.fHe) * r) - (r - 1 - rf.fHe));
+      return Rf::quad_root(r - 1 - rf.fHe, (1 + 2 * rf.fHe) * r);
     }
     if (z > 3500.) return 1 + rf.fHe;
     if (z > zHe) return rf.xtot_He1_saha(z);
@@ -591,13 +646,16 @@ void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const 
         double Hz = sH(std::log(a)) / a / sec_per_nat(), Trad = rf.Tnow * (1 + z);
         du[0] = rf.CT * std::pow(Trad, 4) * xr / (1 + xr + rf.fHe) * (u[0] - Trad) / (Hz * (1 + z)) + 2 * u[0] / (1 + z);
       },
-      1, &T50, zre_ini, zfin, rf.tol, 1e-6, zland, replay ? &fz->tRe : nullptr);
+      1, &T50, zre_ini, zfin, rf.tol, 1e-6, zland, replay ? &fz->tRe : nullptr, replay ? &fz->hRe : nullptr);
   if (fz && !replay) {
     fz->zHe = zHe;
     fz->zHH = zHH;
     fz->tHe = He.t;
     fz->tHHe = HHe.t;
     fz->tRe = Re.t;
+    fz->hHe = He.h;
+    fz->hHHe = HHe.h;
+    fz->hRe = Re.h;
     fz->have = true;
   }
 

@@ -75,15 +75,18 @@ double units_km_s_Mpc_100();
 double units_mass_eV();
 
 // The discretisation choices of one RECFAST run: the two Saha switch
-// redshifts (root finds) and the accepted abscissae of its three Tsit5
-// integrations.  Replaying them makes the tables a smooth function of the
+// redshifts (root finds), the accepted abscissae and step sizes of its three
+// Tsit5 integrations, and the sides of the right-hand side's state-dependent
+// switches at every stage of the accepted steps.  Replaying them makes the tables a smooth function of the
 // parameters, for derivatives by central differences; the switch redshifts
 // are held fixed as the reference's ForwardDiff gradient does
 // (recfast.jl:451-456, assume_nondual).
 struct RecfastFreeze {
   bool have = false;
   double zHe = 0.0, zHH = 0.0;
-  std::vector<double> tHe, tHHe, tRe;
+  std::vector<double> tHe, tHHe, tRe;  // accepted abscissae
+  std::vector<double> hHe, hHHe, hRe;  // accepted step sizes
+  std::vector<uint8_t> bHe, bHHe;      // sides of the right-hand side's switches taken
 };
 
 // Builds Background + RECFAST + IonizationHistory.  Throws std::runtime_error.

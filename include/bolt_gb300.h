@@ -68,6 +68,17 @@ double bolt_km_s_Mpc_100(void);   /* 100 km/s/Mpc in Mpc^-1 (src/Bolt.jl:49) */
 int bolt_host_tables(const bolt_params* par, const bolt_grid* grid, int nq, const bolt_recfast* rf,
                      double* nodes, double* scalars, char* errbuf, int errlen);
 
+/* Host-only: the tables of `par` built on the RECFAST discretisation of
+ * `base` (its Saha switch redshifts and the accepted steps of its three
+ * Tsit5 integrations, replayed without error control), as the engine builds
+ * the parameter sets of a gradient.  The tables are then a smooth function
+ * of par near base; par == base gives bolt_host_tables' nodes exactly.
+ * No counterpart in the reference (its ForwardDiff gradient differentiates
+ * through one discretisation in the same way).  nodes[BOLT_T_COUNT][n]. */
+int bolt_host_tables_frozen(const bolt_params* base, const bolt_params* par, const bolt_grid* grid, int nq,
+                            const bolt_recfast* rf_base, const bolt_recfast* rf, double* nodes, char* errbuf,
+                            int errlen);
+
 /* Creates a context bound to one GPU. */
 int bolt_ctx_create(const bolt_opts* opts, bolt_ctx** out);
 void bolt_ctx_destroy(bolt_ctx* ctx);

@@ -259,19 +259,26 @@ struct Recfast {
     f[0] = f1; f[1] = f2; f[2] = f3;
   }
 
+  // Root 0.5 (sqrt(b^2 + 4c) - b) of the Saha equations (recfast.jl:373-411),
+  // written as 2c / (sqrt(b^2 + 4c) + b) when b > 0: the same number without
+  // the cancellation that leaves ~1e-6 of rounding noise at early times.
+  static double quad_root(double b, double c) {
+    double s = std::sqrt(b * b + 4.0 * c);
+    return b > 0.0 ? 2.0 * c / (s + b) : 0.5 * (s - b);
+  }
   double saha_rhs(double z, double CB) const {
     return std::exp(1.5 * std::log(CR * Tnow / (1 + z)) - CB / (Tnow * (1 + z))) / Nnow;
   }
   // recfast.jl:373-380
   double end_of_saha_condition(double z) const {
     double rhs = saha_rhs(z, CB1_He1) * 4;
-    double x0 = 0.5 * (std::sqrt((rhs - 1) * (rhs - 1) + 4 * (1 + fHe) * rhs) - (rhs - 1));
+    double x0 = quad_root(rhs - 1, (1 + fHe) * rhs);
     return (x0 - 1) / fHe - 0.99;
   }
   // recfast.jl:402-408
   double x_H0_H_Saha(double z) const {
     double rhs = saha_rhs(z, CB1);
-    return 0.5 * (std::sqrt(rhs * rhs + 4 * rhs) - rhs);
+    return quad_root(rhs, rhs);
   }
   double end_He_evo_condition(double z) const { return x_H0_H_Saha(z) - 0.985; }
 };
@@ -328,7 +335,7 @@ struct RecfastHistory {
     double y2[2];
     {
       double rhs = r->saha_rhs(z_He_evo_start, r->CB1_He1) * 4.0;
-      double x0 = 0.5 * (std::sqrt((rhs - 1) * (rhs - 1) + 4 * (1 + r->fHe) * rhs) - (rhs - 1));
+      double x0 = Recfast::quad_root(rhs - 1, (1 + r->fHe) * rhs);
       y2[0] = (x0 - 1) / r->fHe;
       y2[1] = r->Tnow * (1 + z_He_evo_start);
     }
@@ -361,12 +368,12 @@ struct RecfastHistory {
     if (z > 8000.) return 1 + 2 * r->fHe;
     if (z > 5000.) {
       double rhs = r->saha_rhs(z, r->CB1_He2);
-      return 0.5 * (std::sqrt(std::pow(rhs - 1 - r->fHe, 2) + 4 * (1 + 2 * r->fHe) * rhs) - (rhs - 1 - r->fHe));
+      return Recfast::quad_root(rhs - 1 - r->fHe, (1 + 2 * r->fHe) * rhs);
     }
     if (z > 3500.) return 1 + r->fHe;
     if (z > z_He_evo_start) {
       double rhs = r->saha_rhs(z, r->CB1_He1) * 4;
-      return 0.5 * (std::sqrt((rhs - 1) * (rhs - 1) + 4 * (1 + r->fHe) * rhs) - (rhs - 1));
+      return Recfast::quad_root(rhs - 1, (1 + r->fHe) * rhs);
     }
     if (z > z_H_He_evo_start) return r->x_H0_H_Saha(z) + r->fHe * sol_He.at(z, 0);
     double u[3];
