@@ -117,7 +117,7 @@ def io_bytes(d):
     """Host->device input and device->host output bytes of one request (the
     request's k grid, multipoles, 2003-node tables of every parameter set and
     mode records; results, statuses and step counters)."""
-    nsets = 13 if d["kind"] == "grad" else 1
+    nsets = 7 if d["kind"] == "grad" else 1
     nk = d["nk"]
     tab = nsets * (2003 * 16 + 30) * 8
     if d["kind"] == "plin":
@@ -203,7 +203,7 @@ def barrier(dist):
 def cpu_stream_seconds(stream):
     """CPU oracle seconds for the stream, from timed samples of each request
     type scaled by its size (modes x state length for the solves, multipoles
-    for the projection; a gradient is 13 parameter sets, as central
+    for the projection; a gradient is 7 parameter sets, as forward
     differences over six parameters need).  About 10-30 s of CPU work."""
     from concurrent.futures import ThreadPoolExecutor
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -232,7 +232,7 @@ def cpu_stream_seconds(stream):
     t_ell = (time.perf_counter() - t0) / ells.size
     total = 0.0
     for d in stream:
-        nsets = 13 if d["kind"] == "grad" else 1
+        nsets = 7 if d["kind"] == "grad" else 1
         if d["kind"] == "plin":
             total += t_tab + d["nk"] * t_plin_k
         else:
@@ -241,7 +241,7 @@ def cpu_stream_seconds(stream):
     sample = (f"CPU oracle (C++ restatement of Bolt's CPU algorithm) on {cores} threads: tables {t_tab:.3f} s, "
               f"P_lin {t_plin_k * 1e3:.1f} ms/k ({ks.size} k), source grid {t_mode * 1e3:.1f} ms/mode at N={n35} "
               f"({kc.size} modes, scaled by state length), C_l {t_ell * 1e3:.2f} ms/l ({ells.size} l); "
-              f"gradients = 13 parameter sets; scaled to the {len(stream)}-request stream")
+              f"gradients = 7 parameter sets; scaled to the {len(stream)}-request stream")
     return total, cores, sample
 
 

@@ -7,7 +7,7 @@
 // to theta = (h, omega_b, omega_c, n, A, Sigma m_nu).
 //
 //   submit ──> host worker threads: Background + RECFAST tables
-//              (13 table sets for a gradient: the cosmology and theta ± d)
+//              (7 table sets for a gradient: the cosmology and theta_j + d_j)
 //          ──> ready FIFO ──> scheduler thread: admits ready requests while
 //              the in-flight device footprint fits the budget, forms a batch
 //              and enqueues it on an idle lane (stream):
@@ -21,14 +21,16 @@
 // tail of the previous batch leaves idle, so requests that arrive while
 // others are on the GPU are admitted as memory and lanes free up.
 //
-// Gradients are central differences of the discrete pipeline with every
+// Gradients are forward differences of the discrete pipeline with every
 // discretisation choice frozen: the perturbed modes replay the accepted
 // steps of the unperturbed mode (MODE_RECORD / MODE_REPLAY), RECFAST replays
-// its steps and switch redshifts (RecfastFreeze), and the k grids and the
-// Bessel grid are those of the unperturbed cosmology, as the reference's
-// ForwardDiff gradient holds them (spectra.jl:46-66, recfast.jl:451-456).
-// The pipeline is then a smooth function of theta, and the relative step
-// 1e-5 leaves truncation errors ~1e-10 and round-off ~1e-9 (relative).
+// its steps, step sizes, switch redshifts and right-hand-side branches
+// (RecfastFreeze), and the k grids and the Bessel grid are those of the
+// unperturbed cosmology, as the reference's ForwardDiff gradient holds them
+// (spectra.jl:46-66, recfast.jl:451-456).  The pipeline is then a smooth,
+// deterministic function of theta, so one-sided differences with the
+// relative step 1e-6 carry truncation and round-off errors of ~1e-6
+// (relative): 7 parameter sets per gradient request.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -90,7 +92,7 @@ namespace {
 
 constexpr int kTheta = 6;
 constexpr int kRecCap = 12288;      // recorded steps per mode (gradient requests)
-constexpr double kRelStep = 1e-5;   // central-difference step, relative to |theta_j|
+constexpr double kRelStep = 1e-6;   // forward-difference step, relative to |theta_j|
 constexpr int kNb = 5001;           // Bessel grid points (spectra.jl:52)
 constexpr int kNkd = 5000;          // dense LOS k grid (spectra.jl:133)
 
@@ -180,7 +182,6 @@ struct Req {
   int nsets = 1;
   std::vector<CosmoParamsH> pars;  // [nsets]
   double step[kTheta] = {0, 0, 0, 0, 0, 0};
-  bool one_sided[kTheta] = {false, false, false, false, false, false};
   std::vector<CosmoTables> T;      // [nsets]
   RecfastFreeze fz;
   int tables_left = 0;
@@ -777,13 +778,8 @@ void finalize_request(bolt_engine* E, Lane& L, Req* r) {
         break;
       }
     }
-  auto deriv = [&](const double* f, size_t stride, int j, size_t i) -> double {
-    const double h = r->step[j];
-    const double fa = f[size_t(1 + 2 * j) * stride + i], fb = f[size_t(2 + 2 * j) * stride + i];
-    if (r->one_sided[j]) {  // sets: +h, +2h
-      return (-3.0 * f[i] + 4.0 * fa - fb) / (2.0 * h);
-    }
-    return (fa - fb) / (2.0 * h);
+  auto deriv = [&](const double* f, size_t stride, int j, size_t i) -> double {  // set 1 + j: theta_j + h
+    return (f[size_t(1 + j) * stride + i] - f[i]) / r->step[j];
   };
   if (r->r.kind == BOLT_REQ_PLIN) {
     const double* P = reinterpret_cast<const double*>(down + r->h_plin);
@@ -1081,20 +1077,17 @@ int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
                       q->par.N_nu, q->par.Sigma_m_nu};
     r->pars.push_back(base);
     if (q->grad) {
-      r->nsets = 1 + 2 * kTheta;
+      r->nsets = 1 + kTheta;
       double th[kTheta];
       theta_of(base, th);
       for (int j = 0; j < kTheta; ++j) {
+        // step = 1e-6 |theta_j| (Sigma m_nu: at least 1e-7 eV, so it works at 0)
         double hstep = kRelStep * std::max(std::fabs(th[j]), j == 5 ? 0.1 : 1e-30);
         r->step[j] = hstep;
-        r->one_sided[j] = (j == 5 && th[j] < 2.0 * hstep);
-        double a[kTheta], b[kTheta];
+        double a[kTheta];
         std::copy(th, th + kTheta, a);
-        std::copy(th, th + kTheta, b);
-        if (r->one_sided[j]) { a[j] += hstep; b[j] += 2.0 * hstep; }
-        else { a[j] += hstep; b[j] -= hstep; }
+        a[j] += hstep;
         r->pars.push_back(params_of(base, a));
-        r->pars.push_back(params_of(base, b));
       }
     }
     r->T.resize(r->nsets);

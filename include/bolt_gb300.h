@@ -183,12 +183,13 @@ int bolt_fp64_peak(int device, double* tflops);
  * Gradients (grad = 1) are with respect to
  *   theta = (h, omega_b = Omega_b h^2, omega_c = Omega_c h^2, n, A, Sigma m_nu [eV])
  * with Omega_r, Y_p and N_nu held fixed: d/dtheta of the discrete pipeline
- * by central differences (relative step 1e-5; one-sided at Sigma m_nu ~ 0)
- * with every discretisation choice frozen -- the perturbed modes replay the
- * accepted steps of the unperturbed solve, RECFAST replays its steps and
- * switch redshifts, and the k grids and the Bessel grid stay those of the
- * unperturbed cosmology (the reference's assume_nondual points,
- * spectra.jl:46-66, recfast.jl:451-456).  Layout d*[6][n].
+ * by forward differences (relative step 1e-6, accurate to ~1e-6) with every
+ * discretisation choice frozen -- the perturbed modes replay the accepted
+ * steps of the unperturbed solve, RECFAST replays its steps, switch
+ * redshifts and right-hand-side branches, and the k grids and the Bessel
+ * grid stay those of the unperturbed cosmology (the reference's
+ * assume_nondual points, spectra.jl:46-66, recfast.jl:451-456).  Layout
+ * d*[6][n].
  *
  * Output arrays are caller-owned host memory that must stay valid (and
  * untouched) until the request has completed.
