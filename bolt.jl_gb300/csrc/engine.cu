@@ -82,6 +82,25 @@ int launch_jl_prefilter(int nb, int nslots, int ncz, const double* d_raw, const 
 int launch_sdense(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_ST, const double* d_SE, int nm,
                   const double* d_kmid, const double* d_dx, double* d_SdT, double* d_SdE, cudaStream_t st);
 int launch_los_cl(const LosArgs& a, int ncz, cudaStream_t st);
+struct LosGradArgs {
+  int nb, nslots, nrow, nm;
+  const int* ells;
+  const double* coef;
+  const double* inv_dg;
+  const double* yv;
+  const double* dyv;
+  const double* kmid;
+  const double* wts;
+  const double* dwts;
+  int dstride;
+  const double* Sd;
+  const double* dSd;
+  double* tt;
+  double* dtt;
+};
+int launch_sdense_diff(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_Sa, const double* d_Sb,
+                       double scale, int nm, const double* d_kmid, const double* d_dx, double* d_out, cudaStream_t st);
+int launch_los_tt_grad(const LosGradArgs& a, cudaStream_t st);
 void fill_cosmo_dev(const CosmoTables& T, double* d_tab, double* h_tab, CosmoDev& d);
 size_t cosmo_table_doubles(const CosmoTables& T);
 }  // namespace bolt
@@ -199,6 +218,7 @@ struct Req {
   size_t h_stat = 0, h_plin = 0, h_cl = 0, h_cnt = 0;
   int cos0 = 0;  // first CosmoDev index of the request in the batch
   bool wantE = false;
+  bool los_tangent = false;  // C_l^TT gradient from the tangent of the LOS integral
 };
 
 struct Tuner {  // seconds per mode-step by batch-size bucket and warps per mode
@@ -254,7 +274,7 @@ struct Lane {
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // start, phase 1, phase 2, LOS, done
   int* d_queue = nullptr;  // [2] work-queue counters of the two solver phases
   Graph graph[3][2];       // [warps-per-mode variant][phase]
-  GrowDev scr, los_raw, los_norm, los_coef, los_SdT, los_SdE;
+  GrowDev scr, los_raw, los_norm, los_coef, los_SdT, los_SdE, los_dSd;
   GrowHost up, down;
   bool busy = false;
   std::vector<Req*> batch;
@@ -463,9 +483,10 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   int ncos = 0, m1 = 0, m2 = 0, maxN = 0, maxnq = 1, maxL = 3;
   size_t max_sd = 0;
   int max_slots = 0;
-  bool anyE = false;
+  bool anyE = false, anyTangent = false;
   for (Req* r : batch) {
     layout_request(r, off);
+    anyTangent |= r->los_tangent;
     r->cos0 = ncos;
     ncos += r->nsets;
     m1 += r->r.nk;
@@ -510,6 +531,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     SdT = static_cast<double*>(L.los_SdT.get(max_sd * 8));
     if (anyE) SdE = static_cast<double*>(L.los_SdE.get(max_sd * 8));
   }
+  double* dSd = anyTangent ? static_cast<double*>(L.los_dSd.get(size_t(kTheta) * max_sd * 8)) : nullptr;
   // ---- host staging (pinned, compact): input segments only
   struct Seg {
     size_t dev, host, bytes;
@@ -679,6 +701,12 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
       for (int m = 0; m < nm; ++m) wts[m] = T.par.A * std::pow(kmid[m] / 0.05, T.par.n - 1.0) * dk[m] / kmid[m];
       for (int i = 0; i < nrow; ++i) yv[i] = T.eta0 - spline_eval(T.coef[T_ETA].data(), n, g.x0, g.h, g.at(i0 + i));
     }
+    if (r->los_tangent)  // sets 1..6 -> derivatives of the weights and of y along theta_j
+      for (int j = 0; j < kTheta; ++j) {
+        double* d = per + size_t(1 + j) * (nm + n);
+        const double inv = 1.0 / r->step[j];
+        for (int q = 0; q < nm + nrow; ++q) d[q] = (d[q] - per[q]) * inv;
+      }
     plans.push_back({r, i0, nrow, nm, ns, r->uniq.back(), head});
   }
   // ---- enqueue
@@ -727,6 +755,22 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     launches += 2;
     const double* src = reinterpret_cast<const double*>(dev + r->o_src);
     double* cl = reinterpret_cast<double*>(dev + r->o_cl);
+    if (r->los_tangent) {
+      rc = launch_sdense(n, P.i0, P.nrow, nk, kg, src, nullptr, P.nm, kmid, dxs, SdT, nullptr, st);
+      for (int j = 0; j < kTheta && rc == 0; ++j)
+        rc = launch_sdense_diff(n, P.i0, P.nrow, nk, kg, src + size_t(1 + j) * nk * n, src, 1.0 / r->step[j], P.nm,
+                                kmid, dxs, dSd + size_t(j) * P.nrow * P.nm, st);
+      if (rc != 0) throw EngErr(-3, std::string("source resampling: ") + cudaGetErrorString(cudaError_t(rc)));
+      LosGradArgs a;
+      a.nb = kNb; a.nslots = P.ns; a.nrow = P.nrow; a.nm = P.nm;
+      a.ells = ells; a.coef = coef; a.inv_dg = misc + 1;
+      a.wts = per; a.yv = per + P.nm; a.dwts = per + (P.nm + n); a.dyv = per + (P.nm + n) + P.nm; a.dstride = P.nm + n;
+      a.kmid = kmid; a.Sd = SdT; a.dSd = dSd; a.tt = cl; a.dtt = cl + P.ns;
+      rc = launch_los_tt_grad(a, st);
+      if (rc != 0) throw EngErr(-3, std::string("line of sight (tangent): ") + cudaGetErrorString(cudaError_t(rc)));
+      launches += 2 + kTheta;
+      continue;
+    }
     for (int s = 0; s < r->nsets; ++s) {
       const double* ST = src + size_t(s) * nk * n;
       const double* SE = r->wantE ? src + size_t(r->nsets) * nk * n + size_t(s) * nk * n : nullptr;
@@ -794,6 +838,14 @@ void finalize_request(bolt_engine* E, Lane& L, Req* r) {
     double* outs[3] = {r->r.tt, r->r.te, r->r.ee};
     double* douts[3] = {r->r.dtt, r->r.dte, r->r.dee};
     const int bits[3] = {BOLT_CL_TT, BOLT_CL_TE, BOLT_CL_EE};
+    if (r->los_tangent) {  // [0, nsl): C_l^TT, then [6][nsl] its derivatives
+      for (int e = 0; e < r->r.nell; ++e) {
+        int sl = int(std::lower_bound(r->uniq.begin(), r->uniq.end(), r->ells[e]) - r->uniq.begin());
+        r->r.tt[e] = cl[sl];
+        for (int j = 0; j < kTheta; ++j) r->r.dtt[size_t(j) * r->r.nell + e] = cl[size_t(1 + j) * nsl + sl];
+      }
+      return;
+    }
     for (int q = 0; q < 3; ++q) {
       if (!(r->r.cl_want & bits[q])) continue;
       for (int e = 0; e < r->r.nell; ++e) {
@@ -1035,6 +1087,7 @@ void bolt_engine_destroy(bolt_engine* E) {
         if (G.g) cudaGraphDestroy(G.g);
       }
     L.scr.release(); L.los_raw.release(); L.los_norm.release(); L.los_coef.release(); L.los_SdT.release();
+    L.los_dSd.release();
     L.los_SdE.release(); L.up.release(); L.down.release();
     cudaFree(L.d_queue);
     for (auto& e : L.ev) cudaEventDestroy(e);
@@ -1062,6 +1115,7 @@ int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
       std::sort(r->uniq.begin(), r->uniq.end());
       r->uniq.erase(std::unique(r->uniq.begin(), r->uniq.end()), r->uniq.end());
       r->wantE = (q->cl_want & (BOLT_CL_TE | BOLT_CL_EE)) != 0;
+      r->los_tangent = q->grad && q->cl_want == BOLT_CL_TT;
     } else {
       r->r.ells = nullptr;
       r->r.nell = 0;

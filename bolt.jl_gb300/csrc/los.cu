@@ -300,6 +300,163 @@ __global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
   }
 }
 
+// -------------------------------------------------- C_l^TT and its tangent
+// Derivatives of C_l^TT along six parameter directions j at a frozen Bessel
+// grid and frozen k grids (the derivative the reference's ForwardDiff
+// gradient of cltt takes, spectra.jl:46-160):
+//   Delta      = sum_i j_l(k y_i) S_i dx_i
+//   dDelta_j   = sum_i [ j_l'(k y_i) k dy_ij S_i + j_l(k y_i) dS_ij ] dx_i
+//   C          = 4 pi sum_m w_m Delta^2
+//   dC_j       = 4 pi sum_m [ 2 w_m Delta dDelta_j + dw_jm Delta^2 ]
+// with y_i = eta0 - eta(x_i), dy_ij its derivative, S / dS resampled with dx
+// folded in (sdense), dw_jm the derivative of A (k/0.05)^(n-1) dk/k.  One
+// j_l spline evaluation (value and slope) serves all six directions.
+constexpr int kDir = 6;
+
+struct LosGradArgs {
+  int nb, nslots, nrow, nm;
+  const int* ells;
+  const double* coef;   // [nslots][nb+2]
+  const double* inv_dg; // [1]
+  const double* yv;     // [nrow]
+  const double* dyv;    // [kDir][dstride]
+  const double* kmid;   // [nm]
+  const double* wts;    // [nm]
+  const double* dwts;   // [kDir][dstride]
+  int dstride;          // stride of dwts and dyv per direction
+  const double* Sd;     // [nrow][nm]
+  const double* dSd;    // [kDir][nrow][nm]
+  double* tt;           // [nslots]
+  double* dtt;          // [kDir][nslots]
+};
+
+__global__ void __launch_bounds__(256) los_tt_grad_kernel(LosGradArgs a) {
+  extern __shared__ double sh[];
+  const int s = blockIdx.x;
+  const int nb2 = a.nb + 2;
+  double* cs = sh;                   // nb + 2 coefficients
+  double* yl = sh + nb2;             // nrow scaled arguments
+  double* dyl = yl + a.nrow;         // kDir * nrow scaled argument derivatives
+  double* red = dyl + kDir * a.nrow; // (1 + kDir) * blockDim
+  const double* src = a.coef + (size_t)s * nb2;
+  for (int j = threadIdx.x; j < nb2; j += blockDim.x) cs[j] = src[j];
+  const double idg = a.inv_dg[0];
+  for (int j = threadIdx.x; j < a.nrow; j += blockDim.x) yl[j] = a.yv[j] * idg;
+  for (int j = threadIdx.x; j < kDir * a.nrow; j += blockDim.x)
+    dyl[j] = a.dyv[(size_t)(j / a.nrow) * a.dstride + j % a.nrow] * idg;
+  // zero-skip bound as in los_cl_kernel
+  double cmax = 0.0;
+  for (int j = threadIdx.x; j < nb2; j += blockDim.x) cmax = fmax(cmax, fabs(cs[j]));
+  red[threadIdx.x] = cmax;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  const double thr = kSkipRel * red[0];
+  int jfirst = nb2;
+  for (int j = threadIdx.x; j < nb2; j += blockDim.x)
+    if (fabs(cs[j]) > thr) { jfirst = j; break; }
+  __syncthreads();
+  reinterpret_cast<int*>(red)[threadIdx.x] = jfirst;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      int* ir = reinterpret_cast<int*>(red);
+      ir[threadIdx.x] = min(ir[threadIdx.x], ir[threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  const double ulo = double(reinterpret_cast<int*>(red)[0] - 3);
+  __syncthreads();
+  const double umax = double(a.nb - 2);
+  const size_t plane = (size_t)a.nrow * a.nm;
+  double stt = 0.0, dstt[kDir];
+#pragma unroll
+  for (int j = 0; j < kDir; ++j) dstt[j] = 0.0;
+  for (int m = threadIdx.x; m < a.nm; m += blockDim.x) {
+    const double k = a.kmid[m];
+    int iend = 0;
+    if (k * yl[0] >= ulo) {
+      int lo = 0, hi = a.nrow;
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (k * yl[mid] >= ulo) lo = mid; else hi = mid;
+      }
+      iend = hi;
+    }
+    double th = 0.0, dth[kDir];
+#pragma unroll
+    for (int j = 0; j < kDir; ++j) dth[j] = 0.0;
+    for (int i = 0; i < iend; ++i) {
+      double u = k * yl[i];
+      double f = floor(u);
+      f = fmin(f, umax);
+      int jj = (int)f;
+      double t = u - f, sm = 1.0 - t, t2 = t * t, s2 = sm * sm;
+      double w0 = s2 * sm, w3 = t2 * t;
+      double w1 = 4.0 - 6.0 * t2 + 3.0 * w3;
+      double w2 = 4.0 - 6.0 * s2 + 3.0 * w0;
+      const double c0 = cs[jj], c1 = cs[jj + 1], c2 = cs[jj + 2], c3 = cs[jj + 3];
+      double jv = (c0 * w0 + c1 * w1 + c2 * w2 + c3 * w3) * (1.0 / 6.0);
+      // d/du of the cubic B-spline (per grid unit)
+      double jd = (-0.5 * s2) * c0 + (-2.0 * t + 1.5 * t2) * c1 + (2.0 * sm - 1.5 * s2) * c2 + (0.5 * t2) * c3;
+      const size_t q = (size_t)i * a.nm + m;
+      const double S = a.Sd[q];
+      th = fma(jv, S, th);
+      const double jdS = jd * S * k;
+#pragma unroll
+      for (int j = 0; j < kDir; ++j)
+        dth[j] = fma(jdS, dyl[j * a.nrow + i], fma(jv, a.dSd[j * plane + q], dth[j]));
+    }
+    const double w = a.wts[m];
+    stt = fma(th * th, w, stt);
+#pragma unroll
+    for (int j = 0; j < kDir; ++j)
+      dstt[j] = fma(2.0 * w * th, dth[j], fma(a.dwts[(size_t)j * a.dstride + m], th * th, dstt[j]));
+  }
+  red[threadIdx.x] = stt;
+#pragma unroll
+  for (int j = 0; j < kDir; ++j) red[(1 + j) * blockDim.x + threadIdx.x] = dstt[j];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int j = 0; j <= kDir; ++j) red[j * blockDim.x + threadIdx.x] += red[j * blockDim.x + threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double fp = 4.0 * M_PI;
+    a.tt[s] = fp * red[0];
+    for (int j = 0; j < kDir; ++j) a.dtt[(size_t)j * a.nslots + s] = fp * red[(1 + j) * blockDim.x];
+  }
+}
+
+// (S_a - S_b) * scale resampled like sdense_kernel (dx folded in).
+__global__ void sdense_diff_kernel(int nx, int i0, int nrow, int nk, const double* __restrict__ kgrid,
+                                   const double* __restrict__ Sa, const double* __restrict__ Sb, double scale, int nm,
+                                   const double* __restrict__ kmid, const double* __restrict__ dxs,
+                                   double* __restrict__ out) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y;
+  if (m >= nm || i >= nrow) return;
+  double k = kmid[m];
+  int lo = 0, hi = nk - 1;
+  if (k >= kgrid[nk - 1]) lo = nk - 2;
+  else if (k < kgrid[0]) lo = 0;
+  else {
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (kgrid[mid] <= k) lo = mid; else hi = mid;
+    }
+    if (lo > nk - 2) lo = nk - 2;
+  }
+  double wk = (k - kgrid[lo]) / (kgrid[lo + 1] - kgrid[lo]);
+  int ix = i0 + i;
+  double d0 = Sa[(size_t)lo * nx + ix] - Sb[(size_t)lo * nx + ix];
+  double d1 = Sa[(size_t)(lo + 1) * nx + ix] - Sb[(size_t)(lo + 1) * nx + ix];
+  out[(size_t)i * nm + m] = ((1.0 - wk) * d0 + wk * d1) * dxs[i] * scale;
+}
+
 // ------------------------------------------------------------ launchers ----
 int launch_jl_raw(int nb, const double* d_dgs, int ncz, int Lmax, const int* d_slot_of_l, int nslots, double* d_raw,
                   double* d_norm, int* d_flags, cudaStream_t st) {
@@ -319,6 +476,22 @@ int launch_sdense(int nx, int i0, int nrow, int nk, const double* d_kgrid, const
                   const double* d_kmid, const double* d_dx, double* d_SdT, double* d_SdE, cudaStream_t st) {
   dim3 g((nm + 255) / 256, nrow);
   sdense_kernel<<<g, 256, 0, st>>>(nx, i0, nrow, nk, d_kgrid, d_ST, d_SE, nm, d_kmid, d_dx, d_SdT, d_SdE);
+  return cudaGetLastError();
+}
+
+int launch_sdense_diff(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_Sa, const double* d_Sb,
+                       double scale, int nm, const double* d_kmid, const double* d_dx, double* d_out, cudaStream_t st) {
+  dim3 g((nm + 255) / 256, nrow);
+  sdense_diff_kernel<<<g, 256, 0, st>>>(nx, i0, nrow, nk, d_kgrid, d_Sa, d_Sb, scale, nm, d_kmid, d_dx, d_out);
+  return cudaGetLastError();
+}
+
+int launch_los_tt_grad(const LosGradArgs& a, cudaStream_t st) {
+  const int threads = 256;
+  size_t smem = (size_t(a.nb + 2) + size_t(1 + kDir) * a.nrow + size_t(1 + kDir) * threads) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(los_tt_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return e;
+  los_tt_grad_kernel<<<a.nslots, threads, smem, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -5,7 +5,8 @@ points and the oracle.
   (bolt_cl_pipeline, bolt_plin on the same host-built tables).
 * Requests give the same result alone (one request per batch) and in a mix
   submitted together (batched, several lanes in flight).
-* Gradients (central differences of the frozen-step pipeline) agree with
+* Gradients (forward differences of the frozen-step pipeline; the C_l^TT
+  part from the tangent of the LOS integral) agree with
   central finite differences of the oracle (tight tolerances, the k grids and
   the Bessel grid of the unperturbed cosmology held fixed as the reference's
   assume_nondual does) within 1e-3.
@@ -165,3 +166,21 @@ def test_plin_gradient_vs_oracle_fd():
                                   for k in ks]))
         fd = (vals[0] - vals[1]) / (2e-4 * abs(th[j]))
         assert np.max(np.abs(r.dplin[j] - fd)) < 1e-3 * np.max(np.abs(fd)), (B.THETA_NAMES[j], r.dplin[j], fd)
+
+
+def test_tangent_los_matches_difference_los():
+    """C_l^TT gradients from the tangent of the LOS integral (TT-only
+    requests) against forward differences of the full LOS (TT + EE
+    requests), both on the same frozen-step source grids."""
+    par = _par(h=0.66, mnu=0.09)
+    ks = _ks(par, nk=50, kmax_h0=400.0)
+    ells = np.array([2, 30, 150, 400, 900], dtype=np.int32)
+    with B.Engine(lanes=1) as eng:
+        a = eng.run(B.Request("cl", par, ks, hier=HIER, ells=ells, cl=("tt",), grad=True))
+        b = eng.run(B.Request("cl", par, ks, hier=HIER, ells=ells, cl=("tt", "ee"), grad=True))
+    assert a.rc == 0 and b.rc == 0, (a.err, b.err)
+    assert _rel(a.cl["tt"], b.cl["tt"]) < 1e-12
+    for j in range(6):
+        scale = np.max(np.abs(b.dcl["tt"][j]))
+        assert np.max(np.abs(a.dcl["tt"][j] - b.dcl["tt"][j])) < 1e-4 * scale, (B.THETA_NAMES[j], a.dcl["tt"][j],
+                                                                                 b.dcl["tt"][j])
