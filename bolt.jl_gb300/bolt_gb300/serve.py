@@ -131,9 +131,11 @@ class Engine:
     """Native batching / serving engine on one GPU (bolt_engine_*)."""
 
     def __init__(self, device: int = 0, lanes: int = 2, host_threads: int = 0, max_batch: int = 0,
-                 mem_budget_gb: float = 150.0, warps_per_mode: int = 0, max_steps: int = 0):
+                 mem_budget_gb: float = 150.0, warps_per_mode: int = 0, max_steps: int = 0,
+                 batch_window_s: float = 0.0):
         self.lib = L.load()
-        cfg = L.BoltEngineCfg(device, lanes, host_threads, max_batch, mem_budget_gb, warps_per_mode, max_steps)
+        cfg = L.BoltEngineCfg(device, lanes, host_threads, max_batch, mem_budget_gb, warps_per_mode, max_steps,
+                              batch_window_s)
         h = C.c_void_p()
         rc = self.lib.bolt_engine_create(C.byref(cfg), C.byref(h))
         if rc != 0:

@@ -114,6 +114,7 @@ constexpr int kRecCap = 12288;      // recorded steps per mode (gradient request
 constexpr double kRelStep = 1e-6;   // forward-difference step, relative to |theta_j|
 constexpr int kNb = 5001;           // Bessel grid points (spectra.jl:52)
 constexpr int kNkd = 5000;          // dense LOS k grid (spectra.jl:133)
+constexpr double kFillModes = 24.0;  // modes per SM that make a launch worth starting while others run
 
 struct EngErr : std::runtime_error {
   int code;
@@ -224,9 +225,12 @@ struct Req {
 struct Tuner {  // seconds per mode-step by batch-size bucket and warps per mode
   double sps[48][3];
   int n[48][3];
+  int picks[48];
   Tuner() {
-    for (int b = 0; b < 48; ++b)
+    for (int b = 0; b < 48; ++b) {
+      picks[b] = 0;
       for (int v = 0; v < 3; ++v) { sps[b][v] = 0.0; n[b][v] = 0; }
+    }
   }
   static int bucket(int nmodes) {
     int b = 0;
@@ -234,25 +238,36 @@ struct Tuner {  // seconds per mode-step by batch-size bucket and warps per mode
     return b;
   }
   static int vidx(int wpm) { return wpm == 1 ? 0 : (wpm == 2 ? 1 : 2); }
-  int pick(int nmodes, int nsm) const {
-    // Candidates, in the order they are explored: only launches that fill
-    // the GPU several times over benefit from the instruction-lean narrow
-    // variants (measured crossover between 8 and 32 modes per SM).
-    int cands[3] = {4, 0, 0}, nc = 1;
-    if (nmodes >= 16 * nsm) {
-      cands[0] = 1; cands[1] = 2; cands[2] = 4; nc = 3;
-    } else if (nmodes > 4 * nsm) {
-      cands[1] = 2; cands[2] = 1; nc = 3;
-    } else if (nmodes > 2 * nsm) {
-      cands[1] = 2; nc = 2;
-    }
+  // Prior relative cost per mode-step of 4 / 2 / 1 warps per mode against the
+  // launch size in modes per SM, interpolated in log size between two
+  // measurements (N = 473: 7.9 modes/SM -> 1.00 / 1.20 / 1.69, 31.6 modes/SM
+  // -> 1.00 / 0.73 / 0.64).
+  static void prior(double r, double* c) {
+    double t = (std::log(std::max(r, 1e-3)) - std::log(7.9)) / (std::log(31.6) - std::log(7.9));
+    t = std::min(1.0, std::max(-1.0, t));
+    c[2] = 1.0;                           // 4 warps
+    c[1] = 1.20 + (0.73 - 1.20) * t;      // 2 warps
+    c[0] = 1.69 + (0.64 - 1.69) * t;      // 1 warp
+  }
+  // The variant with the lowest estimated cost: measured seconds per
+  // mode-step in this size bucket where available, else the prior scaled by
+  // a measured variant; every eighth launch of a bucket tries the
+  // runner-up so the estimates keep up with the workload.
+  int pick(int nmodes, int nsm) {
+    const double r = double(nmodes) / double(nsm);
+    if (r <= 2.0) return 4;  // one wave: the lowest-latency variant
+    double c[3];
+    prior(r, c);
     const int b = bucket(nmodes);
-    for (int i = 0; i < nc; ++i)
-      if (n[b][vidx(cands[i])] == 0) return cands[i];
-    int best = cands[0];
-    for (int i = 1; i < nc; ++i)
-      if (sps[b][vidx(cands[i])] < sps[b][vidx(best)]) best = cands[i];
-    return best;
+    double base = 0.0;
+    for (int v = 0; v < 3; ++v)
+      if (n[b][v] > 0) { base = sps[b][v] / c[v]; break; }
+    double est[3];
+    for (int v = 0; v < 3; ++v) est[v] = n[b][v] > 0 ? sps[b][v] : (base > 0 ? base * c[v] : c[v]);
+    int order[3] = {0, 1, 2};
+    std::sort(order, order + 3, [&](int x, int y) { return est[x] < est[y]; });
+    const int v = (++picks[b] % 8 == 0) ? order[1] : order[0];
+    return v == 0 ? 1 : (v == 1 ? 2 : 4);
   }
   void update(int nmodes, int wpm, double secs, double steps) {
     if (!(steps > 0) || !(secs > 0)) return;
@@ -927,7 +942,21 @@ void scheduler(bolt_engine* E) {
       else any_busy = true;
     }
     if (E->stop && !any_busy) break;
-    // new batches on idle lanes
+    // new batches on idle lanes.  With a batching window, while another lane
+    // keeps the GPU busy a batch waits until its ready requests hold at
+    // least kFillModes modes per SM or the oldest has waited the window:
+    // fewer, larger launches; an idle GPU takes whatever is ready at once.
+    if (!E->stop && !E->ready.empty() && E->cfg.batch_window_s > 0) {
+      bool busy_other = false;
+      for (Lane& L : E->lanes) busy_other |= L.busy;
+      double ready_modes = 0.0;
+      for (Req* r : E->ready) ready_modes += double(r->r.nk) * r->nsets;
+      const double waited = now_s(E->t0) - E->ready.front()->t[1];
+      if (busy_other && ready_modes < kFillModes * E->nsm && waited < E->cfg.batch_window_s) {
+        E->cv_sched.wait_for(lk, std::chrono::microseconds(200));
+        continue;
+      }
+    }
     if (!E->stop) {
       for (Lane& L : E->lanes) {
         if (L.busy || E->ready.empty()) continue;

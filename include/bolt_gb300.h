@@ -227,6 +227,8 @@ typedef struct {
   double mem_budget_gb;  /* device memory admitted to in-flight requests (0 = 150) */
   int warps_per_mode;    /* 0 = autotune per batch size, else 1, 2 or 4 */
   long long max_steps;   /* per mode (0 = 10^5, OrdinaryDiffEq's default maxiters) */
+  double batch_window_s; /* > 0: while another batch runs, hold ready requests up to this long
+                            until they fill the GPU (24 modes per SM); 0 = launch at once */
 } bolt_engine_cfg;
 
 typedef struct bolt_engine bolt_engine;
