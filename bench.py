@@ -24,7 +24,8 @@ completion; ``roofline`` = the Rosenbrock kernel's FP64 rate in the plain leg
 (no overlap between requests) against the FP64 peak measured in this run;
 ``cpu_baseline`` = the CPU oracle (C++ restatement of Bolt's CPU algorithm,
 threaded over k / l) on a bounded sample of every request type, scaled to
-the stream.
+the stream; ``cl_grad`` = a stream of C_l^TT + Jacobian requests only (the
+metric's request type), served vs one per call.
 
 ``--workload pipeline``: the full CMB pipeline for one cosmology (1200 k,
 l <= 2500, N = 473) with device-timed throughput (the profiling case).
@@ -81,12 +82,13 @@ def draw_theta(rng):
                      rng.uniform(0.92, 1.0), math.exp(rng.uniform(2.9, 3.2)) / 1e10, rng.uniform(0.0, 0.3)])
 
 
-def make_stream(n, offset=0):
+def make_stream(n, offset=0, kinds=None):
     """Seeded request descriptions (plain dicts, no library objects)."""
     rng = np.random.default_rng(SEED + offset)
+    kinds = kinds or KINDS
     out = []
     for i in range(n):
-        kind = KINDS[(i + offset) % len(KINDS)]
+        kind = kinds[(i + offset) % len(kinds)]
         th = draw_theta(rng)
         d = {"kind": kind, "theta": th}
         if kind == "plin":
@@ -308,6 +310,28 @@ def run_serving(args):
         s1 = eng.stats()
     for r in res:
         assert r.rc == 0, r.err
+    # ---- the metric's own request type alone: C_l^TT + 6-parameter Jacobian
+    gstream = make_stream(args.grad_requests, offset=500 + rank * 7919, kinds=["grad"])
+    g_plain = []
+    with B.Engine(device=local, lanes=1, max_batch=1) as eng:
+        eng.run(to_request(B, make_stream(1, offset=900, kinds=["grad"])[0]))
+        for d in gstream:
+            t0 = time.perf_counter()
+            r = eng.run(to_request(B, d))
+            g_plain.append(time.perf_counter() - t0)
+            assert r.rc == 0, r.err
+    with B.Engine(device=local, lanes=3) as eng:
+        eng.run(to_request(B, make_stream(1, offset=900, kinds=["grad"])[0]))
+        gres = [eng.wait(t) for t in [eng.submit(to_request(B, d)) for d in gstream]]
+    for r in gres:
+        assert r.rc == 0, r.err
+    g_win = max(r.times[3] for r in gres) - min(r.times[2] for r in gres)
+    g_lat = np.array([r.latency for r in gres])
+    cl_grad = {"served": len(gstream) / g_win, "plain": len(gstream) / sum(g_plain),
+               "served_over_plain": sum(g_plain) / g_win, "unit": UNIT, "requests": len(gstream),
+               "p50_s": float(np.percentile(g_lat, 50)), "p99_s": float(np.percentile(g_lat, 99)),
+               "workload": "C_l^TT l<=2000 + 6-parameter Jacobian, cfg-3 box draws, 64-1024 log k in [0.1,1000] H0, "
+                           "l_gamma=l_nu in {20,35,50}; served: all submitted at once"}
     lat = np.array([r.latency for r in res])
     gpu_window = max_over_ranks(max(r.times[3] for r in res) - min(r.times[2] for r in res), dist)
     e2e_window = max_over_ranks(max(r.times[3] for r in res) - min(r.times[0] for r in res), dist)
@@ -348,6 +372,7 @@ def run_serving(args):
                "plain": {"value": plain, "unit": UNIT, "p50_s": float(np.percentile(plain_lat, 50)),
                          "p99_s": float(np.percentile(plain_lat, 99))},
                "served_over_plain": value / plain,
+               "cl_grad": cl_grad,
                "latency": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                            "arrival_rate_per_s": RATE},
                "clocks": clocks,
@@ -459,6 +484,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="serving", choices=["serving", "pipeline"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grad-requests", type=int, default=6, help="serving: size of the C_l+gradient-only stream")
     ap.add_argument("--nk", type=int, default=1200, help="pipeline: source-grid wavenumbers")
     ap.add_argument("--kmax-h0", type=float, default=5000.0, help="pipeline: largest wavenumber in units of H0")
     ap.add_argument("--lmax", type=int, default=2500, help="pipeline: largest multipole")

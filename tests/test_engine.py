@@ -184,3 +184,44 @@ def test_tangent_los_matches_difference_los():
         scale = np.max(np.abs(b.dcl["tt"][j]))
         assert np.max(np.abs(a.dcl["tt"][j] - b.dcl["tt"][j])) < 1e-4 * scale, (B.THETA_NAMES[j], a.dcl["tt"][j],
                                                                                  b.dcl["tt"][j])
+
+
+def test_request_validation_errors():
+    par = _par()
+    ks = _ks(par, nk=20)
+    with B.Engine(lanes=1) as eng:
+        with pytest.raises(ValueError, match="ascending"):
+            eng.submit(B.Request("plin", par, ks[::-1].copy(), hier=HIER))
+        with pytest.raises(ValueError, match="truncations"):
+            eng.submit(B.Request("plin", par, ks, hier=(2, 20, 10, 15)))
+        with pytest.raises(ValueError, match="multipoles"):
+            eng.submit(B.Request("cl", par, ks, hier=HIER, ells=np.array([1, 5], dtype=np.int32)))
+        with pytest.raises(ValueError, match="plin_x"):
+            eng.submit(B.Request("plin", par, ks, hier=HIER, plin_x=0.5))
+        # the engine still serves after rejected submissions
+        r = eng.run(B.Request("plin", par, ks[:4], hier=HIER))
+        assert r.rc == 0, r.err
+
+
+def test_budget_rejects_oversized_request():
+    par = _par()
+    with B.Engine(lanes=1, mem_budget_gb=1e-4) as eng:  # 100 kB
+        r = eng.run(B.Request("cl", par, _ks(par, nk=64), hier=HIER, ells=np.arange(2, 100, dtype=np.int32)))
+    assert r.rc == -5 and "budget" in r.err
+
+
+def test_failing_request_does_not_affect_others():
+    """A request that exhausts the step cap (tight tolerances) reports its
+    status; a request submitted with it completes normally."""
+    par = _par()
+    ks = _ks(par, nk=16)
+    with B.Engine(lanes=2, max_steps=5000) as eng:
+        bad = eng.submit(B.Request("plin", par, ks, hier=HIER, reltol=1e-13, abstol=1e-15))
+        good = eng.submit(B.Request("plin", par, ks, hier=HIER))
+        rb, rg = eng.wait(bad), eng.wait(good)
+    assert rb.rc == -4 and "status" in rb.err
+    assert np.any((rb.status & 0xFF) == 1)  # max iterations
+    assert rg.rc == 0, rg.err
+    with B.Engine(lanes=1) as eng:
+        ref = eng.run(B.Request("plin", par, ks, hier=HIER))
+    assert _rel(rg.plin, ref.plin) < 1e-12
