@@ -786,24 +786,26 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       PT(7)
     }
     // error estimate: the last stage increment (in b)
-    double en = 0.0;
+    double en = 0.0, fac = 1.0;
     bool fin = true;
-    for (int i = tid; i < N; i += nth) {
-      double yn = S.yt[i] + S.b[i];
-      double sc = atol + rtol * fmax(fabs(G.y[i]), fabs(yn));
-      double e = S.b[i] / sc;
-      en += e * e;
-      fin = fin && isfinite(yn);
-    }
-    en = sqrt(block_sum<WPM>(en, red, tid) / N);
-    fin = __syncthreads_and(fin);
-    if (!fin || !(en == en)) en = 1e10;
-    if (replay) {
+    if (replay) {  // the recorded step is taken as it is: only check the state
+      for (int i = tid; i < N; i += nth) fin = fin && isfinite(S.yt[i] + S.b[i]);
+      fin = __syncthreads_and(fin);
       if (!fin) { status = ST_NONFINITE; break; }
-      en = 0.0;
+    } else {
+      for (int i = tid; i < N; i += nth) {
+        double yn = S.yt[i] + S.b[i];
+        double sc = atol + rtol * fmax(fabs(G.y[i]), fabs(yn));
+        double e = S.b[i] / sc;
+        en += e * e;
+        fin = fin && isfinite(yn);
+      }
+      en = sqrt(block_sum<WPM>(en, red, tid) / N);
+      fin = __syncthreads_and(fin);
+      if (!fin || !(en == en)) en = 1e10;
+      fac = 0.9 * pow(fmax(en, 1e-12), -0.25);
+      fac = fmin(6.0, fmax(0.2, fac));
     }
-    double fac = 0.9 * pow(fmax(en, 1e-12), -0.25);
-    fac = fmin(6.0, fmax(0.2, fac));
     if (en <= 1.0) {
       for (int i = tid; i < N; i += nth) G.y[i] = S.yt[i] + S.b[i];
       if (record && tid == 0) {
