@@ -85,6 +85,19 @@ struct RodasNodeArgs {
   void* ptrs[7];
 };
 
+// Reciprocal: the hardware approximation (rcp.approx.ftz.f64) refined by two
+// Newton-Raphson iterations r <- r + r (1 - x r) (quadratic convergence to
+// about an ulp of 1/x).  For finite, nonzero, normal x; 0 and non-finite x
+// give non-finite results, which the callers test for.
+__device__ __forceinline__ double frcp(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
 // ---------------------------------------------------------------- duals ----
 struct dd {
   double v, d;

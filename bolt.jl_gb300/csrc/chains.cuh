@@ -29,7 +29,7 @@ struct Pack {
   int* chain;    // [threads] chain id of the lane
   int* idx;      // [threads][em] state indices in elimination order, -1 = pad (at the end)
   int* owner;    // [kMaxChains] thread holding the chain's l = 0 element
-  int* E;        // [1] elements per lane; E[1] = thread for the CDM pair + Phi
+  int* E;        // [0] elements per lane, [1] thread for the CDM pair + Phi, [2] lanes of the longest segment
   int em;        // largest elements per lane (kLaneElems / threads)
 };
 
@@ -87,8 +87,11 @@ __device__ bool build_pack(const Mode& m, const Pack& P, int nthreads) {
       }
       P.owner[c] = t0 + (len - 1) / E;
     }
+    int maxseg = 1;  // lanes of the longest segment: the scan levels needed
+    for (int c = 0; c < nc; ++c) maxseg = max(maxseg, (chain_desc(m, c).L + E) / E);
     P.E[0] = E;
     P.E[1] = spare;
+    P.E[2] = maxseg;
     return true;
   }
   return false;
@@ -279,7 +282,7 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
         ec.d += corr;
       }
       double p = ec.lo * ec.upPrev;  // 0 for the chain's first element
-      double id = 1.0 / ec.d;
+      double id = frcp(ec.d);
       double am = -p * id;
       S.fl[i] = am;
       S.fi[i] = id;
@@ -291,7 +294,7 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
   }
   // ---- segmented inclusive scan over lanes: pre = loc * pre(previous)
   M2 inc = loc;
-  for (int off = 1; off < 32; off <<= 1) {
+  for (int off = 1; off < P.E[2]; off <<= 1) {
     M2 o = shfl_up_m2(inc, off);
     if (seg >= 0 && lane - off >= seg) inc = mmul(inc, o);
   }
@@ -305,7 +308,7 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
       if (i < 0) break;
       double am = S.fl[i], bm = S.fi[i], lo = S.yt[i], up = S.b[i];
       double n2 = fma(am, vm, vn), m2 = bm * vn;
-      double fi = m2 / n2;
+      double fi = m2 * frcp(n2);
       S.fi[i] = fi;
       S.fl[i] = lo * fi_prev;
       S.fc[i] = up * fi;
@@ -385,7 +388,7 @@ __device__ void wsolve_scan(const Mode& m, const Shared& S, const Pack& P, doubl
       cnt = e + 1;
     }
   }
-  for (int off = 1; off < 32; off <<= 1) {
+  for (int off = 1; off < P.E[2]; off <<= 1) {
     double oA = __shfl_up_sync(0xffffffffu, A, off), oB = __shfl_up_sync(0xffffffffu, B, off);
     if (seg >= 0 && lane - off >= seg) { B = fma(A, oB, B); A = A * oA; }
   }
@@ -461,7 +464,7 @@ __device__ void wsolve_scan(const Mode& m, const Shared& S, const Pack& P, doubl
     while (l2 < 31 && P.chain[(tid - lane) + l2 + 1] == ch && P.seg[(tid - lane) + l2 + 1] == seg) ++l2;
     segend = l2;
   }
-  for (int off = 1; off < 32; off <<= 1) {
+  for (int off = 1; off < P.E[2]; off <<= 1) {
     double oA = __shfl_down_sync(0xffffffffu, A, off), oB = __shfl_down_sync(0xffffffffu, B, off);
     if (seg >= 0 && lane + off <= segend) { B = fma(A, oB, B); A = A * oA; }
   }

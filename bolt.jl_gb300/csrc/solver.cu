@@ -80,8 +80,8 @@ struct Scratch {
 constexpr int kMiscDoubles = 32 + 9 * 32;  // capacitance, reductions, per-chain partials
 
 // Lane packing of the chains (chains.cuh): seg + chain per thread, the
-// element lists (768 ints for every variant), owners and two counters.
-__host__ __device__ inline int pack_ints(int threads) { return 2 * threads + 768 + 32 + 2; }
+// element lists (768 ints for every variant), owners and three counters.
+__host__ __device__ inline int pack_ints(int threads) { return 2 * threads + 768 + 32 + 4; }
 
 __host__ __device__ inline int per_mode_doubles(int N, int nq, int Lmax, int threads) {
   int nch = nq + 5;
