@@ -73,6 +73,8 @@ EXPORTS = {
     "bolt_cosmo_free": (C.c_int, [C.c_void_p, C.c_int]),
     "bolt_boltsolve": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.POINTER(BoltHier), C.c_double, C.c_double,
                                  _dp, C.c_int, _dp, _i32p]),
+    "bolt_boltsolve_rsa": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.POINTER(BoltHier), C.c_double, C.c_double,
+                                     _dp, _i32p]),
     "bolt_source_grid": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.POINTER(BoltHier), C.c_double,
                                    C.c_double, _dp, _dp, _i32p]),
     "bolt_cl": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int, _ip, C.c_int, _dp, _dp, _dp]),

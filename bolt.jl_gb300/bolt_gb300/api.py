@@ -9,6 +9,7 @@ Bolt.jl):
     IonizationHistory(rf, par, bg)   src/ionization/recfast.jl:674-726
     Hierarchy(integrator, ...)       src/perturbations.jl:7-21
     boltsolve(hierarchy; ...)        src/perturbations.jl:25-33
+    boltsolve_rsa(hierarchy; ...)    src/perturbations.jl:35-111
     source_grid / source_grid_P      src/spectra.jl:6-42
     quadratic_k / log10_k            src/spectra.jl:60-68
     cltt / clte / clee               src/spectra.jl:84-160
@@ -329,6 +330,29 @@ class Perturbation:
         out = np.empty((xs.size, u.shape[2]))
         out[order] = u[0][inv]
         return out[0] if np.ndim(x) == 0 else out
+
+
+def boltsolve_rsa_batch(ih: IonizationHistory, k, lg=8, lnu=8, lmnu=10, nq=15, reltol=1e-6, abstol=1e-6):
+    """boltsolve_rsa (perturbations.jl:90-111) for many k: states on every
+    x-grid node with the radiation-streaming values past the switch,
+    u[ik][ix][N], and the per-mode status."""
+    k = np.ascontiguousarray(np.atleast_1d(k), dtype=np.float64)
+    N = state_len(lg, lnu, lmnu, nq)
+    u = np.zeros((k.size, ih.bg.x_grid.size, N))
+    st = np.zeros(k.size, dtype=np.int32)
+    c = ih.ctx
+    c.check(c.lib.bolt_boltsolve_rsa(c.h, ih.cosmo_id, L.dptr(k), k.size, C.byref(_hier(lg, lnu, lmnu, nq)), reltol,
+                                     abstol, L.dptr(u), L.i32ptr(st)), "bolt_boltsolve_rsa")
+    _check_status(st, "boltsolve_rsa")
+    return u, st
+
+
+def boltsolve_rsa(hierarchy: Hierarchy, ode_alg=None, reltol=1e-6, abstol=1e-6) -> np.ndarray:
+    """boltsolve_rsa(hierarchy; reltol, abstol): the (pertlen, length(x_grid))
+    matrix of states, as the reference returns it."""
+    h = hierarchy
+    u, _ = boltsolve_rsa_batch(h.ih, [h.k], h.lg, h.lnu, h.lmnu, h.nq, reltol, abstol)
+    return u[0].T.copy()
 
 
 def boltsolve(hierarchy: Hierarchy, ode_alg=None, reltol=1e-6, abstol=1e-6) -> Perturbation:

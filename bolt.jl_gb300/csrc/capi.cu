@@ -25,6 +25,8 @@ int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, c
 size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL);
 size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm);
 size_t rodas_scratch_per_warp(int maxN);
+int launch_rsa_post(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const int* d_first, int nout,
+                    cudaStream_t stream);
 struct LosArgs {
   int nb, nslots, nrow, nm;
   const int* ells;
@@ -594,6 +596,56 @@ int bolt_boltsolve(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier
     ck(cudaMemcpyAsync(d_x, x_out, nx * sizeof(double), cudaMemcpyHostToDevice, c->stream), "x_out");
     run_solver(c, id, k, nk, h, reltol, abstol, d_x, nx, MODE_TRAJ, nullptr, nullptr, d_traj, nullptr, status);
     ck(cudaMemcpyAsync(u_out, d_traj, size_t(nk) * nx * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "u_out");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+  });
+}
+
+int bolt_boltsolve_rsa(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h, double reltol, double abstol,
+                       double* u_out, int32_t* status) {
+  return guard(c, [&] {
+    if (!k || !u_out || nk <= 0) throw Err(-1, "null or empty argument");
+    CosmoEntry& e = get_cosmo(c, id);
+    check_hier(h);
+    const CosmoTables& T = e.T;
+    const GridSpec& g = T.grid;
+    const int n = g.n, N = state_len(h);
+    // the switch (perturbations.jl:95-103): first node with k eta > 240,
+    // first node with -tau' H / eta > 100 (evaluated on the node values as the
+    // reference's broadcasts are), the later of the two; later nodes switch
+    int jo = -1;
+    std::vector<double> eta(n);
+    for (int j = 0; j < n; ++j) {
+      const double x = g.at(j);
+      eta[j] = spline_eval(T.coef[T_ETA].data(), n, g.x0, g.h, x);
+      const double od = -spline_eval(T.coef[T_TAUP].data(), n, g.x0, g.h, x) *
+                        spline_eval(T.coef[T_H].data(), n, g.x0, g.h, x) / eta[j];
+      if (jo < 0 && od > 100.0) jo = j;
+    }
+    if (jo < 0) throw Err(-1, "RSA switch undefined: the opacity condition never holds on the x grid");
+    std::vector<int> first(nk);
+    for (int i = 0; i < nk; ++i) {
+      int jh = n - 1;
+      for (int j = 0; j < n; ++j)
+        if (k[i] * eta[j] > 240.0) { jh = j; break; }
+      first[i] = std::max(jh, jo) + 1;
+    }
+    std::vector<double> xs(n);
+    for (int j = 0; j < n; ++j) xs[j] = g.at(j);
+    double* d_x = c->xout.as<double>(n);
+    double* d_traj = c->traj.as<double>(size_t(nk) * n * N);
+    ck(cudaMemcpyAsync(d_x, xs.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "x grid");
+    run_solver(c, id, k, nk, h, reltol, abstol, d_x, n, MODE_TRAJ, nullptr, nullptr, d_traj, nullptr, status);
+    // the solver's mode array is in decreasing-k order (run_solver)
+    std::vector<int> order(nk);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return k[a] > k[b]; });
+    std::vector<int> first_sorted(nk);
+    for (int r = 0; r < nk; ++r) first_sorted[r] = first[order[r]];
+    int* d_first = c->slot_of_l.as<int>(nk);
+    ck(cudaMemcpyAsync(d_first, first_sorted.data(), nk * sizeof(int), cudaMemcpyHostToDevice, c->stream), "switch");
+    int rc = launch_rsa_post(c->modes.as<ModeDev>(nk), nk, c->d_cos.as<CosmoDev>(c->cos.size()), d_first, n, c->stream);
+    if (rc != 0) throw Err(-3, std::string("RSA post-processing: ") + cudaGetErrorString(cudaError_t(rc)));
+    ck(cudaMemcpyAsync(u_out, d_traj, size_t(nk) * n * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "u_out");
     ck(cudaStreamSynchronize(c->stream), "sync");
   });
 }

@@ -832,6 +832,67 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   }
 }
 
+// boltsolve_rsa's post-processing (perturbations.jl:35-111): on the nodes
+// past each mode's RSA switch, the photon and massless-neutrino multipoles of
+// the stored trajectory are replaced by their radiation-streaming values
+// (rsa_perts!, perturbations.jl:35-88): Theta_0, Theta_1, N_0, N_1 from the
+// metric, baryons and opacity; Theta_2 = N_2 = 0; Theta_2..Theta_{lg-1},
+// Theta^P_2..Theta^P_{lg-1}, N_2..N_{l_nu-1} zeroed (the reference's loops
+// leave the top multipoles and Theta^P_0,1 as they are).  One thread per
+// (mode, node); first[mode] is the first node replaced.
+__global__ void rsa_post_kernel(const ModeDev* __restrict__ modes, int nmodes, const CosmoDev* __restrict__ cosmos,
+                                const int* __restrict__ first) {
+  const int r = blockIdx.y;
+  if (r >= nmodes) return;
+  const ModeDev& md = modes[r];
+  const int j = first[r] + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= md.nout) return;
+  const CosmoDev& C = cosmos[md.cosmo];
+  const int lg = md.lg, lnu = md.lnu, lmnu = md.lmnu, nq = md.nq;
+  const int N = 2 * (lg + 1) + (lnu + 1) + (lmnu + 1) * nq + 5;
+  const int iTp = lg + 1, iN = 2 * (lg + 1), iM = iN + lnu + 1, iPhi = iM + (lmnu + 1) * nq;
+  double* u = md.traj + (size_t)j * N;
+  const double x = md.xout[j], k = md.k, a = exp(x);
+  const double Hc = spl_cold(C, C_H, x), tp = spl_cold(C, C_TAUP, x), tpp = spl_cold(C, C_TAUPP, x);
+  const double cs2 = spl_cold(C, C_CSB2, x);
+  // rho_sigma (perturbations.jl:127-143): 4 pi sum w q^2 f0 / (dx/dq) {eps M_0, q^2/eps M_2}
+  double rho = 0.0, sig = 0.0;
+  for (int q = 0; q < nq; ++q) {
+    double lq = C.logqmin + (C.logqmax - C.logqmin) / 2.0 * (C.qx[q] + 1.0);
+    double qq = pow(10.0, lq);
+    double dxdq = (1.0 + (-1.0 + 2.0 / (C.logqmax - C.logqmin) * ((1.0 + C.logqmin) - C.logqmin))) / (qq * log(10.0));
+    double f0 = 2.0 / pow(2.0 * M_PI, 3.0) / (exp(qq / C.Tnu) + 1.0);
+    double Aq = 4.0 * M_PI * qq * qq * f0 / dxdq * C.qw[q];
+    double am = a * C.Sigma_m_nu, eps = sqrt(qq * qq + am * am);
+    rho += Aq * eps * u[iM + q];
+    sig += Aq * qq * qq / eps * u[iM + 2 * nq + q];
+  }
+  const double H0sq = C.H0 * C.H0, Phi = u[iPhi], delta = u[iPhi + 1], delb = u[iPhi + 3], vb = u[iPhi + 4];
+  const double Psi = -Phi - 12.0 * H0sq / (k * k) / (a * a) *
+                                (C.Omega_r * u[2] + C.Omega_nu * u[iN + 2] + sig / C.rho_crit / 4.0);
+  const double Phip = Psi - k * k / (3.0 * Hc * Hc) * Phi +
+                      H0sq / (2.0 * Hc * Hc) *
+                          (C.Omega_c / a * delta + C.Omega_b / a * delb + 4.0 * C.Omega_r / (a * a) * u[0] +
+                           4.0 * C.Omega_nu / (a * a) * u[iN] + rho / (a * a) / C.rho_crit);
+  const double Hk = Hc / k;
+  u[0] = Phi - Hk * tp * vb;
+  u[1] = Hk * (-2.0 * Phip + tp * (Phi - cs2 * delb) + Hk * (tpp - tp) * vb);
+  u[2] = 0.0;
+  u[iN] = Phi;
+  u[iN + 1] = -2.0 * Hk * Phip;
+  u[iN + 2] = 0.0;
+  for (int l = 2; l < lg; ++l) { u[l] = 0.0; u[iTp + l] = 0.0; }
+  for (int l = 2; l < lnu; ++l) u[iN + l] = 0.0;
+}
+
+int launch_rsa_post(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const int* d_first, int nout,
+                    cudaStream_t stream) {
+  if (nmodes <= 0) return 0;
+  dim3 g((nout + 127) / 128, nmodes);
+  rsa_post_kernel<<<g, 128, 0, stream>>>(d_modes, nmodes, d_cosmos, d_first);
+  return cudaGetLastError();
+}
+
 // Persistent CTAs: the first wave takes modes blockIdx.x (modes arrive sorted
 // by decreasing cost, and consecutive blocks land on different SMs, so the
 // longest modes spread one per SM); later modes come from a device queue.

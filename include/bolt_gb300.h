@@ -113,6 +113,15 @@ int bolt_boltsolve(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const b
                    double reltol, double abstol, const double* x_out, int nx, double* u_out,
                    int32_t* status);
 
+/* boltsolve_rsa (src/perturbations.jl:90-111): boltsolve sampled on every
+ * x-grid node, then on the nodes past the radiation-streaming switch (the
+ * later of the first node with k eta > 240 and the first node with
+ * -tau' H / eta > 100) the photon and massless-neutrino multipoles replaced
+ * by rsa_perts! (perturbations.jl:35-88).  u_out[ik][ix][N] on all n_grid
+ * nodes; status[nk]. */
+int bolt_boltsolve_rsa(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const bolt_hier* hier,
+                       double reltol, double abstol, double* u_out, int32_t* status);
+
 /* source_grid + source_grid_P (src/spectra.jl:6-42): S_T[ik][ix] and
  * S_E[ik][ix] on every x-grid node (S_E may be NULL). */
 int bolt_source_grid(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const bolt_hier* hier,

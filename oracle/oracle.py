@@ -86,6 +86,7 @@ def lib():
         L.oracle_cosmo_new_atol.argtypes = [C.POINTER(_Params), C.c_double, C.c_double, C.c_double, C.c_int,
                                             C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                             C.c_double]
+        L.oracle_rsa_perts.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp]
         L.oracle_plin.restype = C.c_double
         L.oracle_plin.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                   C.c_double, C.c_double, _ip]
@@ -226,6 +227,12 @@ class Cosmo:
                                len(ells), kd[0], kd[1], kd[2], -1.0 if bessel_argmax is None else bessel_argmax,
                                _d(tt), _d(te), _d(ee), nthreads)
         return tt, te, ee
+
+    def rsa_perts(self, k, x, u, lg=8, lnu=8, lmnu=10, nq=15):
+        """rsa_perts! (perturbations.jl:35-88) on a copy of the state u at x."""
+        out = np.ascontiguousarray(u, dtype=np.float64).copy()
+        lib().oracle_rsa_perts(self.h, k, lg, lnu, lmnu, nq, x, _d(out))
+        return out
 
     def plin(self, k, nq=15, lg=50, lnu=50, lmnu=20, x=0.0, reltol=1e-5, abstol=1e-6):
         st = C.c_int(0)

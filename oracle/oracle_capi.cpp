@@ -173,6 +173,41 @@ void oracle_initial_conditions(void* h, double k, int lg, int lnu, int lmnu, int
 }
 
 // boltsolve (perturbations.jl:25-33) sampled at ascending xout: u_out[j*N + i]
+// rsa_perts! (perturbations.jl:35-88) applied in place to one state u at x.
+void oracle_rsa_perts(void* h, double k, int lg, int lnu, int lmnu, int nq, double x, double* u) {
+  OCosmo* o = static_cast<OCosmo*>(h);
+  Mode md(&o->C, k, lg, lnu, lmnu, nq);
+  const Params& p = o->C.par;
+  const Background& bg = *o->bg;
+  const Ionization& ih = *o->ih;
+  const double H0sq = bg.H0 * bg.H0;
+  const double Hc = bg.H(x), tp = ih.taup(x), tpp = ih.taupp(x), cs2 = ih.csb2(x);
+  const double a = std::exp(x);
+  const double Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
+  double* Th = u;
+  double* Nn = u + md.iN;
+  const double* M = u + md.iM;
+  double rhoM, sigM;
+  rho_sigma(md, a, M, M + 2 * nq, rhoM, sigM);
+  const double Phi = u[md.iPhi], del = u[md.iPhi + 1], delb = u[md.iPhi + 3], vb = u[md.iPhi + 4];
+  const double Psi = -Phi - 12.0 * H0sq / (k * k) / (a * a) * (p.Omega_r * Th[2] + Omega_nu * Nn[2] + sigM / bg.rho_crit / 4.0);
+  const double Phip = Psi - k * k / (3.0 * Hc * Hc) * Phi +
+                      H0sq / (2.0 * Hc * Hc) *
+                          (p.Omega_c / a * del + p.Omega_b / a * delb + 4.0 * p.Omega_r / (a * a) * Th[0] +
+                           4.0 * Omega_nu / (a * a) * Nn[0] + rhoM / (a * a) / bg.rho_crit);
+  Th[0] = Phi - Hc / k * tp * vb;
+  Th[1] = Hc / k * (-2.0 * Phip + tp * (Phi - cs2 * delb) + Hc / k * (tpp - tp) * vb);
+  Th[2] = 0.0;
+  Nn[0] = Phi;
+  Nn[1] = -2.0 * Hc / k * Phip;
+  Nn[2] = 0.0;
+  for (int l = 3; l <= lg; ++l) {  // Julia u[l], u[(lg+1)+l] for l = 3..lg (1-based)
+    u[l - 1] = 0.0;
+    u[(lg + 1) + l - 1] = 0.0;
+  }
+  for (int l = 3; l <= lnu; ++l) u[2 * (lg + 1) + l - 1] = 0.0;
+}
+
 int oracle_boltsolve(void* h, double k, int lg, int lnu, int lmnu, int nq, double reltol, double abstol,
                      const double* xout, int nx, double* u_out, long* stats) {
   OCosmo* o = static_cast<OCosmo*>(h);

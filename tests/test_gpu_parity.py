@@ -51,6 +51,33 @@ def test_trajectories(fid, lg, lnu, lmnu):
         assert err < 1e-6, (k, err)
 
 
+def test_boltsolve_rsa(fid):
+    """boltsolve_rsa (perturbations.jl:90-111): states on every x-grid node,
+    radiation-streaming values past the switch, against the oracle's solve
+    and its restatement of rsa_perts!."""
+    par, bg, ih, orc = fid
+    ks = np.array([0.05, 0.2])
+    u, st = B.boltsolve_rsa_batch(ih, ks, 8, 8, 10, 15, reltol=1e-10, abstol=1e-10)
+    assert np.all((st & 0xFF) == 0)
+    x = orc.x
+    eta, taup, H = orc.table("eta"), orc.table("taup"), orc.table("H")
+    od = -taup * H / eta
+    jo = int(np.argmax(od > 100))
+    assert od[jo] > 100
+    for j, k in enumerate(ks):
+        uo, _ = orc.boltsolve(k, x, 8, 8, 10, 15, reltol=1e-10, abstol=1e-10)
+        above = k * eta > 240
+        jh = int(np.argmax(above)) if above.any() else x.size - 1
+        jsw = max(jh, jo)
+        assert jsw < x.size - 1  # the switch happens inside the grid at these k
+        for i in range(jsw + 1, x.size):
+            uo[i] = orc.rsa_perts(k, x[i], uo[i], 8, 8, 10, 15)
+        peak = np.maximum(np.max(np.abs(uo), axis=0), 1e-12)
+        err = np.max(np.abs(u[j] - uo) / peak)
+        assert err < 1e-6, (k, err)
+        assert np.all(u[j][jsw + 1:, 3:8] == 0.0)  # Theta_3..Theta_7 zeroed past the switch
+
+
 def test_source_grid(fid):
     par, bg, ih, orc = fid
     kg = B.quadratic_k(0.1 * bg.H0, 1000 * bg.H0, 12)
