@@ -1,5 +1,5 @@
 #!/usr/bin/env python
-"""Benchmark: served vs one-request-per-call spectra/s with gradients, p50/p99.
+"""Benchmark: served vs plain drop-in spectra/s with gradients, p50/p99.
 
 Default workload (serving): a seeded Poisson stream (10 requests/s) of
 requests over one GB300.  Each request is one cosmology drawn uniformly from
@@ -16,16 +16,19 @@ FP64 throughout, reltol 1e-8 / abstol 3e-7.  One step = one request.
 
 Reported: ``value`` = served spectra/s over the GPU window of the timed
 stream (first batch launched to last request completed), requests in flight
-batched by the engine (continuous batching, 3 lanes); ``e2e`` = the same
+batched by the engine (continuous batching, 6 lanes); ``e2e`` = the same
 stream end to end (first submission to last completion: host table builds,
-uploads, solves, projections, downloads); ``plain`` = the same requests one
-per call (nothing else in flight); ``latency`` = p50 / p99 of submission to
+uploads, solves, projections, downloads); ``plain`` = the same requests
+through the plain drop-in C-ABI, one cosmology per call with nothing else in
+flight (the drop-in has no Jacobian: a gradient request is 1 + 6 calls whose
+forward differences give it); ``latency`` = p50 / p99 of submission to
 completion; ``roofline`` = the Rosenbrock kernel's FP64 rate in the plain leg
-(no overlap between requests) against the FP64 peak measured in this run;
+(no overlap between calls) against the FP64 peak measured in this run;
 ``cpu_baseline`` = the CPU oracle (C++ restatement of Bolt's CPU algorithm,
 threaded over k / l) on a bounded sample of every request type, scaled to
 the stream; ``cl_grad`` = a stream of C_l^TT + Jacobian requests only (the
-metric's request type), served vs one per call.
+metric's request type), served vs the drop-in and vs the engine one request
+per call.
 
 ``--workload pipeline``: the full CMB pipeline for one cosmology (1200 k,
 l <= 2500, N = 473) with device-timed throughput (the profiling case).
@@ -127,6 +130,62 @@ def io_bytes(d):
     nl = d["lmax"] - 1
     h2d = tab + nk * 8 + 4999 * 8 * (1 + nsets) + 2001 * 8 * (1 + nsets) + nl * 8 + nsets * nk * 120
     return h2d, nsets * nk * 20 + nsets * 3 * nl * 8
+
+
+FD_REL_STEP = 1e-4  # forward-difference step of the drop-in gradient, relative to |theta_j|
+
+
+def dropin_request(B, ctx, d):
+    """One request through the plain drop-in C-ABI, one cosmology per call
+    (the calls Bolt's Julia API makes through ccall): bolt_cosmo_build (host
+    background + RECFAST tables, uploaded), bolt_plin or bolt_cl_pipeline,
+    bolt_cosmo_free.  The drop-in has no Jacobian, so a gradient request is
+    1 + 6 calls whose forward differences give dC_l^TT/dtheta (central
+    differences would take 13).  Returns (result, calls, solver seconds,
+    algorithmic solver FLOPs) with the solver figures from bolt_last_stats."""
+    import ctypes as C
+    L = B._lib
+    lib = ctx.lib
+    th0 = np.asarray(d["theta"], dtype=np.float64)
+    sets = [th0]
+    if d["kind"] == "grad":
+        sets += [th0 + np.eye(6)[j] * FD_REL_STEP * abs(th0[j]) for j in range(6)]
+    lg, lnu, lmnu, nq = d["hier"]
+    hier = L.BoltHier(lg, lnu, lmnu, nq)
+    fpstep = solver_flops_per_step(state_len(*d["hier"]), nq)
+    solver_s, flops, outs = 0.0, 0.0, []
+    for th in sets:
+        par = B.params_of(B.CosmoParams(), th)
+        H0 = par.h * B.km_s_Mpc_100()
+        rf = L.BoltRecfast(par.Y_p, par.Omega_b, par.Omega_r, -1.0, 1e-8)
+        cid = C.c_int(-1)
+        ctx.check(lib.bolt_cosmo_build(ctx.h, C.byref(par.c()), C.byref(L.BoltGrid(-20.0, 0.01, 0.0)), nq,
+                                       C.byref(rf), C.byref(cid)), "bolt_cosmo_build")
+        if d["kind"] == "plin":
+            ks = B.log10_k(1e-4 * par.h, 1.0 * par.h, d["nk"])
+            out = np.zeros(ks.size)
+            st = np.zeros(ks.size, dtype=np.int32)
+            ctx.check(lib.bolt_plin(ctx.h, cid.value, L.dptr(ks), ks.size, C.byref(hier), 0.0, RELTOL, ABSTOL,
+                                    L.dptr(out), L.i32ptr(st)), "bolt_plin")
+        else:
+            ks = B.log10_k(0.1 * H0, 1000.0 * H0, d["nk"])
+            ells = np.arange(2, d["lmax"] + 1, dtype=np.int32)
+            out = np.zeros((3, ells.size))
+            te, ee = (out[1], out[2]) if d["kind"] == "cl" else (None, None)
+            st = np.zeros(ks.size, dtype=np.int32)
+            ctx.check(lib.bolt_cl_pipeline(ctx.h, cid.value, L.dptr(ks), ks.size, C.byref(hier), RELTOL, ABSTOL,
+                                           L.iptr(ells), ells.size, L.dptr(out[0]), L.dptr(te), L.dptr(ee),
+                                           L.i32ptr(st)), "bolt_cl_pipeline")
+        assert not np.any((st & 0xFF) != 0), "drop-in solver status"
+        s = ctx.stats()
+        solver_s += s["solver_us"] / 1e6
+        flops += (s["accepted_steps"] + s["rejected_steps"]) * fpstep
+        lib.bolt_cosmo_free(ctx.h, cid.value)
+        outs.append(out)
+    if d["kind"] == "grad":
+        jac = np.array([(outs[1 + j][0] - outs[0][0]) / (FD_REL_STEP * abs(th0[j])) for j in range(6)])
+        return (outs[0][0], jac), len(sets), solver_s, flops
+    return outs[0], len(sets), solver_s, flops
 
 
 # ----------------------------------------------------------------- clocks --
@@ -260,30 +319,27 @@ def run_serving(args):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     lib = B._lib.load()
 
-    # ---- plain: one request per call, nothing else in flight
-    plain_lat, plain_solver_s, plain_flops = [], 0.0, 0.0
-    with B.Engine(device=local, lanes=1, max_batch=1) as eng:
-        for d in warm:
-            r = eng.run(to_request(B, d))
-            assert r.rc == 0, r.err
-        barrier(dist)
-        sampler = clocks_sampler()
-        for d in stream:
-            flush.zero_()
-            torch.cuda.synchronize()
-            s0 = eng.stats()
-            t0 = time.perf_counter()
-            r = eng.run(to_request(B, d))
-            plain_lat.append(time.perf_counter() - t0)
-            assert r.rc == 0, r.err
-            s1 = eng.stats()
-            plain_solver_s += (s1["solver_us"] - s0["solver_us"]) / 1e6
-            plain_flops += r.steps * solver_flops_per_step(state_len(*d["hier"]), d["hier"][3])
+    # ---- plain: the drop-in C-ABI, one cosmology per call, nothing else in flight
+    plain_lat, plain_solver_s, plain_flops, plain_calls = [], 0.0, 0.0, 0
+    ctx = B.Context(device=local)
+    for d in warm:
+        dropin_request(B, ctx, d)
+    barrier(dist)
+    sampler = clocks_sampler()
+    for d in stream:
+        flush.zero_()
         torch.cuda.synchronize()
-        plain_wall = max_over_ranks(sum(plain_lat), dist)
+        t0 = time.perf_counter()
+        _, calls, ssec, fl = dropin_request(B, ctx, d)
+        plain_lat.append(time.perf_counter() - t0)
+        plain_solver_s += ssec
+        plain_flops += fl
+        plain_calls += calls
+    torch.cuda.synchronize()
+    plain_wall = max_over_ranks(sum(plain_lat), dist)
 
     # ---- served: Poisson arrivals, continuous batching
-    with B.Engine(device=local, lanes=3) as eng:
+    with B.Engine(device=local, lanes=6, objective="throughput") as eng:
         ts = [eng.submit(to_request(B, d)) for d in warm]
         for t in ts:
             assert eng.wait(t).rc == 0
@@ -312,26 +368,38 @@ def run_serving(args):
         assert r.rc == 0, r.err
     # ---- the metric's own request type alone: C_l^TT + 6-parameter Jacobian
     gstream = make_stream(args.grad_requests, offset=500 + rank * 7919, kinds=["grad"])
+    gwarm = make_stream(1, offset=900, kinds=["grad"])[0]
+    g_dropin = []
+    dropin_request(B, ctx, gwarm)
+    for d in gstream:
+        t0 = time.perf_counter()
+        dropin_request(B, ctx, d)
+        g_dropin.append(time.perf_counter() - t0)
+    ctx.close()
     g_plain = []
     with B.Engine(device=local, lanes=1, max_batch=1) as eng:
-        eng.run(to_request(B, make_stream(1, offset=900, kinds=["grad"])[0]))
+        eng.run(to_request(B, gwarm))
         for d in gstream:
             t0 = time.perf_counter()
             r = eng.run(to_request(B, d))
             g_plain.append(time.perf_counter() - t0)
             assert r.rc == 0, r.err
-    with B.Engine(device=local, lanes=3) as eng:
-        eng.run(to_request(B, make_stream(1, offset=900, kinds=["grad"])[0]))
+    with B.Engine(device=local, lanes=6, objective="throughput") as eng:
+        eng.run(to_request(B, gwarm))
         gres = [eng.wait(t) for t in [eng.submit(to_request(B, d)) for d in gstream]]
     for r in gres:
         assert r.rc == 0, r.err
     g_win = max(r.times[3] for r in gres) - min(r.times[2] for r in gres)
     g_lat = np.array([r.latency for r in gres])
-    cl_grad = {"served": len(gstream) / g_win, "plain": len(gstream) / sum(g_plain),
-               "served_over_plain": sum(g_plain) / g_win, "unit": UNIT, "requests": len(gstream),
+    cl_grad = {"served": len(gstream) / g_win, "plain": len(gstream) / sum(g_dropin),
+               "served_over_plain": sum(g_dropin) / g_win,
+               "plain_engine": len(gstream) / sum(g_plain), "served_over_plain_engine": sum(g_plain) / g_win,
+               "unit": UNIT, "requests": len(gstream),
                "p50_s": float(np.percentile(g_lat, 50)), "p99_s": float(np.percentile(g_lat, 99)),
                "workload": "C_l^TT l<=2000 + 6-parameter Jacobian, cfg-3 box draws, 64-1024 log k in [0.1,1000] H0, "
-                           "l_gamma=l_nu in {20,35,50}; served: all submitted at once"}
+                           "l_gamma=l_nu in {20,35,50}; served: all submitted at once; plain: drop-in, 7 calls "
+                           "per request (forward differences); plain_engine: the engine one request per call "
+                           "(7 parameter sets batched in one launch, tangent LOS)"}
     lat = np.array([r.latency for r in res])
     gpu_window = max_over_ranks(max(r.times[3] for r in res) - min(r.times[2] for r in res), dist)
     e2e_window = max_over_ranks(max(r.times[3] for r in res) - min(r.times[0] for r in res), dist)
@@ -346,7 +414,8 @@ def run_serving(args):
             "frac": ach / peak if (peak and ach) else None, "traffic": None, "kernel": "rodas_kernel",
             "peak_source": "measured in this run: FP64 FMA loop (bolt_fp64_peak); MEASURED_PEAKS.json has no "
                            "FP64 figure",
-            "note": "plain leg (requests one at a time): algorithmic FLOPs of the accepted + rejected steps of every "
+            "note": "plain leg (drop-in calls one at a time, 4 warps per mode): algorithmic FLOPs of the accepted + "
+                    "rejected steps of every "
                     "mode (159 N + 560 (nq+5) + 66 nq + 650 per step) / CUDA-event time of the solver launches; "
                     "DRAM traffic is negligible (per-CTA state slab L2-resident), see profiles/"}
     cpu = None
@@ -366,11 +435,13 @@ def run_serving(args):
                                       "l_gamma=l_nu in {20,35,50}, l_mnu 10, nq 15); one step = one request",
                           "requests": counts, "reltol": RELTOL, "abstol": ABSTOL, "accuracy": ACCURACY,
                           "timing": "value: served stream over the GPU window (first batch launch to last "
-                                    "completion, 3 lanes); plain: one request per call, sum of call times",
+                                    "completion, 6 lanes, autotuner objective throughput); plain: the drop-in C-ABI one cosmology per call (a "
+                                    "gradient request = 7 calls, forward differences), sum of call times",
                           "l2": "plain: flushed (256 MB write) before every request; served: continuous stream",
                           "parallelism": f"replicas x{ws}"},
                "plain": {"value": plain, "unit": UNIT, "p50_s": float(np.percentile(plain_lat, 50)),
-                         "p99_s": float(np.percentile(plain_lat, 99))},
+                         "p99_s": float(np.percentile(plain_lat, 99)), "calls": plain_calls,
+                         "api": "bolt_cosmo_build + bolt_plin / bolt_cl_pipeline + bolt_cosmo_free per cosmology"},
                "served_over_plain": value / plain,
                "cl_grad": cl_grad,
                "latency": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),

@@ -467,12 +467,14 @@ def clee(ells, par, bg, ih, sf_P):
     return r if np.ndim(ells) else r[0]
 
 
-def cl_all(ells, ih, k_grid, lg=8, lnu=8, lmnu=10, nq=None, reltol=1e-11, abstol=1e-6):
-    """Fused source grid + C_l^TT/TE/EE; the source grids never leave HBM."""
+def cl_all(ells, ih, k_grid, lg=8, lnu=8, lmnu=10, nq=None, reltol=1e-11, abstol=1e-6, spectra=("tt", "te", "ee")):
+    """Fused source grid + C_l^TT/TE/EE; the source grids never leave HBM.
+    Spectra not named in ``spectra`` come back as None (TT alone skips the
+    polarization source)."""
     ells_a = np.ascontiguousarray(np.atleast_1d(ells), dtype=np.int32)
     kg = np.ascontiguousarray(k_grid, dtype=np.float64)
     nq = ih.bg.nq if nq is None else nq
-    tt, te, ee = (np.zeros(ells_a.size) for _ in range(3))
+    tt, te, ee = (np.zeros(ells_a.size) if w in spectra else None for w in ("tt", "te", "ee"))
     st = np.zeros(kg.size, dtype=np.int32)
     c = ih.ctx
     c.check(c.lib.bolt_cl_pipeline(c.h, ih.cosmo_id, L.dptr(kg), kg.size, C.byref(_hier(lg, lnu, lmnu, nq)), reltol,

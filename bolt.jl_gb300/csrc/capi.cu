@@ -650,15 +650,17 @@ int bolt_boltsolve_rsa(bolt_ctx* c, int id, const double* k, int nk, const bolt_
   });
 }
 
+// The polarization source is emitted only when want_E is set (*d_SE is null
+// otherwise): TT-only calls skip its stores and the E half of the projection.
 static void source_grid_device(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h, double reltol,
-                               double abstol, double** d_ST, double** d_SE, int32_t* status) {
+                               double abstol, bool want_E, double** d_ST, double** d_SE, int32_t* status) {
   CosmoEntry& e = get_cosmo(c, id);
   const GridSpec& g = e.T.grid;
   std::vector<double> xs(g.n);
   for (int j = 0; j < g.n; ++j) xs[j] = g.at(j);
   double* d_x = c->xout.as<double>(g.n);
   *d_ST = c->srcT.as<double>(size_t(nk) * g.n);
-  *d_SE = c->srcE.as<double>(size_t(nk) * g.n);
+  *d_SE = want_E ? c->srcE.as<double>(size_t(nk) * g.n) : nullptr;
   ck(cudaMemcpyAsync(d_x, xs.data(), g.n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "x grid");
   run_solver(c, id, k, nk, h, reltol, abstol, d_x, g.n, MODE_SOURCES, *d_ST, *d_SE, nullptr, nullptr, status);
 }
@@ -668,7 +670,7 @@ int bolt_source_grid(bolt_ctx* c, int id, const double* k, int nk, const bolt_hi
   return guard(c, [&] {
     if (!k || !S_T) throw Err(-1, "null argument");
     double *d_ST, *d_SE;
-    source_grid_device(c, id, k, nk, h, reltol, abstol, &d_ST, &d_SE, status);
+    source_grid_device(c, id, k, nk, h, reltol, abstol, S_E != nullptr, &d_ST, &d_SE, status);
     const int n = get_cosmo(c, id).T.grid.n;
     ck(cudaMemcpyAsync(S_T, d_ST, size_t(nk) * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "S_T");
     if (S_E) ck(cudaMemcpyAsync(S_E, d_SE, size_t(nk) * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "S_E");
@@ -694,8 +696,8 @@ int bolt_cl_pipeline(bolt_ctx* c, int id, const double* k, int nk, const bolt_hi
   return guard(c, [&] {
     if (!k || !ells) throw Err(-1, "null argument");
     double *d_ST, *d_SE;
-    source_grid_device(c, id, k, nk, h, reltol, abstol, &d_ST, &d_SE, status);
-    run_los(c, id, d_ST, (te || ee) ? d_SE : d_SE, k, nk, ells, nell, tt, te, ee);
+    source_grid_device(c, id, k, nk, h, reltol, abstol, te || ee, &d_ST, &d_SE, status);
+    run_los(c, id, d_ST, d_SE, k, nk, ells, nell, tt, te, ee);
   });
 }
 

@@ -222,15 +222,23 @@ struct Req {
   bool los_tangent = false;  // C_l^TT gradient from the tangent of the LOS integral
 };
 
-struct Tuner {  // seconds per mode-step by batch-size bucket and warps per mode
-  double sps[48][3];
-  int n[48][3];
-  int picks[48];
+// Seconds per mode-step by warps per mode, in two tables.  An isolated
+// launch (the GPU otherwise idle, nothing waiting) is keyed by its own size:
+// a small one is bound by its longest mode's chain of dependent steps, where
+// more warps per mode win.  A shared launch (other lanes' modes in flight or
+// requests waiting) is keyed by the whole load -- its modes, the other lanes'
+// and the waiting ones -- because the GPU stays full and the FP64 issue
+// rate, where one warp per mode wins, sets the pace.
+struct Tuner {
+  double sps[2][48][3];
+  int n[2][48][3];
+  int picks[2][48];
   Tuner() {
-    for (int b = 0; b < 48; ++b) {
-      picks[b] = 0;
-      for (int v = 0; v < 3; ++v) { sps[b][v] = 0.0; n[b][v] = 0; }
-    }
+    for (int t = 0; t < 2; ++t)
+      for (int b = 0; b < 48; ++b) {
+        picks[t][b] = 0;
+        for (int v = 0; v < 3; ++v) { sps[t][b][v] = 0.0; n[t][b][v] = 0; }
+      }
   }
   static int bucket(int nmodes) {
     int b = 0;
@@ -238,43 +246,45 @@ struct Tuner {  // seconds per mode-step by batch-size bucket and warps per mode
     return b;
   }
   static int vidx(int wpm) { return wpm == 1 ? 0 : (wpm == 2 ? 1 : 2); }
-  // Prior relative cost per mode-step of 4 / 2 / 1 warps per mode against the
-  // launch size in modes per SM, interpolated in log size between two
-  // measurements (N = 473: 7.9 modes/SM -> 1.00 / 1.20 / 1.69, 31.6 modes/SM
-  // -> 1.00 / 0.73 / 0.64).
-  static void prior(double r, double* c) {
-    double t = (std::log(std::max(r, 1e-3)) - std::log(7.9)) / (std::log(31.6) - std::log(7.9));
+  // Prior relative cost per mode-step of 4 / 2 / 1 warps per mode.  Isolated:
+  // against the launch size in modes per SM, interpolated in log size
+  // between two measurements (N = 473: 7.9 modes/SM -> 1.00 / 1.20 / 1.69,
+  // 31.6 modes/SM -> 1.00 / 0.73 / 0.64).  Shared: the saturated ratios
+  // (the 31.6 modes/SM figures).
+  static void prior(bool shared, double r, double* c) {
+    double t = shared ? 1.0 : (std::log(std::max(r, 1e-3)) - std::log(7.9)) / (std::log(31.6) - std::log(7.9));
     t = std::min(1.0, std::max(-1.0, t));
     c[2] = 1.0;                           // 4 warps
     c[1] = 1.20 + (0.73 - 1.20) * t;      // 2 warps
     c[0] = 1.69 + (0.64 - 1.69) * t;      // 1 warp
   }
   // The variant with the lowest estimated cost: measured seconds per
-  // mode-step in this size bucket where available, else the prior scaled by
-  // a measured variant; every eighth launch of a bucket tries the
-  // runner-up so the estimates keep up with the workload.
-  int pick(int nmodes, int nsm) {
-    const double r = double(nmodes) / double(nsm);
+  // mode-step in this bucket where available, else the prior scaled by a
+  // measured variant; every eighth launch of a bucket tries the runner-up so
+  // the estimates keep up with the workload.  key = own modes (isolated) or
+  // the whole load (shared).
+  int pick(bool shared, int key, int nsm) {
+    const double r = double(key) / double(nsm);
     if (r <= 2.0) return 4;  // one wave: the lowest-latency variant
     double c[3];
-    prior(r, c);
-    const int b = bucket(nmodes);
+    prior(shared, r, c);
+    const int t = shared ? 1 : 0, b = bucket(key);
     double base = 0.0;
     for (int v = 0; v < 3; ++v)
-      if (n[b][v] > 0) { base = sps[b][v] / c[v]; break; }
+      if (n[t][b][v] > 0) { base = sps[t][b][v] / c[v]; break; }
     double est[3];
-    for (int v = 0; v < 3; ++v) est[v] = n[b][v] > 0 ? sps[b][v] : (base > 0 ? base * c[v] : c[v]);
+    for (int v = 0; v < 3; ++v) est[v] = n[t][b][v] > 0 ? sps[t][b][v] : (base > 0 ? base * c[v] : c[v]);
     int order[3] = {0, 1, 2};
     std::sort(order, order + 3, [&](int x, int y) { return est[x] < est[y]; });
-    const int v = (++picks[b] % 8 == 0) ? order[1] : order[0];
+    const int v = (++picks[t][b] % 8 == 0) ? order[1] : order[0];
     return v == 0 ? 1 : (v == 1 ? 2 : 4);
   }
-  void update(int nmodes, int wpm, double secs, double steps) {
+  void update(bool shared, int key, int wpm, double secs, double steps) {
     if (!(steps > 0) || !(secs > 0)) return;
-    const int b = bucket(nmodes), v = vidx(wpm);
+    const int t = shared ? 1 : 0, b = bucket(key), v = vidx(wpm);
     double x = secs / steps;
-    sps[b][v] = n[b][v] == 0 ? x : 0.7 * sps[b][v] + 0.3 * x;
-    ++n[b][v];
+    sps[t][b][v] = n[t][b][v] == 0 ? x : 0.7 * sps[t][b][v] + 0.3 * x;
+    ++n[t][b][v];
   }
 };
 
@@ -297,6 +307,9 @@ struct Lane {
   size_t block_bytes = 0;
   int wpm[2] = {4, 4};
   int nmodes[2] = {0, 0};
+  int waiting = 0;       // modes of the requests still waiting when the batch was taken
+  int key[2] = {0, 0};   // tuner key of each phase (own modes, or the whole load when shared)
+  bool shared[2] = {false, false};
   int nlaunch = 0;
   std::vector<int> los_flags_dummy;
 };
@@ -526,11 +539,16 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   int wpm[2] = {4, 4}, blocks[2] = {0, 0};
   const int nph = m2 > 0 ? 2 : 1;
   const int nmodes[2] = {m1, m2};
+  int other = 0;  // lanes are launched and finished on this (the scheduler) thread
+  for (Lane& o : E->lanes)
+    if (&o != &L && o.busy) other += o.nmodes[0] + o.nmodes[1];
   for (int ph = 0; ph < nph; ++ph) {
+    L.shared[ph] = other > 0 || L.waiting > 0 || E->cfg.objective == 1;
+    L.key[ph] = L.shared[ph] ? nmodes[ph] + other + L.waiting : nmodes[ph];
     int w = E->cfg.warps_per_mode;
     if (w != 1 && w != 2 && w != 4) {
       std::lock_guard<std::mutex> g(E->mu);
-      w = E->tuner.pick(nmodes[ph], E->nsm);
+      w = E->tuner.pick(L.shared[ph], L.key[ph], E->nsm);
     }
     int rc = rodas_grid_warps(nmodes[ph], maxN, maxnq, maxL, w, &blocks[ph]);
     if (rc != 0) throw EngErr(-3, std::string("solver configuration: ") + cudaGetErrorString(cudaError_t(-rc)));
@@ -892,8 +910,8 @@ void finish_lane(bolt_engine* E, Lane& L) {
       }
     modes += int64_t(r->nsets) * r->r.nk;
   }
-  E->tuner.update(L.nmodes[0], L.wpm[0], ms1 * 1e-3, steps[0]);
-  if (L.nmodes[1] > 0) E->tuner.update(L.nmodes[1], L.wpm[1], ms2 * 1e-3, steps[1]);
+  E->tuner.update(L.shared[0], L.key[0], L.wpm[0], ms1 * 1e-3, steps[0]);
+  if (L.nmodes[1] > 0) E->tuner.update(L.shared[1], L.key[1], L.wpm[1], ms2 * 1e-3, steps[1]);
   const double t = now_s(E->t0);
   for (Req* r : L.batch) {
     finalize_request(E, L, r);
@@ -989,6 +1007,11 @@ void scheduler(bolt_engine* E) {
         for (Req* r : batch) { r->state = 2; r->t[2] = t; }
         L.busy = true;
         L.batch = batch;
+        L.waiting = 0;
+        for (auto& kv : E->reqs) {
+          const Req* q = kv.second.get();
+          if (q->state <= 1) L.waiting += q->r.nk * q->nsets;
+        }
         lk.unlock();
         std::string msg;
         try {
@@ -1053,6 +1076,7 @@ int bolt_engine_create(const bolt_engine_cfg* cfg, bolt_engine** out) {
   *out = nullptr;
   std::unique_ptr<bolt_engine> E(new bolt_engine());
   if (cfg) E->cfg = *cfg;
+  if (E->cfg.objective != 0 && E->cfg.objective != 1) return -1;
   E->device = E->cfg.device;
   if (E->cfg.lanes <= 0) E->cfg.lanes = 2;
   if (E->cfg.lanes > 8) E->cfg.lanes = 8;

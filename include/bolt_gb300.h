@@ -134,7 +134,9 @@ int bolt_source_grid(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const
 int bolt_cl(bolt_ctx* ctx, int cosmo_id, const double* S_T, const double* S_E, const double* k, int nk,
             const int* ells, int nell, double* tt, double* te, double* ee);
 
-/* Fused source_grid + cltt/clte/clee: the source grids stay in HBM. */
+/* Fused source_grid + cltt/clte/clee: the source grids stay in HBM.  Any of
+ * tt / te / ee may be NULL; with te and ee both NULL the polarization source
+ * is neither computed nor projected. */
 int bolt_cl_pipeline(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const bolt_hier* hier,
                      double reltol, double abstol, const int* ells, int nell, double* tt, double* te,
                      double* ee, int32_t* status);
@@ -234,10 +236,13 @@ typedef struct {
   int host_threads;      /* table-building threads (0 = hardware threads) */
   int max_batch;         /* requests per batch (0 = unlimited; 1 = one request per batch) */
   double mem_budget_gb;  /* device memory admitted to in-flight requests (0 = 150) */
-  int warps_per_mode;    /* 0 = autotune per batch size, else 1, 2 or 4 */
+  int warps_per_mode;    /* 0 = autotuned per launch (see objective), else 1, 2 or 4 */
   long long max_steps;   /* per mode (0 = 10^5, OrdinaryDiffEq's default maxiters) */
   double batch_window_s; /* > 0: while another batch runs, hold ready requests up to this long
                             until they fill the GPU (24 modes per SM); 0 = launch at once */
+  int objective;         /* autotuner: 0 = latency-aware (a launch onto an idle GPU with nothing
+                            waiting gets the variant fastest for that launch alone), 1 = throughput
+                            (every launch is costed as part of a full GPU) */
 } bolt_engine_cfg;
 
 typedef struct bolt_engine bolt_engine;
@@ -246,7 +251,7 @@ typedef struct bolt_engine bolt_engine;
  * the requests whose tables are ready (admitted while the in-flight device
  * footprint stays within the budget), runs every k-mode of a batch in one
  * persistent solver launch (a CUDA graph whose kernel node is updated per
- * batch; warps per mode autotuned by batch size), then the line-of-sight
+ * batch; warps per mode autotuned by the load), then the line-of-sight
  * projections, on one of `lanes` streams, so a batch starts while earlier
  * ones are still on the GPU. */
 int bolt_engine_create(const bolt_engine_cfg* cfg, bolt_engine** out);

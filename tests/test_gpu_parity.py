@@ -127,3 +127,16 @@ def test_cl_pipeline_vs_camb(fid):
     fac = ells * (ells + 1) / (2 * np.pi)
     assert np.all(np.abs(fac * tt / np.interp(ells, g["ell"], g["tt"]) - 1) < 1.1e-1)
     assert np.all(np.abs(fac * ee / np.interp(ells, g["ell"], g["ee"]) - 1) < 1.1e-1)
+
+
+def test_cl_pipeline_tt_only(fid):
+    """A TT-only pipeline call (no polarization source, no E projection)
+    gives the TT of the full call (same steps, same T reduction order)."""
+    par, bg, ih, orc = fid
+    kg = B.log10_k(0.1 * bg.H0, 1000 * bg.H0, 48)
+    ells = np.arange(2, 1201, 13)
+    tt, te, ee, st = B.cl_all(ells, ih, kg, 10, 10, 10, reltol=1e-8, abstol=3e-7)
+    tt1, te1, ee1, st1 = B.cl_all(ells, ih, kg, 10, 10, 10, reltol=1e-8, abstol=3e-7, spectra=("tt",))
+    assert te1 is None and ee1 is None
+    assert np.all((st1 & 0xFF) == 0)
+    assert _rel(tt1, tt) < 1e-13
