@@ -16,14 +16,16 @@ FP64 throughout, reltol 1e-8 / abstol 3e-7.  One step = one request.
 
 Reported: ``value`` = served spectra/s over the GPU window of the timed
 stream (first batch launched to last request completed), requests in flight
-batched by the engine (continuous batching, 6 lanes); ``e2e`` = the same
+batched by the engine (continuous batching, 6 lanes, autotuner objective
+throughput); ``e2e`` = the same
 stream end to end (first submission to last completion: host table builds,
 uploads, solves, projections, downloads); ``plain`` = the same requests
 through the plain drop-in C-ABI, one cosmology per call with nothing else in
 flight (the drop-in has no Jacobian: a gradient request is 1 + 6 calls whose
 forward differences give it); ``latency`` = p50 / p99 of submission to
-completion; ``roofline`` = the Rosenbrock kernel's FP64 rate in the plain leg
-(no overlap between calls) against the FP64 peak measured in this run;
+completion; ``roofline`` = the Rosenbrock kernel's aggregate FP64 rate over
+the served window (``roofline_plain``: in the plain leg, no overlap between
+calls) against the FP64 peak measured in this run;
 ``cpu_baseline`` = the CPU oracle (C++ restatement of Bolt's CPU algorithm,
 threaded over k / l) on a bounded sample of every request type, scaled to
 the stream; ``cl_grad`` = a stream of C_l^TT + Jacobian requests only (the
@@ -346,7 +348,7 @@ def run_serving(args):
         barrier(dist)
         s0 = eng.stats()
         rng = np.random.default_rng(SEED + 17 + rank)
-        arrivals = np.cumsum(rng.exponential(1.0 / RATE, K))
+        arrivals = np.cumsum(rng.exponential(1.0 / args.rate, K))
         tickets = [None] * K
         t_start = time.perf_counter()
 
@@ -401,6 +403,7 @@ def run_serving(args):
                            "per request (forward differences); plain_engine: the engine one request per call "
                            "(7 parameter sets batched in one launch, tangent LOS)"}
     lat = np.array([r.latency for r in res])
+    tab = np.array([r.times[1] - r.times[0] for r in res])  # submission to host tables ready
     gpu_window = max_over_ranks(max(r.times[3] for r in res) - min(r.times[2] for r in res), dist)
     e2e_window = max_over_ranks(max(r.times[3] for r in res) - min(r.times[0] for r in res), dist)
     value = ws * K / gpu_window
@@ -409,15 +412,24 @@ def run_serving(args):
     h2d = sum(io_bytes(d)[0] for d in stream) / K
     d2h = sum(io_bytes(d)[1] for d in stream) / K
     peak = ctypes_peak(lib, local)
-    ach = plain_flops / plain_solver_s / 1e12 if plain_solver_s > 0 else None
+    peak_src = "measured in this run: FP64 FMA loop (bolt_fp64_peak); MEASURED_PEAKS.json has no FP64 figure"
+    flop_note = "algorithmic FLOPs of the accepted + rejected steps of every mode (159 N + 560 (nq+5) + 66 nq + 650 " \
+                "per step, nq momentum bins, N state length)"
+    served_flops = sum(r.steps * solver_flops_per_step(state_len(*d["hier"]), d["hier"][3])
+                       for r, d in zip(res, stream))
+    ach = served_flops / gpu_window / 1e12
     roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-            "frac": ach / peak if (peak and ach) else None, "traffic": None, "kernel": "rodas_kernel",
-            "peak_source": "measured in this run: FP64 FMA loop (bolt_fp64_peak); MEASURED_PEAKS.json has no "
-                           "FP64 figure",
-            "note": "plain leg (drop-in calls one at a time, 4 warps per mode): algorithmic FLOPs of the accepted + "
-                    "rejected steps of every "
-                    "mode (159 N + 560 (nq+5) + 66 nq + 650 per step) / CUDA-event time of the solver launches; "
-                    "DRAM traffic is negligible (per-CTA state slab L2-resident), see profiles/"}
+            "frac": ach / peak if peak else None, "traffic": None, "kernel": "rodas_kernel<1>",
+            "peak_source": peak_src,
+            "note": "served leg (the kernel behind value): " + flop_note + " of every request in the stream / the "
+                    "GPU window (solver launches of up to 6 lanes overlap; the window also holds the LOS "
+                    "projections, so this is a lower bound on the solver's rate); DRAM traffic is negligible "
+                    "(per-CTA state slab L2-resident), see profiles/"}
+    ach_p = plain_flops / plain_solver_s / 1e12 if plain_solver_s > 0 else None
+    roof_plain = {"bound": "fp64", "achieved": ach_p, "peak": peak, "unit": "TFLOP/s",
+                  "frac": ach_p / peak if (peak and ach_p) else None, "kernel": "rodas_kernel<4>",
+                  "note": "plain leg (drop-in calls one at a time, 4 warps per mode, launches too small to fill the "
+                          "GPU): " + flop_note + " / CUDA-event time of the solver launches"}
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         secs, cores, sample = cpu_stream_seconds(stream)
@@ -427,8 +439,8 @@ def run_serving(args):
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
                "ms_per_step": 1000.0 * gpu_window / K, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-               "config": {"workload": "serving: seeded Poisson stream (10 req/s) of one-cosmology requests from the "
-                                      "box h 0.6-0.8, omega_b 0.019-0.025, omega_c 0.10-0.14, n_s 0.92-1.0, "
+               "config": {"workload": f"serving: seeded Poisson stream ({args.rate:g} req/s) of one-cosmology "
+                                      "requests from the box h 0.6-0.8, omega_b 0.019-0.025, omega_c 0.10-0.14, n_s 0.92-1.0, "
                                       "ln(1e10 A_s) 2.9-3.2, Sigma m_nu 0-0.3 eV; mix 5:4:1 of P_lin (100-400 log k "
                                       "in [1e-4,1] h/Mpc, l 50/50/20, nq 15), C_l TT/TE/EE (l_max 1000 or 2500) and "
                                       "C_l^TT l<=2000 + 6-parameter Jacobian (both: 64-1024 log k in [0.1,1000] H0, "
@@ -445,12 +457,14 @@ def run_serving(args):
                "served_over_plain": value / plain,
                "cl_grad": cl_grad,
                "latency": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-                           "arrival_rate_per_s": RATE},
+                           "arrival_rate_per_s": args.rate,
+                           "host_tables_p50_s": float(np.percentile(tab, 50)),
+                           "host_tables_max_s": float(np.max(tab))},
                "clocks": clocks,
                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]),
                "engine": {k: s1[k] - s0[k] for k in s1},
-               "roofline": roof, "cpu_baseline": cpu}
+               "roofline": roof, "roofline_plain": roof_plain, "cpu_baseline": cpu}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
@@ -556,6 +570,7 @@ def main():
     ap.add_argument("--workload", default="serving", choices=["serving", "pipeline"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grad-requests", type=int, default=6, help="serving: size of the C_l+gradient-only stream")
+    ap.add_argument("--rate", type=float, default=RATE, help="serving: Poisson arrival rate, requests/s")
     ap.add_argument("--nk", type=int, default=1200, help="pipeline: source-grid wavenumbers")
     ap.add_argument("--kmax-h0", type=float, default=5000.0, help="pipeline: largest wavenumber in units of H0")
     ap.add_argument("--lmax", type=int, default=2500, help="pipeline: largest multipole")

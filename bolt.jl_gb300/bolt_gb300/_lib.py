@@ -94,6 +94,8 @@ EXPORTS = {
     "bolt_engine_submit": (C.c_int, [C.c_void_p, C.POINTER(BoltRequest), _i64p]),
     "bolt_engine_wait": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, _ip, _dp, C.c_char_p, C.c_int]),
     "bolt_request_run": (C.c_int, [C.c_void_p, C.POINTER(BoltRequest), C.c_char_p, C.c_int]),
+    "bolt_cl_vjp": (C.c_int, [C.c_void_p, C.POINTER(BoltRequest), _dp, _dp, _dp, _dp, C.c_char_p, C.c_int]),
+    "bolt_plin_vjp": (C.c_int, [C.c_void_p, C.POINTER(BoltRequest), _dp, _dp, C.c_char_p, C.c_int]),
     "bolt_engine_stats": (C.c_int, [C.c_void_p, _i64p]),
 }
 

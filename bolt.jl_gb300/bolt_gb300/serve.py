@@ -172,6 +172,33 @@ class Engine:
         """One request alone (submit + wait)."""
         return self.wait(self.submit(req))
 
+    def vjp(self, req: Request, ybar) -> tuple[Result, np.ndarray]:
+        """Pullback of the rrule (bolt_cl_vjp / bolt_plin_vjp): the request
+        alone with its Jacobian, contracted with the cotangents ``ybar`` --
+        for C_l a dict spectrum -> [nell] (missing spectra count as zero), for
+        P_lin an array [nk].  Returns (result with the primal outputs, grad[6]
+        with respect to theta)."""
+        q = Request(**{**req.__dict__, "grad": False})
+        p = _Pending(q)
+        grad = np.zeros(6)
+        err = C.create_string_buffer(512)
+        if req.kind == "plin":
+            yb = np.ascontiguousarray(ybar, dtype=np.float64)
+            if yb.shape != (p.k.size,):
+                raise ValueError("ybar needs one entry per wavenumber")
+            rc = self.lib.bolt_plin_vjp(self.h, C.byref(p.c), L.dptr(yb), L.dptr(grad), err, 512)
+        else:
+            yb = {}
+            for c, v in dict(ybar).items():
+                if c not in req.cl:
+                    raise ValueError(f"cotangent for {c!r}, which the request does not compute")
+                yb[c] = np.ascontiguousarray(v, dtype=np.float64)
+                if yb[c].shape != (p.ells.size,):
+                    raise ValueError("ybar needs one entry per multipole")
+            rc = self.lib.bolt_cl_vjp(self.h, C.byref(p.c), L.dptr(yb.get("tt")), L.dptr(yb.get("te")),
+                                      L.dptr(yb.get("ee")), L.dptr(grad), err, 512)
+        return p.result(rc, err.value.decode(), np.zeros(5)), grad
+
     def stats(self) -> dict:
         out = np.zeros(11, dtype=np.int64)
         self.lib.bolt_engine_stats(self.h, out.ctypes.data_as(C.POINTER(C.c_int64)))

@@ -265,7 +265,10 @@ struct Tuner {
   // the whole load (shared).
   int pick(bool shared, int key, int nsm) {
     const double r = double(key) / double(nsm);
-    if (r <= 2.0) return 4;  // one wave: the lowest-latency variant
+    // one wave onto an otherwise idle GPU: the lowest-latency variant.  Not
+    // for a shared launch: one that starts small keeps its variant while the
+    // GPU fills up and then runs as the slow tail of the load.
+    if (!shared && r <= 2.0) return 4;
     double c[3];
     prior(shared, r, c);
     const int t = shared ? 1 : 0, b = bucket(key);
@@ -1262,6 +1265,64 @@ int bolt_request_run(bolt_engine* E, const bolt_request* q, char* errbuf, int er
   int out = 0;
   rc = bolt_engine_wait(E, t, -1.0, &out, nullptr, errbuf, errlen);
   return rc == 1 ? out : rc;
+}
+
+// Reverse-mode products: run the request with its Jacobian (library-owned
+// [6][n] buffers), then contract with the caller's cotangents.
+static int run_vjp(bolt_engine* E, const bolt_request* q, int kind, const double* const ybar[3], double* grad,
+                   char* errbuf, int errlen) {
+  auto fail = [&](const char* m) {
+    if (errbuf && errlen > 0) {
+      std::strncpy(errbuf, m, size_t(errlen) - 1);
+      errbuf[errlen - 1] = 0;
+    }
+    return -1;
+  };
+  if (!E || !q || !grad) return fail("null argument");
+  if (q->kind != kind) return fail(kind == BOLT_REQ_CL ? "bolt_cl_vjp needs a C_l request" : "bolt_plin_vjp needs a P_lin request");
+  bolt_request r = *q;
+  r.grad = 1;
+  const int n = kind == BOLT_REQ_CL ? r.nell : r.nk;
+  if (n <= 0) return fail(kind == BOLT_REQ_CL ? "no multipoles" : "no wavenumbers");
+  std::vector<double> prim[3], jac[3];
+  double** outs[3] = {&r.tt, &r.te, &r.ee};
+  double** douts[3] = {&r.dtt, &r.dte, &r.dee};
+  if (kind == BOLT_REQ_CL) {
+    for (int c = 0; c < 3; ++c) {
+      *douts[c] = nullptr;
+      if (!(r.cl_want & (1 << c))) continue;
+      if (!*outs[c]) { prim[c].assign(size_t(n), 0.0); *outs[c] = prim[c].data(); }
+      jac[c].assign(size_t(kTheta) * n, 0.0);
+      *douts[c] = jac[c].data();
+    }
+  } else {
+    if (!r.plin) { prim[0].assign(size_t(n), 0.0); r.plin = prim[0].data(); }
+    jac[0].assign(size_t(kTheta) * n, 0.0);
+    r.dplin = jac[0].data();
+  }
+  int rc = bolt_request_run(E, &r, errbuf, errlen);
+  if (rc != 0) return rc;
+  for (int j = 0; j < kTheta; ++j) {
+    double acc = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      if (jac[c].empty() || !ybar[c]) continue;
+      for (int i = 0; i < n; ++i) acc += ybar[c][i] * jac[c][size_t(j) * n + i];
+    }
+    grad[j] = acc;
+  }
+  return 0;
+}
+
+int bolt_cl_vjp(bolt_engine* E, const bolt_request* q, const double* ybar_tt, const double* ybar_te,
+                const double* ybar_ee, double* grad, char* errbuf, int errlen) {
+  const double* yb[3] = {ybar_tt, ybar_te, ybar_ee};
+  return run_vjp(E, q, BOLT_REQ_CL, yb, grad, errbuf, errlen);
+}
+
+int bolt_plin_vjp(bolt_engine* E, const bolt_request* q, const double* ybar, double* grad, char* errbuf,
+                  int errlen) {
+  const double* yb[3] = {ybar, nullptr, nullptr};
+  return run_vjp(E, q, BOLT_REQ_PLIN, yb, grad, errbuf, errlen);
 }
 
 int bolt_engine_stats(bolt_engine* E, int64_t* out) {

@@ -274,6 +274,21 @@ int bolt_engine_wait(bolt_engine* eng, int64_t ticket, double timeout_s, int* rc
 /* One request, alone: submit + wait (the one-request-per-call path). */
 int bolt_request_run(bolt_engine* eng, const bolt_request* req, char* errbuf, int errlen);
 
+/* Reverse-mode products, the pullback of an rrule over cltt / clte / clee
+ * (src/spectra.jl:132-160) and plin (src/spectra.jl:163-198): the request runs
+ * alone with its Jacobian (req->grad is taken as 1; its d* pointers are
+ * ignored, the Jacobian stays in library memory) and
+ *   bolt_cl_vjp:   grad[j] = sum over the spectra X in req->cl_want of
+ *                  sum_l ybar_X[l] dC_l^X/dtheta_j  (ybar_X [nell]; NULL = 0)
+ *   bolt_plin_vjp: grad[j] = sum_k ybar[k] dP_lin(k)/dtheta_j  (ybar [nk])
+ * for theta = (h, omega_b, omega_c, n_s, A_s, Sigma m_nu [eV]), grad[6].  The
+ * primal outputs named in req are written too (NULL ones are not).  Returns
+ * 0 or a negative code with the message in errbuf. */
+int bolt_cl_vjp(bolt_engine* eng, const bolt_request* req, const double* ybar_tt, const double* ybar_te,
+                const double* ybar_ee, double* grad, char* errbuf, int errlen);
+int bolt_plin_vjp(bolt_engine* eng, const bolt_request* req, const double* ybar, double* grad, char* errbuf,
+                  int errlen);
+
 /* Engine counters: [0] batches, [1] requests completed, [2] modes solved,
  * [3] solver microseconds (sum over batches), [4] LOS microseconds,
  * [5] accepted + rejected steps, [6] kernel launches, [7] graph launches,

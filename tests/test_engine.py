@@ -225,3 +225,27 @@ def test_failing_request_does_not_affect_others():
     with B.Engine(lanes=1) as eng:
         ref = eng.run(B.Request("plin", par, ks, hier=HIER))
     assert _rel(rg.plin, ref.plin) < 1e-12
+
+
+def test_vjp_matches_jacobian_contraction():
+    """bolt_cl_vjp / bolt_plin_vjp equal the cotangent contracted with the
+    Jacobian of the same request."""
+    rng = np.random.default_rng(3)
+    par = _par(h=0.69, mnu=0.08)
+    ks = _ks(par, nk=40, kmax_h0=300.0)
+    ells = np.arange(2, 500, 9, dtype=np.int32)
+    with B.Engine(lanes=1) as eng:
+        full = eng.run(B.Request("cl", par, ks, hier=HIER, ells=ells, cl=("tt", "ee"), grad=True))
+        yb = {"tt": rng.standard_normal(ells.size), "ee": rng.standard_normal(ells.size)}
+        res, g = eng.vjp(B.Request("cl", par, ks, hier=HIER, ells=ells, cl=("tt", "ee")), yb)
+        kp = B.log10_k(1e-3 * par.h, 0.5 * par.h, 12)
+        pf = eng.run(B.Request("plin", par, kp, hier=HIER, grad=True))
+        ybp = rng.standard_normal(kp.size)
+        rp, gp = eng.vjp(B.Request("plin", par, kp, hier=HIER), ybp)
+    assert full.rc == 0 and res.rc == 0 and pf.rc == 0 and rp.rc == 0, (full.err, res.err, pf.err, rp.err)
+    want = full.dcl["tt"] @ yb["tt"] + full.dcl["ee"] @ yb["ee"]
+    assert np.max(np.abs(g - want)) <= 1e-12 * np.max(np.abs(want))
+    assert _rel(res.cl["tt"], full.cl["tt"]) < 1e-12
+    wantp = pf.dplin @ ybp
+    assert np.max(np.abs(gp - wantp)) <= 1e-12 * np.max(np.abs(wantp))
+    assert _rel(rp.plin, pf.plin) < 1e-12
