@@ -115,6 +115,15 @@ constexpr double kRelStep = 1e-6;   // forward-difference step, relative to |the
 constexpr int kNb = 5001;           // Bessel grid points (spectra.jl:52)
 constexpr int kNkd = 5000;          // dense LOS k grid (spectra.jl:133)
 constexpr double kFillModes = 24.0;  // modes per SM that make a launch worth starting while others run
+constexpr int kThetaN = 3, kThetaA = 4;  // n_s and A_s in theta
+
+// n_s and A_s enter only the primordial spectrum A (k/0.05)^(n-1) of the
+// C_l sum and of P_lin (spectra.jl:92, 195-196), not the tables or the
+// perturbation solve: their parameter sets of a gradient request reuse the
+// unperturbed set's solver outputs and launch no modes.
+bool solve_free(int j) { return j == kThetaN || j == kThetaA; }
+// Parameter set s of request r takes no solver modes.
+bool skips_solve(int nsets, int s) { return nsets > 1 && s >= 1 && solve_free(s - 1); }
 
 struct EngErr : std::runtime_error {
   int code;
@@ -521,7 +530,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     r->cos0 = ncos;
     ncos += r->nsets;
     m1 += r->r.nk;
-    m2 += (r->nsets - 1) * r->r.nk;
+    for (int s = 1; s < r->nsets; ++s) m2 += skips_solve(r->nsets, s) ? 0 : r->r.nk;
     maxN = std::max(maxN, r->N);
     maxnq = std::max(maxnq, r->r.hier.nq);
     maxL = std::max(maxL, std::max(r->r.hier.lg, std::max(r->r.hier.lnu, r->r.hier.lmnu)));
@@ -644,7 +653,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     int64_t* dcnt = reinterpret_cast<int64_t*>(dev + r->o_cnt);
     double* drec = reinterpret_cast<double*>(dev + r->o_rec);
     for (int s = 0; s < ns; ++s)
-      for (int i = 0; i < nk; ++i) {
+      for (int i = 0; i < nk && !skips_solve(ns, s); ++i) {
         ModeDev m;
         std::memset(&m, 0, sizeof(m));
         m.k = r->k[i];
@@ -740,6 +749,12 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     if (r->los_tangent)  // sets 1..6 -> derivatives of the weights and of y along theta_j
       for (int j = 0; j < kTheta; ++j) {
         double* d = per + size_t(1 + j) * (nm + n);
+        if (solve_free(j)) {  // exact: dw/dn = w ln(k/0.05), dw/dA = w/A; y does not depend on them
+          for (int m = 0; m < nm; ++m)
+            d[m] = j == kThetaN ? per[m] * std::log(kmid[m] / 0.05) : per[m] / T0.par.A;
+          for (int i = 0; i < nrow; ++i) d[nm + i] = 0.0;
+          continue;
+        }
         const double inv = 1.0 / r->step[j];
         for (int q = 0; q < nm + nrow; ++q) d[q] = (d[q] - per[q]) * inv;
       }
@@ -793,9 +808,14 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     double* cl = reinterpret_cast<double*>(dev + r->o_cl);
     if (r->los_tangent) {
       rc = launch_sdense(n, P.i0, P.nrow, nk, kg, src, nullptr, P.nm, kmid, dxs, SdT, nullptr, st);
-      for (int j = 0; j < kTheta && rc == 0; ++j)
+      for (int j = 0; j < kTheta && rc == 0; ++j) {
+        if (solve_free(j)) {  // the sources do not depend on theta_j
+          rc = int(cudaMemsetAsync(dSd + size_t(j) * P.nrow * P.nm, 0, size_t(P.nrow) * P.nm * 8, st));
+          continue;
+        }
         rc = launch_sdense_diff(n, P.i0, P.nrow, nk, kg, src + size_t(1 + j) * nk * n, src, 1.0 / r->step[j], P.nm,
                                 kmid, dxs, dSd + size_t(j) * P.nrow * P.nm, st);
+      }
       if (rc != 0) throw EngErr(-3, std::string("source resampling: ") + cudaGetErrorString(cudaError_t(rc)));
       LosGradArgs a;
       a.nb = kNb; a.nslots = P.ns; a.nrow = P.nrow; a.nm = P.nm;
@@ -808,8 +828,9 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
       continue;
     }
     for (int s = 0; s < r->nsets; ++s) {
-      const double* ST = src + size_t(s) * nk * n;
-      const double* SE = r->wantE ? src + size_t(r->nsets) * nk * n + size_t(s) * nk * n : nullptr;
+      const int ss = skips_solve(r->nsets, s) ? 0 : s;  // parameter set whose sources hold for set s
+      const double* ST = src + size_t(ss) * nk * n;
+      const double* SE = r->wantE ? src + size_t(r->nsets) * nk * n + size_t(ss) * nk * n : nullptr;
       rc = launch_sdense(n, P.i0, P.nrow, nk, kg, ST, SE, P.nm, kmid, dxs, SdT, SE ? SdE : nullptr, st);
       if (rc != 0) throw EngErr(-3, std::string("source resampling: ") + cudaGetErrorString(cudaError_t(rc)));
       const double* wts = per + size_t(s) * (P.nm + n);
@@ -848,7 +869,7 @@ void finalize_request(bolt_engine* E, Lane& L, Req* r) {
   const int32_t* st = reinterpret_cast<const int32_t*>(down + r->h_stat);
   if (r->r.status) std::copy(st, st + nk, r->r.status);
   for (int s = 0; s < ns && r->rc == 0; ++s)
-    for (int i = 0; i < nk; ++i) {
+    for (int i = 0; i < nk && !skips_solve(ns, s); ++i) {
       int v = st[size_t(s) * nk + i];
       if ((v & 0xFF) != 0 || (s == 0 && ns > 1 && (v & ST_REC_OVERFLOW))) {
         r->rc = -4;
@@ -866,7 +887,10 @@ void finalize_request(bolt_engine* E, Lane& L, Req* r) {
     std::copy(P, P + nk, r->r.plin);
     if (ns > 1)
       for (int j = 0; j < kTheta; ++j)
-        for (int i = 0; i < nk; ++i) r->r.dplin[size_t(j) * nk + i] = deriv(P, nk, j, i);
+        for (int i = 0; i < nk; ++i)  // P = (2 pi^2 / k^3) delta_m^2 A (k/0.05)^(n-1) (spectra.jl:195-197)
+          r->r.dplin[size_t(j) * nk + i] = j == kThetaN   ? P[i] * std::log(r->k[i] / 0.05)
+                                           : j == kThetaA ? P[i] / r->T[0].par.A
+                                                          : deriv(P, nk, j, i);
   } else {
     const double* cl = reinterpret_cast<const double*>(down + r->h_cl);
     const int nsl = int(r->uniq.size());
@@ -906,12 +930,12 @@ void finish_lane(bolt_engine* E, Lane& L) {
   for (Req* r : L.batch) {
     const int64_t* cnt = reinterpret_cast<const int64_t*>(down + r->h_cnt);
     for (int s = 0; s < r->nsets; ++s)
-      for (int i = 0; i < r->r.nk; ++i) {
+      for (int i = 0; i < r->r.nk && !skips_solve(r->nsets, s); ++i) {
         size_t q = 2 * (size_t(s) * r->r.nk + i);
         steps[s == 0 ? 0 : 1] += double(cnt[q] + cnt[q + 1]);
         r->steps += double(cnt[q] + cnt[q + 1]);
       }
-    modes += int64_t(r->nsets) * r->r.nk;
+    for (int s = 0; s < r->nsets; ++s) modes += skips_solve(r->nsets, s) ? 0 : r->r.nk;
   }
   E->tuner.update(L.shared[0], L.key[0], L.wpm[0], ms1 * 1e-3, steps[0]);
   if (L.nmodes[1] > 0) E->tuner.update(L.shared[1], L.key[1], L.wpm[1], ms2 * 1e-3, steps[1]);
