@@ -34,6 +34,9 @@ per call.
 
 ``--workload pipeline``: the full CMB pipeline for one cosmology (1200 k,
 l <= 2500, N = 473) with device-timed throughput (the profiling case).
+``--workload batch`` / ``grad``: K cosmologies submitted at once (C_l^TT +
+P_lin from one solve each; or the Jacobians of C_l^TT and P_lin) against the
+plain drop-in, cosmologies/s.
 ``--impl reference``: the CPU oracle alone on the serving stream.
 """
 from __future__ import annotations
@@ -141,16 +144,21 @@ def dropin_request(B, ctx, d):
     """One request through the plain drop-in C-ABI, one cosmology per call
     (the calls Bolt's Julia API makes through ccall): bolt_cosmo_build (host
     background + RECFAST tables, uploaded), bolt_plin or bolt_cl_pipeline,
-    bolt_cosmo_free.  The drop-in has no Jacobian, so a gradient request is
-    1 + 6 calls whose forward differences give dC_l^TT/dtheta (central
-    differences would take 13).  Returns (result, calls, solver seconds,
-    algorithmic solver FLOPs) with the solver figures from bolt_last_stats."""
+    bolt_cosmo_free.  Kinds: "plin" (log k in [1e-4, 1] h/Mpc), "plin_on_k"
+    (P_lin on the C_l k grid), "cl" (TT/TE/EE), "tt" (TT alone), "grad"
+    (C_l^TT Jacobian), "plin_fd" (P_lin Jacobian).  The drop-in has no
+    Jacobian, so a gradient request is 1 + 6 calls whose forward differences
+    give it (central differences would take 13).  Returns (result, calls,
+    solver seconds, algorithmic solver FLOPs) with the solver figures from
+    bolt_last_stats."""
     import ctypes as C
     L = B._lib
     lib = ctx.lib
     th0 = np.asarray(d["theta"], dtype=np.float64)
+    kind = d["kind"]
+    grad = kind in ("grad", "plin_fd")
     sets = [th0]
-    if d["kind"] == "grad":
+    if grad:
         sets += [th0 + np.eye(6)[j] * FD_REL_STEP * abs(th0[j]) for j in range(6)]
     lg, lnu, lmnu, nq = d["hier"]
     hier = L.BoltHier(lg, lnu, lmnu, nq)
@@ -163,8 +171,9 @@ def dropin_request(B, ctx, d):
         cid = C.c_int(-1)
         ctx.check(lib.bolt_cosmo_build(ctx.h, C.byref(par.c()), C.byref(L.BoltGrid(-20.0, 0.01, 0.0)), nq,
                                        C.byref(rf), C.byref(cid)), "bolt_cosmo_build")
-        if d["kind"] == "plin":
-            ks = B.log10_k(1e-4 * par.h, 1.0 * par.h, d["nk"])
+        if kind in ("plin", "plin_fd", "plin_on_k"):
+            ks = (B.log10_k(0.1 * H0, 1000.0 * H0, d["nk"]) if kind == "plin_on_k" else
+                  B.log10_k(1e-4 * par.h, 1.0 * par.h, d["nk"]))
             out = np.zeros(ks.size)
             st = np.zeros(ks.size, dtype=np.int32)
             ctx.check(lib.bolt_plin(ctx.h, cid.value, L.dptr(ks), ks.size, C.byref(hier), 0.0, RELTOL, ABSTOL,
@@ -173,7 +182,7 @@ def dropin_request(B, ctx, d):
             ks = B.log10_k(0.1 * H0, 1000.0 * H0, d["nk"])
             ells = np.arange(2, d["lmax"] + 1, dtype=np.int32)
             out = np.zeros((3, ells.size))
-            te, ee = (out[1], out[2]) if d["kind"] == "cl" else (None, None)
+            te, ee = (out[1], out[2]) if kind == "cl" else (None, None)
             st = np.zeros(ks.size, dtype=np.int32)
             ctx.check(lib.bolt_cl_pipeline(ctx.h, cid.value, L.dptr(ks), ks.size, C.byref(hier), RELTOL, ABSTOL,
                                            L.iptr(ells), ells.size, L.dptr(out[0]), L.dptr(te), L.dptr(ee),
@@ -184,9 +193,10 @@ def dropin_request(B, ctx, d):
         flops += (s["accepted_steps"] + s["rejected_steps"]) * fpstep
         lib.bolt_cosmo_free(ctx.h, cid.value)
         outs.append(out)
-    if d["kind"] == "grad":
-        jac = np.array([(outs[1 + j][0] - outs[0][0]) / (FD_REL_STEP * abs(th0[j])) for j in range(6)])
-        return (outs[0][0], jac), len(sets), solver_s, flops
+    if grad:
+        f = [o if o.ndim == 1 else o[0] for o in outs]
+        jac = np.array([(f[1 + j] - f[0]) / (FD_REL_STEP * abs(th0[j])) for j in range(6)])
+        return (f[0], jac), len(sets), solver_s, flops
     return outs[0], len(sets), solver_s, flops
 
 
@@ -492,6 +502,107 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+# ------------------------------------------------------ batch / gradients --
+def cosmology_requests(workload, n, seed_offset):
+    """cfg 3 (batch): per cosmology one C_l^TT (l <= 2000) request on its own
+    64-1024 log k in [0.1, 1000] H0 with l_gamma = l_nu in {20, 35, 50},
+    l_mnu 10, returning P_lin(k) at x = 0 from the same solve.  cfg 4
+    (grad): per cosmology the C_l^TT Jacobian (same draw) and the P_lin
+    Jacobian on 200 log k in [1e-4, 1] h/Mpc (l 50/50/20)."""
+    rng = np.random.default_rng(SEED + seed_offset)
+    out = []
+    for _ in range(n):
+        th = draw_theta(rng)
+        lg = int(rng.choice([20, 35, 50]))
+        nk = int(rng.integers(64, 1025))
+        if workload == "batch":
+            out.append({"kind": "cltt_plin", "theta": th, "nk": nk, "hier": (lg, lg, 10, 15), "lmax": 2000})
+        else:
+            out.append({"kind": "grad", "theta": th, "nk": nk, "hier": (lg, lg, 10, 15), "lmax": 2000})
+            out.append({"kind": "plin_grad", "theta": th, "nk": 200, "hier": (50, 50, 20, 15)})
+    return out
+
+
+def batch_request(B, d):
+    par = B.params_of(B.CosmoParams(), d["theta"])
+    H0 = par.h * B.km_s_Mpc_100()
+    if d["kind"] == "plin_grad":
+        return B.Request("plin", par, B.log10_k(1e-4 * par.h, par.h, d["nk"]), hier=d["hier"], grad=True,
+                         reltol=RELTOL, abstol=ABSTOL)
+    ks = B.log10_k(0.1 * H0, 1000.0 * H0, d["nk"])
+    ells = np.arange(2, d["lmax"] + 1, dtype=np.int32)
+    return B.Request("cl", par, ks, hier=d["hier"], ells=ells, cl=("tt",), grad=d["kind"] == "grad",
+                     with_plin=d["kind"] == "cltt_plin", reltol=RELTOL, abstol=ABSTOL)
+
+
+def batch_dropin(B, ctx, d):
+    """The same request through the plain drop-in, one cosmology per call:
+    C_l^TT + P_lin = bolt_cl_pipeline (TT) + bolt_plin on the same k and
+    hierarchy; a Jacobian = 1 + 6 calls (forward differences)."""
+    if d["kind"] == "cltt_plin":
+        dropin_request(B, ctx, {**d, "kind": "tt"})
+        dropin_request(B, ctx, {**d, "kind": "plin_on_k"})
+        return 2
+    if d["kind"] == "plin_grad":
+        return dropin_request(B, ctx, {**d, "kind": "plin_fd"})[1]
+    return dropin_request(B, ctx, d)[1]
+
+
+def run_batch(args):
+    """cfg 3 / cfg 4: every request of K cosmologies submitted at once to the
+    engine (6 lanes, objective throughput) against the plain drop-in one
+    cosmology per call; cosmologies per second."""
+    import torch
+    torch.cuda.set_device(0)
+    import bolt_gb300 as B
+    K = args.steps
+    reqs = cosmology_requests(args.workload, K, 3000 if args.workload == "batch" else 4000)
+    warm = cosmology_requests(args.workload, 1, 9000)
+    ctx = B.Context(device=0)
+    for d in warm:
+        batch_dropin(B, ctx, d)
+    sampler = clocks_sampler()
+    t0 = time.perf_counter()
+    calls = sum(batch_dropin(B, ctx, d) for d in reqs)
+    plain_s = time.perf_counter() - t0
+    ctx.close()
+    with B.Engine(device=0, lanes=6, objective="throughput") as eng:
+        for d in warm:
+            assert eng.run(batch_request(B, d)).rc == 0
+        s0 = eng.stats()
+        res = [eng.wait(t) for t in [eng.submit(batch_request(B, d)) for d in reqs]]
+        s1 = eng.stats()
+    clocks = clocks_summary(sampler)
+    for r in res:
+        assert r.rc == 0, r.err
+    win = max(r.times[3] for r in res) - min(r.times[2] for r in res)
+    e2e = max(r.times[3] for r in res) - min(r.times[0] for r in res)
+    flops = sum(r.steps * solver_flops_per_step(state_len(*d["hier"]), d["hier"][3]) for r, d in zip(res, reqs))
+    peak = ctypes_peak(B._lib.load(), 0)
+    what = ("cfg 3 batch: C_l^TT (l 2..2000) + P_lin(k) at x = 0 per cosmology, one solve each"
+            if args.workload == "batch" else
+            "cfg 4 gradients: 6-parameter Jacobians of C_l^TT (l 2..2000) and of P_lin (200 log k in [1e-4,1] h/Mpc)")
+    out = {"metric": f"{what}: cosmologies/s on 1 GB300 (served vs plain drop-in)", "value": K / win,
+           "unit": "cosmologies/s", "n_gpus": 1, "steps": K, "warmup": len(warm), "ms_per_step": 1000.0 * win / K,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": what + "; cosmologies from the cfg-3 box, 64-1024 log k in [0.1,1000] H0, "
+                                         "l_gamma = l_nu in {20,35,50}, l_mnu 10, nq 15; all submitted at once",
+                      "reltol": RELTOL, "abstol": ABSTOL},
+           "plain": {"value": K / plain_s, "unit": "cosmologies/s", "calls": calls,
+                     "api": "drop-in C-ABI one cosmology per call (bolt_cl_pipeline TT, bolt_plin; Jacobians as "
+                            "1 + 6 calls)"},
+           "served_over_plain": plain_s / win,
+           "e2e": {"value": K / e2e, "unit": "cosmologies/s"},
+           "latency": {"p50_s": float(np.percentile([r.latency for r in res], 50)),
+                       "p99_s": float(np.percentile([r.latency for r in res], 99))},
+           "clocks": clocks, "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]),
+           "engine": {k: s1[k] - s0[k] for k in s1},
+           "roofline": {"bound": "fp64", "achieved": flops / win / 1e12, "peak": peak, "unit": "TFLOP/s",
+                        "frac": flops / win / 1e12 / peak if peak else None, "kernel": "rodas_kernel",
+                        "note": "algorithmic solver FLOPs of every request / the served window"}}
+    print(json.dumps(out))
+
+
 # --------------------------------------------------------------- pipeline --
 def run_pipeline(args):
     """Full CMB pipeline for one cosmology, device-timed (the profiling case)."""
@@ -567,7 +678,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20, help="timed requests (serving) or spectra (pipeline)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="serving", choices=["serving", "pipeline"])
+    ap.add_argument("--workload", default="serving", choices=["serving", "pipeline", "batch", "grad"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grad-requests", type=int, default=6, help="serving: size of the C_l+gradient-only stream")
     ap.add_argument("--rate", type=float, default=RATE, help="serving: Poisson arrival rate, requests/s")
@@ -581,6 +692,8 @@ def main():
         run_reference(args)
     elif args.workload == "pipeline":
         run_pipeline(args)
+    elif args.workload in ("batch", "grad"):
+        run_batch(args)
     else:
         run_serving(args)
 

@@ -50,6 +50,7 @@ class Request:
     plin_x: float = 0.0
     ells: np.ndarray | None = None
     cl: tuple = ("tt",)             # any of "tt", "te", "ee"
+    with_plin: bool = False         # "cl": also P_lin(k) at the end of the x grid from the same solve
 
 
 @dataclass
@@ -92,13 +93,13 @@ class _Pending:
         self.status = np.zeros(k.size, dtype=np.int32)
         c.status = L.i32ptr(self.status)
         self.out = {}
-        if req.kind == "plin":
+        if req.kind == "plin" or req.with_plin:
             self.out["plin"] = np.zeros(k.size)
             c.plin = L.dptr(self.out["plin"])
             if req.grad:
                 self.out["dplin"] = np.zeros((6, k.size))
                 c.dplin = L.dptr(self.out["dplin"])
-        else:
+        if req.kind != "plin":
             ells = np.ascontiguousarray(req.ells, dtype=np.int32)
             self.ells = ells
             c.ells = L.iptr(ells)
@@ -116,10 +117,9 @@ class _Pending:
 
     def result(self, rc, err, times) -> Result:
         r = Result(rc=rc, err=err, times=times, status=self.status)
-        if self.req.kind == "plin":
-            r.plin = self.out["plin"]
-            r.dplin = self.out.get("dplin")
-        else:
+        r.plin = self.out.get("plin")
+        r.dplin = self.out.get("dplin")
+        if self.req.kind != "plin":
             for q in self.req.cl:
                 r.cl[q] = self.out[q]
                 if self.req.grad:

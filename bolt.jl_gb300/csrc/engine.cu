@@ -110,7 +110,7 @@ using namespace bolt;
 namespace {
 
 constexpr int kTheta = 6;
-constexpr int kRecCap = 12288;      // recorded steps per mode (gradient requests)
+constexpr int kRecCapMax = 65536;   // recorded steps per mode (gradient requests): min(max_steps, this)
 constexpr double kRelStep = 1e-6;   // forward-difference step, relative to |theta_j|
 constexpr int kNb = 5001;           // Bessel grid points (spectra.jl:52)
 constexpr int kNkd = 5000;          // dense LOS k grid (spectra.jl:133)
@@ -228,6 +228,8 @@ struct Req {
   size_t h_stat = 0, h_plin = 0, h_cl = 0, h_cnt = 0;
   int cos0 = 0;  // first CosmoDev index of the request in the batch
   bool wantE = false;
+  bool wantP = false;        // P_lin at x = grid end (BOLT_REQ_PLIN, or a C_l request with plin set)
+  int rec_cap = 0;           // recorded steps per mode (gradient requests)
   bool los_tangent = false;  // C_l^TT gradient from the tangent of the LOS integral
 };
 
@@ -385,6 +387,7 @@ void check_request(const bolt_request* q) {
       if (q->ells[i] < 2 || q->ells[i] > 20000) throw EngErr(-1, "multipoles must be in 2..20000");
     const int w = q->cl_want;
     if (w <= 0 || w > 7) throw EngErr(-1, "cl_want must name TT, TE and/or EE");
+    if (q->plin && q->grad && !q->dplin) throw EngErr(-1, "dplin output is null");
     if (((w & BOLT_CL_TT) && !q->tt) || ((w & BOLT_CL_TE) && !q->te) || ((w & BOLT_CL_EE) && !q->ee))
       throw EngErr(-1, "C_l output is null");
     if (q->grad && (((w & BOLT_CL_TT) && !q->dtt) || ((w & BOLT_CL_TE) && !q->dte) || ((w & BOLT_CL_EE) && !q->dee)))
@@ -419,7 +422,7 @@ void layout_request(Req* r, size_t& off) {
   r->o_cnt = off;
   off = align_up(off + size_t(ns) * nk * 16);
   r->o_rec = off;
-  if (r->nsets > 1) off = align_up(off + size_t(nk) * kRecCap * 8);
+  if (r->nsets > 1) off = align_up(off + size_t(nk) * r->rec_cap * 8);
   if (r->r.kind == BOLT_REQ_CL) {
     r->o_src = off;
     off = align_up(off + size_t(ns) * nk * n * 8 * (r->wantE ? 2 : 1));
@@ -429,7 +432,8 @@ void layout_request(Req* r, size_t& off) {
     const int nm = kNkd - 1;
     off = align_up(off + size_t(nk + nm + n + 8) * 8 + size_t(r->uniq.back() + 1 + r->uniq.size()) * 4 +
                    size_t(ns) * (nm + n) * 8 + 1024);
-  } else {
+  }
+  if (r->wantP) {
     r->o_plin = off;
     off = align_up(off + size_t(ns) * nk * 8);
   }
@@ -617,7 +621,8 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     if (r->r.kind == BOLT_REQ_CL) {
       r->h_cl = doff;
       doff = align_up(doff + size_t(ns) * 3 * r->uniq.size() * 8);
-    } else {
+    }
+    if (r->wantP) {
       r->h_plin = doff;
       doff = align_up(doff + size_t(ns) * nk * 8);
     }
@@ -666,16 +671,17 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
           m.flags = MODE_SOURCES;
           m.src_T = src + (size_t(s) * nk + i) * n;
           m.src_E = r->wantE ? src + size_t(ns) * nk * n + (size_t(s) * nk + i) * n : nullptr;
-        } else {
-          m.flags = MODE_PLIN;
+        }
+        if (r->wantP) {  // at the last node: plin_x, or the end of the x grid for a C_l request
+          m.flags |= MODE_PLIN;
           m.plin = reinterpret_cast<double*>(dev + r->o_plin) + size_t(s) * nk + i;
         }
         m.status = dstat + size_t(s) * nk + i;
         m.counters = dcnt + 2 * (size_t(s) * nk + i);
         if (ns > 1) {
           m.flags |= s == 0 ? MODE_RECORD : MODE_REPLAY;
-          m.rec = drec + size_t(i) * kRecCap;
-          m.rec_cap = kRecCap;
+          m.rec = drec + size_t(i) * r->rec_cap;
+          m.rec_cap = r->rec_cap;
         }
         if (s == 0) modes.push_back(m);
         else modes2.push_back(m);
@@ -853,7 +859,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     if (r->r.kind == BOLT_REQ_CL)
       ck(cudaMemcpyAsync(down + r->h_cl, dev + r->o_cl, size_t(ns) * 3 * r->uniq.size() * 8, cudaMemcpyDeviceToHost,
                          st), "C_l");
-    else
+    if (r->wantP)
       ck(cudaMemcpyAsync(down + r->h_plin, dev + r->o_plin, size_t(ns) * nk * 8, cudaMemcpyDeviceToHost, st), "P_lin");
   }
   ck(cudaFreeAsync(L.d_block, st), "cudaFreeAsync batch");
@@ -873,8 +879,12 @@ void finalize_request(bolt_engine* E, Lane& L, Req* r) {
       int v = st[size_t(s) * nk + i];
       if ((v & 0xFF) != 0 || (s == 0 && ns > 1 && (v & ST_REC_OVERFLOW))) {
         r->rc = -4;
-        char buf[160];
-        std::snprintf(buf, sizeof(buf), "mode k=%.6g (parameter set %d) ended with status %d", r->k[i], s, v);
+        char buf[192];
+        if ((v & 0xFF) == 0)
+          std::snprintf(buf, sizeof(buf), "mode k=%.6g took more than %d accepted steps, the step record of a "
+                        "gradient request (raise max_steps)", r->k[i], r->rec_cap);
+        else
+          std::snprintf(buf, sizeof(buf), "mode k=%.6g (parameter set %d) ended with status %d", r->k[i], s, v);
         r->err = buf;
         break;
       }
@@ -882,7 +892,7 @@ void finalize_request(bolt_engine* E, Lane& L, Req* r) {
   auto deriv = [&](const double* f, size_t stride, int j, size_t i) -> double {  // set 1 + j: theta_j + h
     return (f[size_t(1 + j) * stride + i] - f[i]) / r->step[j];
   };
-  if (r->r.kind == BOLT_REQ_PLIN) {
+  if (r->wantP) {
     const double* P = reinterpret_cast<const double*>(down + r->h_plin);
     std::copy(P, P + nk, r->r.plin);
     if (ns > 1)
@@ -891,7 +901,8 @@ void finalize_request(bolt_engine* E, Lane& L, Req* r) {
           r->r.dplin[size_t(j) * nk + i] = j == kThetaN   ? P[i] * std::log(r->k[i] / 0.05)
                                            : j == kThetaA ? P[i] / r->T[0].par.A
                                                           : deriv(P, nk, j, i);
-  } else {
+  }
+  if (r->r.kind == BOLT_REQ_CL) {
     const double* cl = reinterpret_cast<const double*>(down + r->h_cl);
     const int nsl = int(r->uniq.size());
     const size_t stride = size_t(3) * nsl;
@@ -1196,7 +1207,9 @@ int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
       r->uniq.erase(std::unique(r->uniq.begin(), r->uniq.end()), r->uniq.end());
       r->wantE = (q->cl_want & (BOLT_CL_TE | BOLT_CL_EE)) != 0;
       r->los_tangent = q->grad && q->cl_want == BOLT_CL_TT;
+      r->wantP = q->plin != nullptr;
     } else {
+      r->wantP = true;
       r->r.ells = nullptr;
       r->r.nell = 0;
     }
@@ -1212,6 +1225,7 @@ int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
     r->pars.push_back(base);
     if (q->grad) {
       r->nsets = 1 + kTheta;
+      r->rec_cap = int(std::min<long long>(E->cfg.max_steps, kRecCapMax));
       double th[kTheta];
       theta_of(base, th);
       for (int j = 0; j < kTheta; ++j) {
@@ -1308,10 +1322,14 @@ static int run_vjp(bolt_engine* E, const bolt_request* q, int kind, const double
   r.grad = 1;
   const int n = kind == BOLT_REQ_CL ? r.nell : r.nk;
   if (n <= 0) return fail(kind == BOLT_REQ_CL ? "no multipoles" : "no wavenumbers");
-  std::vector<double> prim[3], jac[3];
+  std::vector<double> prim[3], jac[3], jac_p;
   double** outs[3] = {&r.tt, &r.te, &r.ee};
   double** douts[3] = {&r.dtt, &r.dte, &r.dee};
   if (kind == BOLT_REQ_CL) {
+    if (r.plin) {  // P_lin asked for alongside: its Jacobian is computed but not contracted
+      jac_p.assign(size_t(kTheta) * r.nk, 0.0);
+      r.dplin = jac_p.data();
+    }
     for (int c = 0; c < 3; ++c) {
       *douts[c] = nullptr;
       if (!(r.cl_want & (1 << c))) continue;

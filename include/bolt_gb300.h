@@ -223,7 +223,8 @@ typedef struct {
   int nell;
   int cl_want;           /* BOLT_CL_* bits */
   /* outputs */
-  double* plin;          /* [nk] */
+  double* plin;          /* [nk]: BOLT_REQ_PLIN, P_lin at plin_x; BOLT_REQ_CL, optional (NULL = none),
+                            P_lin at the end of the x grid from the source-grid solve (same modes) */
   double* dplin;         /* [6][nk] (grad) */
   double *tt, *te, *ee;  /* [nell] each, per cl_want */
   double *dtt, *dte, *dee; /* [6][nell] each (grad), per cl_want */

@@ -249,3 +249,24 @@ def test_vjp_matches_jacobian_contraction():
     wantp = pf.dplin @ ybp
     assert np.max(np.abs(gp - wantp)) <= 1e-12 * np.max(np.abs(wantp))
     assert _rel(rp.plin, pf.plin) < 1e-12
+
+
+def test_cl_request_with_plin():
+    """A C_l request with with_plin also returns P_lin(k) at the end of the x
+    grid from the same modes: it matches a P_lin request on the same k and
+    hierarchy (another step sequence, so to the solver tolerance), its C_l
+    are those of the request without it, and its Jacobian keeps
+    dP/dA = P/A."""
+    par = _par(h=0.71, mnu=0.07)
+    ks = _ks(par, nk=32, kmax_h0=300.0)
+    ells = np.arange(2, 300, 7, dtype=np.int32)
+    with B.Engine(lanes=1) as eng:
+        a = eng.run(B.Request("cl", par, ks, hier=HIER, ells=ells, cl=("tt",), with_plin=True, grad=True))
+        b = eng.run(B.Request("cl", par, ks, hier=HIER, ells=ells, cl=("tt",), grad=True))
+        p = eng.run(B.Request("plin", par, ks, hier=HIER))
+    assert a.rc == 0 and b.rc == 0 and p.rc == 0, (a.err, b.err, p.err)
+    assert _rel(a.cl["tt"], b.cl["tt"]) < 1e-12
+    assert _rel(a.dcl["tt"], b.dcl["tt"]) < 1e-12
+    # two solves with different step sequences at abstol 3e-7: ~1e-5 apart at the lowest k
+    assert np.max(np.abs(a.plin / p.plin - 1)) < 1e-4
+    assert np.max(np.abs(a.dplin[4] * par.A / a.plin - 1)) < 1e-12
