@@ -71,6 +71,8 @@ struct SolverCfg {
   double reltol, abstol, h0;
   double x_dense;  // source nodes below this x come from dense output
   long long max_steps;
+  int land_stride;  // source nodes at or above x_dense: every land_stride-th (and the last) is landed on,
+                    // the others come from dense output (1: every node is landed on)
 };
 
 // Argument block of one solver launch captured as a graph kernel node.

@@ -233,6 +233,7 @@ void run_solver(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h
   cfg.h0 = 1e-3;
   cfg.x_dense = c->x_dense;
   cfg.max_steps = c->max_steps;
+  cfg.land_stride = 1;
   int Lmax = std::max(h->lg, std::max(h->lnu, h->lmnu));
   const int wpb = c->wpb;  // warps per mode (0: four)
   size_t pw = rodas_smem_per_mode(N, h->nq, Lmax, wpb);  // shared memory of one mode (one CTA)

@@ -779,6 +779,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   cfg.h0 = 1e-3;
   cfg.x_dense = -8.5;
   cfg.max_steps = E->cfg.max_steps > 0 ? E->cfg.max_steps : 100000;
+  cfg.land_stride = E->cfg.land_stride > 1 ? E->cfg.land_stride : 1;
   for (int ph = 0; ph < nph; ++ph) {
     RodasNodeArgs args;
     cudaKernelNodeParams kp;
@@ -1115,6 +1116,7 @@ int bolt_engine_create(const bolt_engine_cfg* cfg, bolt_engine** out) {
   std::unique_ptr<bolt_engine> E(new bolt_engine());
   if (cfg) E->cfg = *cfg;
   if (E->cfg.objective != 0 && E->cfg.objective != 1) return -1;
+  if (E->cfg.land_stride < 0 || E->cfg.land_stride > 64) return -1;
   E->device = E->cfg.device;
   if (E->cfg.lanes <= 0) E->cfg.lanes = 2;
   if (E->cfg.lanes > 8) E->cfg.lanes = 8;

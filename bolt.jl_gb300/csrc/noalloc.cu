@@ -196,6 +196,7 @@ extern "C" int bolt_source_grid_static(const bolt_params* par, const bolt_grid* 
   cfg.h0 = 1e-3;
   cfg.x_dense = -8.5;
   cfg.max_steps = 10000000;
+  cfg.land_stride = 1;
   const int Lmax = hier->lg > hier->lnu ? (hier->lg > hier->lmnu ? hier->lg : hier->lmnu)
                                         : (hier->lnu > hier->lmnu ? hier->lnu : hier->lmnu);
   int blocks = 0;

@@ -686,8 +686,12 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       break;
     }
     // next landing target: the first node at or above x_dense strictly past x
+    // whose index from the first such node is a multiple of the stride (or
+    // the last node); nodes passed on the way come from dense output
     int jt = max(jo, jd);
     while (jt < md.nout && md.xout[jt] <= x) ++jt;
+    if (dense_ok && cfg.land_stride > 1)
+      while (jt < md.nout - 1 && (jt - jd) % cfg.land_stride != 0) ++jt;
     double target = jt < md.nout ? md.xout[jt] : xend;
     bool landing = false;
     double hs = h;
@@ -716,7 +720,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     double* K0 = G.K;
     if (x != x_done) {
       // outputs that fall on this abscissa or inside the last accepted step
-      if (dense_ok && have_prev && jo < jd) {
+      if (dense_ok && have_prev && jo < md.nout && md.xout[jo] < x) {
         copy_vec(N, S.b, K0, tid, nth);  // f at x, kept while interpolating
         __syncthreads();
         while (jo < md.nout && md.xout[jo] < x) {

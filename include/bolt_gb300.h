@@ -244,6 +244,9 @@ typedef struct {
   int objective;         /* autotuner: 0 = latency-aware (a launch onto an idle GPU with nothing
                             waiting gets the variant fastest for that launch alone), 1 = throughput
                             (every launch is costed as part of a full GPU) */
+  int land_stride;       /* source grids: the solver lands on every land_stride-th x node at x >= -8.5
+                            (and the last) and takes the others from cubic Hermite dense output, as it
+                            does below -8.5 (0 or 1 = lands on every node there; at most 64) */
 } bolt_engine_cfg;
 
 typedef struct bolt_engine bolt_engine;

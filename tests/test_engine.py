@@ -270,3 +270,22 @@ def test_cl_request_with_plin():
     # two solves with different step sequences at abstol 3e-7: ~1e-5 apart at the lowest k
     assert np.max(np.abs(a.plin / p.plin - 1)) < 1e-4
     assert np.max(np.abs(a.dplin[4] * par.A / a.plin - 1)) < 1e-12
+
+
+def test_land_stride_changes_cl_by_the_interpolation_error_only():
+    """land_stride = 2 (every other x node at x >= -8.5 from dense output):
+    fewer steps, C_l within the cubic interpolation error of landing on
+    every node."""
+    par = _par(h=0.67)
+    ks = _ks(par, nk=48, kmax_h0=400.0)
+    ells = np.arange(2, 1200, 11, dtype=np.int32)
+    out = {}
+    for stride in (1, 2):
+        with B.Engine(lanes=1, land_stride=stride) as eng:
+            out[stride] = eng.run(B.Request("cl", par, ks, hier=HIER, ells=ells, cl=("tt", "ee")))
+        assert out[stride].rc == 0, out[stride].err
+    assert out[2].steps < out[1].steps
+    for c in ("tt", "ee"):
+        assert _rel(out[2].cl[c], out[1].cl[c]) < 1e-5
+    with pytest.raises(RuntimeError):
+        B.Engine(land_stride=65)
