@@ -93,3 +93,17 @@ def test_ctypes_structs_match_header_layout(tmp_path):
         assert C.sizeof(py) == got[(cname, "size")], cname
         for f in structs[cname]:
             assert getattr(py, f).offset == got[(cname, f)], (cname, f)
+
+
+def test_engine_config_validation_without_gpu():
+    """bolt_engine_create rejects an invalid objective or landing stride
+    before it touches the device."""
+    _build.build()
+    lib = _lib.load()
+    for bad in ({"objective": 2}, {"objective": -1}, {"land_stride": 65}, {"land_stride": -1}):
+        cfg = _lib.BoltEngineCfg(0, 2, 0, 0, 150.0, 0, 0, 0.0, 0, 1)
+        for k, v in bad.items():
+            setattr(cfg, k, v)
+        h = C.c_void_p()
+        assert lib.bolt_engine_create(C.byref(cfg), C.byref(h)) == -1, bad
+        assert not h.value
