@@ -325,7 +325,6 @@ struct Lane {
   int key[2] = {0, 0};   // tuner key of each phase (own modes, or the whole load when shared)
   bool shared[2] = {false, false};
   int nlaunch = 0;
-  std::vector<int> los_flags_dummy;
 };
 
 }  // namespace
@@ -493,7 +492,7 @@ void set_done(bolt_engine* E, Req* r, int s, const std::string& err) {
   }
 }
 
-Graph& lane_graph(bolt_engine* E, Lane& L, int wpm, int phase, const cudaKernelNodeParams& kp) {
+Graph& lane_graph(Lane& L, int wpm, int phase, const cudaKernelNodeParams& kp) {
   const int v = wpm == 1 ? 0 : (wpm == 2 ? 1 : 2);
   Graph& G = L.graph[v][phase];
   if (!G.exec) {
@@ -513,7 +512,6 @@ Graph& lane_graph(bolt_engine* E, Lane& L, int wpm, int phase, const cudaKernelN
   } else {
     ck(cudaGraphExecKernelNodeSetParams(G.exec, G.knode, &kp), "cudaGraphExecKernelNodeSetParams");
   }
-  (void)E;
   return G;
 }
 
@@ -785,7 +783,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     cudaKernelNodeParams kp;
     rodas_node_params(wpm[ph], d_modes + (ph ? m1 : 0), nmodes[ph], d_cos, cfg, L.d_queue + ph, maxN, maxnq, maxL,
                       blocks[ph], d_scr, &args, &kp);
-    Graph& G = lane_graph(E, L, wpm[ph], ph, kp);
+    Graph& G = lane_graph(L, wpm[ph], ph, kp);
     ck(cudaGraphLaunch(G.exec, st), "cudaGraphLaunch");
     L.wpm[ph] = wpm[ph];
     L.nmodes[ph] = nmodes[ph];
@@ -870,7 +868,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
 }
 
 // Outputs of one request from the lane's download area (lock held).
-void finalize_request(bolt_engine* E, Lane& L, Req* r) {
+void finalize_request(Lane& L, Req* r) {
   const char* down = static_cast<const char*>(L.down.p);
   const int nk = r->r.nk, ns = r->nsets;
   const int32_t* st = reinterpret_cast<const int32_t*>(down + r->h_stat);
@@ -928,7 +926,6 @@ void finalize_request(bolt_engine* E, Lane& L, Req* r) {
       }
     }
   }
-  (void)E;
 }
 
 void finish_lane(bolt_engine* E, Lane& L) {
@@ -953,7 +950,7 @@ void finish_lane(bolt_engine* E, Lane& L) {
   if (L.nmodes[1] > 0) E->tuner.update(L.shared[1], L.key[1], L.wpm[1], ms2 * 1e-3, steps[1]);
   const double t = now_s(E->t0);
   for (Req* r : L.batch) {
-    finalize_request(E, L, r);
+    finalize_request(L, r);
     r->state = 3;
     r->t[3] = t;
     E->inflight_bytes -= r->bytes;

@@ -478,8 +478,6 @@ struct Rf {
         Cft = Cft / (Rutr + Cft);
       }
     }
-    double tTh = (1.0 / (CT * std::pow(Trad, 4))) * (1 + x + fHe) / x;
-    double tH = 2.0 / (3.0 * HO * std::pow(zp, 1.5));
     double f1;
     if (br & 8) f1 = 0.0;
     else if (br & 16) f1 = (x * xH * n * Rdown - Rup * (1 - xH) * std::exp(-CL / Tm)) / (Hz * zp);
