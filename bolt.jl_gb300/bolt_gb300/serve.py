@@ -130,7 +130,7 @@ class _Pending:
 class Engine:
     """Native batching / serving engine on one GPU (bolt_engine_*)."""
 
-    def __init__(self, device: int = 0, lanes: int = 2, host_threads: int = 0, max_batch: int = 0,
+    def __init__(self, device: int = 0, lanes: int = 6, host_threads: int = 0, max_batch: int = 0,
                  mem_budget_gb: float = 150.0, warps_per_mode: int = 0, max_steps: int = 0,
                  batch_window_s: float = 0.0, objective: str = "latency", land_stride: int = 1):
         if objective not in ("latency", "throughput"):

@@ -235,7 +235,13 @@ void run_solver(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h
   cfg.max_steps = c->max_steps;
   cfg.land_stride = 1;
   int Lmax = std::max(h->lg, std::max(h->lnu, h->lmnu));
-  const int wpb = c->wpb;  // warps per mode (0: four)
+  // warps per mode: 0 chooses by the launch size alone, one warp per mode
+  // from about 20 modes per SM (where the FP64 issue rate, not the longest
+  // mode's chain of dependent steps, bounds a launch; measured at N = 473),
+  // else four
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+  const int wpb = c->wpb != 0 ? c->wpb : (nk >= 20 * std::max(nsm, 1) ? 1 : 4);
   size_t pw = rodas_smem_per_mode(N, h->nq, Lmax, wpb);  // shared memory of one mode (one CTA)
   if (pw > 227 * 1024) throw Err(-1, "hierarchy too large for shared memory");
   int blocks = 0;

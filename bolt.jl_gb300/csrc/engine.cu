@@ -1115,7 +1115,7 @@ int bolt_engine_create(const bolt_engine_cfg* cfg, bolt_engine** out) {
   if (E->cfg.objective != 0 && E->cfg.objective != 1) return -1;
   if (E->cfg.land_stride < 0 || E->cfg.land_stride > 64) return -1;
   E->device = E->cfg.device;
-  if (E->cfg.lanes <= 0) E->cfg.lanes = 2;
+  if (E->cfg.lanes <= 0) E->cfg.lanes = 6;
   if (E->cfg.lanes > 8) E->cfg.lanes = 8;
   if (E->cfg.max_steps <= 0) E->cfg.max_steps = 100000;  // OrdinaryDiffEq's default maxiters
   E->budget = size_t((E->cfg.mem_budget_gb > 0 ? E->cfg.mem_budget_gb : 150.0) * 1073741824.0);

@@ -47,7 +47,8 @@ typedef struct {
 
 typedef struct {
   int device;          /* CUDA device ordinal */
-  int warps_per_block; /* solver CTA size in warps (0 = autotune) */
+  int warps_per_block; /* warps per k-mode in the solver, 1, 2 or 4 (0 = by launch size: one from
+                          about 20 modes per SM, else four) */
   long long max_steps; /* per mode (0 = 10^5, OrdinaryDiffEq's default maxiters) */
 } bolt_opts;
 
@@ -233,7 +234,7 @@ typedef struct {
 
 typedef struct {
   int device;
-  int lanes;             /* batches in flight on separate streams (0 = 2) */
+  int lanes;             /* batches in flight on separate streams (0 = 6; at most 8) */
   int host_threads;      /* table-building threads (0 = hardware threads) */
   int max_batch;         /* requests per batch (0 = unlimited; 1 = one request per batch) */
   double mem_budget_gb;  /* device memory admitted to in-flight requests (0 = 150) */
