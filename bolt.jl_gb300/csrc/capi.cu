@@ -280,9 +280,18 @@ std::vector<double> quadratic_k(double kmin, double kmax, int nk) {  // spectra.
   return out;
 }
 
-// LOS on device source grids (d_ST, d_SE: [nk][nx]).
-void run_los(bolt_ctx* c, int id, const double* d_ST, const double* d_SE, const double* k, int nk, const int* ells,
-             int nell, double* tt, double* te, double* ee) {
+// First x node the line-of-sight sums use: findfirst(x_grid .> -8)
+// (spectra.jl:86).
+int los_first_node(const GridSpec& g) {
+  int i0 = 0;
+  while (i0 < g.n && !(g.at(i0) > -8.0)) ++i0;
+  return i0;
+}
+
+// LOS on device source grids (d_ST, d_SE: [nk][nx - src_from], x nodes
+// src_from .. nx-1; src_from <= los_first_node).
+void run_los(bolt_ctx* c, int id, const double* d_ST, const double* d_SE, int src_from, const double* k, int nk,
+             const int* ells, int nell, double* tt, double* te, double* ee) {
   CosmoEntry& e = get_cosmo(c, id);
   const CosmoTables& T = e.T;
   const GridSpec& g = T.grid;
@@ -312,10 +321,10 @@ void run_los(bolt_ctx* c, int id, const double* d_ST, const double* d_SE, const 
   double argmax = kd[nkd - 1] * T.eta0;
   double dg = argmax / 5000.0;
   double inv_dg = 1.0 / dg;
-  int i0 = 0;
-  while (i0 < nx && !(g.at(i0) > -8.0)) ++i0;
+  const int i0 = los_first_node(g);
   const int nrow = nx - 1 - i0;
   if (nrow <= 0) throw Err(-1, "x grid does not reach x > -8");
+  if (src_from < 0 || src_from > i0) throw Err(-1, "source grid starts past the first x > -8");
   std::vector<double> yv(nrow), dxs(nrow);
   for (int i = 0; i < nrow; ++i) {
     double x = g.at(i0 + i);
@@ -356,7 +365,8 @@ void run_los(bolt_ctx* c, int id, const double* d_ST, const double* d_SE, const 
   ck(cudaEventRecord(c->ev[2], st), "event");
   int rc = launch_jl_raw(nb, d_dg, 1, Lmax, d_sl, ns, d_raw, d_norm, d_flags, st);
   if (!rc) rc = launch_jl_prefilter(nb, ns, 1, d_raw, d_norm, d_w, d_coef, st);
-  if (!rc) rc = launch_sdense(nx, i0, nrow, nk, d_kg, d_ST, d_SE, nm, d_kmid, d_dx, d_SdT, d_SdE, st);
+  if (!rc)
+    rc = launch_sdense(nx - src_from, i0 - src_from, nrow, nk, d_kg, d_ST, d_SE, nm, d_kmid, d_dx, d_SdT, d_SdE, st);
   if (rc) throw Err(-3, std::string("LOS launch: ") + cudaGetErrorString(cudaError_t(rc)));
   LosArgs a;
   a.nb = nb; a.nslots = ns; a.nrow = nrow; a.nm = nm;
@@ -657,19 +667,21 @@ int bolt_boltsolve_rsa(bolt_ctx* c, int id, const double* k, int nk, const bolt_
   });
 }
 
-// The polarization source is emitted only when want_E is set (*d_SE is null
-// otherwise): TT-only calls skip its stores and the E half of the projection.
+// Sources on the x nodes from .. n-1 ([nk][n - from]).  The polarization
+// source is emitted only when want_E is set (*d_SE is null otherwise):
+// TT-only calls skip its stores and the E half of the projection.
 static void source_grid_device(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h, double reltol,
-                               double abstol, bool want_E, double** d_ST, double** d_SE, int32_t* status) {
+                               double abstol, bool want_E, int from, double** d_ST, double** d_SE, int32_t* status) {
   CosmoEntry& e = get_cosmo(c, id);
   const GridSpec& g = e.T.grid;
-  std::vector<double> xs(g.n);
-  for (int j = 0; j < g.n; ++j) xs[j] = g.at(j);
-  double* d_x = c->xout.as<double>(g.n);
-  *d_ST = c->srcT.as<double>(size_t(nk) * g.n);
-  *d_SE = want_E ? c->srcE.as<double>(size_t(nk) * g.n) : nullptr;
-  ck(cudaMemcpyAsync(d_x, xs.data(), g.n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "x grid");
-  run_solver(c, id, k, nk, h, reltol, abstol, d_x, g.n, MODE_SOURCES, *d_ST, *d_SE, nullptr, nullptr, status);
+  const int nout = g.n - from;
+  std::vector<double> xs(nout);
+  for (int j = 0; j < nout; ++j) xs[j] = g.at(from + j);
+  double* d_x = c->xout.as<double>(nout);
+  *d_ST = c->srcT.as<double>(size_t(nk) * nout);
+  *d_SE = want_E ? c->srcE.as<double>(size_t(nk) * nout) : nullptr;
+  ck(cudaMemcpyAsync(d_x, xs.data(), nout * sizeof(double), cudaMemcpyHostToDevice, c->stream), "x grid");
+  run_solver(c, id, k, nk, h, reltol, abstol, d_x, nout, MODE_SOURCES, *d_ST, *d_SE, nullptr, nullptr, status);
 }
 
 int bolt_source_grid(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h, double reltol, double abstol,
@@ -677,7 +689,7 @@ int bolt_source_grid(bolt_ctx* c, int id, const double* k, int nk, const bolt_hi
   return guard(c, [&] {
     if (!k || !S_T) throw Err(-1, "null argument");
     double *d_ST, *d_SE;
-    source_grid_device(c, id, k, nk, h, reltol, abstol, S_E != nullptr, &d_ST, &d_SE, status);
+    source_grid_device(c, id, k, nk, h, reltol, abstol, S_E != nullptr, 0, &d_ST, &d_SE, status);
     const int n = get_cosmo(c, id).T.grid.n;
     ck(cudaMemcpyAsync(S_T, d_ST, size_t(nk) * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "S_T");
     if (S_E) ck(cudaMemcpyAsync(S_E, d_SE, size_t(nk) * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "S_E");
@@ -694,7 +706,7 @@ int bolt_cl(bolt_ctx* c, int id, const double* S_T, const double* S_E, const dou
     double* d_SE = S_E ? c->srcE.as<double>(size_t(nk) * n) : nullptr;
     ck(cudaMemcpyAsync(d_ST, S_T, size_t(nk) * n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "S_T");
     if (S_E) ck(cudaMemcpyAsync(d_SE, S_E, size_t(nk) * n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "S_E");
-    run_los(c, id, d_ST, d_SE, k, nk, ells, nell, tt, te, ee);
+    run_los(c, id, d_ST, d_SE, 0, k, nk, ells, nell, tt, te, ee);
   });
 }
 
@@ -703,8 +715,11 @@ int bolt_cl_pipeline(bolt_ctx* c, int id, const double* k, int nk, const bolt_hi
   return guard(c, [&] {
     if (!k || !ells) throw Err(-1, "null argument");
     double *d_ST, *d_SE;
-    source_grid_device(c, id, k, nk, h, reltol, abstol, te || ee, &d_ST, &d_SE, status);
-    run_los(c, id, d_ST, d_SE, k, nk, ells, nell, tt, te, ee);
+    // the projection reads the sources at x > -8 only: the solve emits no
+    // others (no dense output below, no landing on the nodes in between)
+    const int from = los_first_node(get_cosmo(c, id).T.grid);
+    source_grid_device(c, id, k, nk, h, reltol, abstol, te || ee, from, &d_ST, &d_SE, status);
+    run_los(c, id, d_ST, d_SE, from, k, nk, ells, nell, tt, te, ee);
   });
 }
 

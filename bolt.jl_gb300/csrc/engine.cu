@@ -230,6 +230,7 @@ struct Req {
   bool wantE = false;
   bool wantP = false;        // P_lin at x = grid end (BOLT_REQ_PLIN, or a C_l request with plin set)
   int rec_cap = 0;           // recorded steps per mode (gradient requests)
+  int src_from = 0;          // C_l: first x node with sources, findfirst(x_grid .> -8) (spectra.jl:86)
   bool los_tangent = false;  // C_l^TT gradient from the tangent of the LOS integral
 };
 
@@ -415,7 +416,7 @@ void layout_request(Req* r, size_t& off) {
   size_t start = off;
   off = align_up(off + size_t(ns) * tabd * 8);  // tables of every set
   r->o_xout = off;
-  off = align_up(off + size_t(r->r.kind == BOLT_REQ_CL ? n : 1) * 8);
+  off = align_up(off + size_t(r->r.kind == BOLT_REQ_CL ? n - r->src_from : 1) * 8);
   r->o_stat = off;
   off = align_up(off + size_t(ns) * nk * 4);
   r->o_cnt = off;
@@ -424,7 +425,7 @@ void layout_request(Req* r, size_t& off) {
   if (r->nsets > 1) off = align_up(off + size_t(nk) * r->rec_cap * 8);
   if (r->r.kind == BOLT_REQ_CL) {
     r->o_src = off;
-    off = align_up(off + size_t(ns) * nk * n * 8 * (r->wantE ? 2 : 1));
+    off = align_up(off + size_t(ns) * nk * (n - r->src_from) * 8 * (r->wantE ? 2 : 1));
     r->o_cl = off;
     off = align_up(off + size_t(ns) * 3 * r->uniq.size() * 8);
     r->o_los = off;  // k grid, kmid, dx, slots, ells, inv_dg, per-set wts and y
@@ -597,7 +598,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     Req* r = batch[b];
     starts[b] = req_start;
     seg_tab[b] = seg(req_start, size_t(r->nsets) * cosmo_table_doubles(r->T[0]) * 8);
-    seg_x[b] = seg(r->o_xout, size_t(r->r.kind == BOLT_REQ_CL ? r->grid.n : 1) * 8);
+    seg_x[b] = seg(r->o_xout, size_t(r->r.kind == BOLT_REQ_CL ? r->grid.n - r->src_from : 1) * 8);
     if (r->r.kind == BOLT_REQ_CL) {
       const int nm = kNkd - 1, n = r->grid.n, ns = int(r->uniq.size());
       size_t head = align_up(size_t(r->r.nk + nm + n + 8) * 8 + size_t(r->uniq.back() + 1 + ns) * 4);
@@ -635,7 +636,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   modes2.reserve(m2);
   for (size_t b = 0; b < batch.size(); ++b) {
     Req* r = batch[b];
-    const int nk = r->r.nk, ns = r->nsets, n = r->grid.n;
+    const int nk = r->r.nk, ns = r->nsets, nsrc = r->grid.n - r->src_from;
     const size_t tabd = cosmo_table_doubles(r->T[0]);
     for (int s = 0; s < ns; ++s) {
       double* h_tab = reinterpret_cast<double*>(up + segs[seg_tab[b]].host + size_t(s) * tabd * 8);
@@ -645,9 +646,9 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     double* hx = reinterpret_cast<double*>(up + segs[seg_x[b]].host);
     const double* dx = reinterpret_cast<const double*>(dev + r->o_xout);
     int nout;
-    if (r->r.kind == BOLT_REQ_CL) {
-      for (int j = 0; j < n; ++j) hx[j] = r->grid.at(j);
-      nout = n;
+    if (r->r.kind == BOLT_REQ_CL) {  // the nodes the line of sight reads, x > -8
+      for (int j = 0; j < nsrc; ++j) hx[j] = r->grid.at(r->src_from + j);
+      nout = nsrc;
     } else {
       hx[0] = r->r.plin_x;
       nout = 1;
@@ -667,8 +668,8 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
         if (r->r.kind == BOLT_REQ_CL) {
           double* src = reinterpret_cast<double*>(dev + r->o_src);
           m.flags = MODE_SOURCES;
-          m.src_T = src + (size_t(s) * nk + i) * n;
-          m.src_E = r->wantE ? src + size_t(ns) * nk * n + (size_t(s) * nk + i) * n : nullptr;
+          m.src_T = src + (size_t(s) * nk + i) * nsrc;
+          m.src_E = r->wantE ? src + size_t(ns) * nk * nsrc + (size_t(s) * nk + i) * nsrc : nullptr;
         }
         if (r->wantP) {  // at the last node: plin_x, or the end of the x grid for a C_l request
           m.flags |= MODE_PLIN;
@@ -796,7 +797,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   }
   for (auto& P : plans) {
     Req* r = P.r;
-    const int n = r->grid.n, nk = r->r.nk;
+    const int n = r->grid.n, nk = r->r.nk, nsrc = n - r->src_from, i0s = P.i0 - r->src_from;
     char* lb = dev + r->o_los;
     const double* kg = reinterpret_cast<const double*>(lb);
     const double* kmid = kg + nk;
@@ -812,14 +813,14 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     const double* src = reinterpret_cast<const double*>(dev + r->o_src);
     double* cl = reinterpret_cast<double*>(dev + r->o_cl);
     if (r->los_tangent) {
-      rc = launch_sdense(n, P.i0, P.nrow, nk, kg, src, nullptr, P.nm, kmid, dxs, SdT, nullptr, st);
+      rc = launch_sdense(nsrc, i0s, P.nrow, nk, kg, src, nullptr, P.nm, kmid, dxs, SdT, nullptr, st);
       for (int j = 0; j < kTheta && rc == 0; ++j) {
         if (solve_free(j)) {  // the sources do not depend on theta_j
           rc = int(cudaMemsetAsync(dSd + size_t(j) * P.nrow * P.nm, 0, size_t(P.nrow) * P.nm * 8, st));
           continue;
         }
-        rc = launch_sdense_diff(n, P.i0, P.nrow, nk, kg, src + size_t(1 + j) * nk * n, src, 1.0 / r->step[j], P.nm,
-                                kmid, dxs, dSd + size_t(j) * P.nrow * P.nm, st);
+        rc = launch_sdense_diff(nsrc, i0s, P.nrow, nk, kg, src + size_t(1 + j) * nk * nsrc, src, 1.0 / r->step[j],
+                                P.nm, kmid, dxs, dSd + size_t(j) * P.nrow * P.nm, st);
       }
       if (rc != 0) throw EngErr(-3, std::string("source resampling: ") + cudaGetErrorString(cudaError_t(rc)));
       LosGradArgs a;
@@ -834,9 +835,9 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     }
     for (int s = 0; s < r->nsets; ++s) {
       const int ss = skips_solve(r->nsets, s) ? 0 : s;  // parameter set whose sources hold for set s
-      const double* ST = src + size_t(ss) * nk * n;
-      const double* SE = r->wantE ? src + size_t(r->nsets) * nk * n + size_t(ss) * nk * n : nullptr;
-      rc = launch_sdense(n, P.i0, P.nrow, nk, kg, ST, SE, P.nm, kmid, dxs, SdT, SE ? SdE : nullptr, st);
+      const double* ST = src + size_t(ss) * nk * nsrc;
+      const double* SE = r->wantE ? src + size_t(r->nsets) * nk * nsrc + size_t(ss) * nk * nsrc : nullptr;
+      rc = launch_sdense(nsrc, i0s, P.nrow, nk, kg, ST, SE, P.nm, kmid, dxs, SdT, SE ? SdE : nullptr, st);
       if (rc != 0) throw EngErr(-3, std::string("source resampling: ") + cudaGetErrorString(cudaError_t(rc)));
       const double* wts = per + size_t(s) * (P.nm + n);
       LosArgs a;
@@ -1214,7 +1215,10 @@ int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
     }
     r->grid = make_grid(q->grid.start, q->grid.step, q->grid.stop);
     if (r->grid.n < 4 || r->grid.n > 100000) throw EngErr(-1, "x grid needs 4..100000 nodes");
-    if (q->kind == BOLT_REQ_CL && !(r->grid.at(r->grid.n - 1) > -8.0)) throw EngErr(-1, "x grid does not reach x > -8");
+    if (q->kind == BOLT_REQ_CL) {
+      if (!(r->grid.at(r->grid.n - 2) > -8.0)) throw EngErr(-1, "x grid needs two nodes at x > -8");
+      while (!(r->grid.at(r->src_from) > -8.0)) ++r->src_from;
+    }
     const bolt_hier& h = q->hier;
     r->N = 2 * (h.lg + 1) + (h.lnu + 1) + (h.lmnu + 1) * h.nq + 5;
     const size_t smem = rodas_smem_per_mode(r->N, h.nq, std::max(h.lg, std::max(h.lnu, h.lmnu)), 4);
