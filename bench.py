@@ -618,7 +618,7 @@ def run_pipeline(args):
     ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg, ctx=ctx)
     ks = B.log10_k(0.1 * bg.H0, args.kmax_h0 * bg.H0, args.nk)
     ells = np.arange(2, args.lmax + 1, dtype=np.int32)
-    hier = (50, 50, 20, 15)
+    hier = (args.lg, args.lg, args.lmnu, 15)
     N = B.state_len(*hier)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
@@ -651,8 +651,8 @@ def run_pipeline(args):
                "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                "config": {"workload": f"full CMB pipeline: fiducial LCDM, {ks.size} log k in "
-                                      f"[0.1,{args.kmax_h0:g}]H0, l 50/50/20, nq 15 (N={N}), S_T/S_E on 2001 x "
-                                      f"nodes, C_l TT/TE/EE l=2..{args.lmax}", "reltol": RELTOL, "abstol": ABSTOL,
+                                      f"[0.1,{args.kmax_h0:g}]H0, l {args.lg}/{args.lg}/{args.lmnu}, nq 15 (N={N}), "
+                                      f"S_T/S_E on the x nodes > -8, C_l TT/TE/EE l=2..{args.lmax}", "reltol": RELTOL, "abstol": ABSTOL,
                           "l2": "flushed (256 MB write) between steps", "parallelism": f"replicas x{ws}"},
                "clocks": clocks, "gpu_launches": launches,
                "roofline": {"bound": "fp64", "achieved": sol, "peak": peak, "unit": "TFLOP/s",
@@ -685,7 +685,10 @@ def main():
     ap.add_argument("--nk", type=int, default=1200, help="pipeline: source-grid wavenumbers")
     ap.add_argument("--kmax-h0", type=float, default=5000.0, help="pipeline: largest wavenumber in units of H0")
     ap.add_argument("--lmax", type=int, default=2500, help="pipeline: largest multipole")
-    ap.add_argument("--warps-per-mode", type=int, default=0, help="pipeline: solver warps per mode (0: four)")
+    ap.add_argument("--warps-per-mode", type=int, default=0,
+                    help="pipeline: solver warps per mode (0: by launch size)")
+    ap.add_argument("--lg", type=int, default=50, help="pipeline: l_gamma = l_nu of the hierarchy")
+    ap.add_argument("--lmnu", type=int, default=20, help="pipeline: l_mnu of the hierarchy")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
