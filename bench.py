@@ -408,7 +408,8 @@ def run_serving(args):
                "plain_engine": len(gstream) / sum(g_plain), "served_over_plain_engine": sum(g_plain) / g_win,
                "unit": UNIT, "requests": len(gstream),
                "p50_s": float(np.percentile(g_lat, 50)), "p99_s": float(np.percentile(g_lat, 99)),
-               "workload": "C_l^TT l<=2000 + 6-parameter Jacobian, cfg-3 box draws, 64-1024 log k in [0.1,1000] H0, "
+               "workload": "C_l^TT l<=2000 + 6-parameter Jacobian, draws from the serving box, 64-1024 log k in "
+                           "[0.1,1000] H0, "
                            "l_gamma=l_nu in {20,35,50}; served: all submitted at once; plain: drop-in, 7 calls "
                            "per request (forward differences); plain_engine: the engine one request per call "
                            "(7 parameter sets batched in one launch, tangent LOS)"}
@@ -504,10 +505,10 @@ def run_reference(args):
 
 # ------------------------------------------------------ batch / gradients --
 def cosmology_requests(workload, n, seed_offset):
-    """cfg 3 (batch): per cosmology one C_l^TT (l <= 2000) request on its own
-    64-1024 log k in [0.1, 1000] H0 with l_gamma = l_nu in {20, 35, 50},
-    l_mnu 10, returning P_lin(k) at x = 0 from the same solve.  cfg 4
-    (grad): per cosmology the C_l^TT Jacobian (same draw) and the P_lin
+    """Batch workload: per cosmology one C_l^TT (l <= 2000) request on its
+    own 64-1024 log k in [0.1, 1000] H0 with l_gamma = l_nu in {20, 35, 50},
+    l_mnu 10, returning P_lin(k) at x = 0 from the same solve.  Gradient
+    workload: per cosmology the C_l^TT Jacobian (same draw) and the P_lin
     Jacobian on 200 log k in [1e-4, 1] h/Mpc (l 50/50/20)."""
     rng = np.random.default_rng(SEED + seed_offset)
     out = []
@@ -549,9 +550,9 @@ def batch_dropin(B, ctx, d):
 
 
 def run_batch(args):
-    """cfg 3 / cfg 4: every request of K cosmologies submitted at once to the
-    engine (6 lanes, objective throughput) against the plain drop-in one
-    cosmology per call; cosmologies per second."""
+    """Batch / gradient workloads: every request of K cosmologies submitted
+    at once to the engine (6 lanes, objective throughput) against the plain
+    drop-in one cosmology per call; cosmologies per second."""
     import torch
     torch.cuda.set_device(0)
     import bolt_gb300 as B
@@ -579,13 +580,13 @@ def run_batch(args):
     e2e = max(r.times[3] for r in res) - min(r.times[0] for r in res)
     flops = sum(r.steps * solver_flops_per_step(state_len(*d["hier"]), d["hier"][3]) for r, d in zip(res, reqs))
     peak = ctypes_peak(B._lib.load(), 0)
-    what = ("cfg 3 batch: C_l^TT (l 2..2000) + P_lin(k) at x = 0 per cosmology, one solve each"
+    what = ("batch: C_l^TT (l 2..2000) + P_lin(k) at x = 0 per cosmology, one solve each"
             if args.workload == "batch" else
-            "cfg 4 gradients: 6-parameter Jacobians of C_l^TT (l 2..2000) and of P_lin (200 log k in [1e-4,1] h/Mpc)")
+            "gradients: 6-parameter Jacobians of C_l^TT (l 2..2000) and of P_lin (200 log k in [1e-4,1] h/Mpc)")
     out = {"metric": f"{what}: cosmologies/s on 1 GB300 (served vs plain drop-in)", "value": K / win,
            "unit": "cosmologies/s", "n_gpus": 1, "steps": K, "warmup": len(warm), "ms_per_step": 1000.0 * win / K,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": what + "; cosmologies from the cfg-3 box, 64-1024 log k in [0.1,1000] H0, "
+           "config": {"workload": what + "; cosmologies from the box h 0.6-0.8, omega_b 0.019-0.025, omega_c 0.10-0.14, n_s 0.92-1.0, ln(1e10 A_s) 2.9-3.2, Sigma m_nu 0-0.3 eV, 64-1024 log k in [0.1,1000] H0, "
                                          "l_gamma = l_nu in {20,35,50}, l_mnu 10, nq 15; all submitted at once",
                       "reltol": RELTOL, "abstol": ABSTOL},
            "plain": {"value": K / plain_s, "unit": "cosmologies/s", "calls": calls,
