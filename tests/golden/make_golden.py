@@ -35,6 +35,7 @@ def main(ref):
     camb = np.loadtxt(os.path.join(data, "camb_rough_ttteee_unlensed.dat"))
     np.savez_compressed(os.path.join(HERE, "camb_rough.npz"), ell=camb[0][:2600], tt=camb[1][:2600],
                         te=camb[2][:2600], ee=camb[3][:2600])
+    camb_pk(data)
     # spherical Bessel j_l(x) known answers from mpmath (50 digits)
     import mpmath as mp
     mp.mp.dps = 50
@@ -47,6 +48,15 @@ def main(ref):
             v = mp.sqrt(mp.pi / (2 * mp.mpf(x))) * mp.besselj(int(l) + mp.mpf(1) / 2, mp.mpf(x))
             vals[i, j] = float(v) if abs(v) > mp.mpf("1e-300") else 0.0
     np.savez_compressed(os.path.join(HERE, "sph_bessel_mpmath.npz"), ell=ls, x=xs, j=vals)
+
+
+def camb_pk(data):
+    """CAMB linear P(k) at z = 0 (test/data/camb_pk_x0.dat: k in h/Mpc, P in
+    (Mpc/h)^3), made by test/camb_v_class_2022.ipynb for h 0.7, Omega_r
+    5.042e-5, Omega_b 0.046, Omega_c 0.224, n_s 1.0, Y_p 0.24, N_eff 3.046,
+    Sigma m_nu 0.06 eV, A_s = exp(3.043) 1e-10; every 10th of its 1000 k."""
+    d = np.loadtxt(os.path.join(data, "camb_pk_x0.dat"))
+    np.savez_compressed(os.path.join(HERE, "camb_pk_x0.npz"), k_hMpc=d[0][::10], pk=d[1][::10])
 
 
 if __name__ == "__main__":

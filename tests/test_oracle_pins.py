@@ -4,7 +4,10 @@ Reference tests restated (Bolt.jl test/runtests.jl):
   RECFAST Xe(z) vs Fortran RECFAST, 1e-4 absolute          (runtests.jl:38-48)
   Phi, delta_b at k = 0.03 h/Mpc vs CLASS, 1e-3 relative   (runtests.jl:83-147)
   C_l^TT, C_l^EE vs CAMB, 1.1e-1 relative                   (runtests.jl:149-185)
-plus j_l(x) against mpmath and the exactness of the Jacobian split.
+plus j_l(x) against mpmath, the exactness of the Jacobian split, and P_lin at
+z = 0 against the CAMB linear P(k) in the reference's test data
+(test/data/camb_pk_x0.dat, made by test/camb_v_class_2022.ipynb; the
+reference compares the two by eye in scripts/first_plin.jl), 3e-3 relative.
 """
 import os
 
@@ -84,3 +87,20 @@ def test_cl_vs_camb():
     fac = ells * (ells + 1) / (2 * np.pi)
     assert np.all(np.abs(fac * tt / np.interp(ells, g["ell"], g["tt"]) - 1) < 1.1e-1)
     assert np.all(np.abs(fac * ee / np.interp(ells, g["ell"], g["ee"]) - 1) < 1.1e-1)
+
+
+def test_plin_vs_camb():
+    """P_lin(k) at z = 0 against CAMB for the notebook's cosmology (Bolt's
+    defaults with Omega_r 5.042e-5, n_s 1, ln(1e10 A_s) 3.043): within 0.1 %
+    from 1e-3 to 0.5 h/Mpc, pinned at 3e-3."""
+    from concurrent.futures import ThreadPoolExecutor
+    g = np.load(os.path.join(GOLDEN, "camb_pk_x0.npz"))
+    p = O.Params(Omega_r=5.042e-5, A=1e-10 * np.exp(3.043), n=1.0)
+    c = O.Cosmo(p)
+    # fixture nodes near 1e-3, 1e-2, 0.05, 0.2 and 0.5 h/Mpc (no interpolation across the BAO wiggles)
+    idx = [int(np.argmin(np.abs(np.log(g["k_hMpc"] / t)))) for t in (1e-3, 1e-2, 0.05, 0.2, 0.5)]
+    khs, camb = g["k_hMpc"][idx], g["pk"][idx]
+    with ThreadPoolExecutor(len(khs)) as ex:
+        P = np.array(list(ex.map(lambda kh: c.plin(kh * p.h, lg=50, lnu=50, lmnu=20, reltol=1e-8, abstol=1e-8),
+                                 khs)))
+    assert np.all(np.abs(P * p.h ** 3 / camb - 1) < 3e-3), P * p.h ** 3 / camb
