@@ -49,7 +49,7 @@ class BoltError(RuntimeError):
 
 
 STATUS_NAMES = {0: "ok", 1: "max iterations", 2: "step underflow", 3: "non-finite state",
-                4: "singular step matrix", 5: "bad input"}
+                4: "singular step matrix", 5: "bad input", 6: "replay ran past the recorded steps"}
 
 
 def _check_status(status, what):

@@ -1,16 +1,17 @@
 /* C ABI of the GB300 Boltzmann library (libbolt_gb300.so).
  *
  * Drop-in boundary for Bolt.jl's hot path.  Each entry point replaces one
- * reference function; the Julia side binds them with ccall (see
- * INTEGRATION.md).  Conventions:
+ * reference function; the Julia side binds them with ccall.  Conventions:
  *   - every function returns 0 on success, a negative code on error; the
  *     message is available from bolt_last_error(ctx);
  *   - all arrays are caller-owned host memory (Julia arrays are column
  *     major; the layouts below are given as [slow][fast]);
  *   - a context is not thread safe; use one per host thread.
  *   - per-mode status codes: 0 ok, 1 max iterations, 2 step underflow,
- *     3 non-finite state, 4 singular step matrix, 5 bad input; bit 8 (256)
- *     is OR-ed in when the radiation-streaming switch fired.
+ *     3 non-finite state, 4 singular step matrix, 5 bad input, 6 a replayed
+ *     mode ran past its recorded steps; bit 8 (256) is OR-ed in when the
+ *     radiation-streaming switch fired, bit 9 (512) when a recorded mode
+ *     outgrew its step record (gradient requests).
  */
 #ifndef BOLT_GB300_H
 #define BOLT_GB300_H
