@@ -17,13 +17,18 @@
 //
 // The first call on a device (the current device) looks up the array's
 // device address with cudaGetSymbolAddress; make that first call before any
-// stream capture.  Every call shares the array, so calls whose work overlaps
-// on the GPU race with each other; serialise them (one stream, or wait for
-// the previous call).  The work-queue counter is cleared at the start of
-// every call; everything else in the array is overwritten before use.
+// stream capture.  The address is kept per device for the life of the
+// process: after a reset of the device's primary context (cudaDeviceReset)
+// the library must be reloaded.  Every call shares the array, so calls whose
+// work overlaps on the GPU race with each other; serialise them (one stream,
+// or wait for the previous call).  The work-queue counter is cleared at the
+// start of every call; everything else in the array is overwritten before
+// use.  Each mode stops after 10^5 steps (OrdinaryDiffEq's default maxiters),
+// as in bolt_source_grid with default options.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -62,13 +67,27 @@ constexpr size_t kOffQueue = align256(kOffCounters + 2 * kMaxModes * sizeof(int6
 constexpr size_t kOffSlabs = align256(kOffQueue + 256);
 constexpr size_t kSlabDoubles = size_t(10) * kMaxN;  // the solver's per-CTA global scratch
 constexpr size_t kStaticBytes = align256(kOffSlabs + kMaxCTAs * kSlabDoubles * sizeof(double));
+constexpr long long kMaxSteps = 100000;  // per mode, OrdinaryDiffEq's default maxiters
+
+// The regions hold their largest cases: every table of a 4097-node grid with
+// nq = 27 Gauss-Legendre nodes and weights, 2048 mode records and counters,
+// and kMaxCTAs solver slabs of 10 N doubles at N = 512 (the kernel's per-CTA
+// scratch, checked again against rodas_scratch_per_warp at run time).
+static_assert(kOffTables + kTableDoubles * sizeof(double) <= kOffModes, "table region overlaps the mode records");
+static_assert(kOffModes + kMaxModes * sizeof(ModeDev) <= kOffX, "mode records overlap the x nodes");
+static_assert(kOffX + kMaxGrid * sizeof(double) <= kOffCounters, "x nodes overlap the counters");
+static_assert(kOffCounters + 2 * kMaxModes * sizeof(int64_t) <= kOffQueue, "counters overlap the queue");
+static_assert(kOffSlabs + size_t(kMaxCTAs) * kSlabDoubles * sizeof(double) <= kStaticBytes, "slabs overrun the array");
+static_assert(kOffTables % 256 == 0 && kOffModes % 256 == 0 && kOffSlabs % 256 == 0, "regions are 256-byte aligned");
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
 // Device address of g_static_scratch, per device (host code must not use the
-// symbol itself as a pointer: on the host it names a stand-in object).
+// symbol itself as a pointer: on the host it names a stand-in object).  Two
+// host threads making their first call at once may both look it up; they
+// store the same address.
 constexpr int kMaxDevices = 64;
-unsigned char* g_addr[kMaxDevices] = {nullptr};
+std::atomic<unsigned char*> g_addr[kMaxDevices] = {};
 
 int fail(char* errbuf, int errlen, int code, const char* msg) {
   if (errbuf && errlen > 0) std::snprintf(errbuf, errlen, "%s", msg);
@@ -99,13 +118,14 @@ extern "C" int bolt_source_grid_static(const bolt_params* par, const bolt_grid* 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return fail(errbuf, errlen, -3, "no current CUDA device");
-  if (!g_addr[dev]) {
+  unsigned char* base = g_addr[dev].load(std::memory_order_acquire);
+  if (!base) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
     if (e != cudaSuccess || !p) return fail(errbuf, errlen, -3, cudaGetErrorString(e));
-    g_addr[dev] = static_cast<unsigned char*>(p);
+    base = static_cast<unsigned char*>(p);
+    g_addr[dev].store(base, std::memory_order_release);
   }
-  unsigned char* base = g_addr[dev];
   cudaStream_t st = static_cast<cudaStream_t>(stream);
 
   // host side: spline tables from the caller's node values (as bolt_cosmo_upload)
@@ -195,7 +215,7 @@ extern "C" int bolt_source_grid_static(const bolt_params* par, const bolt_grid* 
   cfg.abstol = abstol;
   cfg.h0 = 1e-3;
   cfg.x_dense = -8.5;
-  cfg.max_steps = 10000000;
+  cfg.max_steps = kMaxSteps;
   cfg.land_stride = 1;
   const int Lmax = hier->lg > hier->lnu ? (hier->lg > hier->lmnu ? hier->lg : hier->lmnu)
                                         : (hier->lnu > hier->lmnu ? hier->lnu : hier->lmnu);

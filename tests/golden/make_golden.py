@@ -60,4 +60,6 @@ def camb_pk(data):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/Bolt.jl")
+    main(sys.argv[1])
