@@ -105,10 +105,17 @@ struct ElemC {
 };
 
 __device__ __forceinline__ ElemC elem_coef(const Mode& m, const Shared& S, const Scal<double>& s, double ig, int c,
-                                           int l, int L) {
+                                           int l, int L, bool rsa) {
+  ElemC e;
+  if (rsa && c <= 2) {  // radiation streaming: the photon and massless-nu rows of f are zero
+    e.d = ig;
+    e.lo = 0.0;
+    e.up = 0.0;
+    e.upPrev = 0.0;
+    return e;
+  }
   double mu = c >= 3 ? S.qe[c - 3] : 1.0;  // slot 0 (q / eps at x)
   double mk = mu * s.kH;
-  ElemC e;
   double jd;
   if (l == L) jd = -(L + 1.0) * s.iHe + (c <= 1 ? s.tp : 0.0);
   else jd = (c == 1 || (c == 0 && l >= 1)) ? s.tp : 0.0;
@@ -142,7 +149,7 @@ __device__ __forceinline__ M2 shfl_up_m2(const M2& v, int off) {
 // Baryon pair (delta_b, v_b) hanging off Theta_1: eliminated first.  Returns
 // lb = M[Theta1][vb] / piv_vb and the correction to Theta_1's diagonal.
 __device__ __forceinline__ double baryon_pair(const Mode& m, const Shared& S, const Scal<double>& s, double ig,
-                                              double hg, double& dT1_corr) {
+                                              double hg, bool rsa, double& dT1_corr) {
   int idb = m.iPhi + 3, ivb = m.iPhi + 4;
   double Mdb_vb = -s.kH;               // M[db][vb]
   double Mvb_db = s.kH * s.cs2;        // M[vb][db]
@@ -156,7 +163,7 @@ __device__ __forceinline__ double baryon_pair(const Mode& m, const Shared& S, co
   S.fc[ivb] = Mvb_T1 * ipvb;
   S.fi[idb] = hg;
   S.fc[idb] = Mdb_vb * hg;
-  double lb = (-s.tp / 3.0) * ipvb;  // M[Theta1][vb] / piv_vb
+  double lb = rsa ? 0.0 : (-s.tp / 3.0) * ipvb;  // M[Theta1][vb] / piv_vb (no Theta_1 row under streaming)
   S.fl[idb] = lb;                     // stored in delta_b's unused multiplier slot
   dT1_corr = -lb * Mvb_T1;
   return lb;
@@ -165,8 +172,8 @@ __device__ __forceinline__ double baryon_pair(const Mode& m, const Shared& S, co
 // Border tails of chain c, written to shared memory: U (coefficients of
 // Phi', Psi, Pi in the chain's last rows) into uf, W (gradients of Phi', Psi,
 // Pi on those rows) into wt; slots as in tail_index().
-__device__ __forceinline__ void border_tails(const Mode& m, const Shared& S, const Scal<double>& s, int c, double* U,
-                                             double* W) {
+__device__ __forceinline__ void border_tails(const Mode& m, const Shared& S, const Scal<double>& s, int c, bool rsa,
+                                             double* U, double* W) {
   const CosmoDev& C = *m.C;
   for (int a = 0; a < kTail * kBorder; ++a) { U[a] = 0.0; W[a] = 0.0; }
   double ia = 1.0 / s.a;
@@ -177,11 +184,12 @@ __device__ __forceinline__ void border_tails(const Mode& m, const Shared& S, con
     WW(0, 0) = s.dphi * 4.0 * C.Omega_r * ia * ia;
     WW(2, 1) = -s.cpsi * C.Omega_r; WW(2, 0) = WW(2, 1); WW(2, 2) = 1.0;
     WW(4, 0) = s.dphi * C.Omega_b * ia;
+    if (rsa) { UU(0, 0) = 0.0; UU(1, 1) = 0.0; UU(2, 2) = 0.0; }  // photon rows are zero; baryon rows stay
   } else if (c == 1) {
-    UU(0, 2) = -s.tp / 2.0; UU(2, 2) = -s.tp / 10.0;
+    if (!rsa) { UU(0, 2) = -s.tp / 2.0; UU(2, 2) = -s.tp / 10.0; }
     WW(0, 2) = 1.0; WW(2, 2) = 1.0;
   } else if (c == 2) {
-    UU(0, 0) = -1.0; UU(1, 1) = s.kH / 3.0;
+    if (!rsa) { UU(0, 0) = -1.0; UU(1, 1) = s.kH / 3.0; }
     WW(0, 0) = s.dphi * 4.0 * C.Omega_nu * ia * ia;
     WW(2, 1) = -s.cpsi * C.Omega_nu; WW(2, 0) = WW(2, 1);
   } else if (c < 3 + m.nq) {
@@ -258,6 +266,7 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
   const int lane = tid & 31;
   const Scal<double> s = get_scal<double>(S, 0);
   const double ig = 1.0 / hg;
+  const bool rsa = rsa_switch(m, s);
   const int E = P.E[0];
   const int c = P.chain[tid];
   const int seg = P.seg[tid];
@@ -275,10 +284,10 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
       const int i = idx[e];
       if (i < 0) break;
       int l = (i - cd.base) / cd.stride;
-      ElemC ec = elem_coef(m, S, s, ig, c, l, cd.L);
+      ElemC ec = elem_coef(m, S, s, ig, c, l, cd.L, rsa);
       if (c == 0 && l == 1) {
         double corr;
-        baryon_pair(m, S, s, ig, hg, corr);
+        baryon_pair(m, S, s, ig, hg, rsa, corr);
         ec.d += corr;
       }
       double p = ec.lo * ec.upPrev;  // 0 for the chain's first element
@@ -334,7 +343,7 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
     if (cc < 0) continue;
     double* uf = S.Uf + cc * kTail * kBorder;
     double* wt = S.Wt + cc * kTail * kBorder;
-    border_tails(m, S, s, cc, uf, wt);
+    border_tails(m, S, s, cc, rsa, uf, wt);
     for (int b = 0; b < kBorder; ++b) tail_minv_u(m, S, cc, uf, wt, b, part + cc * 9);
   }
   __syncthreads();

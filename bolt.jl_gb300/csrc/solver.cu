@@ -223,6 +223,13 @@ template <class T> __device__ __forceinline__ T warp_sum_t(T v);
 template <> __device__ __forceinline__ double warp_sum_t<double>(double v) { return warp_sum(v); }
 template <> __device__ __forceinline__ dd warp_sum_t<dd>(dd v) { return mk(warp_sum(v.v), warp_sum(v.d)); }
 
+// The radiation-streaming switch of hierarchy! (perturbations.jl:216) from
+// the stage scalars: k eta > 240 and -tau' H / eta > 100.
+template <class T>
+__device__ __forceinline__ bool rsa_switch(const Mode& m, const Scal<T>& s) {
+  return (m.k * vof(s.eta) > 240.0) && (-vof(s.tp) * vof(s.Hc) / vof(s.eta) > 100.0);
+}
+
 // Metric potentials Psi and Phi' (perturbations.jl:182-194) from the state u.
 template <class T>
 __device__ __forceinline__ void metric(const Mode& m, const Shared& S, int sl, const Scal<T>& s, const double* u,
@@ -248,6 +255,28 @@ __device__ __forceinline__ void metric(const Mode& m, const Shared& S, int sl, c
                    (4.0 * C.Omega_r * u[0] + 4.0 * Omega_nu * u[m.iN] + rho * (1.0 / C.rho_crit)) * (ia * ia));
 }
 
+// The state overwrite of hierarchy!'s radiation-streaming branch
+// (perturbations.jl:217-227), applied to the accepted state u at the step's
+// end abscissa (stage slot 4; OrdinaryDiffEq hands the integrator's own
+// state to the right-hand side at the end of a step, so the reference's
+// accepted state carries these values): Theta_0, Theta_1 from the metric and
+// the baryons, Theta_2 = 0, N_0 = Phi, N_1 = -2 H Phi' / k, N_2 = 0, with
+// Phi' formed from u before the overwrite.  One warp; lane 0 writes.
+__device__ void rsa_overwrite(const Mode& m, const Shared& S, double x, double* u, int lane) {
+  const Scal<double> s = get_scal<double>(S, 4);
+  double Psi, Phip;
+  metric<double>(m, S, 4, s, u, lane, Psi, Phip);
+  if (lane != 0) return;
+  const double Phi = u[m.iPhi], delb = u[m.iPhi + 3], vb = u[m.iPhi + 4];
+  const double Hk = s.Hc / m.k, tpp = spl_cold(*m.C, C_TAUPP, x);
+  u[0] = Phi - Hk * s.tp * vb;
+  u[1] = Hk * (-2.0 * Phip + s.tp * (Phi - s.cs2 * delb) + Hk * (tpp - s.tp) * vb);
+  u[2] = 0.0;
+  u[m.iN] = Phi;
+  u[m.iN + 1] = -2.0 * Hk * Phip;
+  u[m.iN + 2] = 0.0;
+}
+
 // hierarchy! (perturbations.jl:161-271): writes f into out (and df/dx into
 // out_d for T = dd), one row per thread over the whole CTA.  Every warp
 // forms the metric potentials itself (two nq-term sums), so no barrier is
@@ -263,7 +292,7 @@ __device__ bool rhs_rows(const Mode& m, const Shared& S, int sl, const double* u
   const int lg = m.lg, lnu = m.lnu, lmnu = m.lmnu, nq = m.nq;
   const double* cl1 = S.cl1;
   const double* cl2 = S.cl2;
-  const bool rsa = (m.k * vof(s.eta) > 240.0) && (-vof(s.tp) * vof(s.Hc) / vof(s.eta) > 100.0);
+  const bool rsa = rsa_switch(m, s);
   const double Pi = u[2] + u[m.iTp + 2] + u[m.iTp];
   const double vb = u[m.iPhi + 4];
   for (int i = tid; i < m.N; i += nth) {
@@ -817,6 +846,10 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
         else rec_over = true;
       }
       __syncthreads();
+      if (rsa_switch(m, get_scal<double>(S, 4))) {  // uniform over the CTA
+        if (warp == 0) rsa_overwrite(m, S, xn, G.y, lane);
+        __syncthreads();
+      }
       x = xn;
       ++nacc;
       double hp = hs * fac;

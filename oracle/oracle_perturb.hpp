@@ -63,6 +63,15 @@ inline void rho_sigma(const Mode& md, S a, const double* M0, const double* M2, S
 
 struct RhsInfo { bool rsa = false; };
 
+// The radiation-streaming switch of hierarchy! (perturbations.jl:216):
+// k eta > 240 and -tau' H / eta > 100.
+inline bool rsa_switch(const Mode& md, double x) {
+  const Background& bg = *md.C->bg;
+  const Ionization& ih = *md.C->ih;
+  double eta = bg.eta.eval(x), tp = ih.taup.eval(x), Hc = bg.H.eval(x);
+  return (md.k * eta > 240.0) && (-tp * Hc / eta > 100.0);
+}
+
 // hierarchy! (perturbations.jl:161-271).  S = double for the plain RHS,
 // S = D1 (value, d/dx) to obtain the explicit x-derivative of the RHS that a
 // Rosenbrock method needs for a non-autonomous system.
@@ -112,13 +121,12 @@ inline void hierarchy_rhs(const Mode& md, S x, const double* u, S* du, RhsInfo* 
       dMm[l * nq + iq] = k / Hc * q / ((2.0 * l + 1.0) * eps) * (l * Mm[(l - 1) * nq + iq] - (l + 1) * Mm[(l + 1) * nq + iq]);
     dMm[lmnu * nq + iq] = q / eps * k / Hc * Mm[(lmnu - 1) * nq + iq] - (lmnu + 1.0) / (Hc * eta) * Mm[lmnu * nq + iq];
   }
-  bool rsa_on = (k * val(eta) > 240.0) && (-val(tp) * val(Hc) / val(eta) > 100.0);
+  bool rsa_on = rsa_switch(md, val(x));
   if (info) info->rsa = rsa_on;
   if (rsa_on) {
-    // The reference overwrites the photon / massless-neutrino entries of u
-    // here (perturbations.jl:217-227) and zeroes their derivatives.  The
-    // oracle zeroes the derivatives and reports the switch; the mutation of
-    // the stage vector has no counterpart in a one-step method.
+    // The reference also overwrites Theta_0..2 and N_0..2 of u here
+    // (perturbations.jl:217-227); the solver applies that to the accepted
+    // state after each step (rsa_overwrite).  Nothing below reads them.
     for (int l = 0; l <= lnu; ++l) dNn[l] = S(0.0);
     for (int l = 0; l <= lg; ++l) { dTh[l] = S(0.0); dTp[l] = S(0.0); }
   } else {
@@ -145,6 +153,40 @@ inline void hierarchy_rhs(const Mode& md, S x, const double* u, S* du, RhsInfo* 
   du[md.iPhi + 2] = dv;
   du[md.iPhi + 3] = ddelb;
   du[md.iPhi + 4] = dvb;
+}
+
+// The state overwrite of hierarchy!'s radiation-streaming branch
+// (perturbations.jl:217-227) at x: Theta_0, Theta_1 from the metric and the
+// baryons, Theta_2 = 0, N_0 = Phi, N_1 = -2 H Phi' / k, N_2 = 0, with Phi'
+// formed from u before the overwrite (as the reference forms it).  OrdinaryDiffEq
+// passes the integrator's own state to the right-hand side at the end of a
+// step, so the accepted state carries these values into the next step; the
+// solver applies them there.
+inline void rsa_overwrite(const Mode& md, double x, double* u) {
+  const Cosmo& C = *md.C;
+  const Params& p = C.par;
+  const Background& bg = *C.bg;
+  const Ionization& ih = *C.ih;
+  const double k = md.k, H0sq = bg.H0 * bg.H0, a = std::exp(x);
+  const double Hc = bg.H(x), tp = ih.taup(x), tpp = ih.taupp(x), cs2 = ih.csb2(x);
+  double Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
+  const int nq = md.nq;
+  std::vector<double> M0(nq), M2(nq);
+  for (int i = 0; i < nq; ++i) { M0[i] = u[md.iM + i]; M2[i] = u[md.iM + 2 * nq + i]; }
+  double rhoM, sigM;
+  rho_sigma(md, a, M0.data(), M2.data(), rhoM, sigM);
+  const double Phi = u[md.iPhi], del = u[md.iPhi + 1], delb = u[md.iPhi + 3], vb = u[md.iPhi + 4];
+  double Psi = -Phi - 12.0 * H0sq / (k * k) / (a * a) * (p.Omega_r * u[2] + Omega_nu * u[md.iN + 2] + sigM / bg.rho_crit / 4.0);
+  double Phip = Psi - k * k / (3.0 * Hc * Hc) * Phi +
+                H0sq / (2.0 * Hc * Hc) *
+                    (p.Omega_c / a * del + p.Omega_b / a * delb + 4.0 * p.Omega_r / (a * a) * u[0] +
+                     4.0 * Omega_nu / (a * a) * u[md.iN] + rhoM / (a * a) / bg.rho_crit);
+  u[0] = Phi - Hc / k * tp * vb;
+  u[1] = Hc / k * (-2.0 * Phip + tp * (Phi - cs2 * delb) + Hc / k * (tpp - tp) * vb);
+  u[2] = 0.0;
+  u[md.iN] = Phi;
+  u[md.iN + 1] = -2.0 * Hc / k * Phip;
+  u[md.iN + 2] = 0.0;
 }
 
 // initial_conditions (perturbations.jl:274-338)
@@ -351,7 +393,13 @@ inline void jacobian_split(const Mode& md, double x, JacSplit& J) {
   J.N = N;
   J.L.clear();
   for (int r = 0; r < 3; ++r) { J.U[r].assign(N, 0.0); J.W[r].assign(N, 0.0); }
-  auto add = [&](int r, int c, double v) { J.L.push_back({r, c, v}); };
+  // with the radiation-streaming switch on, the photon and massless-neutrino
+  // rows of the right-hand side are zero, and so are their Jacobian rows
+  const bool rsa = rsa_switch(md, x);
+  const int rad_end = md.iM;  // rows 0 .. iM-1: photon T, photon P, massless nu
+  auto add = [&](int r, int c, double v) {
+    if (!(rsa && r < rad_end)) J.L.push_back({r, c, v});
+  };
   const int iPhi = md.iPhi, idel = iPhi + 1, iv = iPhi + 2, idelb = iPhi + 3, ivb = iPhi + 4;
   // gradients of Psi and Phi'
   double cpsi = 12.0 * H0sq / (k * k) / (a * a);
@@ -451,6 +499,9 @@ inline void jacobian_split(const Mode& md, double x, JacSplit& J) {
   add(lg, lg, -((lg + 1.0) / (Hc * eta) - tp));
   add(md.iTp + lg, md.iTp + lg - 1, kH);
   add(md.iTp + lg, md.iTp + lg, -((lg + 1.0) / (Hc * eta) - tp));
+  if (rsa)
+    for (int r = 0; r < 3; ++r)
+      for (int i = 0; i < rad_end; ++i) J.U[r][i] = 0.0;
 }
 
 // ---------------------------------------------------------- Rodas4 ---------
@@ -604,6 +655,7 @@ inline SolveStats solve_mode(const Mode& md, double reltol, double abstol, const
     if (en <= 1.0) {
       x = xn;
       std::swap(y, ynew);
+      if (rsa_switch(md, x)) rsa_overwrite(md, x, y.data());
       ++stats.steps;
       while (jo < xout.size() && xout[jo] <= x + 1e-14 * std::fabs(x)) { emit(int(jo), xout[jo], y.data()); ++jo; }
       double hp = hs * fac;

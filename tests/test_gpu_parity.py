@@ -79,6 +79,40 @@ def test_boltsolve_rsa(fid):
         assert np.all(u[j][jsw + 1:, 3:8] == 0.0)  # Theta_3..Theta_7 zeroed past the switch
 
 
+def test_rsa_switch_on_vs_oracle(fid):
+    """hierarchy!'s radiation-streaming branch driven on (k = 30 Mpc^-1 up to
+    x = -10.7, the case of tests/test_oracle_rsa.py): the status reports the
+    switch; where it is on the state carries the reference's overwrite
+    (Theta_2 = N_2 = 0 and N_0 = Phi exactly, Theta_0 = Phi - H tau' v_b / k)
+    and the untouched radiation multipoles stay frozen, exactly; the trajectory
+    matches the oracle's within 2e-3 of each component's peak (both at
+    reltol = abstol = 1e-6 through ~2e5 steps)."""
+    from test_oracle_rsa import HIER, K, rsa_case
+    par, bg, ih0, orc = fid
+    ctx = B.Context(max_steps=2_000_000)
+    ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg, ctx=ctx)
+    xo, uo, sto, on, H, tp = rsa_case(orc)
+    u, st = B.boltsolve_batch(ih, np.array([K]), xo, *HIER, reltol=1e-6, abstol=1e-6)
+    ih.close()
+    ctx.close()
+    assert (st[0] & 0xFF) == 0 and (st[0] & 256), st
+    u = u[0]
+    lg, lnu, lmnu, nq = HIER
+    iTp, iN = lg + 1, 2 * (lg + 1)
+    iPhi = iN + lnu + 1 + (lmnu + 1) * nq
+    i = np.where(on)[0]
+    assert np.all(u[i, 2] == 0.0) and np.all(u[i, iN + 2] == 0.0)
+    np.testing.assert_allclose(u[i, iN], u[i, iPhi], rtol=0, atol=0)
+    # H and tau' from the oracle's tables (the GPU's agree to ~1e-9)
+    np.testing.assert_allclose(u[i, 0], u[i, iPhi] - H[i] / K * tp[i] * u[i, iPhi + 4], rtol=1e-7, atol=0)
+    frozen = np.r_[3:lg + 1, iTp:iTp + lg + 1, iN + 3:iN + lnu + 1]
+    for j in i[np.diff(np.r_[i, -5]) == 1]:
+        np.testing.assert_array_equal(u[j + 1, frozen], u[j, frozen])
+    peak = np.maximum(np.max(np.abs(uo), axis=0), 1e-12)
+    err = np.max(np.abs(u - uo) / peak)
+    assert err < 2e-3, err
+
+
 def test_source_grid(fid):
     par, bg, ih, orc = fid
     kg = B.quadratic_k(0.1 * bg.H0, 1000 * bg.H0, 12)
