@@ -1,0 +1,155 @@
+"""GPU parity at the configurations' own sizes: the CUDA path (through the C
+ABI) against the CPU oracle.
+
+* Trajectories at the reference plin default hierarchy l 50/50/20, nq 15
+  (N = 473, the largest shared-memory layout) and at the trajectory
+  configuration (100 log k in [0.1, 1000] H0, l 20/20/10, 1000 uniform x in
+  [-20, 0], N = 233) with its P_lin(k) at z = 0: both sides at
+  reltol = abstol = 1e-10, every component within 1e-6 of its peak over x,
+  P_lin within 1e-6.
+* P_lin on 200 log k in [1e-4, 1] h/Mpc at N = 473 against the oracle at
+  1e-10 (fixture): 1e-6 at reltol = abstol = 1e-10; 1e-4 at the served
+  tolerances (reltol 1e-8, abstol 3e-7).
+* C_l^TT/TE/EE, l = 2..2500, of the serving stream's hardest C_l request
+  (1024 log k in [0.1, 1000] H0, l_gamma = l_nu = 50) at the served
+  tolerances against the oracle's converged (1e-11) solution (fixture): TT
+  and EE within 1e-4 relative at every l, TE within 1e-4 of its peak.
+* Jacobians of C_l^TT (l = 2..2000) and of P_lin (200 k) with respect to
+  (h, omega_b, omega_c, n_s, A_s, Sigma m_nu) from a served gradient request
+  against the oracle's central differences (fixtures; relative steps 1e-3
+  and 1e-4 agree with each other): every element whose magnitude exceeds
+  1e-3 of its parameter's peak within 1e-3 relative.
+The fixtures come from tests/golden/make_oracle_fixtures.py.
+"""
+import os
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import pytest
+
+import bolt_gb300 as B
+import oracle as O
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+CORES = os.cpu_count() or 1
+SERVED = dict(reltol=1e-8, abstol=3e-7)
+
+
+def _fixture(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def _fid():
+    par = B.CosmoParams(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Sigma_m_nu=0.06 * B.mass_natural())
+    bg = B.Background(par)
+    ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg)
+    orc = O.Cosmo(O.Params(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Sigma_m_nu_eV=0.06))
+    return par, bg, ih, orc
+
+
+@pytest.fixture(scope="module")
+def fid():
+    return _fid()
+
+
+def _traj_err(u, uo):
+    peak = np.maximum(np.max(np.abs(uo), axis=0), 1e-12)
+    return np.max(np.abs(u - uo) / peak)
+
+
+def test_trajectories_n473(fid):
+    par, bg, ih, orc = fid
+    hier = (50, 50, 20, 15)
+    assert B.state_len(*hier) == 473
+    ks = np.array([0.002, 0.03, 0.1, 0.21])
+    xo = np.linspace(-20.0, 0.0, 41)
+    u, st = B.boltsolve_batch(ih, ks, xo, *hier, reltol=1e-10, abstol=1e-10)
+    assert np.all(st == 0)
+    with ThreadPoolExecutor(CORES) as ex:
+        ref = list(ex.map(lambda k: orc.boltsolve(k, xo, *hier, reltol=1e-10, abstol=1e-10)[0], ks))
+    for j, k in enumerate(ks):
+        err = _traj_err(u[j], ref[j])
+        assert err < 1e-6, (k, err)
+
+
+def test_trajectories_and_plin_config1(fid):
+    """100 log k in [0.1, 1000] H0 on 1000 uniform x in [-20, 0], l 20/20/10,
+    nq 15, and P_lin(k) at z = 0 on the same k."""
+    par, bg, ih, orc = fid
+    hier = (20, 20, 10, 15)
+    assert B.state_len(*hier) == 233
+    ks = B.log10_k(0.1 * bg.H0, 1000.0 * bg.H0, 100)
+    xo = np.linspace(-20.0, 0.0, 1000)
+    u, st = B.boltsolve_batch(ih, ks, xo, *hier, reltol=1e-10, abstol=1e-10)
+    assert u.shape == (100, 1000, 233) and np.all(st == 0)
+    pick = [0, 19, 43, 67, 88, 99]
+    with ThreadPoolExecutor(CORES) as ex:
+        ref = list(ex.map(lambda k: orc.boltsolve(k, xo, *hier, reltol=1e-10, abstol=1e-10)[0], ks[pick]))
+    for j, uo in zip(pick, ref):
+        err = _traj_err(u[j], uo)
+        assert err < 1e-6, (ks[j], err)
+    P = B.plin(ks, par, bg, ih, 15, 20, 20, 10, 0.0, 1e-10, 1e-10)
+    with ThreadPoolExecutor(CORES) as ex:
+        Po = np.array(list(ex.map(lambda k: orc.plin(k, 15, 20, 20, 10, 0.0, 1e-10, 1e-10), ks)))
+    assert np.max(np.abs(P / Po - 1)) < 1e-6
+
+
+@pytest.mark.parametrize("tol,bound", [((1e-10, 1e-10), 1e-6), ((1e-8, 3e-7), 1e-4)], ids=["tight", "served"])
+def test_plin_n473_200k(fid, tol, bound):
+    par, bg, ih, orc = fid
+    f = _fixture("oracle_plin_n473")
+    assert tuple(f["hier"]) == (50, 50, 20, 15) and f["ks"].size == 200
+    P = B.plin(f["ks"], par, bg, ih, 15, 50, 50, 20, 0.0, *tol)
+    err = np.abs(P / f["plin"] - 1)
+    assert np.max(err) < bound, (f["ks"][np.argmax(err)], np.max(err))
+
+
+def test_cl_served_hardest_request_vs_converged_oracle(fid):
+    par, bg, ih, orc = fid
+    f = _fixture("oracle_cl_l50_1024k")
+    ks, ells = f["ks"], f["ells"]
+    assert ks.size == 1024 and ells[0] == 2 and ells[-1] == 2500
+    np.testing.assert_allclose(ks, B.log10_k(0.1 * bg.H0, 1000.0 * bg.H0, 1024), rtol=1e-14)
+    tt, te, ee, st = B.cl_all(ells, ih, ks, 50, 50, 10, 15, **SERVED)
+    assert np.all((st & 0xFF) == 0)
+    assert np.max(np.abs(tt / f["tt"] - 1)) < 1e-4
+    assert np.max(np.abs(ee / f["ee"] - 1)) < 1e-4
+    assert np.max(np.abs(te - f["te"])) < 1e-4 * np.max(np.abs(f["te"]))
+
+
+def _per_element(J, Jref, name):
+    """Relative error of every element above 1e-3 of its parameter's peak."""
+    worst = 0.0
+    for j in range(6):
+        ref = Jref[j]
+        big = np.abs(ref) > 1e-3 * np.max(np.abs(ref))
+        rel = np.abs(J[j][big] - ref[big]) / np.abs(ref[big])
+        worst = max(worst, float(np.max(rel)))
+        assert np.max(rel) < 1e-3, (name, B.THETA_NAMES[j], np.max(rel), int(np.argmax(rel)))
+    return worst
+
+
+def test_cltt_jacobian_per_element_vs_oracle_fd():
+    f = _fixture("oracle_jac_cltt")
+    par = B.params_of(B.CosmoParams(), f["theta"])
+    ks, ells = f["ks"], f["ells"]
+    _per_element(f["J_0.0001"], f["J_0.001"], "oracle steps 1e-4 vs 1e-3")
+    with B.Engine(lanes=1) as eng:
+        r = eng.run(B.Request("cl", par, ks, hier=tuple(int(v) for v in f["hier"]), ells=ells, cl=("tt",), grad=True, **SERVED))
+    assert r.rc == 0, r.err
+    assert np.max(np.abs(r.cl["tt"] / f["tt"] - 1)) < 1e-4
+    _per_element(r.dcl["tt"], f["J_0.0001"], "C_l^TT")
+
+
+def test_plin_jacobian_per_element_vs_oracle_fd():
+    f = _fixture("oracle_jac_plin")
+    par = B.params_of(B.CosmoParams(), f["theta"])
+    ks = f["ks"]
+    _per_element(f["J_0.0001"], f["J_0.001"], "oracle steps 1e-4 vs 1e-3")
+    with B.Engine(lanes=1) as eng:
+        r = eng.run(B.Request("plin", par, ks, hier=tuple(int(v) for v in f["hier"]), grad=True, **SERVED))
+    assert r.rc == 0, r.err
+    assert np.max(np.abs(r.plin / f["plin"] - 1)) < 1e-4
+    _per_element(r.dplin, f["J_0.0001"], "P_lin")
