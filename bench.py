@@ -27,17 +27,25 @@ completion; ``roofline`` = the Rosenbrock kernel's aggregate FP64 rate over
 the served window (``roofline_plain``: in the plain leg, no overlap between
 calls) against the FP64 peak measured in this run;
 ``cpu_baseline`` = the CPU oracle (C++ restatement of Bolt's CPU algorithm,
-threaded over k / l) on a bounded sample of every request type, scaled to
-the stream; ``cl_grad`` = a stream of C_l^TT + Jacobian requests only (the
+threaded over k / l) on the stream's first requests, each run in full
+(about 30 s of CPU work); ``cl_grad`` = a stream of C_l^TT + Jacobian requests only (the
 metric's request type), served vs the drop-in and vs the engine one request
 per call.
+
+``rates`` = the same stream served at Poisson arrival rates of 10, 100, 500
+and 2000 requests/s (the serving configuration's sweep), each through a fresh
+engine: spectra/s, p50 / p99 latency, requests that waited for a lane or the
+memory budget, host table-build times and the largest device footprint in
+flight; ``roofline_los`` = the line-of-sight kernels' FP64 rate in the plain
+leg from the terms they evaluated.
 
 ``--workload pipeline``: the full CMB pipeline for one cosmology (1200 k,
 l <= 2500, N = 473) with device-timed throughput (the profiling case).
 ``--workload batch`` / ``grad``: K cosmologies submitted at once (C_l^TT +
 P_lin from one solve each; or the Jacobians of C_l^TT and P_lin) against the
 plain drop-in, cosmologies/s.
-``--impl reference``: the CPU oracle alone on the serving stream.
+``--impl reference``: the CPU oracle alone on the whole serving stream, every
+request run in full.
 """
 from __future__ import annotations
 
@@ -75,9 +83,16 @@ def solver_flops_per_step(N, nq):
     return 159 * N + 560 * (nq + 5) + 66 * nq + 650
 
 
-def los_flops(nslots, nm, nrow):
-    """line-of-sight reduction: 27 FLOPs per (l, k, x) term with T and E."""
-    return 27.0 * nslots * nm * nrow
+LOS_FLOPS_TE = 27  # FLOPs per evaluated (l, k, x) term of los_cl_kernel with T and E (FMA = 2)
+LOS_FLOPS_T = 25   # the same with T alone
+
+
+def los_flops(terms, with_e=True):
+    """Line-of-sight reduction FLOPs from the (l, k, x) terms the kernel
+    evaluated (its counter; terms below the Bessel turning point are
+    skipped): spline weights 12, j_l 8, the argument 3, the S_T product 2
+    (+2 for S_E)."""
+    return float(terms) * (LOS_FLOPS_TE if with_e else LOS_FLOPS_T)
 
 
 def state_len(lg, lnu, lmnu, nq):
@@ -149,8 +164,8 @@ def dropin_request(B, ctx, d):
     (C_l^TT Jacobian), "plin_fd" (P_lin Jacobian).  The drop-in has no
     Jacobian, so a gradient request is 1 + 6 calls whose forward differences
     give it (central differences would take 13).  Returns (result, calls,
-    solver seconds, algorithmic solver FLOPs) with the solver figures from
-    bolt_last_stats."""
+    solver seconds, algorithmic solver FLOPs, LOS figures) with the solver
+    and LOS figures from bolt_last_stats."""
     import ctypes as C
     L = B._lib
     lib = ctx.lib
@@ -164,6 +179,7 @@ def dropin_request(B, ctx, d):
     hier = L.BoltHier(lg, lnu, lmnu, nq)
     fpstep = solver_flops_per_step(state_len(*d["hier"]), nq)
     solver_s, flops, outs = 0.0, 0.0, []
+    los = {"us": 0, "terms": 0, "flops": 0.0}
     for th in sets:
         par = B.params_of(B.CosmoParams(), th)
         H0 = par.h * B.km_s_Mpc_100()
@@ -191,13 +207,16 @@ def dropin_request(B, ctx, d):
         s = ctx.stats()
         solver_s += s["solver_us"] / 1e6
         flops += (s["accepted_steps"] + s["rejected_steps"]) * fpstep
+        los["us"] += s["los_us"]
+        los["terms"] += s["los_terms"]
+        los["flops"] += los_flops(s["los_terms"], with_e=(kind == "cl"))
         lib.bolt_cosmo_free(ctx.h, cid.value)
         outs.append(out)
     if grad:
         f = [o if o.ndim == 1 else o[0] for o in outs]
         jac = np.array([(f[1 + j] - f[0]) / (FD_REL_STEP * abs(th0[j])) for j in range(6)])
-        return (f[0], jac), len(sets), solver_s, flops
-    return outs[0], len(sets), solver_s, flops
+        return (f[0], jac), len(sets), solver_s, flops, los
+    return outs[0], len(sets), solver_s, flops, los
 
 
 # ----------------------------------------------------------------- clocks --
@@ -273,52 +292,114 @@ def barrier(dist):
 
 
 # ----------------------------------------------------------- CPU baseline --
-def cpu_stream_seconds(stream):
-    """CPU oracle seconds for the stream, from timed samples of each request
-    type scaled by its size (modes x state length for the solves, multipoles
-    for the projection; a gradient is 7 parameter sets, as forward
-    differences over six parameters need).  About 10-30 s of CPU work."""
-    from concurrent.futures import ThreadPoolExecutor
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
+    return O
+
+
+def oracle_request(O, d, cores):
+    """One request of the stream, run in full on the CPU oracle (C++ FP64
+    restatement of Bolt's CPU algorithm) with `cores` threads: Background +
+    RECFAST tables, then P_lin threaded over k, or the source grid (OpenMP
+    over k) and the C_l projection (OpenMP over l).  A gradient request is
+    forward differences on frozen k and Bessel grids: four more source grids
+    (h, omega_b, omega_c, Sigma m_nu) and six more C_l^TT projections (n_s
+    and A_s change only the primordial spectrum).  Returns seconds."""
+    from concurrent.futures import ThreadPoolExecutor
+    t0 = time.perf_counter()
+    th = np.asarray(d["theta"], dtype=np.float64)
+
+    def cosmo(t):
+        h = t[0]
+        return O.Cosmo(O.Params(h=h, Omega_b=t[1] / h ** 2, Omega_c=t[2] / h ** 2, n=t[3], A=t[4],
+                                Sigma_m_nu_eV=t[5]))
+    c = cosmo(th)
+    lg, lnu, lmnu, nq = d["hier"]
+    if d["kind"] == "plin":
+        ks = O.log10_k(1e-4 * th[0], 1.0 * th[0], d["nk"])
+        with ThreadPoolExecutor(cores) as ex:
+            list(ex.map(lambda k: c.plin(k, nq, lg, lnu, lmnu, 0.0, RELTOL, ABSTOL), ks))
+        return time.perf_counter() - t0
+    ks = O.log10_k(0.1 * c.H0, 1000.0 * c.H0, d["nk"])
+    ells = np.arange(2, d["lmax"] + 1, dtype=np.int32)
+    kd = (0.01 * c.H0, 1000.0 * c.H0, 5000)
+    argmax = kd[1] * c.eta0
+    ST, SE, _ = c.source_grid(ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL, nthreads=cores)
+    c.cl(ST, SE, ks, ells, kd=kd, bessel_argmax=argmax, nthreads=cores)
+    if d["kind"] == "grad":
+        for j in range(6):
+            t = th.copy()
+            t[j] += FD_REL_STEP * abs(th[j])
+            cj = cosmo(t)
+            if j in (3, 4):
+                S1, S2 = ST, SE
+            else:
+                S1, S2, _ = cj.source_grid(ks, lg, lnu, lmnu, nq, reltol=RELTOL, abstol=ABSTOL, nthreads=cores)
+            cj.cl(S1, S2, ks, ells, kd=kd, bessel_argmax=argmax, nthreads=cores)
+    return time.perf_counter() - t0
+
+
+def cpu_prefix(stream, budget_s=30.0):
+    """The CPU oracle on the stream's first requests, each run in full, until
+    about budget_s seconds have been spent (at least one request): requests/s
+    over that prefix, on all host cores."""
+    O = _oracle()
     cores = os.cpu_count() or 1
-    par = O.Params(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Sigma_m_nu_eV=0.06)
-    t0 = time.perf_counter()
-    c = O.Cosmo(par)
-    t_tab = time.perf_counter() - t0
-    # P_lin: 2 * cores wavenumbers across [1e-4, 1] h/Mpc, threaded over k
-    ks = O.log10_k(1e-4 * 0.7, 0.7, 2 * cores)
-    t0 = time.perf_counter()
-    with ThreadPoolExecutor(cores) as ex:
-        list(ex.map(lambda k: c.plin(k, lg=50, lnu=50, lmnu=20, reltol=RELTOL, abstol=ABSTOL), ks))
-    t_plin_k = (time.perf_counter() - t0) / ks.size  # seconds per k with all cores busy
-    # source grid: 2 * cores modes across [0.1, 1000] H0 at l_gamma = 35, OpenMP over k
-    kc = O.log10_k(0.1 * c.H0, 1000 * c.H0, 2 * cores)
-    t0 = time.perf_counter()
-    ST, SE, _ = c.source_grid(kc, 35, 35, 10, 15, reltol=RELTOL, abstol=ABSTOL, nthreads=cores)
-    t_mode = (time.perf_counter() - t0) / kc.size
-    n35 = state_len(35, 35, 10, 15)
-    # projection: 2 * cores multipoles spread over 2..2500 (TT/TE/EE)
-    ells = np.linspace(2, 2500, 2 * cores).astype(np.int32)
-    t0 = time.perf_counter()
-    c.cl(ST, SE, kc, ells, nthreads=cores)
-    t_ell = (time.perf_counter() - t0) / ells.size
-    total = 0.0
+    secs, n = 0.0, 0
     for d in stream:
-        nsets = 7 if d["kind"] == "grad" else 1
-        if d["kind"] == "plin":
-            total += t_tab + d["nk"] * t_plin_k
-        else:
-            N = state_len(*d["hier"])
-            total += nsets * (t_tab + d["nk"] * t_mode * N / n35 + (d["lmax"] - 1) * t_ell)
-    sample = (f"CPU oracle (C++ restatement of Bolt's CPU algorithm) on {cores} threads: tables {t_tab:.3f} s, "
-              f"P_lin {t_plin_k * 1e3:.1f} ms/k ({ks.size} k), source grid {t_mode * 1e3:.1f} ms/mode at N={n35} "
-              f"({kc.size} modes, scaled by state length), C_l {t_ell * 1e3:.2f} ms/l ({ells.size} l); "
-              f"gradients = 7 parameter sets; scaled to the {len(stream)}-request stream")
-    return total, cores, sample
+        secs += oracle_request(O, d, cores)
+        n += 1
+        if secs >= budget_s:
+            break
+    kinds = {k: sum(1 for d in stream[:n] if d["kind"] == k) for k in ("plin", "cl", "grad")}
+    sample = (f"CPU oracle (C++ restatement of Bolt's CPU algorithm) on {cores} threads: the first {n} requests of "
+              f"the stream ({kinds['plin']} P_lin, {kinds['cl']} C_l, {kinds['grad']} C_l^TT+Jacobian), each run in "
+              f"full (no scaling model), {secs:.1f} s")
+    return n / secs, cores, sample
 
 
 # ---------------------------------------------------------------- serving --
+SWEEP_RATES = (10.0, 100.0, 500.0, 2000.0)  # requests/s, the serving configuration's range
+
+
+def serve_at_rate(B, local, stream, rate, seed):
+    """The stream through a fresh engine (6 lanes, objective throughput) with
+    seeded Poisson arrivals at `rate`: spectra/s over the GPU window and end
+    to end, p50 / p99 latency, how many requests waited after their tables
+    were ready (lanes or the memory budget busy), host table-build times and
+    the largest device footprint in flight."""
+    with B.Engine(device=local, lanes=6, objective="throughput") as eng:
+        warm = make_stream(2, offset=1000)
+        for t in [eng.submit(to_request(B, d)) for d in warm]:
+            assert eng.wait(t).rc == 0
+        arrivals = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, len(stream)))
+        tickets = [None] * len(stream)
+        reqs = [to_request(B, d) for d in stream]
+        t_start = time.perf_counter()
+        for i, req in enumerate(reqs):
+            delay = t_start + arrivals[i] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            tickets[i] = eng.submit(req)
+        res = [eng.wait(t) for t in tickets]
+        st = eng.stats()
+    for r in res:
+        assert r.rc == 0, r.err
+    times = np.array([r.times for r in res])
+    win = times[:, 3].max() - times[:, 2].min()
+    e2e = times[:, 3].max() - times[:, 0].min()
+    lat = times[:, 3] - times[:, 0]
+    tab = times[:, 1] - times[:, 0]
+    wait = times[:, 2] - times[:, 1]
+    return {"rate_per_s": rate, "value": len(stream) / win, "e2e": len(stream) / e2e,
+            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "queued": int(np.sum(wait > 1e-3)), "admitted_at_once": int(np.sum(wait <= 1e-3)),
+            "queue_wait_p50_s": float(np.percentile(wait, 50)), "queue_wait_max_s": float(np.max(wait)),
+            "host_tables_p50_s": float(np.percentile(tab, 50)), "host_tables_max_s": float(np.max(tab)),
+            "peak_device_gb": st["peak_inflight_bytes"] / 1e9, "batches": st["batches"]}
+
+
 def run_serving(args):
     rank, ws, dist = dist_init()
     import torch
@@ -333,6 +414,7 @@ def run_serving(args):
 
     # ---- plain: the drop-in C-ABI, one cosmology per call, nothing else in flight
     plain_lat, plain_solver_s, plain_flops, plain_calls = [], 0.0, 0.0, 0
+    plain_los = {"us": 0, "terms": 0, "flops": 0.0}
     ctx = B.Context(device=local)
     for d in warm:
         dropin_request(B, ctx, d)
@@ -342,11 +424,13 @@ def run_serving(args):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        _, calls, ssec, fl = dropin_request(B, ctx, d)
+        _, calls, ssec, fl, lo = dropin_request(B, ctx, d)
         plain_lat.append(time.perf_counter() - t0)
         plain_solver_s += ssec
         plain_flops += fl
         plain_calls += calls
+        for key in plain_los:
+            plain_los[key] += lo[key]
     torch.cuda.synchronize()
     plain_wall = max_over_ranks(sum(plain_lat), dist)
 
@@ -413,6 +497,8 @@ def run_serving(args):
                            "l_gamma=l_nu in {20,35,50}; served: all submitted at once; plain: drop-in, 7 calls "
                            "per request (forward differences); plain_engine: the engine one request per call "
                            "(7 parameter sets batched in one launch, tangent LOS)"}
+    # ---- the arrival-rate sweep of the serving configuration (same stream)
+    sweep = [serve_at_rate(B, local, stream, rate, SEED + 31 + rank) for rate in SWEEP_RATES] if args.sweep else []
     lat = np.array([r.latency for r in res])
     tab = np.array([r.times[1] - r.times[0] for r in res])  # submission to host tables ready
     gpu_window = max_over_ranks(max(r.times[3] for r in res) - min(r.times[2] for r in res), dist)
@@ -436,6 +522,13 @@ def run_serving(args):
                     "GPU window (solver launches of up to 6 lanes overlap; the window also holds the LOS "
                     "projections, so this is a lower bound on the solver's rate); DRAM traffic is negligible "
                     "(per-CTA state slab L2-resident), see profiles/"}
+    ach_los = plain_los["flops"] / (plain_los["us"] / 1e6) / 1e12 if plain_los["us"] > 0 else None
+    roof_los = {"bound": "fp64", "achieved": ach_los, "peak": peak, "unit": "TFLOP/s",
+                "frac": ach_los / peak if (peak and ach_los) else None, "kernel": "los_cl_kernel (+ j_l tables)",
+                "terms": plain_los["terms"],
+                "note": "plain leg: FLOPs of the (l, k, x) terms the kernel evaluated (its counter; 27 per term with "
+                        "T and E, 25 with T alone) / CUDA-event time of the projection launches (Bessel tables, "
+                        "resampling and the reduction)"}
     ach_p = plain_flops / plain_solver_s / 1e12 if plain_solver_s > 0 else None
     roof_plain = {"bound": "fp64", "achieved": ach_p, "peak": peak, "unit": "TFLOP/s",
                   "frac": ach_p / peak if (peak and ach_p) else None, "kernel": "rodas_kernel<4>",
@@ -443,8 +536,8 @@ def run_serving(args):
                           "GPU): " + flop_note + " / CUDA-event time of the solver launches"}
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        secs, cores, sample = cpu_stream_seconds(stream)
-        cpu = {"value": K / secs, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        v, cores, sample = cpu_prefix(stream)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     counts = {k: sum(1 for d in stream if d["kind"] == k) for k in ("plin", "cl", "grad")}
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
@@ -474,31 +567,43 @@ def run_serving(args):
                "clocks": clocks,
                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]),
-               "engine": {k: s1[k] - s0[k] for k in s1},
-               "roofline": roof, "roofline_plain": roof_plain, "cpu_baseline": cpu}
+               "engine": {k: s1[k] - s0[k] for k in s1 if k != "peak_inflight_bytes"},
+               "roofline": roof, "roofline_plain": roof_plain, "roofline_los": roof_los, "cpu_baseline": cpu,
+               "rates": sweep}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
 
 
 def run_reference(args):
+    """The CPU oracle (C++ restatement of Bolt's CPU algorithm; Julia is not
+    available) on the whole serving stream of the GPU arm, every request run
+    in full on all host cores: steps = requests, timed one after another.
+    Warm-up: W requests of the warm-up stream cut to 32 wavenumbers and
+    l <= 200 (untimed; they load the library and start the thread pools)."""
     rank, ws, dist = dist_init()
     if rank != 0:
         return
+    O = _oracle()
+    cores = os.cpu_count() or 1
     stream = make_stream(args.steps)
-    vals, last = [], None
-    for i in range(args.warmup + 1):  # the sample timings themselves warm the host caches
-        secs, cores, sample = cpu_stream_seconds(stream)
-        if i >= args.warmup:
-            vals.append(len(stream) / secs)
-            last = (cores, sample)
-    v = statistics.median(vals)
+    for d in make_stream(args.warmup, offset=1000):
+        oracle_request(O, {**d, "nk": min(d["nk"], 32), "lmax": min(d.get("lmax", 200), 200)}, cores)
+    per = []
+    for d in stream:
+        per.append(oracle_request(O, d, cores))
+    total = sum(per)
+    v = len(stream) / total
+    by_kind = {k: round(sum(t for t, d in zip(per, stream) if d["kind"] == k), 2) for k in ("plin", "cl", "grad")}
+    sample = (f"CPU oracle (C++ restatement of Bolt's CPU algorithm) on {cores} threads: the whole {len(stream)}-request "
+              f"stream of the GPU arm, every request in full, {total:.1f} s (seconds by kind {by_kind})")
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "the serving stream of the GPU arm (bench.py module docstring), CPU oracle",
-                      "parallelism": "host cores"},
-           "cpu_baseline": {"value": v, "unit": UNIT, "cores": last[0], "kind": "port", "sample": last[1]},
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(stream),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "the serving stream of the GPU arm (bench.py module docstring), CPU oracle, "
+                                  "requests one after another", "parallelism": f"{cores} host threads",
+                      "reltol": RELTOL, "abstol": ABSTOL},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -597,7 +702,7 @@ def run_batch(args):
            "latency": {"p50_s": float(np.percentile([r.latency for r in res], 50)),
                        "p99_s": float(np.percentile([r.latency for r in res], 99))},
            "clocks": clocks, "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]),
-           "engine": {k: s1[k] - s0[k] for k in s1},
+           "engine": {k: s1[k] - s0[k] for k in s1 if k != "peak_inflight_bytes"},
            "roofline": {"bound": "fp64", "achieved": flops / win / 1e12, "peak": peak, "unit": "TFLOP/s",
                         "frac": flops / win / 1e12 / peak if peak else None, "kernel": "rodas_kernel",
                         "note": "algorithmic solver FLOPs of every request / the served window"}}
@@ -628,7 +733,7 @@ def run_pipeline(args):
     torch.cuda.synchronize()
     barrier(dist)
     sampler = clocks_sampler()
-    dev_ms, solver_us, los_us, steps, launches = [], 0, 0, 0, 0
+    dev_ms, solver_us, los_us, steps, launches, terms = [], 0, 0, 0, 0, 0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -639,13 +744,14 @@ def run_pipeline(args):
         los_us += s["los_us"]
         steps += s["accepted_steps"] + s["rejected_steps"]
         launches += s["kernel_launches"]
+        terms += s["los_terms"]
     torch.cuda.synchronize()
     clocks = clocks_summary(sampler)
     total_ms = max_over_ranks(sum(dev_ms), dist)
     value = ws * args.steps / (total_ms / 1000.0)
     peak = ctypes_peak(B._lib.load(), local)
     sol = steps * solver_flops_per_step(N, 15) / (solver_us / 1e6) / 1e12
-    los = los_flops(ells.size, 4999, 799) * args.steps / (los_us / 1e6) / 1e12
+    los = los_flops(terms) / (los_us / 1e6) / 1e12
     if rank == 0:
         out = {"metric": "C_l spectra/s, full CMB pipeline, one cosmology per call (device time)", "value": value,
                "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -660,6 +766,9 @@ def run_pipeline(args):
                             "frac": sol / peak if peak else None, "traffic": None, "kernel": "rodas_kernel",
                             "breakdown": {"rodas_kernel_ms_per_step": solver_us / 1000.0 / args.steps,
                                           "los_ms_per_step": los_us / 1000.0 / args.steps, "los_cl_tflops": los,
+                                          "los_cl_frac": los / peak if peak else None,
+                                          "los_terms_per_step": terms / args.steps,
+                                          "los_terms_nominal": ells.size * 4999 * 799,
                                           "steps_per_spectrum": steps / args.steps}}}
         print(json.dumps(out))
     if dist is not None:
@@ -681,6 +790,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="serving", choices=["serving", "pipeline", "batch", "grad"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sweep", dest="sweep", action="store_false", help="serving: skip the arrival-rate sweep")
     ap.add_argument("--grad-requests", type=int, default=6, help="serving: size of the C_l+gradient-only stream")
     ap.add_argument("--rate", type=float, default=RATE, help="serving: Poisson arrival rate, requests/s")
     ap.add_argument("--nk", type=int, default=1200, help="pipeline: source-grid wavenumbers")

@@ -83,8 +83,8 @@ class Context:
         out = np.zeros(8, dtype=np.int64)
         self.lib.bolt_last_stats(self.h, out.ctypes.data_as(C.POINTER(C.c_int64)))
         keys = ["accepted_steps", "rejected_steps", "solver_us", "los_us", "modes", "solver_launches",
-                "kernel_launches"]
-        return dict(zip(keys, (int(v) for v in out[:7])))
+                "kernel_launches", "los_terms"]
+        return dict(zip(keys, (int(v) for v in out)))
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:

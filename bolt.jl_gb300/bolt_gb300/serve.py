@@ -200,10 +200,10 @@ class Engine:
         return p.result(rc, err.value.decode(), np.zeros(5)), grad
 
     def stats(self) -> dict:
-        out = np.zeros(11, dtype=np.int64)
+        out = np.zeros(12, dtype=np.int64)
         self.lib.bolt_engine_stats(self.h, out.ctypes.data_as(C.POINTER(C.c_int64)))
         keys = ["batches", "requests", "modes", "solver_us", "los_us", "steps", "kernel_launches",
-                "graph_launches", "batches_wpm1", "batches_wpm2", "batches_wpm4"]
+                "graph_launches", "batches_wpm1", "batches_wpm2", "batches_wpm4", "peak_inflight_bytes"]
         return dict(zip(keys, (int(v) for v in out)))
 
     def close(self):

@@ -179,4 +179,41 @@ __device__ __forceinline__ double spl_cold(const CosmoDev& c, int id, double x) 
           p[i + 3] * t2 * t) * (1.0 / 6.0);
 }
 
+// Arguments of the line-of-sight kernels (los.cu): the C_l reduction of
+// cltt / clte / clee (spectra.jl:70-160) over ncz cosmologies, and the C_l^TT
+// reduction with its tangent along six parameter directions.
+struct LosArgs {
+  int nb, nslots, nrow, nm;
+  const int* ells;          // [nslots]
+  const double* coef;       // [ncz][nslots][nb+2]
+  const double* inv_dg;     // [ncz]
+  const double* yv;         // [ncz][nrow]  eta0 - eta(x_i)
+  const double* kmid;       // [ncz][nm]
+  const double* wts;        // [ncz][nm]
+  const double* SdT;        // [ncz][nrow][nm]
+  const double* SdE;        // [ncz][nrow][nm] or null
+  double* tt;               // [ncz][nslots]
+  double* te;
+  double* ee;
+  unsigned long long* terms;  // (l, k, x) terms evaluated, accumulated (null: not counted)
+};
+
+struct LosGradArgs {
+  int nb, nslots, nrow, nm;
+  const int* ells;
+  const double* coef;   // [nslots][nb+2]
+  const double* inv_dg; // [1]
+  const double* yv;     // [nrow]
+  const double* dyv;    // [6][dstride]
+  const double* kmid;   // [nm]
+  const double* wts;    // [nm]
+  const double* dwts;   // [6][dstride]
+  int dstride;          // stride of dwts and dyv per direction
+  const double* Sd;     // [nrow][nm]
+  const double* dSd;    // [6][nrow][nm]
+  double* tt;           // [nslots]
+  double* dtt;          // [6][nslots]
+  unsigned long long* terms;  // (l, k, x) terms evaluated, accumulated (null: not counted)
+};
+
 }  // namespace bolt

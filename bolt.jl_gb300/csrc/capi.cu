@@ -27,20 +27,6 @@ size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm);
 size_t rodas_scratch_per_warp(int maxN);
 int launch_rsa_post(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const int* d_first, int nout,
                     cudaStream_t stream);
-struct LosArgs {
-  int nb, nslots, nrow, nm;
-  const int* ells;
-  const double* coef;
-  const double* inv_dg;
-  const double* yv;
-  const double* kmid;
-  const double* wts;
-  const double* SdT;
-  const double* SdE;
-  double* tt;
-  double* te;
-  double* ee;
-};
 int launch_jl_raw(int nb, const double* d_dgs, int ncz, int Lmax, const int* d_slot_of_l, int nslots, double* d_raw,
                   double* d_norm, int* d_flags, cudaStream_t st);
 int launch_jl_prefilter(int nb, int nslots, int ncz, const double* d_raw, const double* d_norm, const double* d_w,
@@ -104,7 +90,7 @@ struct bolt_ctx {
   std::vector<CosmoEntry> cos;
   DBuf d_cos;
   DBuf modes, xout, srcT, srcE, traj, plin, status, counters, queue, flags, scratch;
-  DBuf kgrid, raw, norm, coef, w, slot_of_l, ells, SdT, SdE, kmid, wts, yv, dx, dgs, idg, out;
+  DBuf kgrid, raw, norm, coef, w, slot_of_l, ells, SdT, SdE, kmid, wts, yv, dx, dgs, idg, out, terms;
   std::string err;
   int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
@@ -362,6 +348,8 @@ void run_los(bolt_ctx* c, int id, const double* d_ST, const double* d_SE, int sr
   ck(cudaMemcpyAsync(d_ells, uniq.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st), "ells");
   ck(cudaMemcpyAsync(d_dg, dgv, 2 * sizeof(double), cudaMemcpyHostToDevice, st), "dg");
   ck(cudaMemsetAsync(d_flags, 0, sizeof(int), st), "flags");
+  unsigned long long* d_terms = c->terms.as<unsigned long long>(1);
+  ck(cudaMemsetAsync(d_terms, 0, sizeof(unsigned long long), st), "terms");
   ck(cudaEventRecord(c->ev[2], st), "event");
   int rc = launch_jl_raw(nb, d_dg, 1, Lmax, d_sl, ns, d_raw, d_norm, d_flags, st);
   if (!rc) rc = launch_jl_prefilter(nb, ns, 1, d_raw, d_norm, d_w, d_coef, st);
@@ -373,12 +361,16 @@ void run_los(bolt_ctx* c, int id, const double* d_ST, const double* d_SE, int sr
   a.ells = d_ells; a.coef = d_coef; a.inv_dg = d_dg + 1; a.yv = d_yv; a.kmid = d_kmid; a.wts = d_wts;
   a.SdT = d_SdT; a.SdE = d_SdE;
   a.tt = d_out; a.te = d_SE ? d_out + ns : nullptr; a.ee = d_SE ? d_out + 2 * ns : nullptr;
+  a.terms = d_terms;
   rc = launch_los_cl(a, 1, st);
   if (rc) throw Err(-3, std::string("LOS launch: ") + cudaGetErrorString(cudaError_t(rc)));
   ck(cudaEventRecord(c->ev[3], st), "event");
   std::vector<double> out(3 * size_t(ns));
+  unsigned long long terms = 0;
   ck(cudaMemcpyAsync(out.data(), d_out, 3 * ns * sizeof(double), cudaMemcpyDeviceToHost, st), "cl out");
+  ck(cudaMemcpyAsync(&terms, d_terms, sizeof(terms), cudaMemcpyDeviceToHost, st), "terms");
   ck(cudaStreamSynchronize(st), "los");
+  c->stats[7] += int64_t(terms);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
   c->stats[3] += int64_t(ms * 1000.0);

@@ -62,20 +62,6 @@ int rodas_node_params(int wpm, const ModeDev* d_modes, int nmodes, const CosmoDe
                       cudaKernelNodeParams* p);
 size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm);
 size_t rodas_scratch_per_warp(int maxN);
-struct LosArgs {
-  int nb, nslots, nrow, nm;
-  const int* ells;
-  const double* coef;
-  const double* inv_dg;
-  const double* yv;
-  const double* kmid;
-  const double* wts;
-  const double* SdT;
-  const double* SdE;
-  double* tt;
-  double* te;
-  double* ee;
-};
 int launch_jl_raw(int nb, const double* d_dgs, int ncz, int Lmax, const int* d_slot_of_l, int nslots, double* d_raw,
                   double* d_norm, int* d_flags, cudaStream_t st);
 int launch_jl_prefilter(int nb, int nslots, int ncz, const double* d_raw, const double* d_norm, const double* d_w,
@@ -83,22 +69,6 @@ int launch_jl_prefilter(int nb, int nslots, int ncz, const double* d_raw, const 
 int launch_sdense(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_ST, const double* d_SE, int nm,
                   const double* d_kmid, const double* d_dx, double* d_SdT, double* d_SdE, cudaStream_t st);
 int launch_los_cl(const LosArgs& a, int ncz, cudaStream_t st);
-struct LosGradArgs {
-  int nb, nslots, nrow, nm;
-  const int* ells;
-  const double* coef;
-  const double* inv_dg;
-  const double* yv;
-  const double* dyv;
-  const double* kmid;
-  const double* wts;
-  const double* dwts;
-  int dstride;
-  const double* Sd;
-  const double* dSd;
-  double* tt;
-  double* dtt;
-};
 int launch_sdense_diff(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_Sa, const double* d_Sb,
                        double scale, int nm, const double* d_kmid, const double* d_dx, double* d_out, cudaStream_t st);
 int launch_los_tt_grad(const LosGradArgs& a, cudaStream_t st);
@@ -280,7 +250,7 @@ struct bolt_engine {
   size_t inflight_bytes = 0;
   size_t budget = 0;
   Tuner tuner;
-  int64_t stats[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t stats[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   double* d_w = nullptr;  // Bessel prefilter pivots (constant)
   int* d_flags = nullptr;
 };
@@ -760,6 +730,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
       a.ells = ells; a.coef = coef; a.inv_dg = misc + 1;
       a.wts = per; a.yv = per + P.nm; a.dwts = per + (P.nm + n); a.dyv = per + (P.nm + n) + P.nm; a.dstride = P.nm + n;
       a.kmid = kmid; a.Sd = SdT; a.dSd = dSd; a.tt = cl; a.dtt = cl + P.ns;
+      a.terms = nullptr;
       rc = launch_los_tt_grad(a, st);
       if (rc != 0) throw EngErr(-3, std::string("line of sight (tangent): ") + cudaGetErrorString(cudaError_t(rc)));
       launches += 2 + kTheta;
@@ -778,6 +749,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
       a.SdT = SdT; a.SdE = SE ? SdE : nullptr;
       double* out = cl + size_t(s) * 3 * P.ns;
       a.tt = out; a.te = SE ? out + P.ns : nullptr; a.ee = SE ? out + 2 * P.ns : nullptr;
+      a.terms = nullptr;
       rc = launch_los_cl(a, 1, st);
       if (rc != 0) throw EngErr(-3, std::string("line of sight: ") + cudaGetErrorString(cudaError_t(rc)));
       launches += 2;
@@ -972,6 +944,7 @@ void scheduler(bolt_engine* E) {
         }
         if (batch.empty()) continue;
         E->inflight_bytes += bytes;
+        E->stats[11] = std::max<int64_t>(E->stats[11], int64_t(E->inflight_bytes));
         const double t = now_s(E->t0);
         for (Req* r : batch) { r->state = 2; r->t[2] = t; }
         L.busy = true;
@@ -1305,7 +1278,7 @@ int bolt_plin_vjp(bolt_engine* E, const bolt_request* q, const double* ybar, dou
 int bolt_engine_stats(bolt_engine* E, int64_t* out) {
   if (!E || !out) return -1;
   std::lock_guard<std::mutex> g(E->mu);
-  std::copy(E->stats, E->stats + 11, out);
+  std::copy(E->stats, E->stats + 12, out);
   return 0;
 }
 

@@ -184,22 +184,16 @@ __global__ void sdense_kernel(int nx, int i0, int nrow, int nk, const double* __
 // shared memory; each thread owns k midpoints and runs the x sum for them.
 // wts[m] = A (k_m/0.05)^(n-1) dk_m / k_m.  The block reduction is in a
 // fixed order so results are bitwise reproducible run to run.
-struct LosArgs {
-  int nb, nslots, nrow, nm;
-  const int* ells;          // [nslots]
-  const double* coef;       // [ncz][nslots][nb+2]
-  const double* inv_dg;     // [ncz]
-  const double* yv;         // [ncz][nrow]  eta0 - eta(x_i)
-  const double* kmid;       // [ncz][nm]
-  const double* wts;        // [ncz][nm]
-  const double* SdT;        // [ncz][nrow][nm]
-  const double* SdE;        // [ncz][nrow][nm] or null
-  double* tt;               // [ncz][nslots]
-  double* te;
-  double* ee;
-};
 
 constexpr double kSkipRel = 1e-14;
+
+// Adds the warp's evaluated-term count to *terms (one atomic per warp).
+__device__ __forceinline__ void count_terms(unsigned long long* terms, unsigned long long n) {
+  if (!terms) return;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(terms, n);
+}
 
 __global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
   extern __shared__ double sh[];
@@ -248,6 +242,7 @@ __global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
   const double* wm = a.wts + (size_t)cz * a.nm;
   const double umax = double(a.nb - 2);
   double stt = 0.0, ste = 0.0, see = 0.0;
+  unsigned long long nterm = 0;
   for (int m = threadIdx.x; m < a.nm; m += blockDim.x) {
     const double k = km[m];
     double th = 0.0, ep = 0.0;
@@ -261,6 +256,7 @@ __global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
       }
       iend = hi;
     }
+    nterm += iend;
     for (int i = 0; i < iend; ++i) {
       double u = k * yl[i];
       double f = floor(u);
@@ -280,6 +276,7 @@ __global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
     ste = fma(th * ep, w, ste);
     see = fma(ep * ep, w, see);
   }
+  count_terms(a.terms, nterm);
   red[threadIdx.x] = stt;
   red[blockDim.x + threadIdx.x] = ste;
   red[2 * blockDim.x + threadIdx.x] = see;
@@ -313,22 +310,6 @@ __global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
 // j_l spline evaluation (value and slope) serves all six directions.
 constexpr int kDir = 6;
 
-struct LosGradArgs {
-  int nb, nslots, nrow, nm;
-  const int* ells;
-  const double* coef;   // [nslots][nb+2]
-  const double* inv_dg; // [1]
-  const double* yv;     // [nrow]
-  const double* dyv;    // [kDir][dstride]
-  const double* kmid;   // [nm]
-  const double* wts;    // [nm]
-  const double* dwts;   // [kDir][dstride]
-  int dstride;          // stride of dwts and dyv per direction
-  const double* Sd;     // [nrow][nm]
-  const double* dSd;    // [kDir][nrow][nm]
-  double* tt;           // [nslots]
-  double* dtt;          // [kDir][nslots]
-};
 
 __global__ void __launch_bounds__(256) los_tt_grad_kernel(LosGradArgs a) {
   extern __shared__ double sh[];
@@ -372,6 +353,7 @@ __global__ void __launch_bounds__(256) los_tt_grad_kernel(LosGradArgs a) {
   const double umax = double(a.nb - 2);
   const size_t plane = (size_t)a.nrow * a.nm;
   double stt = 0.0, dstt[kDir];
+  unsigned long long nterm = 0;
 #pragma unroll
   for (int j = 0; j < kDir; ++j) dstt[j] = 0.0;
   for (int m = threadIdx.x; m < a.nm; m += blockDim.x) {
@@ -385,6 +367,7 @@ __global__ void __launch_bounds__(256) los_tt_grad_kernel(LosGradArgs a) {
       }
       iend = hi;
     }
+    nterm += iend;
     double th = 0.0, dth[kDir];
 #pragma unroll
     for (int j = 0; j < kDir; ++j) dth[j] = 0.0;
@@ -415,6 +398,7 @@ __global__ void __launch_bounds__(256) los_tt_grad_kernel(LosGradArgs a) {
     for (int j = 0; j < kDir; ++j)
       dstt[j] = fma(2.0 * w * th, dth[j], fma(a.dwts[(size_t)j * a.dstride + m], th * th, dstt[j]));
   }
+  count_terms(a.terms, nterm);
   red[threadIdx.x] = stt;
 #pragma unroll
   for (int j = 0; j < kDir; ++j) red[(1 + j) * blockDim.x + threadIdx.x] = dstt[j];

@@ -155,7 +155,9 @@ int bolt_set_dense_x(bolt_ctx* ctx, double x_dense);
 
 /* Counters of the last call: [0] accepted steps, [1] rejected steps,
  * [2] solver kernel microseconds, [3] LOS kernels microseconds,
- * [4] modes, [5] solver kernel launches, [6] total kernel launches. */
+ * [4] modes, [5] solver kernel launches, [6] total kernel launches,
+ * [7] (l, k, x) terms the line-of-sight reduction evaluated (those below
+ * the Bessel turning point are skipped).  out[8]. */
 int bolt_last_stats(bolt_ctx* ctx, int64_t* out);
 
 /* Allocation-free source grid (no counterpart in the reference; added for
@@ -298,7 +300,8 @@ int bolt_plin_vjp(bolt_engine* eng, const bolt_request* req, const double* ybar,
 /* Engine counters: [0] batches, [1] requests completed, [2] modes solved,
  * [3] solver microseconds (sum over batches), [4] LOS microseconds,
  * [5] accepted + rejected steps, [6] kernel launches, [7] graph launches,
- * [8..10] batches run with 1 / 2 / 4 warps per mode. */
+ * [8..10] batches run with 1 / 2 / 4 warps per mode, [11] the largest
+ * device footprint of the batches in flight at once (bytes).  out[12]. */
 int bolt_engine_stats(bolt_engine* eng, int64_t* out);
 
 #ifdef __cplusplus

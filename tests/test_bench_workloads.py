@@ -65,3 +65,22 @@ def test_solver_flop_count_and_state_length():
     assert bench.state_len(20, 20, 10, 15) == 233
     assert bench.state_len(50, 50, 20, 15) == 473
     assert bench.solver_flops_per_step(473, 15) == 159 * 473 + 560 * 20 + 66 * 15 + 650
+
+
+def test_cpu_arm_runs_whole_requests():
+    """The CPU oracle runs each request of the stream in full (no sampling or
+    scaling model); tiny versions of the three request types here."""
+    O = bench._oracle()
+    s = bench.make_stream(10)
+    for kind in ("plin", "cl", "grad"):
+        d = next(x for x in s if x["kind"] == kind)
+        d = {**d, "nk": 4, "lmax": 20, "hier": (8, 8, 10, 15) if kind != "plin" else (8, 8, 10, 15)}
+        assert bench.oracle_request(O, d, 2) > 0.0
+    v, cores, sample = bench.cpu_prefix([{**s[0], "nk": 4, "hier": (8, 8, 10, 15)}], budget_s=0.0)
+    assert v > 0 and cores >= 1 and "first 1 requests" in sample
+
+
+def test_los_flops_from_terms():
+    assert bench.los_flops(1000) == 27000.0
+    assert bench.los_flops(1000, with_e=False) == 25000.0
+    assert bench.SWEEP_RATES == (10.0, 100.0, 500.0, 2000.0)
