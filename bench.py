@@ -33,7 +33,8 @@ metric's request type), served vs the drop-in and vs the engine one request
 per call.
 
 ``rates`` = the same stream served at Poisson arrival rates of 10, 100, 500
-and 2000 requests/s (the serving configuration's sweep), each through a fresh
+and 2000 requests/s (the serving configuration's sweep) and at 1 request/s
+(below the GPU's capacity, for the unloaded latency), each through a fresh
 engine: spectra/s, p50 / p99 latency, requests that waited for a lane or the
 memory budget, host table-build times and the largest device footprint in
 flight; ``roofline_los`` = the line-of-sight kernels' FP64 rate in the plain
@@ -360,7 +361,7 @@ def cpu_prefix(stream, budget_s=30.0):
 
 
 # ---------------------------------------------------------------- serving --
-SWEEP_RATES = (10.0, 100.0, 500.0, 2000.0)  # requests/s, the serving configuration's range
+SWEEP_RATES = (1.0, 10.0, 100.0, 500.0, 2000.0)  # requests/s: the serving configuration's range, and 1/s below it
 
 
 def serve_at_rate(B, local, stream, rate, seed):

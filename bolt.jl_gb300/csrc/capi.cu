@@ -739,7 +739,7 @@ int bolt_set_dense_x(bolt_ctx* c, double x) {
 
 int bolt_last_stats(bolt_ctx* c, int64_t* out) {
   if (!c || !out) return -1;
-  std::copy(c->stats, c->stats + 7, out);
+  std::copy(c->stats, c->stats + 8, out);
   return 0;
 }
 

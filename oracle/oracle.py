@@ -65,6 +65,20 @@ def lib():
         L.oracle_recfast_xe.argtypes = [C.POINTER(_Params), C.c_double, C.c_double, C.c_double, C.c_int,
                                         C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                         _dp, C.c_int, _dp]
+        L.oracle_dual_cosmo_theta.restype = C.c_void_p
+        L.oracle_dual_cosmo_theta.argtypes = [_dp, C.POINTER(_Params), C.c_double, C.c_double, C.c_double, C.c_int,
+                                              C.c_double, C.c_double]
+        L.oracle_dual_cosmo_omega_b.restype = C.c_void_p
+        L.oracle_dual_cosmo_omega_b.argtypes = [C.POINTER(_Params), C.c_double, C.c_double, C.c_double, C.c_int,
+                                                C.c_double]
+        L.oracle_dual_free.argtypes = [C.c_void_p]
+        L.oracle_dual_table.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp]
+        L.oracle_dual_eta0.argtypes = [C.c_void_p, _dp]
+        L.oracle_dual_plin.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                       C.c_double, C.c_double, _dp]
+        L.oracle_dual_cltt.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                       C.c_double, _ip, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, _dp,
+                                       C.c_int]
         L.oracle_rhs.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                  _dp, _dp, _dp]
         L.oracle_jacobian.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
@@ -240,6 +254,74 @@ class Cosmo:
         if st.value != 0:
             raise RuntimeError(f"oracle_plin status {st.value}")
         return v
+
+
+THETA_NAMES = ("h", "omega_b", "omega_c", "n_s", "A_s", "Sigma_m_nu_eV")
+
+
+class DualCosmo:
+    """The gradient oracle: Background + RECFAST + IonizationHistory whose
+    every quantity carries its partial derivatives (oracle/oracle_grad.hpp),
+    the reference's ForwardDiff gradient restated.  Build it from theta =
+    (h, omega_b, omega_c, n_s, A_s, Sigma m_nu [eV]) (partials along theta),
+    or with ``omega_b_only`` from a Params with the single partial along
+    Omega_b (the reference's bg_fwddiff / ih_fwddiff tests).  Results come
+    as (value, partials)."""
+
+    def __init__(self, theta=None, params: Params | None = None, x_grid=(-20.0, 0.01, 0.0), nq=15,
+                 recfast_tol=1e-8, recfast_atol=None, omega_b_only=False):
+        base = params or Params()
+        self._pc = base.c()
+        if omega_b_only:
+            self.h = lib().oracle_dual_cosmo_omega_b(C.byref(self._pc), x_grid[0], x_grid[1], x_grid[2], nq,
+                                                     recfast_tol)
+        else:
+            th = np.ascontiguousarray(theta, dtype=np.float64)
+            self.h = lib().oracle_dual_cosmo_theta(_d(th), C.byref(self._pc), x_grid[0], x_grid[1], x_grid[2], nq,
+                                                   recfast_tol, -1.0 if recfast_atol is None else recfast_atol)
+        if not self.h:
+            raise RuntimeError("gradient oracle construction failed")
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().oracle_dual_free(self.h)
+        except Exception:
+            pass
+
+    def table(self, name, x):
+        x = np.ascontiguousarray(np.atleast_1d(x), dtype=np.float64)
+        out = np.zeros((x.size, 7))
+        if lib().oracle_dual_table(self.h, TABLES.index(name), _d(x), x.size, _d(out)) != 0:
+            raise ValueError(f"table {name} not available in the gradient oracle")
+        return out[:, 0], out[:, 1:]
+
+    def eta0(self):
+        out = np.zeros(7)
+        lib().oracle_dual_eta0(self.h, _d(out))
+        return out[0], out[1:]
+
+    def plin(self, k, nq=15, lg=50, lnu=50, lmnu=20, x=0.0, reltol=1e-5, abstol=1e-6):
+        out = np.zeros(7)
+        st = lib().oracle_dual_plin(self.h, k, nq, lg, lnu, lmnu, x, reltol, abstol, _d(out))
+        if st != 0:
+            raise RuntimeError(f"oracle_dual_plin status {st}")
+        return out[0], out[1:]
+
+    def cltt(self, k_grid, ells, lg=8, lnu=8, lmnu=10, nq=15, reltol=1e-8, abstol=1e-8, kd=None, bessel_argmax=None,
+             nthreads=0):
+        """C_l^TT and its partials on the source-grid k (frozen), the dense k
+        grid kd = (kmin, kmax, n) (frozen) and the Bessel grid's upper end
+        (frozen).  Returns (tt[nell], dtt[6][nell])."""
+        kg = np.ascontiguousarray(k_grid, dtype=np.float64)
+        ells = np.ascontiguousarray(ells, dtype=np.int32)
+        out = np.zeros((ells.size, 7))
+        st = lib().oracle_dual_cltt(self.h, _d(kg), kg.size, lg, lnu, lmnu, nq, reltol, abstol,
+                                    ells.ctypes.data_as(_ip), ells.size, kd[0], kd[1], kd[2], bessel_argmax,
+                                    _d(out), nthreads)
+        if st != 0:
+            raise RuntimeError(f"oracle_dual_cltt status {st}")
+        return out[:, 0], out[:, 1:].T.copy()
 
 
 def recfast_xe(p: Params, z, x_grid=(-20.0, 0.01, 0.0), nq=15, OmegaG=None, Tnow=-1.0, tol=1e-8):

@@ -6,7 +6,7 @@
 #include <cstdio>
 #include <memory>
 
-#include "oracle_perturb.hpp"
+#include "oracle_grad.hpp"
 
 using namespace orc;
 
@@ -226,27 +226,8 @@ int oracle_boltsolve(void* h, double k, int lg, int lnu, int lmnu, int nq, doubl
 int oracle_source_grid(void* h, const double* kg, int nk, int lg, int lnu, int lmnu, int nq, double reltol,
                        double abstol, double* ST, double* SE, long* steps, int nthreads) {
   OCosmo* o = static_cast<OCosmo*>(h);
-  const Grid& g = o->bg->xg;
-  int nx = g.n;
-  std::vector<double> xo(nx);
-  for (int j = 0; j < nx; ++j) xo[j] = g.at(j);
-  int worst = 0;
   if (nthreads > 0) omp_set_num_threads(nthreads);
-#pragma omp parallel for schedule(dynamic, 1) reduction(max : worst)
-  for (int ik = 0; ik < nk; ++ik) {
-    Mode md(&o->C, kg[ik], lg, lnu, lmnu, nq);
-    std::vector<double> du(md.N);
-    SolveStats s = solve_mode(md, reltol, abstol, xo, [&](int j, double x, const double* y) {
-      hierarchy_rhs<double>(md, x, y, du.data());
-      double st, se;
-      source_functions(md, x, y, du.data(), st, se);
-      ST[size_t(ik) * nx + j] = st;
-      SE[size_t(ik) * nx + j] = se;
-    });
-    if (steps) steps[ik] = s.steps;
-    worst = std::max(worst, s.status);
-  }
-  return worst;
+  return source_grid_of(o->C, kg, nk, lg, lnu, lmnu, nq, reltol, abstol, ST, SE, steps);
 }
 
 int oracle_cl_frozen(void* h, const double* ST, const double* SE, const double* kg, int nk, const int* ells, int nell,
@@ -284,71 +265,11 @@ int oracle_cl_frozen(void* h, const double* ST, const double* SE, const double* 
                      double kd_min, double kd_max, int nkd, double argmax_in, double* tt, double* te, double* ee,
                      int nthreads) {
   OCosmo* o = static_cast<OCosmo*>(h);
-  const Background& bg = *o->bg;
-  const Params& par = o->C.par;
-  const Grid& g = bg.xg;
-  int nx = g.n;
   std::vector<double> kd(nkd);
   oracle_quadratic_k(kd_min, kd_max, nkd, kd.data());
-  double argmax = argmax_in > 0 ? argmax_in : kd[nkd - 1] * bg.eta0;
-  double dg = argmax / 5000.0;
-  const int nb = 5001;
-  int Lmax = 0;
-  for (int i = 0; i < nell; ++i) Lmax = std::max(Lmax, ells[i]);
-  // j_l on the Bessel grid, all requested l
-  std::vector<double> jtab(size_t(nell) * nb);
+  double argmax = argmax_in > 0 ? argmax_in : kd[nkd - 1] * o->bg->eta0;
   if (nthreads > 0) omp_set_num_threads(nthreads);
-#pragma omp parallel
-  {
-    std::vector<double> all(Lmax + 1);
-#pragma omp for schedule(dynamic, 16)
-    for (int ib = 0; ib < nb; ++ib) {
-      double xb = ib * dg;
-      sph_bessel_all(Lmax, xb, all.data());
-      for (int i = 0; i < nell; ++i) jtab[size_t(i) * nb + ib] = all[ells[i]];
-    }
-  }
-  int xi = 0;
-  while (xi < nx && !(g.at(xi) > -8.0)) ++xi;
-  std::vector<double> yv(nx), dx(nx);
-  for (int i = xi; i < nx - 1; ++i) {
-    yv[i] = bg.eta0 - bg.eta(g.at(i));
-    dx[i] = g.at(i + 1) - g.at(i);
-  }
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int il = 0; il < nell; ++il) {
-    int l = ells[il];
-    std::vector<double> col(jtab.begin() + size_t(il) * nb, jtab.begin() + size_t(il + 1) * nb);
-    Spline bes(col, 0.0, dg);
-    double lfac = std::sqrt(double(int64_t(l + 2) * int64_t(l + 1) * int64_t(l) * int64_t(l - 1)));
-    double stt = 0.0, ste = 0.0, see = 0.0;
-    for (int m = 0; m < nkd - 1; ++m) {
-      double k = (kd[m] + kd[m + 1]) / 2.0;
-      double dk = kd[m + 1] - kd[m];
-      int j = 0;
-      if (k >= kg[nk - 1]) j = nk - 2;
-      else { while (j < nk - 2 && kg[j + 1] <= k) ++j; }
-      double w = (k - kg[j]) / (kg[j + 1] - kg[j]);
-      const double* sT0 = ST + size_t(j) * nx;
-      const double* sT1 = ST + size_t(j + 1) * nx;
-      const double* sE0 = SE ? SE + size_t(j) * nx : nullptr;
-      const double* sE1 = SE ? SE + size_t(j + 1) * nx : nullptr;
-      double th = 0.0, ep = 0.0;
-      for (int i = xi; i < nx - 1; ++i) {
-        double b = bes(k * yv[i]);
-        th += b * ((1.0 - w) * sT0[i] + w * sT1[i]) * dx[i];
-        if (sE0) ep += b * ((1.0 - w) * sE0[i] + w * sE1[i]) * dx[i];
-      }
-      ep *= lfac;
-      double Pp = par.A * std::pow(k / 0.05, par.n - 1.0);
-      stt += th * th * Pp * dk / k;
-      ste += th * ep * Pp * dk / k;
-      see += ep * ep * Pp * dk / k;
-    }
-    if (tt) tt[il] = 4.0 * M_PI * stt;
-    if (te) te[il] = 4.0 * M_PI * ste;
-    if (ee) ee[il] = 4.0 * M_PI * see;
-  }
+  cl_of(o->C, ST, SE, kg, nk, ells, nell, kd, argmax, tt, te, ee);
   return 0;
 }
 
@@ -356,38 +277,128 @@ int oracle_cl_frozen(void* h, const double* ST, const double* SE, const double* 
 double oracle_plin(void* h, double k, int nq, int lg, int lnu, int lmnu, double x, double reltol, double abstol,
                    int* status) {
   OCosmo* o = static_cast<OCosmo*>(h);
-  const Background& bg = *o->bg;
-  const Params& p = o->C.par;
-  Mode md(&o->C, k, lg, lnu, lmnu, nq);
-  std::vector<double> u(md.N);
-  std::vector<double> xo(1, x);
-  SolveStats s = solve_mode(md, reltol, abstol, xo, [&](int, double, const double* y) {
-    std::copy(y, y + md.N, u.begin());
-  });
-  if (status) *status = s.status;
-  double a = std::exp(x);
-  std::vector<double> M0(nq), M1(nq), M2(nq);
-  for (int i = 0; i < nq; ++i) { M0[i] = u[md.M(0, i)]; M1[i] = u[md.M(1, i)]; M2[i] = u[md.M(2, i)]; }
-  double rho, sig;
-  rho_sigma(md, a, M0.data(), M2.data(), rho, sig);
-  double r0 = bg.rho0M(x);
-  double Mrho = rho / r0;
-  double th = 0.0;
-  for (int i = 0; i < nq; ++i) th += md.Bq[i] * M1[i];
-  double Mth = k * th / r0;
-  double dcN = u[md.iPhi + 1], dbN = u[md.iPhi + 3], vcN = u[md.iPhi + 2], vbN = u[md.iPhi + 4];
-  double vmnuN = -Mth / k;
-  double Tg = std::pow(15.0 / (M_PI * M_PI) * bg.rho_crit * p.Omega_r, 0.25);
-  double nufac = (90.0 * ZETA3 / (11.0 * std::pow(M_PI, 4))) * (p.Omega_r * p.h * p.h / Tg) * std::pow(p.N_nu / 3.0, 0.75);
-  double Omega_nu = p.Sigma_m_nu * nufac / (p.h * p.h);
-  double Om = p.Omega_c + p.Omega_b + Omega_nu;
-  double Hc = bg.H(x);
-  double dc = dcN - 3.0 * Hc * vcN / k;
-  double db = dbN - 3.0 * Hc * vbN / k;
-  double dmnu = Mrho - 3.0 * Hc * vmnuN / k;
-  double dm = (p.Omega_c * dc + p.Omega_b * db + Omega_nu * dmnu) / Om;
-  double Pprim = p.A * std::pow(k / 0.05, p.n - 1.0);
-  return (2.0 * M_PI * M_PI / (k * k * k)) * dm * dm * Pprim;
+  return plin_of(o->C, k, nq, lg, lnu, lmnu, x, reltol, abstol, status);
+}
+
+// ------------------------------------------------------- gradient oracle ---
+// Background + RECFAST + IonizationHistory with every quantity carrying its
+// partial derivatives (G6): the reference's ForwardDiff gradient restated.
+struct ODual {
+  CosmoT<G6> C;
+  std::unique_ptr<BackgroundT<G6>> bg;
+  std::unique_ptr<RecfastT<G6>> rf;
+  std::unique_ptr<IonizationT<G6>> ih;
+};
+
+static void* dual_build(const ParamsT<G6>& par, double x_start, double x_step, double x_stop, int nq,
+                        double recfast_tol, double recfast_atol) {
+  ODual* o = new ODual();
+  o->C.par = par;
+  o->bg.reset(new BackgroundT<G6>(o->C.par, Grid::range(x_start, x_step, x_stop), nq));
+  o->rf.reset(new RecfastT<G6>(o->bg.get(), par.Y_p, par.Omega_b, par.Omega_r, -1.0, recfast_tol));
+  if (recfast_atol > 0) o->rf->atol = recfast_atol;
+  o->ih.reset(new IonizationT<G6>(*o->rf, o->C.par, *o->bg));
+  o->C.bg = o->bg.get();
+  o->C.ih = o->ih.get();
+  return o;
+}
+
+// theta = (h, omega_b, omega_c, n_s, A_s, Sigma m_nu [eV]), partial j along
+// theta_j; Omega_b = omega_b / h^2, Omega_c = omega_c / h^2; Omega_r, Y_p and
+// N_nu from `fixed` (constants).  recfast_atol <= 0 keeps RECFAST's default.
+void* oracle_dual_cosmo_theta(const double* th, const oracle_params* fixed, double x_start, double x_step,
+                              double x_stop, int nq, double recfast_tol, double recfast_atol) {
+  try {
+    ParamsT<G6> q;
+    G6 h = G6::seed(th[0], 0), wb = G6::seed(th[1], 1), wc = G6::seed(th[2], 2);
+    q.h = h;
+    q.Omega_b = wb / (h * h);
+    q.Omega_c = wc / (h * h);
+    q.n = G6::seed(th[3], 3);
+    q.A = G6::seed(th[4], 4);
+    q.Sigma_m_nu = G6::seed(th[5], 5) * units().mass_natural;
+    q.Omega_r = fixed->Omega_r;
+    q.Y_p = fixed->Y_p;
+    q.N_nu = fixed->N_nu;
+    return dual_build(q, x_start, x_step, x_stop, nq, recfast_tol, recfast_atol);
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_dual_cosmo_theta: %s\n", e.what());
+    return nullptr;
+  }
+}
+
+// As above with the parameters of p and partial 0 along Omega_b alone (the
+// reference's bg_fwddiff / ih_fwddiff tests, runtests.jl:54-80).
+void* oracle_dual_cosmo_omega_b(const oracle_params* p, double x_start, double x_step, double x_stop, int nq,
+                                double recfast_tol) {
+  try {
+    ParamsT<G6> q;
+    q.h = p->h; q.Omega_r = p->Omega_r; q.Omega_c = p->Omega_c; q.A = p->A; q.n = p->n;
+    q.Y_p = p->Y_p; q.N_nu = p->N_nu; q.Sigma_m_nu = p->Sigma_m_nu;
+    q.Omega_b = G6::seed(p->Omega_b, 0);
+    return dual_build(q, x_start, x_step, x_stop, nq, recfast_tol, -1.0);
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_dual_cosmo_omega_b: %s\n", e.what());
+    return nullptr;
+  }
+}
+
+void oracle_dual_free(void* h) { delete static_cast<ODual*>(h); }
+
+static void put7(const G6& v, double* out) {
+  out[0] = v.v;
+  for (int j = 0; j < kThetaN; ++j) out[1 + j] = v.d[j];
+}
+
+// Table `which` (as oracle_table_eval) at x: out[i * 7 + 0] the value,
+// out[i * 7 + 1 + j] its partial j.
+int oracle_dual_table(void* h, int which, const double* x, int n, double* out) {
+  ODual* o = static_cast<ODual*>(h);
+  const SplineT<G6>* s = nullptr;
+  switch (which) {
+    case 0: s = &o->bg->H; break;
+    case 3: s = &o->bg->eta; break;
+    case 6: s = &o->bg->rho0M; break;
+    case 7: s = &o->ih->Xe; break;
+    case 8: s = &o->ih->tau; break;
+    case 9: s = &o->ih->taup; break;
+    case 11: s = &o->ih->g; break;
+    case 14: s = &o->ih->Tmat; break;
+    case 15: s = &o->ih->csb2; break;
+    default: return -1;
+  }
+  for (int i = 0; i < n; ++i) put7((*s)(x[i]), out + 7 * size_t(i));
+  return 0;
+}
+
+// eta0 and its partials (out[7]).
+void oracle_dual_eta0(void* h, double* out) { put7(static_cast<ODual*>(h)->bg->eta0, out); }
+
+// plin(k) at x with its partials (out[7]); returns the solver status.
+int oracle_dual_plin(void* h, double k, int nq, int lg, int lnu, int lmnu, double x, double reltol, double abstol,
+                     double* out) {
+  ODual* o = static_cast<ODual*>(h);
+  int st = 0;
+  put7(plin_of(o->C, k, nq, lg, lnu, lmnu, x, reltol, abstol, &st), out);
+  return st;
+}
+
+// cltt (spectra.jl:84-100) with its partials from the source grid on kg
+// (frozen), the dense k grid quadratic_k(kd_min, kd_max, nkd) and the Bessel
+// grid's upper end argmax (both frozen): out[il * 7 + ...].
+int oracle_dual_cltt(void* h, const double* kg, int nk, int lg, int lnu, int lmnu, int nq, double reltol,
+                     double abstol, const int* ells, int nell, double kd_min, double kd_max, int nkd, double argmax,
+                     double* out, int nthreads) {
+  ODual* o = static_cast<ODual*>(h);
+  const int nx = o->bg->xg.n;
+  std::vector<G6> ST(size_t(nk) * nx), SE(size_t(nk) * nx), tt(nell);
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  int st = source_grid_of(o->C, kg, nk, lg, lnu, lmnu, nq, reltol, abstol, ST.data(), SE.data(), nullptr);
+  std::vector<double> kd(nkd);
+  oracle_quadratic_k(kd_min, kd_max, nkd, kd.data());
+  cl_of<G6>(o->C, ST.data(), nullptr, kg, nk, ells, nell, kd, argmax, tt.data(), nullptr, nullptr);
+  for (int i = 0; i < nell; ++i) put7(tt[i], out + 7 * size_t(i));
+  return st;
 }
 
 }  // extern "C"

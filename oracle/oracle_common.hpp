@@ -15,6 +15,7 @@
 #include <cstring>
 #include <functional>
 #include <stdexcept>
+#include <type_traits>
 #include <vector>
 
 namespace orc {
@@ -59,36 +60,165 @@ inline const Units& units() {
   return u;
 }
 
-// CosmoParams (Bolt.jl:56-66).  Sigma_m_nu is in Mpc^-1 like the reference.
-struct Params {
-  double h = 0.7, Omega_r = 5.0469e-5, Omega_b = 0.046, Omega_c = 0.224;
-  double A = 2.097e-9, n = 1.0, Y_p = 0.24, N_nu = 3.046, Sigma_m_nu = 0.0;
-};
 
-// ------------------------------------------------------------ dual (d/dx) --
-struct D1 {
-  double v, d;
-  D1(double v_ = 0.0, double d_ = 0.0) : v(v_), d(d_) {}
+// ------------------------------------------------------- dual numbers -----
+// Dual<P>: a value and its partial derivatives along P directions, the
+// arithmetic of ForwardDiff.Dual (the reference's gradient path).  Math
+// functions propagate the chain rule; comparisons compare values.
+template <int P>
+struct Dual {
+  double v = 0.0;
+  double d[P] = {};
+  Dual() {}
+  Dual(double a) : v(a) {}  // a constant: zero partials
+  static Dual seed(double a, int j) { Dual r(a); r.d[j] = 1.0; return r; }
+  Dual& operator+=(const Dual& b) { v += b.v; for (int i = 0; i < P; ++i) d[i] += b.d[i]; return *this; }
+  Dual& operator-=(const Dual& b) { v -= b.v; for (int i = 0; i < P; ++i) d[i] -= b.d[i]; return *this; }
+  Dual& operator*=(const Dual& b) { *this = *this * b; return *this; }
+  Dual& operator/=(const Dual& b) { *this = *this / b; return *this; }
+  friend Dual operator+(Dual a, const Dual& b) { a += b; return a; }
+  friend Dual operator-(Dual a, const Dual& b) { a -= b; return a; }
+  friend Dual operator-(Dual a) { a.v = -a.v; for (int i = 0; i < P; ++i) a.d[i] = -a.d[i]; return a; }
+  friend Dual operator*(const Dual& a, const Dual& b) {
+    Dual r(a.v * b.v);
+    for (int i = 0; i < P; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    return r;
+  }
+  friend Dual operator/(const Dual& a, const Dual& b) {
+    Dual r(a.v / b.v);
+    const double ib = 1.0 / b.v;
+    for (int i = 0; i < P; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+    return r;
+  }
+  friend Dual operator+(Dual a, double b) { a.v += b; return a; }
+  friend Dual operator+(double b, Dual a) { a.v += b; return a; }
+  friend Dual operator-(Dual a, double b) { a.v -= b; return a; }
+  friend Dual operator-(double b, const Dual& a) { return Dual(b) - a; }
+  friend Dual operator*(Dual a, double b) { a.v *= b; for (int i = 0; i < P; ++i) a.d[i] *= b; return a; }
+  friend Dual operator*(double b, Dual a) { return a * b; }
+  friend Dual operator/(Dual a, double b) { a.v /= b; for (int i = 0; i < P; ++i) a.d[i] /= b; return a; }
+  friend Dual operator/(double b, const Dual& a) { return Dual(b) / a; }
+  friend bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
+  friend bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
+  friend bool operator<(const Dual& a, double b) { return a.v < b; }
+  friend bool operator>(const Dual& a, double b) { return a.v > b; }
+  friend bool operator<=(const Dual& a, double b) { return a.v <= b; }
+  friend bool operator>=(const Dual& a, double b) { return a.v >= b; }
+  friend bool operator<(double a, const Dual& b) { return a < b.v; }
+  friend bool operator>(double a, const Dual& b) { return a > b.v; }
+  friend bool operator==(const Dual& a, double b) { return a.v == b; }
+  friend bool operator!=(const Dual& a, double b) { return a.v != b; }
 };
-inline D1 operator+(D1 a, D1 b) { return {a.v + b.v, a.d + b.d}; }
-inline D1 operator-(D1 a, D1 b) { return {a.v - b.v, a.d - b.d}; }
-inline D1 operator-(D1 a) { return {-a.v, -a.d}; }
-inline D1 operator*(D1 a, D1 b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
-inline D1 operator/(D1 a, D1 b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
-inline D1 operator+(D1 a, double b) { return {a.v + b, a.d}; }
-inline D1 operator+(double b, D1 a) { return {a.v + b, a.d}; }
-inline D1 operator-(D1 a, double b) { return {a.v - b, a.d}; }
-inline D1 operator-(double b, D1 a) { return {b - a.v, -a.d}; }
-inline D1 operator*(D1 a, double b) { return {a.v * b, a.d * b}; }
-inline D1 operator*(double b, D1 a) { return {a.v * b, a.d * b}; }
-inline D1 operator/(D1 a, double b) { return {a.v / b, a.d / b}; }
-inline D1 operator/(double b, D1 a) { return {b / a.v, -b * a.d / (a.v * a.v)}; }
+template <int P> Dual<P> chain(const Dual<P>& a, double f, double df) {
+  Dual<P> r(f);
+  for (int i = 0; i < P; ++i) r.d[i] = df * a.d[i];
+  return r;
+}
+template <int P> Dual<P> exp(const Dual<P>& a) { double e = std::exp(a.v); return chain(a, e, e); }
+template <int P> Dual<P> log(const Dual<P>& a) { return chain(a, std::log(a.v), 1.0 / a.v); }
+template <int P> Dual<P> log10(const Dual<P>& a) { return chain(a, std::log10(a.v), 1.0 / (a.v * std::log(10.0))); }
+template <int P> Dual<P> sqrt(const Dual<P>& a) { double s = std::sqrt(a.v); return chain(a, s, 0.5 / s); }
+template <int P> Dual<P> tanh(const Dual<P>& a) { double t = std::tanh(a.v); return chain(a, t, 1.0 - t * t); }
+template <int P> Dual<P> fabs(const Dual<P>& a) { return a.v < 0 ? -a : a; }
+template <int P> Dual<P> pow(const Dual<P>& a, double b) {
+  double p = std::pow(a.v, b);
+  return chain(a, p, b * std::pow(a.v, b - 1.0));
+}
+template <int P> Dual<P> pow(double a, const Dual<P>& b) { double p = std::pow(a, b.v); return chain(b, p, p * std::log(a)); }
+template <int P> Dual<P> pow(const Dual<P>& a, const Dual<P>& b) { return exp(b * log(a)); }
+
+// The value of a number (a double is its own value).
+inline double val(double a) { return a; }
+template <int P> inline double val(const Dual<P>& a) { return a.v; }
+// Whether a number or any of its partials is nonzero (elimination skips).
+inline bool nonzero(double a) { return a != 0.0; }
+template <int P> inline bool nonzero(const Dual<P>& a) {
+  if (a.v != 0.0) return true;
+  for (int i = 0; i < P; ++i)
+    if (a.d[i] != 0.0) return true;
+  return false;
+}
+// Sum of squares of the value and partials, and their count (error norms).
+inline double sse(double a) { return a * a; }
+template <int P> inline double sse(const Dual<P>& a) {
+  double s = a.v * a.v;
+  for (int i = 0; i < P; ++i) s += a.d[i] * a.d[i];
+  return s;
+}
+
+// The parameter-gradient type of the gradient oracle: partials along
+// theta = (h, omega_b, omega_c, n_s, A_s, Sigma m_nu).
+constexpr int kThetaN = 6;
+using G6 = Dual<kThetaN>;
+
 inline double exp(double a) { return std::exp(a); }
 inline double sqrt(double a) { return std::sqrt(a); }
-inline D1 exp(D1 a) { double e = std::exp(a.v); return {e, e * a.d}; }
-inline D1 sqrt(D1 a) { double s = std::sqrt(a.v); return {s, 0.5 * a.d / s}; }
-inline double val(double a) { return a; }
-inline double val(D1 a) { return a.v; }
+inline double log(double a) { return std::log(a); }
+inline double log10(double a) { return std::log10(a); }
+inline double pow(double a, double b) { return std::pow(a, b); }
+inline double tanh(double a) { return std::tanh(a); }
+inline double fabs(double a) { return std::fabs(a); }
+
+// ------------------------------------------------------------ dual (d/dx) --
+// D1T<V>: a value of type V and its derivative in x (one direction), for the
+// explicit x-derivative of the right-hand side a Rosenbrock step needs.
+template <class V>
+struct D1T {
+  V v, d;
+  D1T() : v(0.0), d(0.0) {}
+  D1T(V a) : v(a), d(0.0) {}
+  D1T(V a, V b) : v(a), d(b) {}
+  template <class W, class = typename std::enable_if<!std::is_same<V, W>::value>::type>
+  D1T(const D1T<W>& o) : v(o.v), d(o.d) {}
+};
+template <class V> inline D1T<V> operator+(const D1T<V>& a, const D1T<V>& b) { return {a.v + b.v, a.d + b.d}; }
+template <class V> inline D1T<V> operator-(const D1T<V>& a, const D1T<V>& b) { return {a.v - b.v, a.d - b.d}; }
+template <class V> inline D1T<V> operator-(const D1T<V>& a) { return {-a.v, -a.d}; }
+template <class V> inline D1T<V> operator*(const D1T<V>& a, const D1T<V>& b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+template <class V> inline D1T<V> operator/(const D1T<V>& a, const D1T<V>& b) {
+  return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)};
+}
+template <class V> inline D1T<V> operator+(const D1T<V>& a, const V& b) { return {a.v + b, a.d}; }
+template <class V> inline D1T<V> operator+(const V& b, const D1T<V>& a) { return {a.v + b, a.d}; }
+template <class V> inline D1T<V> operator-(const D1T<V>& a, const V& b) { return {a.v - b, a.d}; }
+template <class V> inline D1T<V> operator-(const V& b, const D1T<V>& a) { return {b - a.v, -a.d}; }
+template <class V> inline D1T<V> operator*(const D1T<V>& a, const V& b) { return {a.v * b, a.d * b}; }
+template <class V> inline D1T<V> operator*(const V& b, const D1T<V>& a) { return {a.v * b, a.d * b}; }
+template <class V> inline D1T<V> operator/(const D1T<V>& a, const V& b) { return {a.v / b, a.d / b}; }
+template <class V> inline D1T<V> operator/(const V& b, const D1T<V>& a) { return {b / a.v, -b * a.d / (a.v * a.v)}; }
+template <class V, class = typename std::enable_if<!std::is_same<V, double>::value>::type>
+inline D1T<V> operator+(const D1T<V>& a, double b) { return {a.v + b, a.d}; }
+template <class V, class = typename std::enable_if<!std::is_same<V, double>::value>::type>
+inline D1T<V> operator+(double b, const D1T<V>& a) { return {a.v + b, a.d}; }
+template <class V, class = typename std::enable_if<!std::is_same<V, double>::value>::type>
+inline D1T<V> operator-(const D1T<V>& a, double b) { return {a.v - b, a.d}; }
+template <class V, class = typename std::enable_if<!std::is_same<V, double>::value>::type>
+inline D1T<V> operator-(double b, const D1T<V>& a) { return {b - a.v, -a.d}; }
+template <class V, class = typename std::enable_if<!std::is_same<V, double>::value>::type>
+inline D1T<V> operator*(const D1T<V>& a, double b) { return {a.v * b, a.d * b}; }
+template <class V, class = typename std::enable_if<!std::is_same<V, double>::value>::type>
+inline D1T<V> operator*(double b, const D1T<V>& a) { return {a.v * b, a.d * b}; }
+template <class V, class = typename std::enable_if<!std::is_same<V, double>::value>::type>
+inline D1T<V> operator/(const D1T<V>& a, double b) { return {a.v / b, a.d / b}; }
+template <class V, class = typename std::enable_if<!std::is_same<V, double>::value>::type>
+inline D1T<V> operator/(double b, const D1T<V>& a) { return {b / a.v, -b * a.d / (a.v * a.v)}; }
+template <class V> inline D1T<V> exp(const D1T<V>& a) { V e = exp(a.v); return {e, e * a.d}; }
+template <class V> inline D1T<V> sqrt(const D1T<V>& a) { V s = sqrt(a.v); return {s, 0.5 * a.d / s}; }
+using D1 = D1T<double>;
+template <class V> inline double val(const D1T<V>& a) { return val(a.v); }
+// The value part of a number of the gradient type, kept in that type.
+template <class V> inline V base_of(const D1T<V>& a) { return a.v; }
+inline double base_of(double a) { return a; }
+template <int P> inline Dual<P> base_of(const Dual<P>& a) { return a; }
+
+// CosmoParams (Bolt.jl:56-66).  Sigma_m_nu is in Mpc^-1 like the reference.
+// T = double, or a dual number carrying derivatives with respect to theta.
+template <class T>
+struct ParamsT {
+  T h = 0.7, Omega_r = 5.0469e-5, Omega_b = 0.046, Omega_c = 0.224;
+  T A = 2.097e-9, n = 1.0, Y_p = 0.24, N_nu = 3.046, Sigma_m_nu = 0.0;
+};
+using Params = ParamsT<double>;
 
 // ---------------------------------------------------------------- spline ---
 // Uniform grid x_j = (i0 + j) / M  (j = 0..n-1) reproducing Julia's
@@ -121,28 +251,32 @@ struct Grid {
 // (util.jl:11).  Coefficients are padded by one on each side; the boundary
 // rows impose a vanishing second derivative at the first and last data point
 // (c[0] - 2c[1] + c[2] = 0), which fixes c[1] = y[0] and c[n] = y[n-1].
-struct Spline {
+// T is the number type of the data (double, or a dual number when the
+// tables carry parameter derivatives); the abscissa is always a double.
+template <class T>
+struct SplineT {
   double x0 = 0.0, h = 1.0;
   int n = 0;
-  std::vector<double> c;  // n + 2
+  std::vector<T> c;  // n + 2
 
-  Spline() {}
-  Spline(const std::vector<double>& y, double x0_, double h_) { build(y, x0_, h_); }
-  void build(const std::vector<double>& y, double x0_, double h_) {
+  SplineT() {}
+  SplineT(const std::vector<T>& y, double x0_, double h_) { build(y, x0_, h_); }
+  void build(const std::vector<T>& y, double x0_, double h_) {
     x0 = x0_;
     h = h_;
     n = int(y.size());
-    c.assign(n + 2, 0.0);
+    c.assign(n + 2, T(0.0));
     if (n == 1) { c[0] = c[1] = c[2] = y[0]; return; }
     c[1] = y[0];
     c[n] = y[n - 1];
     // interior: c[i-1]/6 + 2/3 c[i] + c[i+1]/6 = y[i-1], i = 2..n-1
     int m = n - 2;
     if (m > 0) {
-      std::vector<double> cp(m), dp(m);
+      std::vector<double> cp(m);
+      std::vector<T> dp(m);
       for (int r = 0; r < m; ++r) {
         int i = r + 2;
-        double rhs = y[i - 1];
+        T rhs = y[i - 1];
         if (r == 0) rhs -= c[1] / 6.0;
         if (r == m - 1) rhs -= c[n] / 6.0;
         double b = 2.0 / 3.0, a = 1.0 / 6.0, cc = 1.0 / 6.0;
@@ -169,7 +303,7 @@ struct Spline {
     i = int(fl);
     t = u - fl;
   }
-  double operator()(double x) const {
+  T operator()(double x) const {
     int i; double t; locate(x, i, t);
     double s = 1.0 - t;
     double w0 = s * s * s / 6.0;
@@ -178,7 +312,7 @@ struct Spline {
     double w3 = t * t * t / 6.0;
     return c[i] * w0 + c[i + 1] * w1 + c[i + 2] * w2 + c[i + 3] * w3;
   }
-  double d1(double x) const {
+  T d1(double x) const {
     int i; double t; locate(x, i, t);
     double s = 1.0 - t;
     double w0 = -s * s / 2.0;
@@ -187,7 +321,7 @@ struct Spline {
     double w3 = t * t / 2.0;
     return (c[i] * w0 + c[i + 1] * w1 + c[i + 2] * w2 + c[i + 3] * w3) / h;
   }
-  double d2(double x) const {
+  T d2(double x) const {
     int i; double t; locate(x, i, t);
     double w0 = 1.0 - t;
     double w1 = -2.0 + 3.0 * t;
@@ -195,21 +329,27 @@ struct Spline {
     double w3 = t;
     return (c[i] * w0 + c[i + 1] * w1 + c[i + 2] * w2 + c[i + 3] * w3) / (h * h);
   }
-  D1 eval(D1 x) const { return {(*this)(x.v), d1(x.v) * x.d}; }
-  double eval(double x) const { return (*this)(x); }
+  D1T<T> eval(D1 x) const { return D1T<T>((*this)(x.v), d1(x.v) * x.d); }
+  T eval(double x) const { return (*this)(x); }
+  // a spline of plain numbers at an abscissa that carries parameter
+  // derivatives (the Bessel argument k (eta0 - eta(x)) under ForwardDiff)
+  template <int P> Dual<P> at(const Dual<P>& x) const { return chain(x, val((*this)(x.v)), val(d1(x.v))); }
 };
+using Spline = SplineT<double>;
 
 // spline_d_x / spline_d_x2 (util.jl:12-13): re-spline the gradient / Hessian
 // of a spline sampled at the grid nodes.
-inline Spline spline_dx(const Spline& s, const Grid& g) {
-  std::vector<double> y(g.n);
+template <class T>
+inline SplineT<T> spline_dx(const SplineT<T>& s, const Grid& g) {
+  std::vector<T> y(g.n);
   for (int j = 0; j < g.n; ++j) y[j] = s.d1(g.at(j));
-  return Spline(y, s.x0, s.h);
+  return SplineT<T>(y, s.x0, s.h);
 }
-inline Spline spline_dx2(const Spline& s, const Grid& g) {
-  std::vector<double> y(g.n);
+template <class T>
+inline SplineT<T> spline_dx2(const SplineT<T>& s, const Grid& g) {
+  std::vector<T> y(g.n);
   for (int j = 0; j < g.n; ++j) y[j] = s.d2(g.at(j));
-  return Spline(y, s.x0, s.h);
+  return SplineT<T>(y, s.x0, s.h);
 }
 
 // ------------------------------------------------------- Gauss-Legendre ----
@@ -249,15 +389,19 @@ inline void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w
 // norm of OrdinaryDiffEq (RMS of err / (abstol + reltol*max|u|)), and
 // landing on every requested output time.  Dense output between stored steps
 // is cubic Hermite (used only where a solution is queried off the landing
-// points).  Integrates forward or backward in t.
-struct Tsit5Sol {
+// points).  Integrates forward or backward in t.  The state may carry
+// parameter derivatives (T a dual number): the step sizes are plain numbers
+// chosen from the values, so the derivatives are those of the discrete
+// solution on the value's steps.
+template <class T>
+struct Tsit5SolT {
   int dim = 0;
   std::vector<double> t;   // accepted step end points (incl. start)
-  std::vector<double> y;   // dim per point
-  std::vector<double> f;   // dim per point
+  std::vector<T> y;        // dim per point
+  std::vector<T> f;        // dim per point
   double t0() const { return t.front(); }
   double t1() const { return t.back(); }
-  void at(double tq, double* out) const {
+  void at(double tq, T* out) const {
     int n = int(t.size());
     bool fwd = t.back() > t.front();
     // binary search for interval
@@ -278,17 +422,21 @@ struct Tsit5Sol {
       out[d] = h00 * y[lo * dim + d] + h10 * hh * f[lo * dim + d] + h01 * y[(lo + 1) * dim + d] +
                h11 * hh * f[(lo + 1) * dim + d];
   }
-  double at(double tq, int idx) const {
-    std::vector<double> o(dim);
+  T at(double tq, int idx) const {
+    std::vector<T> o(dim);
     at(tq, o.data());
     return o[idx];
   }
 };
+using Tsit5Sol = Tsit5SolT<double>;
 
-using Rhs = std::function<void(double t, const double* y, double* dy)>;
+template <class T>
+using RhsT = std::function<void(double t, const T* y, T* dy)>;
+using Rhs = RhsT<double>;
 
-inline Tsit5Sol tsit5(const Rhs& f, int dim, const double* y0, double ta, double tb, double reltol,
-                      double abstol, const std::vector<double>& stops) {
+template <class T>
+inline Tsit5SolT<T> tsit5(const RhsT<T>& f, int dim, const T* y0, double ta, double tb, double reltol,
+                          double abstol, const std::vector<double>& stops) {
   static const double c2 = 0.161, c3 = 0.327, c4 = 0.9, c5 = 0.9800255409045097;
   static const double a21 = 0.161;
   static const double a31 = -0.008480655492356989, a32 = 0.335480655492357;
@@ -302,10 +450,10 @@ inline Tsit5Sol tsit5(const Rhs& f, int dim, const double* y0, double ta, double
   static const double e1 = -0.00178001105222577714, e2 = -0.0008164344596567469,
                       e3 = 0.007880878010261995, e4 = -0.1447110071732629, e5 = 0.5823571654525552,
                       e6 = -0.45808210592918697, e7 = 1.0 / 66.0;
-  Tsit5Sol sol;
+  Tsit5SolT<T> sol;
   sol.dim = dim;
   double dir = tb > ta ? 1.0 : -1.0;
-  std::vector<double> y(y0, y0 + dim), k1(dim), k2(dim), k3(dim), k4(dim), k5(dim), k6(dim), k7(dim),
+  std::vector<T> y(y0, y0 + dim), k1(dim), k2(dim), k3(dim), k4(dim), k5(dim), k6(dim), k7(dim),
       tmp(dim), ynew(dim);
   // landing points strictly inside (ta, tb], sorted in the direction of travel
   std::vector<double> land;
@@ -347,9 +495,9 @@ inline Tsit5Sol tsit5(const Rhs& f, int dim, const double* y0, double ta, double
     f(tn, ynew.data(), k7.data());
     double en = 0.0;
     for (int d = 0; d < dim; ++d) {
-      double e = hh * (e1 * k1[d] + e2 * k2[d] + e3 * k3[d] + e4 * k4[d] + e5 * k5[d] + e6 * k6[d] +
-                       e7 * k7[d]);
-      double sc = abstol + reltol * std::max(std::fabs(y[d]), std::fabs(ynew[d]));
+      double e = hh * (e1 * val(k1[d]) + e2 * val(k2[d]) + e3 * val(k3[d]) + e4 * val(k4[d]) + e5 * val(k5[d]) +
+                       e6 * val(k6[d]) + e7 * val(k7[d]));
+      double sc = abstol + reltol * std::max(std::fabs(val(y[d])), std::fabs(val(ynew[d])));
       en += (e / sc) * (e / sc);
     }
     en = std::sqrt(en / dim);

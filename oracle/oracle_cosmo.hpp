@@ -8,68 +8,74 @@ namespace orc {
 constexpr double ZETA3 = 1.2020569;  // background.jl:3
 
 // ---------------------------------------------------------- background -----
-struct Background {
-  Params par;
+// T = double, or a dual number carrying derivatives with respect to theta.
+template <class T>
+struct BackgroundT {
+  ParamsT<T> par;
   Grid xg;
   int nq = 15;
   std::vector<double> quad_pts, quad_wts;
-  double H0 = 0, eta0 = 0, rho_crit = 0, Omega_Lambda = 0;
-  double Tnu = 0, logqmin = 0, logqmax = 0;
-  Spline H, Hp, Hpp, eta, etap, etapp, rho0M;
+  T H0 = 0.0, eta0 = 0.0, rho_crit = 0.0, Omega_Lambda = 0.0;
+  T Tnu = 0.0, logqmin = 0.0, logqmax = 0.0;
+  SplineT<T> H, Hp, Hpp, eta, etap, etapp, rho0M;
 
   // background.jl:5-6
-  static double H0_of(const Params& p) { return p.h * units().km_s_Mpc_100; }
-  static double rho_crit_of(const Params& p) {
-    double H = H0_of(p);
+  static T H0_of(const ParamsT<T>& p) { return p.h * units().km_s_Mpc_100; }
+  static T rho_crit_of(const ParamsT<T>& p) {
+    T H = H0_of(p);
     return (3.0 / (8.0 * M_PI)) * H * H / units().G_natural;
   }
   // background.jl:7-18
-  static double Omega_Lambda_of(const Params& p) {
-    double Tg = std::pow(15.0 / (M_PI * M_PI) * rho_crit_of(p) * p.Omega_r, 0.25);
-    double nufac = (90.0 * ZETA3 / (11.0 * std::pow(M_PI, 4))) * (p.Omega_r * p.h * p.h / Tg) *
-                   std::pow(p.N_nu / 3.0, 0.75);
-    double Omega_nu = p.Sigma_m_nu * nufac / (p.h * p.h);
-    return 1.0 - (p.Omega_r * (1.0 + (2.0 / 3.0) * (7.0 * p.N_nu / 8.0) * std::pow(4.0 / 11.0, 4.0 / 3.0)) +
+  static T Omega_Lambda_of(const ParamsT<T>& p) {
+    T Tg = pow(15.0 / (M_PI * M_PI) * rho_crit_of(p) * p.Omega_r, 0.25);
+    T nufac = (90.0 * ZETA3 / (11.0 * pow(M_PI, 4))) * (p.Omega_r * p.h * p.h / Tg) *
+                   pow(p.N_nu / 3.0, 0.75);
+    T Omega_nu = p.Sigma_m_nu * nufac / (p.h * p.h);
+    return 1.0 - (p.Omega_r * (1.0 + (2.0 / 3.0) * (7.0 * p.N_nu / 8.0) * pow(4.0 / 11.0, 4.0 / 3.0)) +
                   p.Omega_b + p.Omega_c + Omega_nu);
   }
-  static double Tnu_of(const Params& p) {
-    return std::pow(p.N_nu / 3.0, 0.25) * std::pow(4.0 / 11.0, 1.0 / 3.0) *
-           std::pow(15.0 / (M_PI * M_PI) * rho_crit_of(p) * p.Omega_r, 0.25);
+  static T Tnu_of(const ParamsT<T>& p) {
+    return pow(p.N_nu / 3.0, 0.25) * pow(4.0 / 11.0, 1.0 / 3.0) *
+           pow(15.0 / (M_PI * M_PI) * rho_crit_of(p) * p.Omega_r, 0.25);
   }
   // util.jl:24-27 (q <-> unit interval)
-  static double to_ui(double lq, double lqmi, double lqma) { return -1.0 + (1.0 - (-1.0)) / (lqma - lqmi) * (lq - lqmi); }
-  static double from_ui(double x, double lqmi, double lqma) { return lqmi + (lqma - lqmi) / (1.0 - (-1.0)) * (x - (-1.0)); }
-  static double dxdq(double q, double lqmi, double lqma) { return (1.0 + to_ui(1.0 + lqmi, lqmi, lqma)) / (q * std::log(10.0)); }
-  static double xq2q(double x, double lqmi, double lqma) { return std::pow(10.0, from_ui(x, lqmi, lqma)); }
+  template <class U, class V, class W>
+  static auto to_ui(U lq, V lqmi, W lqma) { return -1.0 + (1.0 - (-1.0)) / (lqma - lqmi) * (lq - lqmi); }
+  template <class U, class V, class W>
+  static auto from_ui(U x, V lqmi, W lqma) { return lqmi + (lqma - lqmi) / (1.0 - (-1.0)) * (x - (-1.0)); }
+  template <class U, class V, class W>
+  static auto dxdq(U q, V lqmi, W lqma) { return (1.0 + to_ui(1.0 + lqmi, lqmi, lqma)) / (q * log(10.0)); }
+  template <class U, class V, class W>
+  static auto xq2q(U x, V lqmi, W lqma) { return pow(10.0, from_ui(x, lqmi, lqma)); }
   // background.jl:21-30
-  double f0(double q) const { return 2.0 / std::pow(2.0 * M_PI, 3) / (std::exp(q / Tnu) + 1.0); }
-  double dlnf0dlnq(double q) const { return -q / Tnu / (1.0 + std::exp(-q / Tnu)); }
+  T f0(const T& q) const { return 2.0 / pow(2.0 * M_PI, 3) / (exp(q / Tnu) + 1.0); }
+  T dlnf0dlnq(const T& q) const { return -q / Tnu / (1.0 + exp(-q / Tnu)); }
   // background.jl:33-48 (energy density of the massive neutrinos)
-  double rhoP0(double a, double* P = nullptr) const {
-    double m = par.Sigma_m_nu, rho = 0.0, pr = 0.0;
+  T rhoP0(double a, T* P = nullptr) const {
+    T m = par.Sigma_m_nu, rho = 0.0, pr = 0.0;
     for (int i = 0; i < nq; ++i) {
-      double q = xq2q(quad_pts[i], logqmin, logqmax);
-      double eps = std::sqrt(q * q + (a * m) * (a * m));
-      double dx = dxdq(q, logqmin, logqmax);
+      T q = xq2q(quad_pts[i], logqmin, logqmax);
+      T eps = sqrt(q * q + (a * m) * (a * m));
+      T dx = dxdq(q, logqmin, logqmax);
       rho += q * q * eps * f0(q) / dx * quad_wts[i];
       pr += q * q * (q * q / eps) * f0(q) / dx * quad_wts[i];
     }
-    if (P) *P = 4.0 * M_PI / 3.0 * std::pow(a, -4) * pr;
-    return 4.0 * M_PI * std::pow(a, -4) * rho;
+    if (P) *P = 4.0 * M_PI / 3.0 * pow(a, -4) * pr;
+    return 4.0 * M_PI * pow(a, -4) * rho;
   }
   // background.jl:58-70
-  double H_a(double a) const {
-    double rho_nu = rhoP0(a);
-    const Params& p = par;
-    return H0 * std::sqrt((p.Omega_c + p.Omega_b) * std::pow(a, -3) + rho_nu / rho_crit +
-                          p.Omega_r * std::pow(a, -4) * (1.0 + (2.0 / 3.0) * (7.0 * p.N_nu / 8.0) * std::pow(4.0 / 11.0, 4.0 / 3.0)) +
+  T H_a(double a) const {
+    T rho_nu = rhoP0(a);
+    const ParamsT<T>& p = par;
+    return H0 * sqrt((p.Omega_c + p.Omega_b) * pow(a, -3) + rho_nu / rho_crit +
+                          p.Omega_r * pow(a, -4) * (1.0 + (2.0 / 3.0) * (7.0 * p.N_nu / 8.0) * pow(4.0 / 11.0, 4.0 / 3.0)) +
                           Omega_Lambda);
   }
-  double Hc_a(double a) const { return a * H_a(a); }
+  T Hc_a(double a) const { return a * H_a(a); }
   // background.jl:73-77
-  double eta_of(double x) const {
-    double lamin = -13.75, lamax = std::log10(std::exp(x));
-    double s = 0.0;
+  T eta_of(double x) const {
+    double lamin = -13.75, lamax = log10(exp(x));
+    T s = 0.0;
     for (int i = 0; i < nq; ++i) {
       double aa = xq2q(quad_pts[i], lamin, lamax);
       s += 1.0 / (aa * Hc_a(aa)) / dxdq(aa, lamin, lamax) * quad_wts[i];
@@ -78,17 +84,17 @@ struct Background {
   }
 
   // background.jl:104-128
-  Background(const Params& p, const Grid& g, int nq_) : par(p), xg(g), nq(nq_) {
+  BackgroundT(const ParamsT<T>& p, const Grid& g, int nq_) : par(p), xg(g), nq(nq_) {
     gauss_legendre(nq, quad_pts, quad_wts);
     H0 = H0_of(p);
     rho_crit = rho_crit_of(p);
     Omega_Lambda = Omega_Lambda_of(p);
     Tnu = Tnu_of(p);
-    logqmin = std::log10(Tnu / 30.0);
-    logqmax = std::log10(Tnu * 30.0);
-    std::vector<double> yr(g.n), yh(g.n), ye(g.n);
+    logqmin = log10(Tnu / 30.0);
+    logqmax = log10(Tnu * 30.0);
+    std::vector<T> yr(g.n), yh(g.n), ye(g.n);
     for (int j = 0; j < g.n; ++j) {
-      double x = g.at(j), a = std::exp(x);
+      double x = g.at(j), a = exp(x);
       yr[j] = rhoP0(a);
       yh[j] = Hc_a(a);
       ye[j] = eta_of(x);
@@ -104,11 +110,13 @@ struct Background {
     eta0 = eta_of(0.0);
   }
 };
+using Background = BackgroundT<double>;
 
 // --------------------------------------------------------------- RECFAST ---
 // recfast.jl:22-121 (SI constants and derived coefficients, same defaults).
-struct Recfast {
-  const Background* bg;
+template <class T>
+struct RecfastT {
+  const BackgroundT<T>* bg;
   double C = 2.99792458e8, k_B = 1.380658e-23, h_P = 6.6260755e-34, m_e = 9.1093897e-31,
          m_H = 1.673575e-27, not4 = 3.9715e0, sigma = 6.6524616e-29, a = 7.565914e-16,
          G = 6.6742e-11;
@@ -125,17 +133,17 @@ struct Recfast {
       CL_He, CT, Bfact;
   double H_frac = 1e-3;
   int Hswitch = 1, Heswitch = 6;
-  double Yp, OmegaB, HO, OmegaG, Tnow, mu_H, mu_T, fHe, Nnow, fu, b_He = 0.86, tol = 1e-8;
+  T Yp, OmegaB, HO, OmegaG, Tnow, mu_H, mu_T, fHe, Nnow;
+  double fu, b_He = 0.86, tol = 1e-8;
   double atol = 1e-6;  // OrdinaryDiffEq's default abstol in recfast.jl's solves
 
   // Tnow < 0 means "derive from OmegaG and the background" (recfast.jl:108)
-  Recfast(const Background* b, double Yp_, double OmegaB_, double OmegaG_, double Tnow_ = -1.0,
-          double tol_ = 1e-8)
+  RecfastT(const BackgroundT<T>* b, T Yp_, T OmegaB_, T OmegaG_, double Tnow_ = -1.0, double tol_ = 1e-8)
       : bg(b), Yp(Yp_), OmegaB(OmegaB_), OmegaG(OmegaG_), tol(tol_) {
-    a_VF = std::pow(10.0, -16.744);
-    T_0 = std::pow(10.0, 0.477121);
-    T_1 = std::pow(10.0, 5.114);
-    a_trip = std::pow(10.0, -16.306);
+    a_VF = pow(10.0, -16.744);
+    T_0 = pow(10.0, 0.477121);
+    T_1 = pow(10.0, 5.114);
+    a_trip = pow(10.0, -16.306);
     Lalpha = 1.0 / L_H_alpha;
     Lalpha_He = 1.0 / L_He_2p;
     DeltaB = h_P * C * (L_H_ion - L_H_alpha);
@@ -153,7 +161,7 @@ struct Recfast {
     CT = (8.0 / 3.0) * (sigma / (m_e * C)) * a;
     Bfact = h_P * C * (L_He_2p - L_He_2s) / k_B;
     HO = bg->H0 / units().H0_conv;
-    Tnow = Tnow_ > 0 ? Tnow_ : std::pow(15.0 / (M_PI * M_PI) * bg->rho_crit * OmegaG, 0.25) * units().K_conv;
+    Tnow = Tnow_ > 0 ? T(Tnow_) : pow(15.0 / (M_PI * M_PI) * bg->rho_crit * OmegaG, 0.25) * units().K_conv;
     mu_H = 1.0 / (1.0 - Yp);
     mu_T = not4 / (not4 - (not4 - 1.0) * Yp);
     fHe = Yp / (not4 * (1.0 - Yp));
@@ -162,99 +170,99 @@ struct Recfast {
   }
 
   // recfast.jl:156-310
-  void ion(const double* y, double z, double* f) const {
-    double f1 = 0, f2 = 0, f3 = 0;
-    double x_H = y[0], x_He = y[1], x = x_H + fHe * x_He, Tmat = y[2];
-    double n = Nnow * std::pow(1 + z, 3), n_He = fHe * Nnow * std::pow(1 + z, 3), Trad = Tnow * (1 + z);
-    double aa = 1.0 / (1 + z), x_a = std::log(aa);
-    double Hz = bg->H(x_a) / aa / units().H0_conv;
-    double dHdz = (-bg->Hp(x_a) + bg->H(x_a)) / units().H0_conv;
-    double Rdown = 1e-19 * a_PPB * std::pow(Tmat / 1e4, b_PPB) / (1.0 + c_PPB * std::pow(Tmat / 1e4, d_PPB));
-    double Rup = Rdown * std::pow(CR * Tmat, 1.5) * std::exp(-CDB / Tmat);
-    double sq_0 = std::sqrt(Tmat / T_0), sq_1 = std::sqrt(Tmat / T_1);
-    double Rdown_He = a_VF / (sq_0 * std::pow(1 + sq_0, 1 - b_VF));
-    Rdown_He = Rdown_He / std::pow(1 + sq_1, 1 + b_VF);
-    double Rup_He = Rdown_He * std::pow(CR * Tmat, 1.5) * std::exp(-CDB_He / Tmat);
+  void ion(const T* y, double z, T* f) const {
+    T f1 = 0.0, f2 = 0.0, f3 = 0.0;
+    T x_H = y[0], x_He = y[1], x = x_H + fHe * x_He, Tmat = y[2];
+    T n = Nnow * pow(1 + z, 3), n_He = fHe * Nnow * pow(1 + z, 3), Trad = Tnow * (1 + z);
+    double aa = 1.0 / (1 + z), x_a = log(aa);
+    T Hz = bg->H(x_a) / aa / units().H0_conv;
+    T dHdz = (-bg->Hp(x_a) + bg->H(x_a)) / units().H0_conv;
+    T Rdown = 1e-19 * a_PPB * pow(Tmat / 1e4, b_PPB) / (1.0 + c_PPB * pow(Tmat / 1e4, d_PPB));
+    T Rup = Rdown * pow(CR * Tmat, 1.5) * exp(-CDB / Tmat);
+    T sq_0 = sqrt(Tmat / T_0), sq_1 = sqrt(Tmat / T_1);
+    T Rdown_He = a_VF / (sq_0 * pow(1 + sq_0, 1 - b_VF));
+    Rdown_He = Rdown_He / pow(1 + sq_1, 1 + b_VF);
+    T Rup_He = Rdown_He * pow(CR * Tmat, 1.5) * exp(-CDB_He / Tmat);
     Rup_He = 4.0 * Rup_He;
-    double He_Boltz = (Bfact / Tmat > 680.0) ? std::exp(680.0) : std::exp(Bfact / Tmat);
-    double K;
+    T He_Boltz = (Bfact / Tmat > 680.0) ? T(exp(680.0)) : exp(Bfact / Tmat);
+    T K;
     if (Hswitch == 0)
       K = CK / Hz;
     else
       K = CK / Hz *
-          (1.0 + AGauss1 * std::exp(-std::pow((std::log(1 + z) - zGauss1) / wGauss1, 2)) +
-           AGauss2 * std::exp(-std::pow((std::log(1 + z) - zGauss2) / wGauss2, 2)));
-    double Rdown_trip = a_trip / (sq_0 * std::pow(1 + sq_0, 1 - b_trip));
-    Rdown_trip = Rdown_trip / std::pow(1 + sq_1, 1 + b_trip);
-    double Rup_trip = Rdown_trip * std::exp(-h_P * C * L_He2St_ion / (k_B * Tmat));
-    Rup_trip = Rup_trip * std::pow(CR * Tmat, 1.5) * (4.0 / 3.0);
+          (1.0 + AGauss1 * exp(-pow((log(1 + z) - zGauss1) / wGauss1, 2)) +
+           AGauss2 * exp(-pow((log(1 + z) - zGauss2) / wGauss2, 2)));
+    T Rdown_trip = a_trip / (sq_0 * pow(1 + sq_0, 1 - b_trip));
+    Rdown_trip = Rdown_trip / pow(1 + sq_1, 1 + b_trip);
+    T Rup_trip = Rdown_trip * exp(-h_P * C * L_He2St_ion / (k_B * Tmat));
+    Rup_trip = Rup_trip * pow(CR * Tmat, 1.5) * (4.0 / 3.0);
     int Heflag = ((x_He < 5.e-9) || (x_He > 0.980)) ? 0 : Heswitch;
-    double K_He = 0, CfHe_t = 0;
+    T K_He = 0.0, CfHe_t = 0.0;
     if (Heflag == 0) {
       K_He = CK_He / Hz;
     } else {
-      double tauHe_s = A2P_s * CK_He * 3 * n_He * (1 - x_He) / Hz;
-      double pHe_s = (1 - std::exp(-tauHe_s)) / tauHe_s;
+      T tauHe_s = A2P_s * CK_He * 3 * n_He * (1 - x_He) / Hz;
+      T pHe_s = (1 - exp(-tauHe_s)) / tauHe_s;
       K_He = 1.0 / (A2P_s * pHe_s * 3 * n_He * (1 - x_He));
       if (((Heflag == 2) || (Heflag >= 5)) && (x_H < 0.9999999)) {
-        double Doppler = 2 * k_B * Tmat / (m_H * not4 * C * C);
-        Doppler = C * L_He_2p * std::sqrt(Doppler);
-        double gamma_2Ps = 3 * A2P_s * fHe * (1 - x_He) * C * C /
-                           (std::sqrt(M_PI) * sigma_He_2Ps * 8 * M_PI * Doppler * (1 - x_H)) /
-                           std::pow(C * L_He_2p, 2);
+        T Doppler = 2 * k_B * Tmat / (m_H * not4 * C * C);
+        Doppler = C * L_He_2p * sqrt(Doppler);
+        T gamma_2Ps = 3 * A2P_s * fHe * (1 - x_He) * C * C /
+                           (sqrt(M_PI) * sigma_He_2Ps * 8 * M_PI * Doppler * (1 - x_H)) /
+                           pow(C * L_He_2p, 2);
         double pb = 0.36, qb = b_He;
-        double AHcon = A2P_s / (1 + pb * std::pow(gamma_2Ps, qb));
+        T AHcon = A2P_s / (1 + pb * pow(gamma_2Ps, qb));
         K_He = 1.0 / ((A2P_s * pHe_s + AHcon) * 3 * n_He * (1 - x_He));
       }
       if (Heflag >= 3) {
-        double tauHe_t = A2P_t * n_He * (1. - x_He) * 3;
-        tauHe_t = tauHe_t / (8 * M_PI * Hz * std::pow(L_He_2Pt, 3));
-        double pHe_t = (1 - std::exp(-tauHe_t)) / tauHe_t;
+        T tauHe_t = A2P_t * n_He * (1. - x_He) * 3;
+        tauHe_t = tauHe_t / (8 * M_PI * Hz * pow(L_He_2Pt, 3));
+        T pHe_t = (1 - exp(-tauHe_t)) / tauHe_t;
         double CL_PSt = h_P * C * (L_He_2Pt - L_He_2St) / k_B;
         if ((Heflag == 3) || (Heflag == 5) || (x_H > 0.99999)) {
-          CfHe_t = A2P_t * pHe_t * std::exp(-CL_PSt / Tmat);
+          CfHe_t = A2P_t * pHe_t * exp(-CL_PSt / Tmat);
           CfHe_t = CfHe_t / (Rup_trip + CfHe_t);
         } else {
-          double Doppler = 2 * k_B * Tmat / (m_H * not4 * C * C);
-          Doppler = C * L_He_2Pt * std::sqrt(Doppler);
-          double gamma_2Pt = 3 * A2P_t * fHe * (1 - x_He) * C * C /
-                             (std::sqrt(M_PI) * sigma_He_2Pt * 8 * M_PI * Doppler * (1 - x_H)) /
-                             std::pow(C * L_He_2Pt, 2);
+          T Doppler = 2 * k_B * Tmat / (m_H * not4 * C * C);
+          Doppler = C * L_He_2Pt * sqrt(Doppler);
+          T gamma_2Pt = 3 * A2P_t * fHe * (1 - x_He) * C * C /
+                             (sqrt(M_PI) * sigma_He_2Pt * 8 * M_PI * Doppler * (1 - x_H)) /
+                             pow(C * L_He_2Pt, 2);
           double pb = 0.66, qb = 0.9;
-          double AHcon = A2P_t / (1 + pb * std::pow(gamma_2Pt, qb)) / 3;
-          CfHe_t = (A2P_t * pHe_t + AHcon) * std::exp(-CL_PSt / Tmat);
+          T AHcon = A2P_t / (1 + pb * pow(gamma_2Pt, qb)) / 3;
+          CfHe_t = (A2P_t * pHe_t + AHcon) * exp(-CL_PSt / Tmat);
           CfHe_t = CfHe_t / (Rup_trip + CfHe_t);
         }
       }
     }
-    double timeTh = (1.0 / (CT * std::pow(Trad, 4))) * (1 + x + fHe) / x;
-    double timeH = 2.0 / (3.0 * HO * std::pow(1 + z, 1.5));
+    T timeTh = (1.0 / (CT * pow(Trad, 4))) * (1 + x + fHe) / x;
+    T timeH = 2.0 / (3.0 * HO * pow(1 + z, 1.5));
     if (x_H > 0.99) {
-      f1 = 0.0;
+      f1 = T(0.0);
     } else if (x_H > 0.985) {
-      f1 = (x * x_H * n * Rdown - Rup * (1 - x_H) * std::exp(-CL / Tmat)) / (Hz * (1 + z));
+      f1 = (x * x_H * n * Rdown - Rup * (1 - x_H) * exp(-CL / Tmat)) / (Hz * (1 + z));
     } else {
-      f1 = ((x * x_H * n * Rdown - Rup * (1.0 - x_H) * std::exp(-CL / Tmat)) *
+      f1 = ((x * x_H * n * Rdown - Rup * (1.0 - x_H) * exp(-CL / Tmat)) *
             (1.0 + K * Lambda * n * (1.0 - x_H))) /
            (Hz * (1.0 + z) * (1.0 / fu + K * Lambda * n * (1.0 - x_H) / fu + K * Rup * n * (1.0 - x_H)));
     }
     if (x_He < 1e-15) {
-      f2 = 0.0;
+      f2 = T(0.0);
     } else {
-      f2 = ((x * x_He * n * Rdown_He - Rup_He * (1 - x_He) * std::exp(-CL_He / Tmat)) *
+      f2 = ((x * x_He * n * Rdown_He - Rup_He * (1 - x_He) * exp(-CL_He / Tmat)) *
             (1 + K_He * Lambda_He * n_He * (1 - x_He) * He_Boltz)) /
            (Hz * (1 + z) * (1 + K_He * (Lambda_He + Rup_He) * n_He * (1 - x_He) * He_Boltz));
       if (Heflag >= 3)
         f2 = f2 + (x * x_He * n * Rdown_trip -
-                   (1 - x_He) * 3 * Rup_trip * std::exp(-h_P * C * L_He_2St / (k_B * Tmat))) *
+                   (1 - x_He) * 3 * Rup_trip * exp(-h_P * C * L_He_2St / (k_B * Tmat))) *
                       CfHe_t / (Hz * (1 + z));
     }
     if (timeTh < H_frac * timeH) {
-      double epsilon = Hz * (1 + x + fHe) / (CT * std::pow(Trad, 3) * x);
+      T epsilon = Hz * (1 + x + fHe) / (CT * pow(Trad, 3) * x);
       f3 = Tnow + epsilon * ((1 + fHe) / (1 + fHe + x)) * ((f1 + fHe * f2) / x) - epsilon * dHdz / Hz +
            3 * epsilon / (1 + z);
     } else {
-      f3 = CT * std::pow(Trad, 4) * x / (1 + x + fHe) * (Tmat - Trad) / (Hz * (1 + z)) + 2 * Tmat / (1 + z);
+      f3 = CT * pow(Trad, 4) * x / (1 + x + fHe) * (Tmat - Trad) / (Hz * (1 + z)) + 2 * Tmat / (1 + z);
     }
     f[0] = f1; f[1] = f2; f[2] = f3;
   }
@@ -262,26 +270,27 @@ struct Recfast {
   // Root 0.5 (sqrt(b^2 + 4c) - b) of the Saha equations (recfast.jl:373-411),
   // written as 2c / (sqrt(b^2 + 4c) + b) when b > 0: the same number without
   // the cancellation that leaves ~1e-6 of rounding noise at early times.
-  static double quad_root(double b, double c) {
-    double s = std::sqrt(b * b + 4.0 * c);
+  static T quad_root(const T& b, const T& c) {
+    T s = sqrt(b * b + 4.0 * c);
     return b > 0.0 ? 2.0 * c / (s + b) : 0.5 * (s - b);
   }
-  double saha_rhs(double z, double CB) const {
-    return std::exp(1.5 * std::log(CR * Tnow / (1 + z)) - CB / (Tnow * (1 + z))) / Nnow;
+  T saha_rhs(double z, double CB) const {
+    return exp(1.5 * log(CR * Tnow / (1 + z)) - CB / (Tnow * (1 + z))) / Nnow;
   }
   // recfast.jl:373-380
-  double end_of_saha_condition(double z) const {
-    double rhs = saha_rhs(z, CB1_He1) * 4;
-    double x0 = quad_root(rhs - 1, (1 + fHe) * rhs);
+  T end_of_saha_condition(double z) const {
+    T rhs = saha_rhs(z, CB1_He1) * 4;
+    T x0 = quad_root(rhs - 1, (1 + fHe) * rhs);
     return (x0 - 1) / fHe - 0.99;
   }
   // recfast.jl:402-408
-  double x_H0_H_Saha(double z) const {
-    double rhs = saha_rhs(z, CB1);
+  T x_H0_H_Saha(double z) const {
+    T rhs = saha_rhs(z, CB1);
     return quad_root(rhs, rhs);
   }
-  double end_He_evo_condition(double z) const { return x_H0_H_Saha(z) - 0.985; }
+  T end_He_evo_condition(double z) const { return x_H0_H_Saha(z) - 0.985; }
 };
+using Recfast = RecfastT<double>;
 
 // NonlinearSolve 0.3 Falsi on an interval: regula-falsi steps, then
 // bisection once those stall, to floating-point resolution; returns the end
@@ -321,129 +330,136 @@ inline double falsi(const std::function<double(double)>& f, double left, double 
 }
 
 // recfastsolve + tanh_reio_solve (recfast.jl:446-536)
-struct RecfastHistory {
-  const Recfast* r;
+// The two switch redshifts come from root finds on the values alone: the
+// reference wraps them in assume_nondual (recfast.jl:451,456), so under
+// ForwardDiff they carry no derivative.
+template <class T>
+struct RecfastHistoryT {
+  const RecfastT<T>* r;
   double zinitial = 10000.0, zfinal = 0.0, z_He_evo_start = 0, z_H_He_evo_start = 0;
   double zre_ini = 50.0;
-  Tsit5Sol sol_He, sol_H_He, sol_reio;
+  Tsit5SolT<T> sol_He, sol_H_He, sol_reio;
 
-  RecfastHistory(const Recfast* rr, const std::vector<double>& zout) : r(rr) {
+  RecfastHistoryT(const RecfastT<T>* rr, const std::vector<double>& zout) : r(rr) {
     double zb = std::min(zinitial, 3500.0);
-    z_He_evo_start = falsi([&](double z) { return r->end_of_saha_condition(z); }, zb, zfinal);
-    z_H_He_evo_start = falsi([&](double z) { return r->end_He_evo_condition(z); }, z_He_evo_start, zfinal);
+    z_He_evo_start = falsi([&](double z) { return val(r->end_of_saha_condition(z)); }, zb, zfinal);
+    z_H_He_evo_start = falsi([&](double z) { return val(r->end_He_evo_condition(z)); }, z_He_evo_start, zfinal);
     // He + Tmat with H in Saha (recfast.jl:383-389, 462-465)
-    double y2[2];
+    T y2[2];
     {
-      double rhs = r->saha_rhs(z_He_evo_start, r->CB1_He1) * 4.0;
-      double x0 = Recfast::quad_root(rhs - 1, (1 + r->fHe) * rhs);
+      T rhs = r->saha_rhs(z_He_evo_start, r->CB1_He1) * 4.0;
+      T x0 = RecfastT<T>::quad_root(rhs - 1, (1 + r->fHe) * rhs);
       y2[0] = (x0 - 1) / r->fHe;
       y2[1] = r->Tnow * (1 + z_He_evo_start);
     }
-    Rhs fHe = [this](double z, const double* u, double* du) {
-      double yy[3] = {r->x_H0_H_Saha(z), u[0], u[1]}, d[3];
+    RhsT<T> fHe = [this](double z, const T* u, T* du) {
+      T yy[3] = {r->x_H0_H_Saha(z), u[0], u[1]}, d[3];
       r->ion(yy, z, d);
       du[0] = d[1];
       du[1] = d[2];
     };
     sol_He = tsit5(fHe, 2, y2, z_He_evo_start, z_H_He_evo_start, r->tol, r->atol, zout);
     double z3 = z_H_He_evo_start;
-    double y3[3] = {r->x_H0_H_Saha(z3), sol_He.y[sol_He.y.size() - 2], sol_He.y[sol_He.y.size() - 1]};
-    Rhs fH = [this](double z, const double* u, double* du) { r->ion(u, z, du); };
+    T y3[3] = {r->x_H0_H_Saha(z3), sol_He.y[sol_He.y.size() - 2], sol_He.y[sol_He.y.size() - 1]};
+    RhsT<T> fH = [this](double z, const T* u, T* du) { r->ion(u, z, du); };
     std::vector<double> stops3 = zout;
     stops3.push_back(zre_ini);
     sol_H_He = tsit5(fH, 3, y3, z3, zfinal, r->tol, r->atol, stops3);
-    double T50 = Tmat_RECFAST(zre_ini);
-    Rhs fR = [this](double z, const double* u, double* du) {
-      double x_reio = reionization_Xe(z);
-      double aa = 1.0 / (1 + z), x_a = std::log(aa);
-      double Hz = r->bg->H(x_a) / aa / units().H0_conv;
-      double Trad = r->Tnow * (1 + z);
-      du[0] = r->CT * std::pow(Trad, 4) * x_reio / (1 + x_reio + r->fHe) * (u[0] - Trad) / (Hz * (1 + z)) +
+    T T50 = Tmat_RECFAST(zre_ini);
+    RhsT<T> fR = [this](double z, const T* u, T* du) {
+      T x_reio = reionization_Xe(z);
+      double aa = 1.0 / (1 + z), x_a = log(aa);
+      T Hz = r->bg->H(x_a) / aa / units().H0_conv;
+      T Trad = r->Tnow * (1 + z);
+      du[0] = r->CT * pow(Trad, 4) * x_reio / (1 + x_reio + r->fHe) * (u[0] - Trad) / (Hz * (1 + z)) +
               2 * u[0] / (1 + z);
     };
     sol_reio = tsit5(fR, 1, &T50, zre_ini, zfinal, r->tol, r->atol, zout);
   }
   // recfast.jl:413-433
-  double Xe_RECFAST(double z) const {
+  T Xe_RECFAST(double z) const {
     if (z > 8000.) return 1 + 2 * r->fHe;
     if (z > 5000.) {
-      double rhs = r->saha_rhs(z, r->CB1_He2);
-      return Recfast::quad_root(rhs - 1 - r->fHe, (1 + 2 * r->fHe) * rhs);
+      T rhs = r->saha_rhs(z, r->CB1_He2);
+      return RecfastT<T>::quad_root(rhs - 1 - r->fHe, (1 + 2 * r->fHe) * rhs);
     }
     if (z > 3500.) return 1 + r->fHe;
     if (z > z_He_evo_start) {
-      double rhs = r->saha_rhs(z, r->CB1_He1) * 4;
-      return Recfast::quad_root(rhs - 1, (1 + r->fHe) * rhs);
+      T rhs = r->saha_rhs(z, r->CB1_He1) * 4;
+      return RecfastT<T>::quad_root(rhs - 1, (1 + r->fHe) * rhs);
     }
     if (z > z_H_He_evo_start) return r->x_H0_H_Saha(z) + r->fHe * sol_He.at(z, 0);
-    double u[3];
+    T u[3];
     sol_H_He.at(z, u);
     return u[0] + r->fHe * u[1];
   }
   // recfast.jl:435-444
-  double Tmat_RECFAST(double z) const {
+  T Tmat_RECFAST(double z) const {
     if (z > z_He_evo_start) return r->Tnow * (1 + z);
     if (z > z_H_He_evo_start) return sol_He.at(z, 1);
     return sol_H_He.at(z, 2);
   }
   // recfast.jl:478-488
-  double reionization_Xe(double z) const {
-    double X_fin = 1 + r->Yp / (r->not4 * (1 - r->Yp));
-    double zre = 7.6711, al = 1.5, dH = 0.5, zHe = 3.5, dHe = 0.5, fHe = X_fin - 1;
-    double x_orig = Xe_RECFAST(z);
-    double x_reio_H = (X_fin - x_orig) / 2 *
-                          (1 + std::tanh((std::pow(1 + zre, al) - std::pow(1 + z, al)) / (al * std::pow(1 + zre, al - 1)) / dH)) +
+  T reionization_Xe(double z) const {
+    T X_fin = 1 + r->Yp / (r->not4 * (1 - r->Yp));
+    double zre = 7.6711, al = 1.5, dH = 0.5, zHe = 3.5, dHe = 0.5;
+    T fHe = X_fin - 1;
+    T x_orig = Xe_RECFAST(z);
+    T x_reio_H = (X_fin - x_orig) / 2 *
+                          (1 + tanh((pow(1 + zre, al) - pow(1 + z, al)) / (al * pow(1 + zre, al - 1)) / dH)) +
                       x_orig;
-    double x_reio_He = fHe / 2 * (1 + std::tanh((zHe - z) / dHe));
+    T x_reio_He = fHe / 2 * (1 + tanh((zHe - z) / dHe));
     return x_reio_H + x_reio_He;
   }
   // recfast.jl:512-526
-  double Xe_TanhReio(double z) const { return z > zre_ini ? Xe_RECFAST(z) : reionization_Xe(z); }
-  double Tmat_TanhReio(double z) const { return z > zre_ini ? Tmat_RECFAST(z) : sol_reio.at(z, 0); }
+  T Xe_TanhReio(double z) const { return z > zre_ini ? Xe_RECFAST(z) : reionization_Xe(z); }
+  T Tmat_TanhReio(double z) const { return z > zre_ini ? Tmat_RECFAST(z) : sol_reio.at(z, 0); }
 };
+using RecfastHistory = RecfastHistoryT<double>;
 
 // IonizationHistory(RECFAST, par, bg) (recfast.jl:674-726, ionization.jl:107-137)
-struct Ionization {
-  double tau0 = 0;
-  Spline Xe, tau, taup, taupp, g, gp, gpp, Tmat, csb2;
-  std::vector<double> Xe_nodes, Tmat_nodes;
+template <class T>
+struct IonizationT {
+  T tau0 = 0.0;
+  SplineT<T> Xe, tau, taup, taupp, g, gp, gpp, Tmat, csb2;
+  std::vector<T> Xe_nodes, Tmat_nodes;
   double z_He_evo_start = 0, z_H_He_evo_start = 0;
 
-  Ionization(const Recfast& r, const Params& par, const Background& bg) {
+  IonizationT(const RecfastT<T>& r, const ParamsT<T>& par, const BackgroundT<T>& bg) {
     const Grid& g_ = bg.xg;
     int n = g_.n;
     std::vector<double> zout;
     for (int j = 0; j < n; ++j) {
       double x = g_.at(j);
-      double z = 1.0 / std::exp(x) - 1.0;
+      double z = 1.0 / exp(x) - 1.0;
       if (z < 10000.0) zout.push_back(z);
     }
-    RecfastHistory rh(&r, zout);
+    RecfastHistoryT<T> rh(&r, zout);
     z_He_evo_start = rh.z_He_evo_start;
     z_H_He_evo_start = rh.z_H_He_evo_start;
-    double xinit = std::log(1.0 / (rh.zinitial + 1.0));
-    double Xe_initial = rh.Xe_RECFAST(rh.zinitial);
+    double xinit = log(1.0 / (rh.zinitial + 1.0));
+    T Xe_initial = rh.Xe_RECFAST(rh.zinitial);
     Xe_nodes.resize(n);
     Tmat_nodes.resize(n);
     for (int j = 0; j < n; ++j) {
       double x = g_.at(j);
-      double z = 1.0 / std::exp(x) - 1.0;
+      double z = 1.0 / exp(x) - 1.0;
       Xe_nodes[j] = (x < xinit) ? Xe_initial : rh.Xe_TanhReio(z);
       Tmat_nodes[j] = (x < xinit) ? r.Tnow * (1 + z) : rh.Tmat_TanhReio(z);
     }
     // tau' (ionization.jl:122-127) and reverse cumulative trapezoid (ionization.jl:105-115)
     const Units& U = units();
-    double rc = Background::rho_crit_of(par);
-    std::vector<double> tp(n), ti(n);
+    T rc = BackgroundT<T>::rho_crit_of(par);
+    std::vector<T> tp(n), ti(n);
     for (int j = 0; j < n; ++j) {
-      double x = g_.at(j), a = std::exp(x);
-      double nH = par.Omega_b * rc / (U.m_H * a * a * a) * (1 - par.Y_p);
+      double x = g_.at(j), a = exp(x);
+      T nH = par.Omega_b * rc / (U.m_H * a * a * a) * (1 - par.Y_p);
       tp[j] = -Xe_nodes[j] * nH * a * U.sigma_T / bg.H(x);
     }
     {
       // cumul_integrate(reverse(x), reverse(tau')) then reverse
-      std::vector<double> acc(n);
-      acc[0] = 0.0;
+      std::vector<T> acc(n);
+      acc[0] = T(0.0);
       for (int i = 1; i < n; ++i) {
         int jr = n - 1 - i, jp = n - i;
         double dx = g_.at(jr) - g_.at(jp);
@@ -451,18 +467,18 @@ struct Ionization {
       }
       for (int i = 0; i < n; ++i) ti[n - 1 - i] = 0.5 * acc[i];
     }
-    std::vector<double> gt(n);
-    for (int j = 0; j < n; ++j) gt[j] = -tp[j] * std::exp(-ti[j]);
+    std::vector<T> gt(n);
+    for (int j = 0; j < n; ++j) gt[j] = -tp[j] * exp(-ti[j]);
     double x0 = g_.at(0);
     Xe.build(Xe_nodes, x0, g_.h);
     tau.build(ti, x0, g_.h);
     g.build(gt, x0, g_.h);
     Tmat.build(Tmat_nodes, x0, g_.h);
-    Spline Tp = spline_dx(Tmat, g_);
-    std::vector<double> cs(n);
+    SplineT<T> Tp = spline_dx(Tmat, g_);
+    std::vector<T> cs(n);
     for (int j = 0; j < n; ++j) {
       double x = g_.at(j);
-      double pre = std::pow(r.C, -2) * r.k_B / r.m_H * (1.0 / r.mu_T + (1 - r.Yp) * Xe(x));
+      T pre = pow(r.C, -2) * r.k_B / r.m_H * (1.0 / r.mu_T + (1 - r.Yp) * Xe(x));
       cs[j] = pre * (Tmat(x) - 1.0 / 3.0 * Tp(x));
     }
     csb2.build(cs, x0, g_.h);
@@ -473,5 +489,6 @@ struct Ionization {
     tau0 = ti[n - 1];
   }
 };
+using Ionization = IonizationT<double>;
 
 }  // namespace orc

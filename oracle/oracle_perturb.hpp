@@ -12,46 +12,52 @@
 
 namespace orc {
 
-struct Cosmo {
-  Params par;
-  Background* bg = nullptr;
-  Ionization* ih = nullptr;
+// T = double, or G6 (a dual number carrying derivatives with respect to
+// theta) for the gradient oracle.
+template <class T>
+struct CosmoT {
+  ParamsT<T> par;
+  BackgroundT<T>* bg = nullptr;
+  IonizationT<T>* ih = nullptr;
 };
+using Cosmo = CosmoT<double>;
 
 // Hierarchy (perturbations.jl:7-21) plus per-mode constants.
-struct Mode {
-  const Cosmo* C;
+template <class T>
+struct ModeT {
+  const CosmoT<T>* C;
   double k;
   int lg, lnu, lmnu, nq, N;
   int iTp, iN, iM, iPhi;  // offsets (unpack, perturbations.jl:114-125)
-  std::vector<double> q, df0, Aq;  // q nodes, dlnf0/dlnq, 4*pi*q^2 f0 / dxdq * w
-  std::vector<double> Bq;          // 4*pi*q^3 f0 / dxdq * w  (theta integral)
-  Mode(const Cosmo* c, double k_, int lg_, int lnu_, int lmnu_, int nq_)
+  std::vector<T> q, df0, Aq;  // q nodes, dlnf0/dlnq, 4*pi*q^2 f0 / dxdq * w
+  std::vector<T> Bq;          // 4*pi*q^3 f0 / dxdq * w  (theta integral)
+  ModeT(const CosmoT<T>* c, double k_, int lg_, int lnu_, int lmnu_, int nq_)
       : C(c), k(k_), lg(lg_), lnu(lnu_), lmnu(lmnu_), nq(nq_) {
     N = 2 * (lg + 1) + (lnu + 1) + (lmnu + 1) * nq + 5;
     iTp = lg + 1;
     iN = 2 * (lg + 1);
     iM = iN + lnu + 1;
     iPhi = iM + (lmnu + 1) * nq;
-    const Background& bg = *C->bg;
+    const BackgroundT<T>& bg = *C->bg;
     q.resize(nq); df0.resize(nq); Aq.resize(nq); Bq.resize(nq);
     for (int i = 0; i < nq; ++i) {
-      double qq = Background::xq2q(bg.quad_pts[i], bg.logqmin, bg.logqmax);
+      T qq = BackgroundT<T>::xq2q(bg.quad_pts[i], bg.logqmin, bg.logqmax);
       q[i] = qq;
       df0[i] = bg.dlnf0dlnq(qq);
-      double dx = Background::dxdq(qq, bg.logqmin, bg.logqmax);
+      T dx = BackgroundT<T>::dxdq(qq, bg.logqmin, bg.logqmax);
       Aq[i] = 4.0 * M_PI * qq * qq * bg.f0(qq) / dx * bg.quad_wts[i];
       Bq[i] = 4.0 * M_PI * qq * qq * qq * bg.f0(qq) / dx * bg.quad_wts[i];
     }
   }
   int M(int l, int iq) const { return iM + l * nq + iq; }
 };
+using Mode = ModeT<double>;
 
 // rho_sigma (perturbations.jl:127-145): massive-neutrino density and shear
 // q-integrals of the l = 0 and l = 2 moments.
-template <class S>
-inline void rho_sigma(const Mode& md, S a, const double* M0, const double* M2, S& rho, S& sig) {
-  double m = md.C->par.Sigma_m_nu;
+template <class S, class T, class A>
+inline void rho_sigma(const ModeT<T>& md, A a, const T* M0, const T* M2, S& rho, S& sig) {
+  T m = md.C->par.Sigma_m_nu;
   rho = S(0.0);
   sig = S(0.0);
   for (int i = 0; i < md.nq; ++i) {
@@ -65,39 +71,44 @@ struct RhsInfo { bool rsa = false; };
 
 // The radiation-streaming switch of hierarchy! (perturbations.jl:216):
 // k eta > 240 and -tau' H / eta > 100.
-inline bool rsa_switch(const Mode& md, double x) {
-  const Background& bg = *md.C->bg;
-  const Ionization& ih = *md.C->ih;
-  double eta = bg.eta.eval(x), tp = ih.taup.eval(x), Hc = bg.H.eval(x);
+template <class T>
+inline bool rsa_switch(const ModeT<T>& md, double x) {
+  const BackgroundT<T>& bg = *md.C->bg;
+  const IonizationT<T>& ih = *md.C->ih;
+  double eta = val(bg.eta.eval(x)), tp = val(ih.taup.eval(x)), Hc = val(bg.H.eval(x));
   return (md.k * eta > 240.0) && (-tp * Hc / eta > 100.0);
 }
 
-// hierarchy! (perturbations.jl:161-271).  S = double for the plain RHS,
-// S = D1 (value, d/dx) to obtain the explicit x-derivative of the RHS that a
-// Rosenbrock method needs for a non-autonomous system.
-template <class S>
-inline void hierarchy_rhs(const Mode& md, S x, const double* u, S* du, RhsInfo* info = nullptr) {
-  const Cosmo& C = *md.C;
-  const Params& p = C.par;
-  const Background& bg = *C.bg;
-  const Ionization& ih = *C.ih;
+// hierarchy! (perturbations.jl:161-271).  S = T for the plain RHS (x a
+// double), S = D1T<T> (value, d/dx; x a D1) to obtain the explicit
+// x-derivative of the RHS that a Rosenbrock method needs for a
+// non-autonomous system.
+template <class S> struct AbscissaOf { using type = double; };
+template <class V> struct AbscissaOf<D1T<V>> { using type = D1; };
+template <class S, class T>
+inline void hierarchy_rhs(const ModeT<T>& md, typename AbscissaOf<S>::type x, const T* u, S* du,
+                          RhsInfo* info = nullptr) {
+  const CosmoT<T>& C = *md.C;
+  const ParamsT<T>& p = C.par;
+  const BackgroundT<T>& bg = *C.bg;
+  const IonizationT<T>& ih = *C.ih;
   const double k = md.k;
   const int lg = md.lg, lnu = md.lnu, lmnu = md.lmnu, nq = md.nq;
-  const double H0sq = bg.H0 * bg.H0;
+  const T H0sq = bg.H0 * bg.H0;
   S Hc = bg.H.eval(x), eta = bg.eta.eval(x), tp = ih.taup.eval(x), cs2 = ih.csb2.eval(x);
-  S a = exp(x);
+  S a = S(exp(x));
   S R = 4.0 * p.Omega_r / (3.0 * p.Omega_b * a);
-  double Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
-  const double* Th = u;
-  const double* Tp = u + md.iTp;
-  const double* Nn = u + md.iN;
-  const double* Mm = u + md.iM;
-  double Phi = u[md.iPhi], del = u[md.iPhi + 1], v = u[md.iPhi + 2], delb = u[md.iPhi + 3], vb = u[md.iPhi + 4];
+  T Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
+  const T* Th = u;
+  const T* Tp = u + md.iTp;
+  const T* Nn = u + md.iN;
+  const T* Mm = u + md.iM;
+  const T Phi = u[md.iPhi], del = u[md.iPhi + 1], v = u[md.iPhi + 2], delb = u[md.iPhi + 3], vb = u[md.iPhi + 4];
   S* dTh = du;
   S* dTp = du + md.iTp;
   S* dNn = du + md.iN;
   S* dMm = du + md.iM;
-  std::vector<double> M0(nq), M2(nq);
+  std::vector<T> M0(nq), M2(nq);
   for (int i = 0; i < nq; ++i) { M0[i] = Mm[0 * nq + i]; M2[i] = Mm[2 * nq + i]; }
   S rhoM, sigM;
   rho_sigma(md, a, M0.data(), M2.data(), rhoM, sigM);
@@ -110,11 +121,11 @@ inline void hierarchy_rhs(const Mode& md, S x, const double* u, S* du, RhsInfo* 
   S dv = -S(v) - k / Hc * Psi;
   S ddelb = k / Hc * vb - 3.0 * Phip;
   S dvb = -S(vb) - k / Hc * (Psi + cs2 * delb) + tp * R * (3.0 * Th[1] + vb);
-  double m = p.Sigma_m_nu;
+  T m = p.Sigma_m_nu;
   for (int iq = 0; iq < nq; ++iq) {
-    double q = md.q[iq];
+    T q = md.q[iq];
     S eps = sqrt(q * q + (a * m) * (a * m));
-    double df0 = md.df0[iq];
+    T df0 = md.df0[iq];
     dMm[0 * nq + iq] = -k / Hc * (q / eps) * Mm[1 * nq + iq] + Phip * df0;
     dMm[1 * nq + iq] = k / (3.0 * Hc) * ((q / eps) * (Mm[0 * nq + iq] - 2.0 * Mm[2 * nq + iq]) - eps / q * Psi * df0);
     for (int l = 2; l <= lmnu - 1; ++l)
@@ -135,7 +146,7 @@ inline void hierarchy_rhs(const Mode& md, S x, const double* u, S* du, RhsInfo* 
     for (int l = 2; l <= lnu - 1; ++l)
       dNn[l] = k / ((2.0 * l + 1.0) * Hc) * (l * Nn[l - 1] - (l + 1) * Nn[l + 1]);
     dNn[lnu] = k / Hc * Nn[lnu - 1] - (lnu + 1.0) / (Hc * eta) * Nn[lnu];
-    double Pi = Th[2] + Tp[2] + Tp[0];
+    T Pi = Th[2] + Tp[2] + Tp[0];
     dTh[0] = -k / Hc * Th[1] - Phip;
     dTh[1] = k / (3.0 * Hc) * Th[0] - 2.0 * k / (3.0 * Hc) * Th[2] + k / (3.0 * Hc) * Psi + tp * (Th[1] + vb / 3.0);
     for (int l = 2; l <= lg - 1; ++l)
@@ -162,22 +173,24 @@ inline void hierarchy_rhs(const Mode& md, S x, const double* u, S* du, RhsInfo* 
 // passes the integrator's own state to the right-hand side at the end of a
 // step, so the accepted state carries these values into the next step; the
 // solver applies them there.
-inline void rsa_overwrite(const Mode& md, double x, double* u) {
-  const Cosmo& C = *md.C;
-  const Params& p = C.par;
-  const Background& bg = *C.bg;
-  const Ionization& ih = *C.ih;
-  const double k = md.k, H0sq = bg.H0 * bg.H0, a = std::exp(x);
-  const double Hc = bg.H(x), tp = ih.taup(x), tpp = ih.taupp(x), cs2 = ih.csb2(x);
-  double Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
+template <class T>
+inline void rsa_overwrite(const ModeT<T>& md, double x, T* u) {
+  const CosmoT<T>& C = *md.C;
+  const ParamsT<T>& p = C.par;
+  const BackgroundT<T>& bg = *C.bg;
+  const IonizationT<T>& ih = *C.ih;
+  const double k = md.k, a = std::exp(x);
+  const T H0sq = bg.H0 * bg.H0;
+  const T Hc = bg.H(x), tp = ih.taup(x), tpp = ih.taupp(x), cs2 = ih.csb2(x);
+  T Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
   const int nq = md.nq;
-  std::vector<double> M0(nq), M2(nq);
+  std::vector<T> M0(nq), M2(nq);
   for (int i = 0; i < nq; ++i) { M0[i] = u[md.iM + i]; M2[i] = u[md.iM + 2 * nq + i]; }
-  double rhoM, sigM;
+  T rhoM, sigM;
   rho_sigma(md, a, M0.data(), M2.data(), rhoM, sigM);
-  const double Phi = u[md.iPhi], del = u[md.iPhi + 1], delb = u[md.iPhi + 3], vb = u[md.iPhi + 4];
-  double Psi = -Phi - 12.0 * H0sq / (k * k) / (a * a) * (p.Omega_r * u[2] + Omega_nu * u[md.iN + 2] + sigM / bg.rho_crit / 4.0);
-  double Phip = Psi - k * k / (3.0 * Hc * Hc) * Phi +
+  const T Phi = u[md.iPhi], del = u[md.iPhi + 1], delb = u[md.iPhi + 3], vb = u[md.iPhi + 4];
+  T Psi = -Phi - 12.0 * H0sq / (k * k) / (a * a) * (p.Omega_r * u[2] + Omega_nu * u[md.iN + 2] + sigM / bg.rho_crit / 4.0);
+  T Phip = Psi - k * k / (3.0 * Hc * Hc) * Phi +
                 H0sq / (2.0 * Hc * Hc) *
                     (p.Omega_c / a * del + p.Omega_b / a * delb + 4.0 * p.Omega_r / (a * a) * u[0] +
                      4.0 * Omega_nu / (a * a) * u[md.iN] + rhoM / (a * a) / bg.rho_crit);
@@ -190,24 +203,25 @@ inline void rsa_overwrite(const Mode& md, double x, double* u) {
 }
 
 // initial_conditions (perturbations.jl:274-338)
-inline void initial_conditions(const Mode& md, double xi, double* u) {
-  const Cosmo& C = *md.C;
-  const Params& p = C.par;
-  const Background& bg = *C.bg;
-  const Ionization& ih = *C.ih;
+template <class T>
+inline void initial_conditions(const ModeT<T>& md, double xi, T* u) {
+  const CosmoT<T>& C = *md.C;
+  const ParamsT<T>& p = C.par;
+  const BackgroundT<T>& bg = *C.bg;
+  const IonizationT<T>& ih = *C.ih;
   double k = md.k;
   int lg = md.lg, lnu = md.lnu, lmnu = md.lmnu, nq = md.nq;
-  std::fill(u, u + md.N, 0.0);
-  double Hc = bg.H(xi), eta = bg.eta(xi), tp = ih.taup(xi);
+  std::fill(u, u + md.N, T(0.0));
+  T Hc = bg.H(xi), eta = bg.eta(xi), tp = ih.taup(xi);
   double ai = std::exp(xi);
-  double fnu = 1.0 / (1.0 + 1.0 / (7.0 * (3.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0)));
+  T fnu = 1.0 / (1.0 + 1.0 / (7.0 * (3.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0)));
   double Rc = 1.0;
-  double Phi = (4.0 * fnu + 10.0) / (4.0 * fnu + 15.0) * Rc;
-  double Cc = -((15.0 + 4.0 * fnu) / (20.0 + 8.0 * fnu)) * Phi;
-  double* Th = u;
-  double* Tp = u + md.iTp;
-  double* Nn = u + md.iN;
-  double* Mm = u + md.iM;
+  T Phi = (4.0 * fnu + 10.0) / (4.0 * fnu + 15.0) * Rc;
+  T Cc = -((15.0 + 4.0 * fnu) / (20.0 + 8.0 * fnu)) * Phi;
+  T* Th = u;
+  T* Tp = u + md.iTp;
+  T* Nn = u + md.iN;
+  T* Mm = u + md.iM;
   Th[0] = -40.0 * Cc / (15.0 + 4.0 * fnu) / 4.0;
   Th[1] = 10.0 * Cc / (15.0 + 4.0 * fnu) * (k * k * eta) / (3.0 * k);
   Th[2] = -8.0 * k / (15.0 * Hc * tp) * Th[1];
@@ -218,18 +232,18 @@ inline void initial_conditions(const Mode& md, double xi, double* u) {
     Th[l] = -l / (2.0 * l + 1.0) * k / (Hc * tp) * Th[l - 1];
     Tp[l] = -l / (2.0 * l + 1.0) * k / (Hc * tp) * Tp[l - 1];
   }
-  double del = 3.0 / 4.0 * (4.0 * Th[0]);
-  double delb = del;
-  double v = -3.0 * k * Th[1];
-  double vb = v;
+  T del = 3.0 / 4.0 * (4.0 * Th[0]);
+  T delb = del;
+  T v = -3.0 * k * Th[1];
+  T vb = v;
   Nn[0] = Th[0];
   Nn[1] = Th[1];
   Nn[2] = -(k * k * eta * eta) / 15.0 * 1.0 / (1.0 + 2.0 / 5.0 * fnu) * Phi / 2.0;
   for (int l = 3; l <= lnu; ++l) Nn[l] = k / ((2.0 * l + 1.0) * Hc) * Nn[l - 1];
   for (int iq = 0; iq < nq; ++iq) {
-    double q = md.q[iq];
-    double eps = std::sqrt(q * q + (ai * p.Sigma_m_nu) * (ai * p.Sigma_m_nu));
-    double df0 = md.df0[iq];
+    T q = md.q[iq];
+    T eps = sqrt(q * q + (ai * p.Sigma_m_nu) * (ai * p.Sigma_m_nu));
+    T df0 = md.df0[iq];
     Mm[0 * nq + iq] = -Nn[0] * df0;
     Mm[1 * nq + iq] = -eps / q * Nn[1] * df0;
     Mm[2 * nq + iq] = -Nn[2] * df0;
@@ -244,51 +258,52 @@ inline void initial_conditions(const Mode& md, double xi, double* u) {
 }
 
 // source_function (perturbations.jl:343-383) and source_function_P (386-404)
-inline void source_functions(const Mode& md, double x, const double* u, const double* du, double& ST, double& SE) {
-  const Cosmo& C = *md.C;
-  const Params& p = C.par;
-  const Background& bg = *C.bg;
-  const Ionization& ih = *C.ih;
+template <class T>
+inline void source_functions(const ModeT<T>& md, double x, const T* u, const T* du, T& ST, T& SE) {
+  const CosmoT<T>& C = *md.C;
+  const ParamsT<T>& p = C.par;
+  const BackgroundT<T>& bg = *C.bg;
+  const IonizationT<T>& ih = *C.ih;
   double k = md.k;
   int nq = md.nq;
-  double H0sq = bg.H0 * bg.H0;
-  double Hc = bg.H(x), Hcp = bg.Hp(x), Hcpp = bg.Hpp(x);
-  double tau = ih.tau(x), tp = ih.taup(x), tpp = ih.taupp(x);
-  double g = ih.g(x), gp = ih.gp(x), gpp = ih.gpp(x);
+  T H0sq = bg.H0 * bg.H0;
+  T Hc = bg.H(x), Hcp = bg.Hp(x), Hcpp = bg.Hpp(x);
+  T tau = ih.tau(x), tp = ih.taup(x), tpp = ih.taupp(x);
+  T g = ih.g(x), gp = ih.gp(x), gpp = ih.gpp(x);
   double a = std::exp(x);
-  double Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
-  const double* Th = u;
-  const double* Tp = u + md.iTp;
-  const double* Nn = u + md.iN;
-  const double* Mm = u + md.iM;
-  const double* dTh = du;
-  const double* dTp = du + md.iTp;
-  const double* dNn = du + md.iN;
-  const double* dMm = du + md.iM;
-  double Phip = du[md.iPhi], vbp = du[md.iPhi + 4], Phi = u[md.iPhi], vb = u[md.iPhi + 4];
-  std::vector<double> M0(nq), M2(nq), dM0(nq), dM2(nq);
+  T Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
+  const T* Th = u;
+  const T* Tp = u + md.iTp;
+  const T* Nn = u + md.iN;
+  const T* Mm = u + md.iM;
+  const T* dTh = du;
+  const T* dTp = du + md.iTp;
+  const T* dNn = du + md.iN;
+  const T* dMm = du + md.iM;
+  T Phip = du[md.iPhi], vbp = du[md.iPhi + 4], Phi = u[md.iPhi], vb = u[md.iPhi + 4];
+  std::vector<T> M0(nq), M2(nq), dM0(nq), dM2(nq);
   for (int i = 0; i < nq; ++i) {
     M0[i] = Mm[i]; M2[i] = Mm[2 * nq + i];
     dM0[i] = dMm[i]; dM2[i] = dMm[2 * nq + i];
   }
-  double r_, sigM, sigMp;
+  T r_, sigM, sigMp;
   rho_sigma(md, a, M0.data(), M2.data(), r_, sigM);
   rho_sigma(md, a, dM0.data(), dM2.data(), r_, sigMp);
-  double Psi = -Phi - 12.0 * H0sq / (k * k) / (a * a) * (p.Omega_r * Th[2] + Omega_nu * Nn[2] + sigM / bg.rho_crit / 4.0);
-  double Psip = -Phip - 12.0 * H0sq / (k * k) / (a * a) *
+  T Psi = -Phi - 12.0 * H0sq / (k * k) / (a * a) * (p.Omega_r * Th[2] + Omega_nu * Nn[2] + sigM / bg.rho_crit / 4.0);
+  T Psip = -Phip - 12.0 * H0sq / (k * k) / (a * a) *
                             (p.Omega_r * (dTh[2] - 2.0 * Th[2]) + Omega_nu * (dNn[2] - 2.0 * Nn[2]) +
                              (sigMp - 2.0 * sigM) / bg.rho_crit / 4.0);
-  double Pi = Th[2] + Tp[2] + Tp[0];
-  double Pip = dTh[2] + dTp[2] + dTp[0];
-  double term1 = g * (Th[0] + Psi + Pi / 4.0) + std::exp(-tau) * (Psip - Phip);
-  double term2 = (-1.0 / k) * (Hcp * g * vb + Hc * gp * vb + Hc * g * vbp);
-  double Pipp = 2.0 * k / (5.0 * Hc) * (-Hcp / Hc * Th[1] + dTh[1]) + (3.0 / 10.0) * (tpp * Pi + tp * Pip) -
+  T Pi = Th[2] + Tp[2] + Tp[0];
+  T Pip = dTh[2] + dTp[2] + dTp[0];
+  T term1 = g * (Th[0] + Psi + Pi / 4.0) + exp(-tau) * (Psip - Phip);
+  T term2 = (-1.0 / k) * (Hcp * g * vb + Hc * gp * vb + Hc * g * vbp);
+  T Pipp = 2.0 * k / (5.0 * Hc) * (-Hcp / Hc * Th[1] + dTh[1]) + (3.0 / 10.0) * (tpp * Pi + tp * Pip) -
                 3.0 * k / (5.0 * Hc) * (-Hcp / Hc * (Th[3] + Tp[1] + Tp[3]) + (dTh[3] + dTp[1] + dTp[3]));
-  double term3 = (3.0 / (4.0 * k * k)) *
+  T term3 = (3.0 / (4.0 * k * k)) *
                  ((Hcp * Hcp + Hc * Hcpp) * g * Pi + 3.0 * Hc * Hcp * (gp * Pi + g * Pip) +
                   Hc * Hc * (gpp * Pi + 2.0 * gp * Pip + g * Pipp));
   ST = term1 + term2 + term3;
-  double y = k * (bg.eta(bg.xg.at(bg.xg.n - 1)) - bg.eta(x));
+  T y = k * (bg.eta(bg.xg.at(bg.xg.n - 1)) - bg.eta(x));
   SE = (3.0 / (4.0 * y * y)) * g * Pi;
 }
 
@@ -296,43 +311,44 @@ inline void source_functions(const Mode& md, double x, const double* u, const do
 // Banded LU with partial pivoting (LAPACK dgbtf2/dgbtrs layout) for the
 // local part of the Rosenbrock matrix, plus a rank-3 Woodbury correction for
 // the three global couplings (Phi', Psi, Pi) of the hierarchy.
-struct BandLU {
+template <class T>
+struct BandLUT {
   int n = 0, kl = 2, ku = 2, ld = 0, kv = 0;
-  std::vector<double> ab;
+  std::vector<T> ab;
   std::vector<int> ipiv;
   void init(int n_) {
     n = n_;
     kv = kl + ku;
     ld = 2 * kl + ku + 1;
-    ab.assign(size_t(ld) * n, 0.0);
+    ab.assign(size_t(ld) * n, T(0.0));
     ipiv.assign(n, 0);
   }
-  double& at(int i, int j) { return ab[size_t(kv + i - j) + size_t(j) * ld]; }
-  void zero() { std::fill(ab.begin(), ab.end(), 0.0); }
+  T& at(int i, int j) { return ab[size_t(kv + i - j) + size_t(j) * ld]; }
+  void zero() { std::fill(ab.begin(), ab.end(), T(0.0)); }
   bool factor() {
     int ju = 0;
     for (int j = 0; j < n; ++j) {
       int km = std::min(kl, n - 1 - j);
       int jp = 0;
-      double best = std::fabs(at(j, j));
+      double best = std::fabs(val(at(j, j)));
       for (int r = 1; r <= km; ++r)
-        if (std::fabs(at(j + r, j)) > best) { best = std::fabs(at(j + r, j)); jp = r; }
+        if (std::fabs(val(at(j + r, j))) > best) { best = std::fabs(val(at(j + r, j))); jp = r; }
       ipiv[j] = j + jp;
       if (best == 0.0) return false;
       ju = std::max(ju, std::min(j + ku + jp, n - 1));
       if (jp != 0)
         for (int c = j; c <= ju; ++c) std::swap(at(j, c), at(j + jp, c));
-      double piv = at(j, j);
+      T piv = at(j, j);
       for (int r = 1; r <= km; ++r) at(j + r, j) /= piv;
       for (int c = j + 1; c <= ju; ++c) {
-        double ujc = at(j, c);
-        if (ujc != 0.0)
+        T ujc = at(j, c);
+        if (nonzero(ujc))
           for (int r = 1; r <= km; ++r) at(j + r, c) -= at(j + r, j) * ujc;
       }
     }
     return true;
   }
-  void solve(double* b) {
+  void solve(T* b) {
     for (int j = 0; j < n - 1; ++j) {
       int lm = std::min(kl, n - 1 - j);
       int l = ipiv[j];
@@ -341,7 +357,7 @@ struct BandLU {
     }
     for (int j = n - 1; j >= 0; --j) {
       b[j] /= at(j, j);
-      double bj = b[j];
+      T bj = b[j];
       for (int i = std::max(0, j - kl - ku); i < j; ++i) b[i] -= at(i, j) * bj;
     }
   }
@@ -351,16 +367,20 @@ struct BandLU {
 // in a permuted order in which every species is a contiguous chain and the
 // baryon pair (delta_b, v_b) precedes the photon temperature chain, giving
 // bandwidth 2; U and W are the three global couplings (Phi', Psi, Pi).
-struct JacSplit {
+template <class T>
+struct JacSplitT {
   int N = 0;
   std::vector<int> pos;   // state index -> banded position
   std::vector<int> st;    // banded position -> state index
-  struct E { int r, c; double v; };
+  struct E { int r, c; T v; };
   std::vector<E> L;       // local entries (state indices)
-  std::vector<double> U[3], W[3];
+  std::vector<T> U[3], W[3];
 };
+using JacSplit = JacSplitT<double>;
+using BandLU = BandLUT<double>;
 
-inline void build_perm(const Mode& md, std::vector<int>& pos, std::vector<int>& st) {
+template <class T>
+inline void build_perm(const ModeT<T>& md, std::vector<int>& pos, std::vector<int>& st) {
   int N = md.N;
   st.clear();
   st.push_back(md.iPhi + 3);  // delta_b
@@ -377,19 +397,20 @@ inline void build_perm(const Mode& md, std::vector<int>& pos, std::vector<int>& 
   for (int p = 0; p < N; ++p) pos[st[p]] = p;
 }
 
-inline void jacobian_split(const Mode& md, double x, JacSplit& J) {
-  const Cosmo& C = *md.C;
-  const Params& p = C.par;
-  const Background& bg = *C.bg;
-  const Ionization& ih = *C.ih;
+template <class T>
+inline void jacobian_split(const ModeT<T>& md, double x, JacSplitT<T>& J) {
+  const CosmoT<T>& C = *md.C;
+  const ParamsT<T>& p = C.par;
+  const BackgroundT<T>& bg = *C.bg;
+  const IonizationT<T>& ih = *C.ih;
   const double k = md.k;
   const int lg = md.lg, lnu = md.lnu, lmnu = md.lmnu, nq = md.nq, N = md.N;
-  const double H0sq = bg.H0 * bg.H0;
-  double Hc = bg.H(x), eta = bg.eta(x), tp = ih.taup(x), cs2 = ih.csb2(x);
+  const T H0sq = bg.H0 * bg.H0;
+  T Hc = bg.H(x), eta = bg.eta(x), tp = ih.taup(x), cs2 = ih.csb2(x);
   double a = std::exp(x);
-  double R = 4.0 * p.Omega_r / (3.0 * p.Omega_b * a);
-  double Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
-  double m = p.Sigma_m_nu;
+  T R = 4.0 * p.Omega_r / (3.0 * p.Omega_b * a);
+  T Omega_nu = 7.0 * (2.0 / 3.0) * p.N_nu / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * p.Omega_r;
+  T m = p.Sigma_m_nu;
   J.N = N;
   J.L.clear();
   for (int r = 0; r < 3; ++r) { J.U[r].assign(N, 0.0); J.W[r].assign(N, 0.0); }
@@ -397,24 +418,24 @@ inline void jacobian_split(const Mode& md, double x, JacSplit& J) {
   // rows of the right-hand side are zero, and so are their Jacobian rows
   const bool rsa = rsa_switch(md, x);
   const int rad_end = md.iM;  // rows 0 .. iM-1: photon T, photon P, massless nu
-  auto add = [&](int r, int c, double v) {
+  auto add = [&](int r, int c, T v) {
     if (!(rsa && r < rad_end)) J.L.push_back({r, c, v});
   };
   const int iPhi = md.iPhi, idel = iPhi + 1, iv = iPhi + 2, idelb = iPhi + 3, ivb = iPhi + 4;
   // gradients of Psi and Phi'
-  double cpsi = 12.0 * H0sq / (k * k) / (a * a);
-  std::vector<double>& Wpsi = J.W[1];
-  std::vector<double>& Wphp = J.W[0];
+  T cpsi = 12.0 * H0sq / (k * k) / (a * a);
+  std::vector<T>& Wpsi = J.W[1];
+  std::vector<T>& Wphp = J.W[0];
   Wpsi[iPhi] += -1.0;
   Wpsi[2] += -cpsi * p.Omega_r;
   Wpsi[md.iN + 2] += -cpsi * Omega_nu;
-  std::vector<double> eps(nq);
+  std::vector<T> eps(nq);
   for (int iq = 0; iq < nq; ++iq) {
-    eps[iq] = std::sqrt(md.q[iq] * md.q[iq] + (a * m) * (a * m));
+    eps[iq] = sqrt(md.q[iq] * md.q[iq] + (a * m) * (a * m));
     Wpsi[md.M(2, iq)] += -cpsi * md.Aq[iq] * (md.q[iq] * md.q[iq] / eps[iq]) / bg.rho_crit / 4.0;
   }
   Wphp = Wpsi;
-  double d = H0sq / (2.0 * Hc * Hc);
+  T d = H0sq / (2.0 * Hc * Hc);
   Wphp[iPhi] += -k * k / (3.0 * Hc * Hc);
   Wphp[idel] += d * p.Omega_c / a;
   Wphp[idelb] += d * p.Omega_b / a;
@@ -425,10 +446,10 @@ inline void jacobian_split(const Mode& md, double x, JacSplit& J) {
   J.W[2][md.iTp + 2] = 1.0;
   J.W[2][md.iTp + 0] = 1.0;
   // U columns: coefficient of Phi', Psi, Pi in each row
-  std::vector<double>& Uph = J.U[0];
-  std::vector<double>& Ups = J.U[1];
-  std::vector<double>& Upi = J.U[2];
-  double kH = k / Hc;
+  std::vector<T>& Uph = J.U[0];
+  std::vector<T>& Ups = J.U[1];
+  std::vector<T>& Upi = J.U[2];
+  T kH = k / Hc;
   Uph[iPhi] = 1.0;
   Uph[idel] = -3.0;
   Uph[idelb] = -3.0;
@@ -443,14 +464,14 @@ inline void jacobian_split(const Mode& md, double x, JacSplit& J) {
   add(ivb, 1, 3.0 * tp * R);
   // massive neutrinos
   for (int iq = 0; iq < nq; ++iq) {
-    double q = md.q[iq], e = eps[iq], df0 = md.df0[iq];
+    T q = md.q[iq], e = eps[iq], df0 = md.df0[iq];
     Uph[md.M(0, iq)] = df0;
     add(md.M(0, iq), md.M(1, iq), -kH * (q / e));
     add(md.M(1, iq), md.M(0, iq), k / (3.0 * Hc) * (q / e));
     add(md.M(1, iq), md.M(2, iq), -2.0 * k / (3.0 * Hc) * (q / e));
     Ups[md.M(1, iq)] = -k / (3.0 * Hc) * (e / q) * df0;
     for (int l = 2; l <= lmnu - 1; ++l) {
-      double f = kH * q / ((2.0 * l + 1.0) * e);
+      T f = kH * q / ((2.0 * l + 1.0) * e);
       add(md.M(l, iq), md.M(l - 1, iq), f * l);
       add(md.M(l, iq), md.M(l + 1, iq), -f * (l + 1));
     }
@@ -464,7 +485,7 @@ inline void jacobian_split(const Mode& md, double x, JacSplit& J) {
   add(md.iN + 1, md.iN + 2, -2.0 * k / (3.0 * Hc));
   Ups[md.iN + 1] = k / (3.0 * Hc);
   for (int l = 2; l <= lnu - 1; ++l) {
-    double f = k / ((2.0 * l + 1.0) * Hc);
+    T f = k / ((2.0 * l + 1.0) * Hc);
     add(md.iN + l, md.iN + l - 1, f * l);
     add(md.iN + l, md.iN + l + 1, -f * (l + 1));
   }
@@ -479,7 +500,7 @@ inline void jacobian_split(const Mode& md, double x, JacSplit& J) {
   add(1, ivb, tp / 3.0);
   Ups[1] = k / (3.0 * Hc);
   for (int l = 2; l <= lg - 1; ++l) {
-    double f = k / ((2.0 * l + 1.0) * Hc);
+    T f = k / ((2.0 * l + 1.0) * Hc);
     add(l, l - 1, f * l);
     add(l, l + 1, -f * (l + 1));
     add(l, l, tp);
@@ -489,7 +510,7 @@ inline void jacobian_split(const Mode& md, double x, JacSplit& J) {
   add(md.iTp + 0, md.iTp + 0, tp);
   Upi[md.iTp + 0] = -tp / 2.0;
   for (int l = 1; l <= lg - 1; ++l) {
-    double f = k / ((2.0 * l + 1.0) * Hc);
+    T f = k / ((2.0 * l + 1.0) * Hc);
     add(md.iTp + l, md.iTp + l - 1, f * l);
     add(md.iTp + l, md.iTp + l + 1, -f * (l + 1));
     add(md.iTp + l, md.iTp + l, tp);
@@ -524,38 +545,38 @@ struct Rodas4 {
 
 // Integrate one mode from x = -20 (first grid node) to 0, landing on every
 // xout node (ascending), and call emit(j, x, u) there.
-template <class Emit>
-inline SolveStats solve_mode(const Mode& md, double reltol, double abstol, const std::vector<double>& xout,
+template <class T, class Emit>
+inline SolveStats solve_mode(const ModeT<T>& md, double reltol, double abstol, const std::vector<double>& xout,
                              Emit emit, long maxsteps = 20000000) {
   typedef Rodas4 R;
   const int N = md.N;
-  const Background& bg = *md.C->bg;
+  const BackgroundT<T>& bg = *md.C->bg;
   double x = bg.xg.at(0), xend = bg.xg.at(bg.xg.n - 1);
-  std::vector<double> y(N), ynew(N), tmp(N), f(N), fx(N);
-  std::vector<double> k1(N), k2(N), k3(N), k4(N), k5(N), k6(N);
-  std::vector<D1> fd(N);
+  std::vector<T> y(N), ynew(N), tmp(N), f(N), fx(N);
+  std::vector<T> k1(N), k2(N), k3(N), k4(N), k5(N), k6(N);
+  std::vector<D1T<T>> fd(N);
   std::vector<int> pos, st;
   build_perm(md, pos, st);
-  JacSplit J;
-  BandLU B;
+  JacSplitT<T> J;
+  BandLUT<T> B;
   B.init(N);
-  std::vector<double> Z[3];
-  for (int r = 0; r < 3; ++r) Z[r].assign(N, 0.0);
-  double Cinv[3][3];
+  std::vector<T> Z[3];
+  for (int r = 0; r < 3; ++r) Z[r].assign(N, T(0.0));
+  T Cinv[3][3];
   initial_conditions(md, x, y.data());
   SolveStats stats;
   size_t jo = 0;
   while (jo < xout.size() && xout[jo] <= x) { emit(int(jo), x, y.data()); ++jo; }
   double h = 1e-3;
-  std::vector<double> pb(N);
-  auto wsolve = [&](double* b) {  // b <- A^{-1} b (state order)
+  std::vector<T> pb(N);
+  auto wsolve = [&](T* b) {  // b <- A^{-1} b (state order)
     for (int p = 0; p < N; ++p) pb[p] = b[st[p]];
     B.solve(pb.data());
     for (int p = 0; p < N; ++p) b[st[p]] = pb[p];
-    double t[3] = {0, 0, 0};
+    T t[3] = {0, 0, 0};
     for (int r = 0; r < 3; ++r)
       for (int i = 0; i < N; ++i) t[r] += J.W[r][i] * b[i];
-    double s[3];
+    T s[3];
     for (int r = 0; r < 3; ++r) s[r] = Cinv[r][0] * t[0] + Cinv[r][1] * t[1] + Cinv[r][2] * t[2];
     for (int i = 0; i < N; ++i) b[i] += Z[0][i] * s[0] + Z[1][i] * s[1] + Z[2][i] * s[2];
   };
@@ -566,7 +587,7 @@ inline SolveStats solve_mode(const Mode& md, double reltol, double abstol, const
     if (x + hs >= target - 1e-14 * std::fabs(target)) { hs = target - x; landing = true; }
     // Jacobian split, explicit x-derivative, factorisation
     jacobian_split(md, x, J);
-    hierarchy_rhs<D1>(md, D1(x, 1.0), y.data(), fd.data());
+    hierarchy_rhs<D1T<T>>(md, D1(x, 1.0), y.data(), fd.data());
     for (int i = 0; i < N; ++i) { f[i] = fd[i].v; fx[i] = fd[i].d; }
     B.zero();
     double inv = 1.0 / (hs * R::gam);
@@ -583,18 +604,18 @@ inline SolveStats solve_mode(const Mode& md, double reltol, double abstol, const
       B.solve(pb.data());
       for (int p = 0; p < N; ++p) Z[r][st[p]] = pb[p];
     }
-    double Cm[3][3];
+    T Cm[3][3];
     for (int r = 0; r < 3; ++r)
       for (int c = 0; c < 3; ++c) {
-        double s = 0.0;
+        T s = 0.0;
         for (int i = 0; i < N; ++i) s += J.W[r][i] * Z[c][i];
         Cm[r][c] = (r == c ? 1.0 : 0.0) - s;
       }
     {
-      double det = Cm[0][0] * (Cm[1][1] * Cm[2][2] - Cm[1][2] * Cm[2][1]) -
+      T det = Cm[0][0] * (Cm[1][1] * Cm[2][2] - Cm[1][2] * Cm[2][1]) -
                    Cm[0][1] * (Cm[1][0] * Cm[2][2] - Cm[1][2] * Cm[2][0]) +
                    Cm[0][2] * (Cm[1][0] * Cm[2][1] - Cm[1][1] * Cm[2][0]);
-      if (det == 0.0 || !(det == det)) { stats.status = 4; return stats; }
+      if (val(det) == 0.0 || !(val(det) == val(det))) { stats.status = 4; return stats; }
       Cinv[0][0] = (Cm[1][1] * Cm[2][2] - Cm[1][2] * Cm[2][1]) / det;
       Cinv[0][1] = (Cm[0][2] * Cm[2][1] - Cm[0][1] * Cm[2][2]) / det;
       Cinv[0][2] = (Cm[0][1] * Cm[1][2] - Cm[0][2] * Cm[1][1]) / det;
@@ -611,30 +632,30 @@ inline SolveStats solve_mode(const Mode& md, double reltol, double abstol, const
     for (int i = 0; i < N; ++i) k1[i] = f[i] + hd1 * fx[i];
     wsolve(k1.data());
     for (int i = 0; i < N; ++i) tmp[i] = y[i] + R::a21 * k1[i];
-    hierarchy_rhs<double>(md, x + R::c2 * hs, tmp.data(), f.data(), &info);
+    hierarchy_rhs<T>(md, x + R::c2 * hs, tmp.data(), f.data(), &info);
     stats.rsa += info.rsa;
     for (int i = 0; i < N; ++i) k2[i] = f[i] + hd2 * fx[i] + R::C21 * ih * k1[i];
     wsolve(k2.data());
     for (int i = 0; i < N; ++i) tmp[i] = y[i] + R::a31 * k1[i] + R::a32 * k2[i];
-    hierarchy_rhs<double>(md, x + R::c3 * hs, tmp.data(), f.data(), &info);
+    hierarchy_rhs<T>(md, x + R::c3 * hs, tmp.data(), f.data(), &info);
     stats.rsa += info.rsa;
     for (int i = 0; i < N; ++i) k3[i] = f[i] + hd3 * fx[i] + ih * (R::C31 * k1[i] + R::C32 * k2[i]);
     wsolve(k3.data());
     for (int i = 0; i < N; ++i) tmp[i] = y[i] + R::a41 * k1[i] + R::a42 * k2[i] + R::a43 * k3[i];
-    hierarchy_rhs<double>(md, x + R::c4 * hs, tmp.data(), f.data(), &info);
+    hierarchy_rhs<T>(md, x + R::c4 * hs, tmp.data(), f.data(), &info);
     stats.rsa += info.rsa;
     for (int i = 0; i < N; ++i)
       k4[i] = f[i] + hd4 * fx[i] + ih * (R::C41 * k1[i] + R::C42 * k2[i] + R::C43 * k3[i]);
     wsolve(k4.data());
     for (int i = 0; i < N; ++i) tmp[i] = y[i] + R::a51 * k1[i] + R::a52 * k2[i] + R::a53 * k3[i] + R::a54 * k4[i];
     double xn = landing ? target : x + hs;
-    hierarchy_rhs<double>(md, xn, tmp.data(), f.data(), &info);
+    hierarchy_rhs<T>(md, xn, tmp.data(), f.data(), &info);
     stats.rsa += info.rsa;
     for (int i = 0; i < N; ++i)
       k5[i] = f[i] + ih * (R::C51 * k1[i] + R::C52 * k2[i] + R::C53 * k3[i] + R::C54 * k4[i]);
     wsolve(k5.data());
     for (int i = 0; i < N; ++i) tmp[i] += k5[i];
-    hierarchy_rhs<double>(md, xn, tmp.data(), f.data(), &info);
+    hierarchy_rhs<T>(md, xn, tmp.data(), f.data(), &info);
     stats.rsa += info.rsa;
     for (int i = 0; i < N; ++i)
       k6[i] = f[i] + ih * (R::C61 * k1[i] + R::C62 * k2[i] + R::C63 * k3[i] + R::C64 * k4[i] + R::C65 * k5[i]);
@@ -643,10 +664,10 @@ inline SolveStats solve_mode(const Mode& md, double reltol, double abstol, const
     bool finite = true;
     for (int i = 0; i < N; ++i) {
       ynew[i] = tmp[i] + k6[i];
-      double sc = abstol + reltol * std::max(std::fabs(y[i]), std::fabs(ynew[i]));
-      double e = k6[i] / sc;
+      double sc = abstol + reltol * std::max(std::fabs(val(y[i])), std::fabs(val(ynew[i])));
+      double e = val(k6[i]) / sc;
       en += e * e;
-      if (!std::isfinite(ynew[i])) finite = false;
+      if (!std::isfinite(val(ynew[i]))) finite = false;
     }
     en = std::sqrt(en / N);
     if (!finite || !(en == en)) en = 1e10;

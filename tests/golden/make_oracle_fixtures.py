@@ -27,6 +27,10 @@ Fixtures (all FP64; k in Mpc^-1):
                         l 50/50/20 (N = 473), central differences as above.
 Both Jacobians at theta0 below, oracle at reltol = abstol = 1e-10 with
 RECFAST at tol 1e-11 / atol 1e-12 (so the differences are smooth).
+  oracle_jac_cltt_dual, oracle_jac_plin_dual
+                        the same two Jacobians from the gradient oracle
+                        (dual numbers with six partials, the reference's
+                        ForwardDiff gradient restated; oracle_grad.hpp).
 """
 import os
 import sys
@@ -130,8 +134,30 @@ def jac_plin():
     return out
 
 
+def jac_cltt_dual():
+    f = np.load(os.path.join(HERE, "oracle_jac_cltt.npz"))
+    hier = tuple(int(v) for v in f["hier"])
+    d = O.DualCosmo(theta=THETA0, recfast_tol=1e-11, recfast_atol=1e-12)
+    c0 = _cosmo(THETA0)
+    H0 = c0.H0
+    kd = (0.01 * H0, 1000.0 * H0, 5000)
+    tt, J = d.cltt(f["ks"], f["ells"], *hier, reltol=1e-10, abstol=1e-10, kd=kd, bessel_argmax=kd[1] * c0.eta0,
+                   nthreads=CORES)
+    return dict(theta=THETA0, ks=f["ks"], ells=f["ells"], tt=tt, J=J, hier=f["hier"])
+
+
+def jac_plin_dual():
+    f = np.load(os.path.join(HERE, "oracle_jac_plin.npz"))
+    lg, lnu, lmnu, nq = (int(v) for v in f["hier"])
+    d = O.DualCosmo(theta=THETA0, recfast_tol=1e-11, recfast_atol=1e-12)
+    with ThreadPoolExecutor(CORES) as ex:
+        res = list(ex.map(lambda k: d.plin(k, nq, lg, lnu, lmnu, 0.0, 1e-10, 1e-10), f["ks"]))
+    return dict(theta=THETA0, ks=f["ks"], plin=np.array([r[0] for r in res]), J=np.array([r[1] for r in res]).T,
+                hier=f["hier"])
+
+
 MAKERS = {"oracle_cl_l50_1024k": cl_l50_1024k, "oracle_plin_n473": plin_n473, "oracle_jac_cltt": jac_cltt,
-          "oracle_jac_plin": jac_plin}
+          "oracle_jac_plin": jac_plin, "oracle_jac_cltt_dual": jac_cltt_dual, "oracle_jac_plin_dual": jac_plin_dual}
 
 
 def main(names):

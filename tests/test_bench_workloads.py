@@ -83,4 +83,4 @@ def test_cpu_arm_runs_whole_requests():
 def test_los_flops_from_terms():
     assert bench.los_flops(1000) == 27000.0
     assert bench.los_flops(1000, with_e=False) == 25000.0
-    assert bench.SWEEP_RATES == (10.0, 100.0, 500.0, 2000.0)
+    assert bench.SWEEP_RATES == (1.0, 10.0, 100.0, 500.0, 2000.0)
