@@ -486,18 +486,26 @@ def run_serving(args):
         gres = [eng.wait(t) for t in [eng.submit(to_request(B, d)) for d in gstream]]
     for r in gres:
         assert r.rc == 0, r.err
+    with B.Engine(device=local, lanes=6, objective="throughput", grad_scheme="replay") as eng:
+        eng.run(to_request(B, gwarm))
+        gres_rep = [eng.wait(t) for t in [eng.submit(to_request(B, d)) for d in gstream]]
+    for r in gres_rep:
+        assert r.rc == 0, r.err
+    g_win_rep = max(r.times[3] for r in gres_rep) - min(r.times[2] for r in gres_rep)
     g_win = max(r.times[3] for r in gres) - min(r.times[2] for r in gres)
     g_lat = np.array([r.latency for r in gres])
     cl_grad = {"served": len(gstream) / g_win, "plain": len(gstream) / sum(g_dropin),
                "served_over_plain": sum(g_dropin) / g_win,
                "plain_engine": len(gstream) / sum(g_plain), "served_over_plain_engine": sum(g_plain) / g_win,
+               "served_replay": len(gstream) / g_win_rep,
                "unit": UNIT, "requests": len(gstream),
                "p50_s": float(np.percentile(g_lat, 50)), "p99_s": float(np.percentile(g_lat, 99)),
                "workload": "C_l^TT l<=2000 + 6-parameter Jacobian, draws from the serving box, 64-1024 log k in "
                            "[0.1,1000] H0, "
                            "l_gamma=l_nu in {20,35,50}; served: all submitted at once; plain: drop-in, 7 calls "
-                           "per request (forward differences); plain_engine: the engine one request per call "
-                           "(7 parameter sets batched in one launch, tangent LOS)"}
+                           "per request (forward differences); plain_engine: the engine one request per call; "
+                           "served and plain_engine use the tangent-linear solver (one solve per mode carries the "
+                           "four solved derivatives), served_replay the frozen-step replays (five solves per mode)"}
     # ---- the arrival-rate sweep of the serving configuration (same stream)
     sweep = [serve_at_rate(B, local, stream, rate, SEED + 31 + rank) for rate in SWEEP_RATES] if args.sweep else []
     lat = np.array([r.latency for r in res])

@@ -51,7 +51,7 @@ class BoltEngineCfg(C.Structure):
     _fields_ = [("device", C.c_int), ("lanes", C.c_int), ("host_threads", C.c_int), ("max_batch", C.c_int),
                 ("mem_budget_gb", C.c_double), ("warps_per_mode", C.c_int), ("max_steps", C.c_longlong),
                 ("batch_window_s", C.c_double), ("objective", C.c_int),
-                ("land_stride", C.c_int)]
+                ("land_stride", C.c_int), ("grad_scheme", C.c_int)]
 
 
 EXPORTS = {

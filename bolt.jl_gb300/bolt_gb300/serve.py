@@ -132,12 +132,16 @@ class Engine:
 
     def __init__(self, device: int = 0, lanes: int = 6, host_threads: int = 0, max_batch: int = 0,
                  mem_budget_gb: float = 150.0, warps_per_mode: int = 0, max_steps: int = 0,
-                 batch_window_s: float = 0.0, objective: str = "latency", land_stride: int = 1):
+                 batch_window_s: float = 0.0, objective: str = "latency", land_stride: int = 1,
+                 grad_scheme: str = "tangent"):
         if objective not in ("latency", "throughput"):
             raise ValueError("objective is 'latency' or 'throughput'")
+        if grad_scheme not in ("tangent", "replay"):
+            raise ValueError("grad_scheme is 'tangent' or 'replay'")
         self.lib = L.load()
         cfg = L.BoltEngineCfg(device, lanes, host_threads, max_batch, mem_budget_gb, warps_per_mode, max_steps,
-                              batch_window_s, 1 if objective == "throughput" else 0, land_stride)
+                              batch_window_s, 1 if objective == "throughput" else 0, land_stride,
+                              0 if grad_scheme == "tangent" else 1)
         h = C.c_void_p()
         rc = self.lib.bolt_engine_create(C.byref(cfg), C.byref(h))
         if rc != 0:

@@ -48,12 +48,22 @@ struct ModeDev {
   int64_t* counters;  // [2] accepted steps, rejected steps
   double* rec;        // [rec_cap] end abscissae of the accepted steps (MODE_RECORD / MODE_REPLAY)
   int rec_cap;
+  // MODE_TANGENT: the cosmologies (indices) of the four perturbed parameter
+  // sets with 1 / their steps, and where the tangents of the outputs go
+  // (null: not wanted)
+  int tcos[4];
+  double tinv[4];
+  double* tsrc_T[4];  // [nout]
+  double* tsrc_E[4];  // [nout]
+  double* tplin[4];   // [1]
 };
 
 // MODE_RECORD stores the end abscissa of every accepted step; MODE_REPLAY
 // takes exactly those steps (no error control), so a mode of perturbed
 // parameters is integrated on the same discretisation as the recorded one.
-enum ModeFlags { MODE_SOURCES = 1, MODE_TRAJ = 2, MODE_PLIN = 4, MODE_RECORD = 8, MODE_REPLAY = 16 };
+// MODE_TANGENT integrates, with the state, its derivatives with respect to
+// four parameters (the tangent-linear solver, tangent.cuh).
+enum ModeFlags { MODE_SOURCES = 1, MODE_TRAJ = 2, MODE_PLIN = 4, MODE_RECORD = 8, MODE_REPLAY = 16, MODE_TANGENT = 32 };
 
 enum StatusBits {
   ST_OK = 0,
@@ -63,6 +73,7 @@ enum StatusBits {
   ST_LU_FAIL = 4,
   ST_BAD_INPUT = 5,
   ST_REPLAY_SHORT = 6,   // MODE_REPLAY ran past the recorded steps
+  ST_TANGENT_RSA = 7,    // MODE_TANGENT: the radiation-streaming overwrite fired (it has no tangent here)
   ST_RSA_FIRED = 256,    // informational, OR-ed into the code
   ST_REC_OVERFLOW = 512  // MODE_RECORD: more accepted steps than rec_cap (record unusable)
 };
@@ -133,6 +144,118 @@ __device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
 __device__ __forceinline__ dd dsqrt(dd a) { double s = sqrt(a.v); return mk(s, 0.5 * a.d / s); }
 __device__ __forceinline__ double dexp(double a) { return exp(a); }
 __device__ __forceinline__ dd dexp(dd a) { double e = exp(a.v); return mk(e, e * a.d); }
+
+// Tangent numbers of the tangent-linear solver: a value and its derivatives
+// along kTD parameter directions (d4), and the x-dual of such a number (x4:
+// value and d/dx, each a d4), for the explicit x-derivative of the
+// right-hand side's tangent.
+constexpr int kTD = 4;
+struct d4 {
+  double v, t[kTD];
+};
+__device__ __forceinline__ d4 c4(double v) { d4 r; r.v = v; for (int j = 0; j < kTD; ++j) r.t[j] = 0.0; return r; }
+__device__ __forceinline__ d4 operator+(const d4& a, const d4& b) {
+  d4 r; r.v = a.v + b.v;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = a.t[j] + b.t[j];
+  return r;
+}
+__device__ __forceinline__ d4 operator-(const d4& a, const d4& b) {
+  d4 r; r.v = a.v - b.v;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = a.t[j] - b.t[j];
+  return r;
+}
+__device__ __forceinline__ d4 operator-(const d4& a) {
+  d4 r; r.v = -a.v;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = -a.t[j];
+  return r;
+}
+__device__ __forceinline__ d4 operator*(const d4& a, const d4& b) {
+  d4 r; r.v = a.v * b.v;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = fma(a.t[j], b.v, a.v * b.t[j]);
+  return r;
+}
+__device__ __forceinline__ d4 operator*(const d4& a, double b) {
+  d4 r; r.v = a.v * b;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = a.t[j] * b;
+  return r;
+}
+__device__ __forceinline__ d4 operator*(double b, const d4& a) { return a * b; }
+__device__ __forceinline__ d4 operator+(const d4& a, double b) { d4 r = a; r.v += b; return r; }
+__device__ __forceinline__ d4 operator+(double b, const d4& a) { d4 r = a; r.v += b; return r; }
+__device__ __forceinline__ d4 operator-(const d4& a, double b) { d4 r = a; r.v -= b; return r; }
+__device__ __forceinline__ d4 operator-(double b, const d4& a) { return c4(b) - a; }
+__device__ __forceinline__ d4 operator/(const d4& a, const d4& b) {
+  d4 r; r.v = a.v / b.v;
+  const double ib = 1.0 / b.v;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = (a.t[j] - r.v * b.t[j]) * ib;
+  return r;
+}
+__device__ __forceinline__ d4 operator/(const d4& a, double b) {
+  d4 r; r.v = a.v / b;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = a.t[j] / b;
+  return r;
+}
+__device__ __forceinline__ d4 operator/(double a, const d4& b) { return c4(a) / b; }
+__device__ __forceinline__ double vof(const d4& a) { return a.v; }
+template <> __device__ __forceinline__ d4 cst<d4>(double v) { return c4(v); }
+__device__ __forceinline__ d4 dsqrt(const d4& a) {
+  d4 r; r.v = sqrt(a.v);
+  const double h = 0.5 / r.v;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = a.t[j] * h;
+  return r;
+}
+__device__ __forceinline__ d4 dexp(const d4& a) {
+  d4 r; r.v = exp(a.v);
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = a.t[j] * r.v;
+  return r;
+}
+__device__ __forceinline__ d4 dpow(const d4& a, double b) {  // a^b, a > 0
+  d4 r; r.v = pow(a.v, b);
+  const double dr = b * r.v / a.v;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = a.t[j] * dr;
+  return r;
+}
+
+struct x4 {
+  d4 v, d;
+};
+__device__ __forceinline__ x4 mkx(const d4& v, const d4& d) { x4 r; r.v = v; r.d = d; return r; }
+__device__ __forceinline__ x4 operator+(const x4& a, const x4& b) { return mkx(a.v + b.v, a.d + b.d); }
+__device__ __forceinline__ x4 operator-(const x4& a, const x4& b) { return mkx(a.v - b.v, a.d - b.d); }
+__device__ __forceinline__ x4 operator-(const x4& a) { return mkx(-a.v, -a.d); }
+__device__ __forceinline__ x4 operator*(const x4& a, const x4& b) { return mkx(a.v * b.v, a.d * b.v + a.v * b.d); }
+__device__ __forceinline__ x4 operator*(const x4& a, const d4& b) { return mkx(a.v * b, a.d * b); }
+__device__ __forceinline__ x4 operator*(const d4& b, const x4& a) { return mkx(a.v * b, a.d * b); }
+__device__ __forceinline__ x4 operator*(const x4& a, double b) { return mkx(a.v * b, a.d * b); }
+__device__ __forceinline__ x4 operator*(double b, const x4& a) { return mkx(a.v * b, a.d * b); }
+__device__ __forceinline__ x4 operator+(const x4& a, const d4& b) { return mkx(a.v + b, a.d); }
+__device__ __forceinline__ x4 operator+(const d4& b, const x4& a) { return mkx(a.v + b, a.d); }
+__device__ __forceinline__ x4 operator-(const x4& a, const d4& b) { return mkx(a.v - b, a.d); }
+__device__ __forceinline__ x4 operator-(const d4& b, const x4& a) { return mkx(b - a.v, -a.d); }
+__device__ __forceinline__ x4 operator+(const x4& a, double b) { return mkx(a.v + b, a.d); }
+__device__ __forceinline__ x4 operator+(double b, const x4& a) { return mkx(a.v + b, a.d); }
+__device__ __forceinline__ x4 operator-(const x4& a, double b) { return mkx(a.v - b, a.d); }
+__device__ __forceinline__ x4 operator-(double b, const x4& a) { return mkx(b - a.v, -a.d); }
+__device__ __forceinline__ x4 operator/(const x4& a, const x4& b) {
+  d4 q = a.v / b.v;
+  return mkx(q, (a.d - q * b.d) / b.v);
+}
+__device__ __forceinline__ x4 operator/(double a, const x4& b) {
+  d4 q = a / b.v;
+  return mkx(q, -(q * b.d) / b.v);
+}
+__device__ __forceinline__ double vof(const x4& a) { return a.v.v; }
+template <> __device__ __forceinline__ x4 cst<x4>(double v) { return mkx(c4(v), c4(0.0)); }
 
 // ------------------------------------------------------- spline evaluation
 // Cubic B-spline on the uniform grid with Interpolations.jl's OnGrid

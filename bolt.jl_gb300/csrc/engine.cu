@@ -57,6 +57,11 @@
 
 namespace bolt {
 int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, int* blocks);
+int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, bool tan, int* blocks);
+int rodas_node_params(int wpm, bool tan, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos,
+                      const SolverCfg& cfg, int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch,
+                      RodasNodeArgs* args, cudaKernelNodeParams* p);
+size_t rodas_scratch_per_warp(int maxN, bool tan);
 int rodas_node_params(int wpm, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg,
                       int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch, RodasNodeArgs* args,
                       cudaKernelNodeParams* p);
@@ -203,7 +208,16 @@ struct Req {
   int rec_cap = 0;           // recorded steps per mode (gradient requests)
   int src_from = 0;          // C_l: first x node with sources, findfirst(x_grid .> -8) (spectra.jl:86)
   bool los_tangent = false;  // C_l^TT gradient from the tangent of the LOS integral
+  bool tangent = false;      // gradient from tangent-linear modes (sets 1..6 hold derivatives, not perturbed results)
 };
+
+// The four parameters whose derivatives need a solve (theta indices), in the
+// order of the tangent directions of a tangent mode.
+constexpr int kSolvedTheta[kTD] = {0, 1, 2, 5};
+// Whether parameter set s of request r has modes of its own: the perturbed
+// sets of n_s and A_s never do, and those of a tangent request are filled by
+// the base modes' tangents.
+bool set_has_modes(const Req* r, int s) { return !skips_solve(r->nsets, s) && !(r->tangent && s > 0); }
 
 struct Graph {
   cudaGraph_t g = nullptr;
@@ -215,7 +229,7 @@ struct Lane {
   cudaStream_t st = nullptr;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // start, phase 1, phase 2, LOS, done
   int* d_queue = nullptr;  // [2] work-queue counters of the two solver phases
-  Graph graph[3][2];       // [warps-per-mode variant][phase]
+  Graph graph[4][2];       // [kernel variant: warps per mode 1, 2, 4; tangent][phase]
   GrowDev scr, los_raw, los_norm, los_coef, los_SdT, los_SdE, los_dSd;
   GrowHost up, down;
   bool busy = false;
@@ -223,6 +237,7 @@ struct Lane {
   void* d_block = nullptr;
   size_t block_bytes = 0;
   int wpm[2] = {4, 4};
+  bool tan[2] = {false, false};  // phase runs the tangent-linear kernel
   int nmodes[2] = {0, 0};
   int waiting = 0;       // modes of the requests still waiting when the batch was taken
   int key[2] = {0, 0};   // tuner key of each phase (own modes, or the whole load when shared)
@@ -324,7 +339,7 @@ void layout_request(Req* r, size_t& off) {
   r->o_cnt = off;
   off = align_up(off + size_t(ns) * nk * 16);
   r->o_rec = off;
-  if (r->nsets > 1) off = align_up(off + size_t(nk) * r->rec_cap * 8);
+  if (r->nsets > 1 && !r->tangent) off = align_up(off + size_t(nk) * r->rec_cap * 8);
   if (r->r.kind == BOLT_REQ_CL) {
     r->o_src = off;
     off = align_up(off + size_t(ns) * nk * (n - r->src_from) * 8 * (r->wantE ? 2 : 1));
@@ -395,8 +410,8 @@ void set_done(bolt_engine* E, Req* r, int s, const std::string& err) {
   }
 }
 
-Graph& lane_graph(Lane& L, int wpm, int phase, const cudaKernelNodeParams& kp) {
-  const int v = wpm == 1 ? 0 : (wpm == 2 ? 1 : 2);
+Graph& lane_graph(Lane& L, int wpm, bool tan, int phase, const cudaKernelNodeParams& kp) {
+  const int v = tan ? 3 : (wpm == 1 ? 0 : (wpm == 2 ? 1 : 2));
   Graph& G = L.graph[v][phase];
   if (!G.exec) {
     ck(cudaGraphCreate(&G.g, 0), "cudaGraphCreate");
@@ -425,7 +440,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   cudaStream_t st = L.st;
   // ---- device layout of the batch block (inputs and outputs)
   size_t off = 0;
-  int ncos = 0, m1 = 0, m2 = 0, maxN = 0, maxnq = 1, maxL = 3;
+  int ncos = 0, m1 = 0, m2 = 0, mt = 0, maxN = 0, maxnq = 1, maxL = 3;
   size_t max_sd = 0;
   int max_slots = 0;
   bool anyE = false, anyTangent = false;
@@ -434,8 +449,12 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     anyTangent |= r->los_tangent;
     r->cos0 = ncos;
     ncos += r->nsets;
-    m1 += r->r.nk;
-    for (int s = 1; s < r->nsets; ++s) m2 += skips_solve(r->nsets, s) ? 0 : r->r.nk;
+    if (r->tangent) {
+      mt += r->r.nk;
+    } else {
+      m1 += r->r.nk;
+      for (int s = 1; s < r->nsets; ++s) m2 += skips_solve(r->nsets, s) ? 0 : r->r.nk;
+    }
     maxN = std::max(maxN, r->N);
     maxnq = std::max(maxnq, r->r.hier.nq);
     maxL = std::max(maxL, std::max(r->r.hier.lg, std::max(r->r.hier.lnu, r->r.hier.lmnu)));
@@ -450,12 +469,17 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   const size_t o_cos = off;
   off = align_up(off + size_t(ncos) * sizeof(CosmoDev));
   const size_t o_modes = off;
-  off = align_up(off + size_t(m1 + m2) * sizeof(ModeDev));
+  off = align_up(off + size_t(m1 + m2 + mt) * sizeof(ModeDev));
   const size_t total = off;
   // ---- solver configurations of both phases (autotuned) and lane buffers
+  // phase 0: plain modes (and recorded ones); phase 1: their frozen-step
+  // replays, or the tangent modes (a batch never holds both, see scheduler)
   int wpm[2] = {4, 4}, blocks[2] = {0, 0};
-  const int nph = m2 > 0 ? 2 : 1;
-  const int nmodes[2] = {m1, m2};
+  const bool tan1 = mt > 0;
+  const int nph = (m2 > 0 || mt > 0) ? 2 : 1;
+  const int nmodes[2] = {m1, tan1 ? mt : m2};
+  L.tan[0] = false;
+  L.tan[1] = tan1;
   int other = 0;  // lanes are launched and finished on this (the scheduler) thread
   for (Lane& o : E->lanes)
     if (&o != &L && o.busy) other += o.nmodes[0] + o.nmodes[1];
@@ -463,16 +487,24 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     L.shared[ph] = other > 0 || L.waiting > 0 || E->cfg.objective == 1;
     L.key[ph] = L.shared[ph] ? nmodes[ph] + other + L.waiting : nmodes[ph];
     int w = E->cfg.warps_per_mode;
-    if (w != 1 && w != 2 && w != 4) {
+    if (L.tan[ph]) {
+      w = 1;  // the tangent-linear kernel runs one warp per mode
+    } else if (w != 1 && w != 2 && w != 4) {
       std::lock_guard<std::mutex> g(E->mu);
       w = E->tuner.pick(L.shared[ph], L.key[ph], E->nsm);
     }
-    int rc = rodas_grid_warps(nmodes[ph], maxN, maxnq, maxL, w, &blocks[ph]);
+    if (nmodes[ph] == 0) {  // a batch of tangent requests alone has no plain modes
+      blocks[ph] = 0;
+      wpm[ph] = w;
+      continue;
+    }
+    int rc = rodas_grid_warps(nmodes[ph], maxN, maxnq, maxL, w, L.tan[ph], &blocks[ph]);
     if (rc != 0) throw EngErr(-3, std::string("solver configuration: ") + cudaGetErrorString(cudaError_t(-rc)));
     wpm[ph] = w;
   }
   double* d_scr = static_cast<double*>(
-      L.scr.get(size_t(std::max(blocks[0], blocks[1])) * rodas_scratch_per_warp(maxN)));
+      L.scr.get(std::max(size_t(blocks[0]) * rodas_scratch_per_warp(maxN, false),
+                         size_t(blocks[1]) * rodas_scratch_per_warp(maxN, tan1))));
   double *raw = nullptr, *norm = nullptr, *coef = nullptr, *SdT = nullptr, *SdE = nullptr;
   if (max_slots > 0) {
     raw = static_cast<double*>(L.los_raw.get(size_t(max_slots) * kNb * 8));
@@ -509,7 +541,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     req_start += r->bytes;
   }
   const size_t seg_cos = seg(o_cos, size_t(ncos) * sizeof(CosmoDev));
-  const size_t seg_modes = seg(o_modes, size_t(m1 + m2) * sizeof(ModeDev));
+  const size_t seg_modes = seg(o_modes, size_t(m1 + m2 + mt) * sizeof(ModeDev));
   char* up = static_cast<char*>(L.up.get(std::max<size_t>(hoff, 8)));
   // downloads: status + counters + results per request
   size_t doff = 0;
@@ -535,7 +567,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   std::vector<CosmoDev> cos(ncos);
   std::vector<ModeDev> modes, modes2;
   modes.reserve(m1);
-  modes2.reserve(m2);
+  modes2.reserve(m2 + mt);
   for (size_t b = 0; b < batch.size(); ++b) {
     Req* r = batch[b];
     const int nk = r->r.nk, ns = r->nsets, nsrc = r->grid.n - r->src_from;
@@ -559,7 +591,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     int64_t* dcnt = reinterpret_cast<int64_t*>(dev + r->o_cnt);
     double* drec = reinterpret_cast<double*>(dev + r->o_rec);
     for (int s = 0; s < ns; ++s)
-      for (int i = 0; i < nk && !skips_solve(ns, s); ++i) {
+      for (int i = 0; i < nk && set_has_modes(r, s); ++i) {
         ModeDev m;
         std::memset(&m, 0, sizeof(m));
         m.k = r->k[i];
@@ -579,6 +611,22 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
         }
         m.status = dstat + size_t(s) * nk + i;
         m.counters = dcnt + 2 * (size_t(s) * nk + i);
+        if (r->tangent) {  // derivatives into the slots of the perturbed sets of theta 0, 1, 2, 5
+          m.flags |= MODE_TANGENT;
+          for (int d = 0; d < kTD; ++d) {
+            const int sj = 1 + kSolvedTheta[d];
+            m.tcos[d] = r->cos0 + sj;
+            m.tinv[d] = 1.0 / r->step[kSolvedTheta[d]];
+            if (r->r.kind == BOLT_REQ_CL) {
+              double* src = reinterpret_cast<double*>(dev + r->o_src);
+              m.tsrc_T[d] = src + (size_t(sj) * nk + i) * nsrc;
+              m.tsrc_E[d] = r->wantE ? src + size_t(ns) * nk * nsrc + (size_t(sj) * nk + i) * nsrc : nullptr;
+            }
+            if (r->wantP) m.tplin[d] = reinterpret_cast<double*>(dev + r->o_plin) + size_t(sj) * nk + i;
+          }
+          modes2.push_back(m);
+          continue;
+        }
         if (ns > 1) {
           m.flags |= s == 0 ? MODE_RECORD : MODE_REPLAY;
           m.rec = drec + size_t(i) * r->rec_cap;
@@ -682,15 +730,17 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   cfg.max_steps = E->cfg.max_steps > 0 ? E->cfg.max_steps : 100000;
   cfg.land_stride = E->cfg.land_stride > 1 ? E->cfg.land_stride : 1;
   for (int ph = 0; ph < nph; ++ph) {
-    RodasNodeArgs args;
-    cudaKernelNodeParams kp;
-    rodas_node_params(wpm[ph], d_modes + (ph ? m1 : 0), nmodes[ph], d_cos, cfg, L.d_queue + ph, maxN, maxnq, maxL,
-                      blocks[ph], d_scr, &args, &kp);
-    Graph& G = lane_graph(L, wpm[ph], ph, kp);
-    ck(cudaGraphLaunch(G.exec, st), "cudaGraphLaunch");
     L.wpm[ph] = wpm[ph];
     L.nmodes[ph] = nmodes[ph];
-    ++launches;
+    if (nmodes[ph] > 0) {
+      RodasNodeArgs args;
+      cudaKernelNodeParams kp;
+      rodas_node_params(wpm[ph], L.tan[ph], d_modes + (ph ? m1 : 0), nmodes[ph], d_cos, cfg, L.d_queue + ph, maxN,
+                        maxnq, maxL, blocks[ph], d_scr, &args, &kp);
+      Graph& G = lane_graph(L, wpm[ph], L.tan[ph], ph, kp);
+      ck(cudaGraphLaunch(G.exec, st), "cudaGraphLaunch");
+      ++launches;
+    }
     ck(cudaEventRecord(L.ev[1 + ph], st), "event");
   }
   if (nph == 1) {
@@ -721,8 +771,12 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
           rc = int(cudaMemsetAsync(dSd + size_t(j) * P.nrow * P.nm, 0, size_t(P.nrow) * P.nm * 8, st));
           continue;
         }
-        rc = launch_sdense_diff(nsrc, i0s, P.nrow, nk, kg, src + size_t(1 + j) * nk * nsrc, src, 1.0 / r->step[j],
-                                P.nm, kmid, dxs, dSd + size_t(j) * P.nrow * P.nm, st);
+        if (r->tangent)  // the tangent modes stored dS/dtheta_j in set 1 + j
+          rc = launch_sdense(nsrc, i0s, P.nrow, nk, kg, src + size_t(1 + j) * nk * nsrc, nullptr, P.nm, kmid, dxs,
+                             dSd + size_t(j) * P.nrow * P.nm, nullptr, st);
+        else
+          rc = launch_sdense_diff(nsrc, i0s, P.nrow, nk, kg, src + size_t(1 + j) * nk * nsrc, src,
+                                  1.0 / r->step[j], P.nm, kmid, dxs, dSd + size_t(j) * P.nrow * P.nm, st);
       }
       if (rc != 0) throw EngErr(-3, std::string("source resampling: ") + cudaGetErrorString(cudaError_t(rc)));
       LosGradArgs a;
@@ -779,9 +833,9 @@ void finalize_request(Lane& L, Req* r) {
   const int32_t* st = reinterpret_cast<const int32_t*>(down + r->h_stat);
   if (r->r.status) std::copy(st, st + nk, r->r.status);
   for (int s = 0; s < ns && r->rc == 0; ++s)
-    for (int i = 0; i < nk && !skips_solve(ns, s); ++i) {
+    for (int i = 0; i < nk && set_has_modes(r, s); ++i) {
       int v = st[size_t(s) * nk + i];
-      if ((v & 0xFF) != 0 || (s == 0 && ns > 1 && (v & ST_REC_OVERFLOW))) {
+      if ((v & 0xFF) != 0 || (s == 0 && ns > 1 && !r->tangent && (v & ST_REC_OVERFLOW))) {
         r->rc = -4;
         char buf[192];
         if ((v & 0xFF) == 0)
@@ -794,6 +848,7 @@ void finalize_request(Lane& L, Req* r) {
       }
     }
   auto deriv = [&](const double* f, size_t stride, int j, size_t i) -> double {  // set 1 + j: theta_j + h
+    if (r->tangent) return f[size_t(1 + j) * stride + i];  // the tangent itself
     return (f[size_t(1 + j) * stride + i] - f[i]) / r->step[j];
   };
   if (r->wantP) {
@@ -844,15 +899,15 @@ void finish_lane(bolt_engine* E, Lane& L) {
   for (Req* r : L.batch) {
     const int64_t* cnt = reinterpret_cast<const int64_t*>(down + r->h_cnt);
     for (int s = 0; s < r->nsets; ++s)
-      for (int i = 0; i < r->r.nk && !skips_solve(r->nsets, s); ++i) {
+      for (int i = 0; i < r->r.nk && set_has_modes(r, s); ++i) {
         size_t q = 2 * (size_t(s) * r->r.nk + i);
-        steps[s == 0 ? 0 : 1] += double(cnt[q] + cnt[q + 1]);
+        steps[(s == 0 && !r->tangent) ? 0 : 1] += double(cnt[q] + cnt[q + 1]);
         r->steps += double(cnt[q] + cnt[q + 1]);
       }
-    for (int s = 0; s < r->nsets; ++s) modes += skips_solve(r->nsets, s) ? 0 : r->r.nk;
+    for (int s = 0; s < r->nsets; ++s) modes += set_has_modes(r, s) ? r->r.nk : 0;
   }
-  E->tuner.update(L.shared[0], L.key[0], L.wpm[0], ms1 * 1e-3, steps[0]);
-  if (L.nmodes[1] > 0) E->tuner.update(L.shared[1], L.key[1], L.wpm[1], ms2 * 1e-3, steps[1]);
+  if (L.nmodes[0] > 0) E->tuner.update(L.shared[0], L.key[0], L.wpm[0], ms1 * 1e-3, steps[0]);
+  if (L.nmodes[1] > 0 && !L.tan[1]) E->tuner.update(L.shared[1], L.key[1], L.wpm[1], ms2 * 1e-3, steps[1]);
   const double t = now_s(E->t0);
   for (Req* r : L.batch) {
     finalize_request(L, r);
@@ -923,9 +978,15 @@ void scheduler(bolt_engine* E) {
         size_t bytes = 0;
         const int maxb = E->cfg.max_batch > 0 ? E->cfg.max_batch : 1 << 30;
         const double rt = E->ready.front()->r.reltol, at = E->ready.front()->r.abstol;
+        int gkind = -1;  // gradient requests of one batch: all tangent (0) or all replays (1)
         for (auto it = E->ready.begin(); it != E->ready.end() && int(batch.size()) < maxb;) {
           Req* r = *it;
           if (r->r.reltol != rt || r->r.abstol != at) { ++it; continue; }
+          if (r->nsets > 1) {
+            const int kind = r->tangent ? 0 : 1;
+            if (gkind >= 0 && kind != gkind) { ++it; continue; }
+            gkind = kind;
+          }
           size_t off = 0;
           layout_request(r, off);
           if (r->bytes > E->budget) {
@@ -1020,6 +1081,7 @@ int bolt_engine_create(const bolt_engine_cfg* cfg, bolt_engine** out) {
   if (cfg) E->cfg = *cfg;
   if (E->cfg.objective != 0 && E->cfg.objective != 1) return -1;
   if (E->cfg.land_stride < 0 || E->cfg.land_stride > 64) return -1;
+  if (E->cfg.grad_scheme < 0 || E->cfg.grad_scheme > 1) return -1;
   E->device = E->cfg.device;
   if (E->cfg.lanes <= 0) E->cfg.lanes = 6;
   if (E->cfg.lanes > 8) E->cfg.lanes = 8;
@@ -1118,6 +1180,9 @@ int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
       r->r.ells = nullptr;
       r->r.nell = 0;
     }
+    // P_lin and C_l^TT Jacobians come from tangent-linear modes unless the
+    // engine is set to replays; TE / EE Jacobians difference perturbed C_l
+    r->tangent = q->grad && E->cfg.grad_scheme == 0 && (q->kind == BOLT_REQ_PLIN || r->los_tangent);
     r->grid = make_grid(q->grid.start, q->grid.step, q->grid.stop);
     if (r->grid.n < 4 || r->grid.n > 100000) throw EngErr(-1, "x grid needs 4..100000 nodes");
     if (q->kind == BOLT_REQ_CL) {

@@ -71,6 +71,13 @@ struct Shared {
   double *yt, *b, *fl, *fi, *fc;
   double *q, *df0, *Aq, *Bq, *qe, *eq, *qe_d, *eq_d;
   double *Uf, *Wt, *cl1, *cl2, *sc, *sc_d, *misc;
+  // tangent-linear modes only (null otherwise): tangents [..][kTD] of the
+  // stage scalars (slots 0..5, and d/dx at slot 0), q / eps and eps / q,
+  // the perturbed sets' momenta, the tangents of the per-mode q constants
+  // and of the cosmology constants; the tangent stage states yd and
+  // right-hand sides bd ([kTD][N]) and the border partials of the tangent
+  // solves
+  double *sct, *sct_d, *qet, *eqt, *qet_d, *eqt_d, *qpj, *dq, *ddf0, *dAq, *dBq, *cstn, *yd, *bd, *part4;
 };
 
 struct Scratch {
@@ -83,17 +90,31 @@ constexpr int kMiscDoubles = 32 + 9 * 32;  // capacitance, reductions, per-chain
 // element lists (768 ints for every variant), owners and three counters.
 __host__ __device__ inline int pack_ints(int threads) { return 2 * threads + 768 + 32 + 4; }
 
-__host__ __device__ inline int per_mode_doubles(int N, int nq, int Lmax, int threads) {
+// Shared-memory doubles of the tangent part of a tangent mode (tangent.cuh):
+// stage-scalar tangents (6 slots and d/dx), q/eps and eps/q tangents,
+// perturbed q and q-constant tangents, the cosmology-constant tangents, the
+// tangent solves' border partials (32 chains x 3) and the tangent stage
+// states and right-hand sides.
+__host__ __device__ inline int tan_doubles(int N, int nq) {
+  return (kStages + 1) * kScal * kTD + 2 * (kStages + 1) * nq * kTD + 5 * nq * kTD + 8 * kTD + 32 * kBorder * kTD +
+         2 * kTD * N;
+}
+__host__ __device__ inline int per_mode_doubles(int N, int nq, int Lmax, int threads, bool tan = false) {
   int nch = nq + 5;
   return 5 * N + 4 * nq + 2 * kStages * nq + 2 * nq + 2 * nch * kTail * kBorder + 2 * (Lmax + 1) + kStages * kScal +
-         kScal + kMiscDoubles + (pack_ints(threads) + 1) / 2;
+         kScal + kMiscDoubles + (tan ? tan_doubles(N, nq) : 0) + (pack_ints(threads) + 1) / 2;
 }
-__host__ __device__ inline int scratch_per_warp(int N) { return 10 * N; }
+__host__ __device__ inline int scratch_per_warp(int N, bool tan = false) { return 10 * N + (tan ? 9 * kTD * N : 0); }
 
 struct Mode {
   const CosmoDev* C;
   double k;
   int N, lg, lnu, lmnu, nq, iTp, iN, iM, iPhi, nch;
+  // tangent-linear modes: the cosmologies of the kTD perturbed parameter
+  // sets and 1 / their parameter steps (coefficient tangents are their
+  // differences from C over the step)
+  const CosmoDev* tc[kTD];
+  double tinv[kTD];
 };
 
 // The four interleaved hot tables at node j (H, eta, tau', csb2).
@@ -116,10 +137,9 @@ struct Scal {
   T Hc, eta, tp, cs2, a, kH, iHe, R, cpsi, dphi, k2H2;
 };
 
-// Scalars (and their x-derivatives) at x, one lane per abscissa, written to
-// shared-memory slot `slot`; derivatives are kept for slot 0 only.
-__device__ __forceinline__ void stage_scalars_to(const Mode& m, const Shared& S, double x, int slot) {
-  const CosmoDev& C = *m.C;
+// The eleven stage scalars (and their x-derivatives into d, when d is not
+// null) of cosmology C at x for wavenumber k.
+__device__ __forceinline__ void stage_scalars_vals(const CosmoDev& C, double k, double x, double* o, double* od) {
   SplW w;
   spl_weights(C, x, w, true);
   HotCoef c0, c1, c2, c3;
@@ -133,16 +153,35 @@ __device__ __forceinline__ void stage_scalars_to(const Mode& m, const Shared& S,
   dd iH = 1.0 / Hc;
   dd v[11];
   v[0] = Hc; v[1] = eta; v[2] = tp; v[3] = cs2; v[4] = a;
-  v[5] = m.k * iH;
+  v[5] = k * iH;
   v[6] = iH / eta;
   v[7] = (4.0 * C.Omega_r / (3.0 * C.Omega_b)) / a;
-  v[8] = (12.0 * C.H0 * C.H0 / (m.k * m.k)) / (a * a);
+  v[8] = (12.0 * C.H0 * C.H0 / (k * k)) / (a * a);
   v[9] = (C.H0 * C.H0 * 0.5) * iH * iH;
-  v[10] = (m.k * m.k / 3.0) * iH * iH;
-  double* o = S.sc + slot * kScal;
+  v[10] = (k * k / 3.0) * iH * iH;
   for (int f = 0; f < 11; ++f) o[f] = v[f].v;
-  if (slot == 0)
-    for (int f = 0; f < 11; ++f) S.sc_d[f] = v[f].d;
+  if (od)
+    for (int f = 0; f < 11; ++f) od[f] = v[f].d;
+}
+
+// Scalars (and their x-derivatives) at x, one lane per abscissa, written to
+// shared-memory slot `slot`; derivatives are kept for slot 0 only.
+__device__ __forceinline__ void stage_scalars_to(const Mode& m, const Shared& S, double x, int slot) {
+  stage_scalars_vals(*m.C, m.k, x, S.sc + slot * kScal, slot == 0 ? S.sc_d : nullptr);
+}
+
+// Momentum-bin constants of cosmology C for bin q (background.jl:21-30,
+// perturbations.jl:127-158): the momentum q, dlnf0/dlnq, and the weights of
+// the rho / sigma (Aq) and theta (Bq) integrals.
+__device__ __forceinline__ void qconst(const CosmoDev& C, int q, double& qq, double& df0, double& Aq, double& Bq) {
+  double xq = C.qx[q];
+  double lq = C.logqmin + (C.logqmax - C.logqmin) / 2.0 * (xq + 1.0);
+  qq = pow(10.0, lq);
+  double dxdq = (1.0 + (-1.0 + 2.0 / (C.logqmax - C.logqmin) * ((1.0 + C.logqmin) - C.logqmin))) / (qq * log(10.0));
+  double f0 = 2.0 / pow(2.0 * M_PI, 3.0) / (exp(qq / C.Tnu) + 1.0);
+  df0 = -qq / C.Tnu / (1.0 + exp(-qq / C.Tnu));
+  Aq = 4.0 * M_PI * qq * qq * f0 / dxdq * C.qw[q];  // rho: Aq eps M0, sigma: Aq q^2/eps M2
+  Bq = 4.0 * M_PI * qq * qq * qq * f0 / dxdq * C.qw[q];
 }
 
 // Massive-neutrino energies q/eps, eps/q for (slot, q) pairs spread over the CTA.
@@ -208,20 +247,142 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// Number types of a right-hand-side evaluation: T, the type of its stage
+// scalars (double; dd for d/dx; d4 for the tangents along kTD parameter
+// directions; x4 for both), and KT<T>, the type of its per-mode and
+// per-cosmology constants (double, or d4 with their tangents).
+template <class T> struct KT { using type = double; };
+template <> struct KT<d4> { using type = d4; };
+template <> struct KT<x4> { using type = d4; };
+
+// A per-mode constant v[i] (with its tangents t[i * kTD + j] for K = d4).
+template <class K> __device__ __forceinline__ K kval(const double* v, const double* t, int i);
+template <> __device__ __forceinline__ double kval<double>(const double* v, const double*, int i) { return v[i]; }
+template <> __device__ __forceinline__ d4 kval<d4>(const double* v, const double* t, int i) {
+  d4 r;
+  r.v = v[i];
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = t[i * kTD + j];
+  return r;
+}
+
+// Per-cosmology constants: 0.25 / rho_crit, 1 / rho_crit, Omega_c, Omega_b,
+// H0, rho_crit, Sigma_m_nu, h (tangents in S.cstn[id * kTD + j]).
+constexpr int kCosN = 8;
+__device__ __forceinline__ double cos_const(const CosmoDev& C, int id) {
+  switch (id) {
+    case 0: return 0.25 / C.rho_crit;
+    case 1: return 1.0 / C.rho_crit;
+    case 2: return C.Omega_c;
+    case 3: return C.Omega_b;
+    case 4: return C.H0;
+    case 5: return C.rho_crit;
+    case 6: return C.Sigma_m_nu;
+    default: return C.h;
+  }
+}
+template <class K> __device__ __forceinline__ K kcos(const Mode& m, const Shared& S, int id);
+template <> __device__ __forceinline__ double kcos<double>(const Mode& m, const Shared&, int id) {
+  return cos_const(*m.C, id);
+}
+template <> __device__ __forceinline__ d4 kcos<d4>(const Mode& m, const Shared& S, int id) {
+  d4 r;
+  r.v = kcos<double>(m, S, id);
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = S.cstn[id * kTD + j];
+  return r;
+}
+
 template <class T> __device__ __forceinline__ T qe_of(const Shared& S, int sl, int nq, int q);
 template <> __device__ __forceinline__ double qe_of<double>(const Shared& S, int sl, int nq, int q) { return S.qe[sl * nq + q]; }
 template <> __device__ __forceinline__ dd qe_of<dd>(const Shared& S, int sl, int nq, int q) { return mk(S.qe[q], S.qe_d[q]); }
+template <> __device__ __forceinline__ d4 qe_of<d4>(const Shared& S, int sl, int nq, int q) {
+  return kval<d4>(S.qe, S.qet, sl * nq + q);
+}
+template <> __device__ __forceinline__ x4 qe_of<x4>(const Shared& S, int sl, int nq, int q) {
+  return mkx(kval<d4>(S.qe, S.qet, q), kval<d4>(S.qe_d, S.qet_d, q));
+}
 template <class T> __device__ __forceinline__ T eq_of(const Shared& S, int sl, int nq, int q);
 template <> __device__ __forceinline__ double eq_of<double>(const Shared& S, int sl, int nq, int q) { return S.eq[sl * nq + q]; }
 template <> __device__ __forceinline__ dd eq_of<dd>(const Shared& S, int sl, int nq, int q) { return mk(S.eq[q], S.eq_d[q]); }
+template <> __device__ __forceinline__ d4 eq_of<d4>(const Shared& S, int sl, int nq, int q) {
+  return kval<d4>(S.eq, S.eqt, sl * nq + q);
+}
+template <> __device__ __forceinline__ x4 eq_of<x4>(const Shared& S, int sl, int nq, int q) {
+  return mkx(kval<d4>(S.eq, S.eqt, q), kval<d4>(S.eq_d, S.eqt_d, q));
+}
 
-template <class T> __device__ __forceinline__ void put(double* v, double* d, int i, T x);
-template <> __device__ __forceinline__ void put<double>(double* v, double*, int i, double x) { v[i] = x; }
-template <> __device__ __forceinline__ void put<dd>(double* v, double* d, int i, dd x) { v[i] = x.v; d[i] = x.d; }
+template <> __device__ __forceinline__ Scal<d4> get_scal<d4>(const Shared& S, int slot) {
+  const int o = slot * kScal;
+  Scal<d4> s;
+  s.Hc = kval<d4>(S.sc, S.sct, o + 0); s.eta = kval<d4>(S.sc, S.sct, o + 1); s.tp = kval<d4>(S.sc, S.sct, o + 2);
+  s.cs2 = kval<d4>(S.sc, S.sct, o + 3); s.a = kval<d4>(S.sc, S.sct, o + 4); s.kH = kval<d4>(S.sc, S.sct, o + 5);
+  s.iHe = kval<d4>(S.sc, S.sct, o + 6); s.R = kval<d4>(S.sc, S.sct, o + 7); s.cpsi = kval<d4>(S.sc, S.sct, o + 8);
+  s.dphi = kval<d4>(S.sc, S.sct, o + 9); s.k2H2 = kval<d4>(S.sc, S.sct, o + 10);
+  return s;
+}
+template <> __device__ __forceinline__ Scal<x4> get_scal<x4>(const Shared& S, int) {
+  Scal<x4> s;
+#define XS(f, i) s.f = mkx(kval<d4>(S.sc, S.sct, i), kval<d4>(S.sc_d, S.sct_d, i))
+  XS(Hc, 0); XS(eta, 1); XS(tp, 2); XS(cs2, 3); XS(a, 4); XS(kH, 5); XS(iHe, 6); XS(R, 7); XS(cpsi, 8);
+  XS(dphi, 9); XS(k2H2, 10);
+#undef XS
+  return s;
+}
+
+// Where a right-hand side goes: values (and d/dx for dd) into v (d); the
+// tangents of a d4 evaluation into t[j * N + i]; an x4 evaluation writes its
+// value to v, its tangents to t and the tangents of its x-derivative to td.
+struct Sink {
+  double *v, *d, *t, *td;
+  int N;
+};
+template <class T> __device__ __forceinline__ void put(const Sink& o, int i, const T& x);
+template <> __device__ __forceinline__ void put<double>(const Sink& o, int i, const double& x) { o.v[i] = x; }
+template <> __device__ __forceinline__ void put<dd>(const Sink& o, int i, const dd& x) { o.v[i] = x.v; o.d[i] = x.d; }
+template <> __device__ __forceinline__ void put<d4>(const Sink& o, int i, const d4& x) {
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) o.t[j * o.N + i] = x.t[j];
+}
+template <> __device__ __forceinline__ void put<x4>(const Sink& o, int i, const x4& x) {
+  o.v[i] = x.v.v;
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) {
+    o.t[j * o.N + i] = x.v.t[j];
+    o.td[j * o.N + i] = x.d.t[j];
+  }
+}
+__device__ __forceinline__ Sink sink(double* v, double* d = nullptr) { Sink o; o.v = v; o.d = d; o.t = o.td = nullptr; o.N = 0; return o; }
+
+// State read by a right-hand side: plain values, or values with their
+// tangents du[j * N + i].
+struct StP {
+  const double* u;
+  __device__ __forceinline__ double operator[](int i) const { return u[i]; }
+};
+struct StD4 {
+  const double* u;
+  const double* du;
+  int N;
+  __device__ __forceinline__ d4 operator[](int i) const {
+    d4 r;
+    r.v = u[i];
+#pragma unroll
+    for (int j = 0; j < kTD; ++j) r.t[j] = du[j * N + i];
+    return r;
+  }
+};
 
 template <class T> __device__ __forceinline__ T warp_sum_t(T v);
 template <> __device__ __forceinline__ double warp_sum_t<double>(double v) { return warp_sum(v); }
 template <> __device__ __forceinline__ dd warp_sum_t<dd>(dd v) { return mk(warp_sum(v.v), warp_sum(v.d)); }
+template <> __device__ __forceinline__ d4 warp_sum_t<d4>(d4 v) {
+  v.v = warp_sum(v.v);
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) v.t[j] = warp_sum(v.t[j]);
+  return v;
+}
+template <> __device__ __forceinline__ x4 warp_sum_t<x4>(x4 v) { return mkx(warp_sum_t<d4>(v.v), warp_sum_t<d4>(v.d)); }
 
 // The radiation-streaming switch of hierarchy! (perturbations.jl:216) from
 // the stage scalars: k eta > 240 and -tau' H / eta > 100.
@@ -231,28 +392,28 @@ __device__ __forceinline__ bool rsa_switch(const Mode& m, const Scal<T>& s) {
 }
 
 // Metric potentials Psi and Phi' (perturbations.jl:182-194) from the state u.
-template <class T>
-__device__ __forceinline__ void metric(const Mode& m, const Shared& S, int sl, const Scal<T>& s, const double* u,
-                                       int lane, T& Psi, T& Phip, T* rhoM_out = nullptr) {
+template <class T, class U>
+__device__ __forceinline__ void metric(const Mode& m, const Shared& S, int sl, const Scal<T>& s, const U& u,
+                                       int lane, T& Psi, T& Phip) {
+  using K = typename KT<T>::type;
   const CosmoDev& C = *m.C;
   T rho = cst<T>(0.0), sig = cst<T>(0.0);
   for (int q = lane; q < m.nq; q += 32) {
     T qe = qe_of<T>(S, sl, m.nq, q), eq = eq_of<T>(S, sl, m.nq, q);
-    double qq = S.q[q];
+    K qq = kval<K>(S.q, S.dq, q);
     // eps = q * eq ; q^2/eps = q * qe
-    rho = rho + (S.Aq[q] * qq) * eq * u[m.iM + q];
-    sig = sig + (S.Aq[q] * qq) * qe * u[m.iM + 2 * m.nq + q];
+    rho = rho + (kval<K>(S.Aq, S.dAq, q) * qq) * eq * u[m.iM + q];
+    sig = sig + (kval<K>(S.Aq, S.dAq, q) * qq) * qe * u[m.iM + 2 * m.nq + q];
   }
   rho = warp_sum_t<T>(rho);
   sig = warp_sum_t<T>(sig);
-  if (rhoM_out) *rhoM_out = rho;
   const double Omega_nu = C.Omega_nu;
-  double Phi = u[m.iPhi];
-  Psi = -Phi - s.cpsi * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig * (0.25 / C.rho_crit));
+  const auto Phi = u[m.iPhi];
+  Psi = -Phi - s.cpsi * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig * kcos<K>(m, S, 0));
   T ia = 1.0 / s.a;
   Phip = Psi - s.k2H2 * Phi +
-         s.dphi * ((C.Omega_c * u[m.iPhi + 1] + C.Omega_b * u[m.iPhi + 3]) * ia +
-                   (4.0 * C.Omega_r * u[0] + 4.0 * Omega_nu * u[m.iN] + rho * (1.0 / C.rho_crit)) * (ia * ia));
+         s.dphi * ((kcos<K>(m, S, 2) * u[m.iPhi + 1] + kcos<K>(m, S, 3) * u[m.iPhi + 3]) * ia +
+                   (4.0 * C.Omega_r * u[0] + 4.0 * Omega_nu * u[m.iN] + rho * kcos<K>(m, S, 1)) * (ia * ia));
 }
 
 // The state overwrite of hierarchy!'s radiation-streaming branch
@@ -265,7 +426,7 @@ __device__ __forceinline__ void metric(const Mode& m, const Shared& S, int sl, c
 __device__ void rsa_overwrite(const Mode& m, const Shared& S, double x, double* u, int lane) {
   const Scal<double> s = get_scal<double>(S, 4);
   double Psi, Phip;
-  metric<double>(m, S, 4, s, u, lane, Psi, Phip);
+  metric<double>(m, S, 4, s, StP{u}, lane, Psi, Phip);
   if (lane != 0) return;
   const double Phi = u[m.iPhi], delb = u[m.iPhi + 3], vb = u[m.iPhi + 4];
   const double Hk = s.Hc / m.k, tpp = spl_cold(*m.C, C_TAUPP, x);
@@ -282,9 +443,10 @@ __device__ void rsa_overwrite(const Mode& m, const Shared& S, double x, double* 
 // forms the metric potentials itself (two nq-term sums), so no barrier is
 // needed before the rows.  Returns true when the radiation-streaming switch
 // is on.
-template <class T>
-__device__ bool rhs_rows(const Mode& m, const Shared& S, int sl, const double* u, double* out, double* out_d, int tid,
-                         int nth) {
+template <class T, class U>
+__device__ bool rhs_rows(const Mode& m, const Shared& S, int sl, const U& u, const Sink& out, int tid, int nth) {
+  using K = typename KT<T>::type;
+  using E = decltype(u[0]);
   const int lane = tid & 31;
   const Scal<T> s = get_scal<T>(S, sl);
   T Psi, Phip;
@@ -293,8 +455,9 @@ __device__ bool rhs_rows(const Mode& m, const Shared& S, int sl, const double* u
   const double* cl1 = S.cl1;
   const double* cl2 = S.cl2;
   const bool rsa = rsa_switch(m, s);
-  const double Pi = u[2] + u[m.iTp + 2] + u[m.iTp];
-  const double vb = u[m.iPhi + 4];
+  const E Pi = u[2] + u[m.iTp + 2] + u[m.iTp];
+  const E vb = u[m.iPhi + 4];
+  const E zero = cst<E>(0.0);
   for (int i = tid; i < m.N; i += nth) {
     T f;
     if (i < m.iM) {
@@ -303,7 +466,7 @@ __device__ bool rhs_rows(const Mode& m, const Shared& S, int sl, const double* u
       } else if (i < m.iTp) {  // photon temperature
         const int l = i;
         if (l < lg) {
-          double lo = l > 0 ? u[l - 1] : 0.0;
+          E lo = l > 0 ? u[l - 1] : zero;
           f = s.kH * (cl1[l] * lo - cl2[l] * u[l + 1]);
           if (l >= 1) f = f + s.tp * u[l];
           if (l == 0) f = f - Phip;
@@ -313,51 +476,49 @@ __device__ bool rhs_rows(const Mode& m, const Shared& S, int sl, const double* u
           f = s.kH * u[lg - 1] - ((lg + 1.0) * s.iHe - s.tp) * u[lg];
         }
       } else if (i < m.iN) {  // photon polarization
-        const int l = i - m.iTp;
-        const double* P = u + m.iTp;
+        const int l = i - m.iTp, P = m.iTp;
         if (l < lg) {
-          double lo = l > 0 ? P[l - 1] : 0.0;
-          f = s.kH * (cl1[l] * lo - cl2[l] * P[l + 1]) + s.tp * P[l];
+          E lo = l > 0 ? u[P + l - 1] : zero;
+          f = s.kH * (cl1[l] * lo - cl2[l] * u[P + l + 1]) + s.tp * u[P + l];
           if (l == 0) f = f - s.tp * (Pi / 2.0);
           if (l == 2) f = f - s.tp * (Pi / 10.0);
         } else {
-          f = s.kH * P[lg - 1] - ((lg + 1.0) * s.iHe - s.tp) * P[lg];
+          f = s.kH * u[P + lg - 1] - ((lg + 1.0) * s.iHe - s.tp) * u[P + lg];
         }
       } else {  // massless neutrinos
-        const int l = i - m.iN;
-        const double* Nn = u + m.iN;
+        const int l = i - m.iN, Nn = m.iN;
         if (l < lnu) {
-          double lo = l > 0 ? Nn[l - 1] : 0.0;
-          f = s.kH * (cl1[l] * lo - cl2[l] * Nn[l + 1]);
+          E lo = l > 0 ? u[Nn + l - 1] : zero;
+          f = s.kH * (cl1[l] * lo - cl2[l] * u[Nn + l + 1]);
           if (l == 0) f = f - Phip;
           if (l == 1) f = f + (1.0 / 3.0) * s.kH * Psi;
         } else {
-          f = s.kH * Nn[lnu - 1] - (lnu + 1.0) * s.iHe * Nn[lnu];
+          f = s.kH * u[Nn + lnu - 1] - (lnu + 1.0) * s.iHe * u[Nn + lnu];
         }
       }
     } else if (i < m.iPhi) {  // massive neutrinos (MB 57)
       const int j = i - m.iM;
       const int l = j / nq, q = j - l * nq;
-      const double* Mm = u + m.iM;
+      const int Mm = m.iM;
       T qe = qe_of<T>(S, sl, nq, q);
       if (l < lmnu) {
-        double lo = l > 0 ? Mm[j - nq] : 0.0;
-        f = (s.kH * qe) * (cl1[l] * lo - cl2[l] * Mm[j + nq]);
-        if (l == 0) f = f + Phip * S.df0[q];
-        if (l == 1) f = f - (1.0 / 3.0) * s.kH * eq_of<T>(S, sl, nq, q) * Psi * S.df0[q];
+        E lo = l > 0 ? u[Mm + j - nq] : zero;
+        f = (s.kH * qe) * (cl1[l] * lo - cl2[l] * u[Mm + j + nq]);
+        if (l == 0) f = f + Phip * kval<K>(S.df0, S.ddf0, q);
+        if (l == 1) f = f - (1.0 / 3.0) * s.kH * eq_of<T>(S, sl, nq, q) * Psi * kval<K>(S.df0, S.ddf0, q);
       } else {
-        f = qe * s.kH * Mm[j - nq] - (lmnu + 1.0) * s.iHe * Mm[j];
+        f = qe * s.kH * u[Mm + j - nq] - (lmnu + 1.0) * s.iHe * u[Mm + j];
       }
     } else {  // metric and matter
       const int r = i - m.iPhi;
-      const double v = u[m.iPhi + 2], delb = u[m.iPhi + 3];
+      const E v = u[m.iPhi + 2], delb = u[m.iPhi + 3];
       if (r == 0) f = Phip;
       else if (r == 1) f = s.kH * v - 3.0 * Phip;
       else if (r == 2) f = -v - s.kH * Psi;
       else if (r == 3) f = s.kH * vb - 3.0 * Phip;
       else f = -vb - s.kH * (Psi + s.cs2 * delb) + s.tp * s.R * (3.0 * u[1] + vb);
     }
-    put<T>(out, out_d, i, f);
+    put<T>(out, i, f);
   }
   return rsa;
 }
@@ -388,91 +549,132 @@ __device__ __forceinline__ int tail_slots(const Mode& m, int c) {
 }
 
 // ------------------------------------------------------------- outputs ----
+// Table `id` at x: the spline value (double), or the value with its
+// tangents from the perturbed parameter sets' tables (d4).
+template <class T> __device__ __forceinline__ T tabv(const Mode& m, int id, double x);
+template <> __device__ __forceinline__ double tabv<double>(const Mode& m, int id, double x) { return spl_cold(*m.C, id, x); }
+template <> __device__ __forceinline__ d4 tabv<d4>(const Mode& m, int id, double x) {
+  d4 r;
+  r.v = spl_cold(*m.C, id, x);
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) r.t[j] = (spl_cold(*m.tc[j], id, x) - r.v) * m.tinv[j];
+  return r;
+}
+__device__ __forceinline__ double dexp_t(double a) { return exp(a); }
+__device__ __forceinline__ d4 dexp_t(const d4& a) { return dexp(a); }
+
 // source_function and source_function_P (perturbations.jl:343-404) at a
-// grid node, from u and du = hierarchy!(u).
-__device__ void emit_sources(const Mode& m, const Shared& S, double x, const double* u, const double* du, int lane,
-                             double* outT, double* outE) {
+// grid node, from u and du = hierarchy!(u); T = d4 gives their tangents
+// (u and du then carry theirs).  Lane 0 writes outT / outE (wantE).
+template <class T, class U>
+__device__ void emit_sources_t(const Mode& m, const Shared& S, double x, const U& u, const U& du, int lane, T& outT,
+                               T& outE, bool wantE) {
+  using K = typename KT<T>::type;
   const CosmoDev& C = *m.C;
   double a = exp(x);
-  double sig = 0.0, sigp = 0.0;
+  T sig = cst<T>(0.0), sigp = cst<T>(0.0);
+  const K msum = kcos<K>(m, S, 6);
   for (int q = lane; q < m.nq; q += 32) {
-    double am = a * C.Sigma_m_nu, qq = S.q[q];
-    double eps = sqrt(qq * qq + am * am);
-    double w = S.Aq[q] * qq * qq / eps;
-    sig += w * u[m.iM + 2 * m.nq + q];
-    sigp += w * du[m.iM + 2 * m.nq + q];
+    K am = a * msum, qq = kval<K>(S.q, S.dq, q);
+    K eps = dsqrt(qq * qq + am * am);
+    K w = kval<K>(S.Aq, S.dAq, q) * qq * qq / eps;
+    sig = sig + w * u[m.iM + 2 * m.nq + q];
+    sigp = sigp + w * du[m.iM + 2 * m.nq + q];
   }
-  sig = warp_sum(sig);
-  sigp = warp_sum(sigp);
+  sig = warp_sum_t<T>(sig);
+  sigp = warp_sum_t<T>(sigp);
   if (lane != 0) return;
-  double H0sq = C.H0 * C.H0, k = m.k;
-  double Hc = spl_cold(C, C_H, x), Hcp = spl_cold(C, C_HP, x), Hcpp = spl_cold(C, C_HPP, x);
-  double tau = spl_cold(C, C_TAU, x), tp = spl_cold(C, C_TAUP, x), tpp = spl_cold(C, C_TAUPP, x);
-  double g = spl_cold(C, C_G, x), gp = spl_cold(C, C_GP, x), gpp = spl_cold(C, C_GPP, x);
-  double eta = spl_cold(C, C_ETA, x);
+  const K H0 = kcos<K>(m, S, 4), rho_crit = kcos<K>(m, S, 5);
+  const K H0sq = H0 * H0;
+  const double k = m.k;
+  T Hc = tabv<T>(m, C_H, x), Hcp = tabv<T>(m, C_HP, x), Hcpp = tabv<T>(m, C_HPP, x);
+  T tau = tabv<T>(m, C_TAU, x), tp = tabv<T>(m, C_TAUP, x), tpp = tabv<T>(m, C_TAUPP, x);
+  T g = tabv<T>(m, C_G, x), gp = tabv<T>(m, C_GP, x), gpp = tabv<T>(m, C_GPP, x);
+  T eta = tabv<T>(m, C_ETA, x);
   const double Omega_nu = C.Omega_nu;
-  const double* Th = u;
-  const double* Tp = u + m.iTp;
-  const double* dTh = du;
-  const double* dTp = du + m.iTp;
-  double Phi = u[m.iPhi], Phip = du[m.iPhi], vb = u[m.iPhi + 4], vbp = du[m.iPhi + 4];
-  double c = 12.0 * H0sq / (k * k) / (a * a);
-  double Psi = -Phi - c * (C.Omega_r * Th[2] + Omega_nu * u[m.iN + 2] + sig / C.rho_crit / 4.0);
-  double Psip = -Phip - c * (C.Omega_r * (dTh[2] - 2.0 * Th[2]) + Omega_nu * (du[m.iN + 2] - 2.0 * u[m.iN + 2]) +
-                             (sigp - 2.0 * sig) / C.rho_crit / 4.0);
-  double Pi = Th[2] + Tp[2] + Tp[0];
-  double Pip = dTh[2] + dTp[2] + dTp[0];
-  double term1 = g * (Th[0] + Psi + Pi / 4.0) + exp(-tau) * (Psip - Phip);
-  double term2 = (-1.0 / k) * (Hcp * g * vb + Hc * gp * vb + Hc * g * vbp);
-  double Pipp = 2.0 * k / (5.0 * Hc) * (-Hcp / Hc * Th[1] + dTh[1]) + (3.0 / 10.0) * (tpp * Pi + tp * Pip) -
-                3.0 * k / (5.0 * Hc) * (-Hcp / Hc * (Th[3] + Tp[1] + Tp[3]) + (dTh[3] + dTp[1] + dTp[3]));
-  double term3 = (3.0 / (4.0 * k * k)) * ((Hcp * Hcp + Hc * Hcpp) * g * Pi + 3.0 * Hc * Hcp * (gp * Pi + g * Pip) +
-                                          Hc * Hc * (gpp * Pi + 2.0 * gp * Pip + g * Pipp));
-  *outT = term1 + term2 + term3;
+  const int Tp = m.iTp;
+  const auto Phi = u[m.iPhi], Phip = du[m.iPhi], vb = u[m.iPhi + 4], vbp = du[m.iPhi + 4];
+  T c = 12.0 * H0sq / (k * k) / (a * a);
+  T Psi = -Phi - c * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig / rho_crit / 4.0);
+  T Psip = -Phip - c * (C.Omega_r * (du[2] - 2.0 * u[2]) + Omega_nu * (du[m.iN + 2] - 2.0 * u[m.iN + 2]) +
+                        (sigp - 2.0 * sig) / rho_crit / 4.0);
+  const auto Pi = u[2] + u[Tp + 2] + u[Tp];
+  const auto Pip = du[2] + du[Tp + 2] + du[Tp];
+  T term1 = g * (u[0] + Psi + Pi / 4.0) + dexp_t(-tau) * (Psip - Phip);
+  T term2 = (-1.0 / k) * (Hcp * g * vb + Hc * gp * vb + Hc * g * vbp);
+  T Pipp = 2.0 * k / (5.0 * Hc) * (-Hcp / Hc * u[1] + du[1]) + (3.0 / 10.0) * (tpp * Pi + tp * Pip) -
+           3.0 * k / (5.0 * Hc) * (-Hcp / Hc * (u[3] + u[Tp + 1] + u[Tp + 3]) + (du[3] + du[Tp + 1] + du[Tp + 3]));
+  T term3 = (3.0 / (4.0 * k * k)) * ((Hcp * Hcp + Hc * Hcpp) * g * Pi + 3.0 * Hc * Hcp * (gp * Pi + g * Pip) +
+                                     Hc * Hc * (gpp * Pi + 2.0 * gp * Pip + g * Pipp));
+  outT = term1 + term2 + term3;
   // same spline, same evaluation as eta(x): y is exactly 0 at the last node,
   // where the reference's 3 / (4 y^2) is infinite (perturbations.jl:401-403)
-  if (outE) {  // null when the caller wants S_T only
-    double y = (x == C.x_last) ? 0.0 : k * (spl_cold(C, C_ETA, C.x_last) - eta);
-    *outE = (3.0 / (4.0 * y * y)) * g * Pi;
+  if (wantE) {
+    T y = (x == C.x_last) ? cst<T>(0.0) : k * (tabv<T>(m, C_ETA, C.x_last) - eta);
+    outE = (3.0 / (4.0 * y * y)) * g * Pi;
   }
 }
 
-// plin (spectra.jl:163-198) at the final node x.
-__device__ void emit_plin(const Mode& m, const Shared& S, double x, const double* u, int lane, double* out) {
+__device__ void emit_sources(const Mode& m, const Shared& S, double x, const double* u, const double* du, int lane,
+                             double* outT, double* outE) {
+  double t = 0.0, e = 0.0;
+  emit_sources_t<double>(m, S, x, StP{u}, StP{du}, lane, t, e, outE != nullptr);
+  if (lane == 0) {
+    *outT = t;
+    if (outE) *outE = e;
+  }
+}
+
+// plin (spectra.jl:163-198) at the final node x; T = d4 gives its tangents
+// (u then carries theirs).  Lane 0 writes out.
+__device__ __forceinline__ double dpow_t(double a, double b) { return pow(a, b); }
+__device__ __forceinline__ d4 dpow_t(const d4& a, double b) { return dpow(a, b); }
+template <class T, class U>
+__device__ void emit_plin_t(const Mode& m, const Shared& S, double x, const U& u, int lane, T& out) {
+  using K = typename KT<T>::type;
   const CosmoDev& C = *m.C;
   double a = exp(x);
-  double rho = 0.0, th = 0.0;
+  T rho = cst<T>(0.0), th = cst<T>(0.0);
+  const K msum = kcos<K>(m, S, 6);
   for (int q = lane; q < m.nq; q += 32) {
-    double am = a * C.Sigma_m_nu, qq = S.q[q];
-    double eps = sqrt(qq * qq + am * am);
-    rho += S.Aq[q] * eps * u[m.iM + q];
-    th += S.Bq[q] * u[m.iM + m.nq + q];
+    K am = a * msum, qq = kval<K>(S.q, S.dq, q);
+    K eps = dsqrt(qq * qq + am * am);
+    rho = rho + kval<K>(S.Aq, S.dAq, q) * eps * u[m.iM + q];
+    th = th + kval<K>(S.Bq, S.dBq, q) * u[m.iM + m.nq + q];
   }
-  rho = warp_sum(rho);
-  th = warp_sum(th);
+  rho = warp_sum_t<T>(rho);
+  th = warp_sum_t<T>(th);
   if (lane != 0) return;
   double k = m.k;
-  double r0 = spl_cold(C, C_RHO0M, x);
-  double Mrho = rho / r0, Mth = k * th / r0;
-  double dcN = u[m.iPhi + 1], vcN = u[m.iPhi + 2], dbN = u[m.iPhi + 3], vbN = u[m.iPhi + 4];
-  double vmnu = -Mth / k;
-  double Tg = pow(15.0 / (M_PI * M_PI) * C.rho_crit * C.Omega_r, 0.25);
-  double nufac = (90.0 * 1.2020569 / (11.0 * pow(M_PI, 4))) * (C.Omega_r * C.h * C.h / Tg) * pow(C.N_nu / 3.0, 0.75);
-  double Omega_nu = C.Sigma_m_nu * nufac / (C.h * C.h);
-  double Om = C.Omega_c + C.Omega_b + Omega_nu;
-  double Hc = spl_cold(C, C_H, x);
-  double dc = dcN - 3.0 * Hc * vcN / k, db = dbN - 3.0 * Hc * vbN / k, dn = Mrho - 3.0 * Hc * vmnu / k;
-  double dm = (C.Omega_c * dc + C.Omega_b * db + Omega_nu * dn) / Om;
+  const K rho_crit = kcos<K>(m, S, 5), h = kcos<K>(m, S, 7), Omega_c = kcos<K>(m, S, 2), Omega_b = kcos<K>(m, S, 3);
+  T r0 = tabv<T>(m, C_RHO0M, x);
+  T Mrho = rho / r0, Mth = k * th / r0;
+  const auto dcN = u[m.iPhi + 1], vcN = u[m.iPhi + 2], dbN = u[m.iPhi + 3], vbN = u[m.iPhi + 4];
+  T vmnu = -Mth / k;
+  K Tg = dpow_t(15.0 / (M_PI * M_PI) * rho_crit * C.Omega_r, 0.25);
+  K nufac = (90.0 * 1.2020569 / (11.0 * pow(M_PI, 4))) * (C.Omega_r * h * h / Tg) * pow(C.N_nu / 3.0, 0.75);
+  K Omega_nu = msum * nufac / (h * h);
+  K Om = Omega_c + Omega_b + Omega_nu;
+  T Hc = tabv<T>(m, C_H, x);
+  T dc = dcN - 3.0 * Hc * vcN / k, db = dbN - 3.0 * Hc * vbN / k, dn = Mrho - 3.0 * Hc * vmnu / k;
+  T dm = (Omega_c * dc + Omega_b * db + Omega_nu * dn) / Om;
   double Pp = C.A * pow(k / 0.05, C.n_s - 1.0);
-  *out = (2.0 * M_PI * M_PI / (k * k * k)) * dm * dm * Pp;
+  out = (2.0 * M_PI * M_PI / (k * k * k)) * dm * dm * Pp;
 }
 
-// initial_conditions (perturbations.jl:274-338), lane 0 serial (once per mode).
-__device__ void initial_state(const Mode& m, const Shared& S, double xi, double* u, int lane) {
+__device__ void emit_plin(const Mode& m, const Shared& S, double x, const double* u, int lane, double* out) {
+  double v = 0.0;
+  emit_plin_t<double>(m, S, x, StP{u}, lane, v);
+  if (lane == 0) *out = v;
+}
+
+// initial_conditions (perturbations.jl:274-338) of cosmology C with the
+// momentum-bin constants q, df0, lane 0 serial (once per mode).
+__device__ void initial_state(const Mode& m, const CosmoDev& C, const double* qv, const double* df0v, double xi,
+                              double* u, int lane) {
   for (int i = lane; i < m.N; i += 32) u[i] = 0.0;
   __syncwarp();
   if (lane == 0) {
-    const CosmoDev& C = *m.C;
     double k = m.k;
     double Hc = spl_cold(C, C_H, xi), eta = spl_cold(C, C_ETA, xi), tp = spl_cold(C, C_TAUP, xi);
     double ai = exp(xi);
@@ -499,8 +701,8 @@ __device__ void initial_state(const Mode& m, const Shared& S, double xi, double*
     Nn[2] = -(k * k * eta * eta) / 15.0 * 1.0 / (1.0 + 2.0 / 5.0 * fnu) * Phi / 2.0;
     for (int l = 3; l <= m.lnu; ++l) Nn[l] = k / ((2.0 * l + 1.0) * Hc) * Nn[l - 1];
     for (int q = 0; q < m.nq; ++q) {
-      double qq = S.q[q], am = ai * C.Sigma_m_nu;
-      double eps = sqrt(qq * qq + am * am), df0 = S.df0[q];
+      double qq = qv[q], am = ai * C.Sigma_m_nu;
+      double eps = sqrt(qq * qq + am * am), df0 = df0v[q];
       u[m.iM + q] = -Nn[0] * df0;
       u[m.iM + m.nq + q] = -eps / qq * Nn[1] * df0;
       u[m.iM + 2 * m.nq + q] = -Nn[2] * df0;
@@ -517,6 +719,7 @@ __device__ void initial_state(const Mode& m, const Shared& S, double xi, double*
 }
 
 #include "chains.cuh"
+#include "tangent.cuh"
 
 // --------------------------------------------------------------- driver ----
 // Optional per-phase cycle counters (compile with -DBOLT_PHASE_TIMERS): thread
@@ -569,7 +772,7 @@ __device__ __forceinline__ double block_sum(double v, double* red, int tid) {
   return t;
 }
 
-template <int WPM>
+template <int WPM, bool TAN>
 __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const SolverCfg& cfg, double* base,
                           double* gscr, int tid) {
   constexpr int nth = 32 * WPM;
@@ -584,10 +787,16 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   m.iM = m.iN + m.lnu + 1;
   m.iPhi = m.iM + (m.lmnu + 1) * m.nq;
   m.nch = m.nq + 5;
+  for (int j = 0; j < kTD; ++j) {
+    m.tc[j] = TAN ? cosmos + md.tcos[j] : m.C;
+    m.tinv[j] = TAN ? md.tinv[j] : 0.0;
+  }
   const CosmoDev& C = *m.C;
   const int N = m.N, nq = m.nq;
   int Lmax = max(m.lg, max(m.lnu, m.lmnu));
   Shared S;
+  S.sct = S.sct_d = S.qet = S.eqt = S.qet_d = S.eqt_d = S.qpj = S.dq = S.ddf0 = S.dAq = S.dBq = S.cstn = nullptr;
+  S.yd = S.bd = S.part4 = nullptr;
   double* p = base;
   S.yt = p; p += N;
   S.b = p; p += N;
@@ -610,6 +819,23 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   S.sc_d = p; p += kScal;
   S.misc = p;                 // [0..8] capacitance inverse, [16..23] block reductions, [24] flags, [32..] partials
   p += kMiscDoubles;
+  if (TAN) {  // the layout tan_doubles() sizes
+    S.sct = p; p += kStages * kScal * kTD;
+    S.sct_d = p; p += kScal * kTD;
+    S.qet = p; p += kStages * nq * kTD;
+    S.eqt = p; p += kStages * nq * kTD;
+    S.qet_d = p; p += nq * kTD;
+    S.eqt_d = p; p += nq * kTD;
+    S.qpj = p; p += kTD * nq;
+    S.dq = p; p += nq * kTD;
+    S.ddf0 = p; p += nq * kTD;
+    S.dAq = p; p += nq * kTD;
+    S.dBq = p; p += nq * kTD;
+    S.cstn = p; p += 8 * kTD;
+    S.part4 = p; p += 32 * kBorder * kTD;
+    S.yd = p; p += kTD * N;
+    S.bd = p; p += kTD * N;
+  }
   double* red = S.misc + 16;
   Pack PK;
   {
@@ -627,22 +853,17 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   G.K = gscr + 2 * N;
   G.yp = gscr + 8 * N;
   G.fp = gscr + 9 * N;
+  TanScratch T;
+  T.dy = gscr + 10 * N;
+  T.dK = T.dy + kTD * N;
+  T.fxt = T.dK + 6 * kTD * N;
+  T.tmp = T.fxt + kTD * N;
   // per-mode constants (perturbations.jl:164-166; background.jl:21-30)
   for (int l = tid; l <= Lmax; l += nth) {
     S.cl1[l] = double(l) / (2.0 * l + 1.0);
     S.cl2[l] = (l + 1.0) / (2.0 * l + 1.0);
   }
-  for (int q = tid; q < nq; q += nth) {
-    double xq = C.qx[q];
-    double lq = C.logqmin + (C.logqmax - C.logqmin) / 2.0 * (xq + 1.0);
-    double qq = pow(10.0, lq);
-    double dxdq = (1.0 + (-1.0 + 2.0 / (C.logqmax - C.logqmin) * ((1.0 + C.logqmin) - C.logqmin))) / (qq * log(10.0));
-    double f0 = 2.0 / pow(2.0 * M_PI, 3.0) / (exp(qq / C.Tnu) + 1.0);
-    S.q[q] = qq;
-    S.df0[q] = -qq / C.Tnu / (1.0 + exp(-qq / C.Tnu));
-    S.Aq[q] = 4.0 * M_PI * qq * qq * f0 / dxdq * C.qw[q];  // rho: Aq eps M0, sigma: Aq q^2/eps M2
-    S.Bq[q] = 4.0 * M_PI * qq * qq * qq * f0 / dxdq * C.qw[q];
-  }
+  for (int q = tid; q < nq; q += nth) qconst(C, q, S.q[q], S.df0[q], S.Aq[q], S.Bq[q]);
   if (tid == 0) S.misc[25] = build_pack(m, PK, nth) ? 1.0 : 0.0;
   __syncthreads();
   double x = C.x0;
@@ -651,17 +872,22 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     if (tid == 0) { *md.status = ST_BAD_INPUT; if (md.counters) { md.counters[0] = 0; md.counters[1] = 0; } }
     return;
   }
-  if (warp == 0) initial_state(m, S, x, S.yt, lane);
+  if (warp == 0) initial_state(m, C, S.q, S.df0, x, S.yt, lane);
   __syncthreads();
   copy_vec(N, S.yt, G.y, tid, nth);
   __syncthreads();
+  if (TAN) {
+    tan_setup(m, S, tid, nth);
+    tan_initial(m, S, x, G.y, T.dy, tid, nth);
+  }
   int status = ST_OK;
   bool rsa_any = false;
   long long nacc = 0, nrej = 0;
   int jo = 0;
   while (jo < md.nout && md.xout[jo] < x) ++jo;
+  int jtan = jo;  // next node of the tangent outputs (tangent modes land on every node)
   // nodes below x_dense are produced by dense output (sources only)
-  const bool dense_ok = (md.flags & MODE_SOURCES) && !(md.flags & MODE_TRAJ);
+  const bool dense_ok = (md.flags & MODE_SOURCES) && !(md.flags & MODE_TRAJ) && !TAN;
   int jd = 0;
   if (dense_ok)
     while (jd < md.nout - 1 && md.xout[jd] < cfg.x_dense) ++jd;
@@ -681,14 +907,14 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
         double* Kf = G.K + N;
         copy_vec(N, G.y, S.yt, tid, nth);
         __syncthreads();
-        rhs_rows<double>(m, S, 5, S.yt, Kf, nullptr, tid, nth);
+        rhs_rows<double>(m, S, 5, StP{S.yt}, sink(Kf), tid, nth);
         __syncthreads();
         if (dense_ok && have_prev) {
           while (jo < md.nout && md.xout[jo] < x) {
             double xq = md.xout[jo];
             hermite(N, xprev, x, xq, G.yp, G.fp, G.y, Kf, S.yt, tid, nth);
             prepare_other(m, S, xq, tid, nth);
-            rhs_rows<double>(m, S, 5, S.yt, G.K, nullptr, tid, nth);
+            rhs_rows<double>(m, S, 5, StP{S.yt}, sink(G.K), tid, nth);
             __syncthreads();
             if (warp == 0) emit_sources(m, S, xq, S.yt, G.K, lane, md.src_T + jo, md.src_E ? md.src_E + jo : nullptr);
             __syncthreads();
@@ -706,11 +932,30 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
           ++jo;
         }
         __syncthreads();
+        if (TAN && (md.flags & MODE_SOURCES) && jtan < md.nout && md.xout[jtan] == x) {
+          double xs[kStages];
+          xs[5] = x;
+          tan_prepare(m, S, xs, 5, 6, tid, nth);
+          Sink o;
+          o.v = nullptr; o.d = nullptr; o.t = S.bd; o.td = nullptr; o.N = N;
+          rhs_rows<d4>(m, S, 5, StD4{S.yt, T.dy, N}, o, tid, nth);
+          __syncthreads();
+          if (warp == 0) tan_emit_sources(m, S, md, x, S.yt, T.dy, Kf, S.bd, jtan, lane);
+          ++jtan;
+          __syncthreads();
+        }
       }
       if (md.flags & MODE_PLIN) {
         copy_vec(N, G.y, S.yt, tid, nth);
         __syncthreads();
         if (warp == 0) emit_plin(m, S, x, S.yt, lane, md.plin);
+        if (TAN && warp == 0) {
+          d4 dP = c4(0.0);
+          emit_plin_t<d4>(m, S, x, StD4{S.yt, T.dy, N}, lane, dP);
+          if (lane == 0)
+            for (int j = 0; j < kTD; ++j)
+              if (md.tplin[j]) *md.tplin[j] = dP.t[j];
+        }
       }
       break;
     }
@@ -742,7 +987,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     __syncthreads();
     if (!fok) { status = ST_LU_FAIL; break; }
     PT(1)
-    bool r = rhs_rows<dd>(m, S, 0, S.yt, S.b, G.fx, tid, nth);
+    bool r = rhs_rows<dd>(m, S, 0, StP{S.yt}, sink(S.b, G.fx), tid, nth);
     rsa_any |= r;
     __syncthreads();
     PT(2)
@@ -756,7 +1001,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
           double xq = md.xout[jo];
           hermite(N, xprev, x, xq, G.yp, G.fp, G.y, K0, S.yt, tid, nth);
           prepare_other(m, S, xq, tid, nth);
-          rhs_rows<double>(m, S, 5, S.yt, G.K + N, nullptr, tid, nth);
+          rhs_rows<double>(m, S, 5, StP{S.yt}, sink(G.K + N), tid, nth);
           __syncthreads();
           if (warp == 0) emit_sources(m, S, xq, S.yt, G.K + N, lane, md.src_T + jo, md.src_E ? md.src_E + jo : nullptr);
           __syncthreads();
@@ -801,7 +1046,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       __syncthreads();
       PT(5)
       const int sl = st < 4 ? st : 4;
-      r = rhs_rows<double>(m, S, sl, S.yt, S.b, nullptr, tid, nth);
+      r = rhs_rows<double>(m, S, sl, StP{S.yt}, sink(S.b), tid, nth);
       rsa_any |= r;
       // each thread combines the rows it produced (same row assignment)
       const double hd = hs * rodas::kD[st];
@@ -840,13 +1085,16 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
       fac = fmin(6.0, fmax(0.2, fac));
     }
     if (en <= 1.0) {
-      for (int i = tid; i < N; i += nth) G.y[i] = S.yt[i] + S.b[i];
+      if (TAN) tan_step<WPM>(m, S, PK, G, T, md, x, hs, xn, jtan, tid, nth);
+      else
+        for (int i = tid; i < N; i += nth) G.y[i] = S.yt[i] + S.b[i];
       if (record && tid == 0) {
         if (nacc < md.rec_cap) md.rec[nacc] = xn;
         else rec_over = true;
       }
       __syncthreads();
       if (rsa_switch(m, get_scal<double>(S, 4))) {  // uniform over the CTA
+        if (TAN) { status = ST_TANGENT_RSA; break; }
         if (warp == 0) rsa_overwrite(m, S, xn, G.y, lane);
         __syncthreads();
       }
@@ -933,7 +1181,8 @@ int launch_rsa_post(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos
 // Persistent CTAs: the first wave takes modes blockIdx.x (modes arrive sorted
 // by decreasing cost, and consecutive blocks land on different SMs, so the
 // longest modes spread one per SM); later modes come from a device queue.
-template <int WPM>
+// TAN: every mode of the launch is a tangent mode (MODE_TANGENT).
+template <int WPM, bool TAN>
 __global__ void __launch_bounds__(32 * WPM) rodas_kernel(const ModeDev* __restrict__ modes, int nmodes,
                                                          const CosmoDev* __restrict__ cosmos, SolverCfg cfg,
                                                          int* __restrict__ queue, double* __restrict__ scratch,
@@ -944,7 +1193,7 @@ __global__ void __launch_bounds__(32 * WPM) rodas_kernel(const ModeDev* __restri
   double* gscr = scratch + (size_t)blockIdx.x * scr_per_mode;
   int mi = blockIdx.x;
   while (mi < nmodes) {
-    solve_one<WPM>(modes[mi], cosmos, cfg, smem, gscr, tid);
+    solve_one<WPM, TAN>(modes[mi], cosmos, cfg, smem, gscr, tid);
     __syncthreads();
     if (tid == 0) s_mode = gridDim.x + atomicAdd(queue, 1);
     __syncthreads();
@@ -953,63 +1202,78 @@ __global__ void __launch_bounds__(32 * WPM) rodas_kernel(const ModeDev* __restri
 }
 
 namespace {
-template <int WPM>
-int grid_for(int nmodes, size_t smem, int* blocks) {
-  cudaError_t e = cudaFuncSetAttribute(rodas_kernel<WPM>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+// The kernel variant: warps per mode 1, 2 or 4; tangent modes with one warp.
+const void* kernel_of(int wpm, bool tan) {
+  if (tan) return (const void*)rodas_kernel<1, true>;
+  return wpm == 1 ? (const void*)rodas_kernel<1, false>
+                  : (wpm == 2 ? (const void*)rodas_kernel<2, false> : (const void*)rodas_kernel<4, false>);
+}
+int norm_wpm(int wpm, bool tan) { return tan ? 1 : ((wpm == 1 || wpm == 2) ? wpm : 4); }
+size_t smem_of(int maxN, int maxnq, int maxL, int wpm, bool tan) {
+  return size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * wpm, tan)) * sizeof(double);
+}
+}  // namespace
+
+// Host helpers.  wpm: warps per mode (1, 2 or 4; anything else means 4;
+// tangent launches use one).  Writes the number of persistent CTAs to
+// launch (one mode each at a time).
+int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, bool tan, int* blocks) {
+  wpm = norm_wpm(wpm, tan);
+  const size_t smem = smem_of(maxN, maxnq, maxL, wpm, tan);
+  const void* f = kernel_of(wpm, tan);
+  cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return -int(e);
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int bps = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, rodas_kernel<WPM>, 32 * WPM, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, f, 32 * wpm, smem);
   if (e != cudaSuccess) return -int(e);
   if (bps < 1) return -int(cudaErrorInvalidConfiguration);
   *blocks = std::min(nmodes, nsm * bps);
   return 0;
 }
-int norm_wpm(int wpm) { return (wpm == 1 || wpm == 2) ? wpm : 4; }
-}  // namespace
-
-// Host helpers.  wpm: warps per mode (1, 2 or 4; anything else means 4).
-// Writes the number of persistent CTAs to launch (one mode each at a time).
 int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, int* blocks) {
-  wpm = norm_wpm(wpm);
-  size_t smem = size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * wpm)) * sizeof(double);
-  if (wpm == 1) return grid_for<1>(nmodes, smem, blocks);
-  if (wpm == 2) return grid_for<2>(nmodes, smem, blocks);
-  return grid_for<4>(nmodes, smem, blocks);
+  return rodas_grid_warps(nmodes, maxN, maxnq, maxL, wpm, false, blocks);
 }
 
 int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
-                 int maxN, int maxnq, int maxL, int wpm, int blocks, double* d_scratch, cudaStream_t stream) {
-  wpm = norm_wpm(wpm);
-  size_t smem = size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * wpm)) * sizeof(double);
+                 int maxN, int maxnq, int maxL, int wpm, bool tan, int blocks, double* d_scratch, cudaStream_t stream) {
+  wpm = norm_wpm(wpm, tan);
+  const size_t smem = smem_of(maxN, maxnq, maxL, wpm, tan);
   cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  const int spm = scratch_per_warp(maxN);
-  if (wpm == 1)
-    rodas_kernel<1><<<blocks, 32, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+  const int spm = scratch_per_warp(maxN, tan);
+  if (tan)
+    rodas_kernel<1, true><<<blocks, 32, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+  else if (wpm == 1)
+    rodas_kernel<1, false><<<blocks, 32, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
   else if (wpm == 2)
-    rodas_kernel<2><<<blocks, 64, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+    rodas_kernel<2, false><<<blocks, 64, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
   else
-    rodas_kernel<4><<<blocks, 128, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+    rodas_kernel<4, false><<<blocks, 128, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
   return cudaGetLastError();
+}
+int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
+                 int maxN, int maxnq, int maxL, int wpm, int blocks, double* d_scratch, cudaStream_t stream) {
+  return launch_rodas(d_modes, nmodes, d_cosmos, cfg, d_queue, maxN, maxnq, maxL, wpm, false, blocks, d_scratch,
+                      stream);
 }
 
 // Kernel-node description of one solver launch, for CUDA graphs whose
 // node parameters are updated per batch.  args must stay alive until the
 // node parameters have been set (the values are copied then).
-int rodas_node_params(int wpm, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg,
-                      int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch, RodasNodeArgs* args,
-                      cudaKernelNodeParams* p) {
-  wpm = norm_wpm(wpm);
+int rodas_node_params(int wpm, bool tan, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos,
+                      const SolverCfg& cfg, int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch,
+                      RodasNodeArgs* args, cudaKernelNodeParams* p) {
+  wpm = norm_wpm(wpm, tan);
   args->modes = d_modes;
   args->nmodes = nmodes;
   args->cosmos = d_cosmos;
   args->cfg = cfg;
   args->queue = d_queue;
   args->scratch = d_scratch;
-  args->spm = scratch_per_warp(maxN);
+  args->spm = scratch_per_warp(maxN, tan);
   args->ptrs[0] = &args->modes;
   args->ptrs[1] = &args->nmodes;
   args->ptrs[2] = &args->cosmos;
@@ -1017,20 +1281,30 @@ int rodas_node_params(int wpm, const ModeDev* d_modes, int nmodes, const CosmoDe
   args->ptrs[4] = &args->queue;
   args->ptrs[5] = &args->scratch;
   args->ptrs[6] = &args->spm;
-  p->func = wpm == 1 ? (void*)rodas_kernel<1> : (wpm == 2 ? (void*)rodas_kernel<2> : (void*)rodas_kernel<4>);
+  p->func = const_cast<void*>(kernel_of(wpm, tan));
   p->gridDim = dim3(blocks);
   p->blockDim = dim3(32 * wpm);
-  p->sharedMemBytes = unsigned(size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * wpm)) * sizeof(double));
+  p->sharedMemBytes = unsigned(smem_of(maxN, maxnq, maxL, wpm, tan));
   p->kernelParams = args->ptrs;
   p->extra = nullptr;
   return 0;
 }
+int rodas_node_params(int wpm, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg,
+                      int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch, RodasNodeArgs* args,
+                      cudaKernelNodeParams* p) {
+  return rodas_node_params(wpm, false, d_modes, nmodes, d_cosmos, cfg, d_queue, maxN, maxnq, maxL, blocks, d_scratch,
+                           args, p);
+}
 
+size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm, bool tan) {
+  return smem_of(maxN, maxnq, maxL, norm_wpm(wpm, tan), tan);
+}
 size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm) {
-  return size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * norm_wpm(wpm))) * sizeof(double);
+  return rodas_smem_per_mode(maxN, maxnq, maxL, wpm, false);
 }
 size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL) { return rodas_smem_per_mode(maxN, maxnq, maxL, 4); }
-size_t rodas_scratch_per_warp(int maxN) { return size_t(scratch_per_warp(maxN)) * sizeof(double); }
+size_t rodas_scratch_per_warp(int maxN, bool tan) { return size_t(scratch_per_warp(maxN, tan)) * sizeof(double); }
+size_t rodas_scratch_per_warp(int maxN) { return rodas_scratch_per_warp(maxN, false); }
 
 #ifdef BOLT_PHASE_TIMERS
 int rodas_phase_cycles(unsigned long long* out, bool reset) {

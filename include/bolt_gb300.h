@@ -251,6 +251,10 @@ typedef struct {
   int land_stride;       /* source grids: the solver lands on every land_stride-th x node at x >= -8.5
                             (and the last) and takes the others from cubic Hermite dense output, as it
                             does below -8.5 (0 or 1 = lands on every node there; at most 64) */
+  int grad_scheme;       /* Jacobians of P_lin and C_l^TT requests: 0 = the tangent-linear solver (one
+                            solve carries the state and its derivatives along h, omega_b, omega_c and
+                            Sigma m_nu, sharing each step's factorisation), 1 = forward differences of
+                            four frozen-step replays; C_l requests with TE or EE Jacobians always replay */
 } bolt_engine_cfg;
 
 typedef struct bolt_engine bolt_engine;

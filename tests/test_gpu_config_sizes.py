@@ -16,9 +16,11 @@ ABI) against the CPU oracle.
   and EE within 1e-4 relative at every l, TE within 1e-4 of its peak.
 * Jacobians of C_l^TT (l = 2..2000) and of P_lin (200 k) with respect to
   (h, omega_b, omega_c, n_s, A_s, Sigma m_nu) from a served gradient request
-  against the oracle's central differences (fixtures; relative steps 1e-3
-  and 1e-4 agree with each other): every element whose magnitude exceeds
-  1e-3 of its parameter's peak within 1e-3 relative.
+  (tangent-linear solver, and frozen-step replays) against the oracle's
+  central differences (relative steps 1e-3 and 1e-4 agree with each other)
+  and against the dual-number oracle (the reference's ForwardDiff gradient
+  restated): every element whose magnitude exceeds 1e-3 of its parameter's
+  peak within 1e-3 relative.
 The fixtures come from tests/golden/make_oracle_fixtures.py.
 """
 import os
@@ -138,25 +140,32 @@ def _per_element(J, Jref, name):
     return worst
 
 
-def test_cltt_jacobian_per_element_vs_oracle_fd():
+@pytest.mark.parametrize("scheme", ["tangent", "replay"])
+def test_cltt_jacobian_per_element_vs_oracle(scheme):
     f = _fixture("oracle_jac_cltt")
+    g = _fixture("oracle_jac_cltt_dual")
     par = B.params_of(B.CosmoParams(), f["theta"])
     ks, ells = f["ks"], f["ells"]
     _per_element(f["J_0.0001"], f["J_0.001"], "oracle steps 1e-4 vs 1e-3")
-    with B.Engine(lanes=1) as eng:
-        r = eng.run(B.Request("cl", par, ks, hier=tuple(int(v) for v in f["hier"]), ells=ells, cl=("tt",), grad=True, **SERVED))
+    with B.Engine(lanes=1, grad_scheme=scheme) as eng:
+        r = eng.run(B.Request("cl", par, ks, hier=tuple(int(v) for v in f["hier"]), ells=ells, cl=("tt",), grad=True,
+                              **SERVED))
     assert r.rc == 0, r.err
     assert np.max(np.abs(r.cl["tt"] / f["tt"] - 1)) < 1e-4
-    _per_element(r.dcl["tt"], f["J_0.0001"], "C_l^TT")
+    _per_element(r.dcl["tt"], f["J_0.0001"], "C_l^TT vs central differences")
+    _per_element(r.dcl["tt"], g["J"], "C_l^TT vs the dual-number oracle")
 
 
-def test_plin_jacobian_per_element_vs_oracle_fd():
+@pytest.mark.parametrize("scheme", ["tangent", "replay"])
+def test_plin_jacobian_per_element_vs_oracle(scheme):
     f = _fixture("oracle_jac_plin")
+    g = _fixture("oracle_jac_plin_dual")
     par = B.params_of(B.CosmoParams(), f["theta"])
     ks = f["ks"]
     _per_element(f["J_0.0001"], f["J_0.001"], "oracle steps 1e-4 vs 1e-3")
-    with B.Engine(lanes=1) as eng:
+    with B.Engine(lanes=1, grad_scheme=scheme) as eng:
         r = eng.run(B.Request("plin", par, ks, hier=tuple(int(v) for v in f["hier"]), grad=True, **SERVED))
     assert r.rc == 0, r.err
     assert np.max(np.abs(r.plin / f["plin"] - 1)) < 1e-4
-    _per_element(r.dplin, f["J_0.0001"], "P_lin")
+    _per_element(r.dplin, f["J_0.0001"], "P_lin vs central differences")
+    _per_element(r.dplin, g["J"], "P_lin vs the dual-number oracle")
