@@ -59,6 +59,7 @@ import subprocess
 import sys
 import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "bolt.jl_gb300"))
@@ -486,26 +487,54 @@ def run_serving(args):
         gres = [eng.wait(t) for t in [eng.submit(to_request(B, d)) for d in gstream]]
     for r in gres:
         assert r.rc == 0, r.err
-    with B.Engine(device=local, lanes=6, objective="throughput", grad_scheme="replay") as eng:
+    with B.Engine(device=local, lanes=6, objective="throughput", grad_scheme="tangent") as eng:
         eng.run(to_request(B, gwarm))
-        gres_rep = [eng.wait(t) for t in [eng.submit(to_request(B, d)) for d in gstream]]
-    for r in gres_rep:
+        gres_tan = [eng.wait(t) for t in [eng.submit(to_request(B, d)) for d in gstream]]
+    for r in gres_tan:
         assert r.rc == 0, r.err
-    g_win_rep = max(r.times[3] for r in gres_rep) - min(r.times[2] for r in gres_rep)
+    g_win_tan = max(r.times[3] for r in gres_tan) - min(r.times[2] for r in gres_tan)
     g_win = max(r.times[3] for r in gres) - min(r.times[2] for r in gres)
     g_lat = np.array([r.latency for r in gres])
     cl_grad = {"served": len(gstream) / g_win, "plain": len(gstream) / sum(g_dropin),
                "served_over_plain": sum(g_dropin) / g_win,
                "plain_engine": len(gstream) / sum(g_plain), "served_over_plain_engine": sum(g_plain) / g_win,
-               "served_replay": len(gstream) / g_win_rep,
+               "served_tangent": len(gstream) / g_win_tan,
                "unit": UNIT, "requests": len(gstream),
                "p50_s": float(np.percentile(g_lat, 50)), "p99_s": float(np.percentile(g_lat, 99)),
                "workload": "C_l^TT l<=2000 + 6-parameter Jacobian, draws from the serving box, 64-1024 log k in "
                            "[0.1,1000] H0, "
                            "l_gamma=l_nu in {20,35,50}; served: all submitted at once; plain: drop-in, 7 calls "
                            "per request (forward differences); plain_engine: the engine one request per call; "
-                           "served and plain_engine use the tangent-linear solver (one solve per mode carries the "
-                           "four solved derivatives), served_replay the frozen-step replays (five solves per mode)"}
+                           "served and plain_engine take the derivatives from frozen-step replays (five solves per "
+                           "mode), served_tangent from the tangent-linear solver (one solve per mode carries the "
+                           "four solved derivatives)"}
+    # ---- pullbacks (bolt_cl_vjp) of the same requests with random cotangents:
+    # the replays' Jacobian contracted, against the discrete adjoint
+    rng = np.random.default_rng(SEED + 77 + rank)
+    ybars = [rng.standard_normal(d["lmax"] - 1) for d in gstream]
+    pull, pgrads = {}, {}
+    for scheme in ("replay", "adjoint"):
+        with B.Engine(device=local, lanes=6, objective="throughput", grad_scheme=scheme) as eng:
+            eng.vjp(to_request(B, gwarm), {"tt": np.ones(gwarm["lmax"] - 1)})
+            t0 = time.perf_counter()
+            r0, _ = eng.vjp(to_request(B, gstream[0]), {"tt": ybars[0]})
+            alone = time.perf_counter() - t0
+            assert r0.rc == 0, r0.err
+            with ThreadPoolExecutor(len(gstream)) as ex:
+                t0 = time.perf_counter()
+                outs = list(ex.map(lambda a: eng.vjp(to_request(B, a[0]), {"tt": a[1]}), zip(gstream, ybars)))
+                win = time.perf_counter() - t0
+        for r, _ in outs:
+            assert r.rc == 0, r.err
+        pgrads[scheme] = np.array([g for _, g in outs])
+        pull[scheme] = {"alone_s": alone, "served": len(gstream) / win}
+    gr, ga = pgrads["replay"], pgrads["adjoint"]
+    pullback = {**pull, "unit": "pullbacks/s (served), s per call (alone)", "requests": len(gstream),
+                "adjoint_vs_replay_max_rel": float(np.max(np.abs(ga - gr)) / np.max(np.abs(gr))),
+                "workload": "bolt_cl_vjp of the C_l^TT + Jacobian requests above (random cotangents over l): "
+                            "replay = the frozen-step replays' Jacobian contracted in the library; adjoint = one "
+                            "checkpointed forward solve, the adjoint of the line of sight and one reverse sweep per "
+                            "mode; alone: one call; served: all calls concurrently from host threads"}
     # ---- the arrival-rate sweep of the serving configuration (same stream)
     sweep = [serve_at_rate(B, local, stream, rate, SEED + 31 + rank) for rate in SWEEP_RATES] if args.sweep else []
     lat = np.array([r.latency for r in res])
@@ -569,6 +598,7 @@ def run_serving(args):
                          "api": "bolt_cosmo_build + bolt_plin / bolt_cl_pipeline + bolt_cosmo_free per cosmology"},
                "served_over_plain": value / plain,
                "cl_grad": cl_grad,
+               "pullback": pullback,
                "latency": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                            "arrival_rate_per_s": args.rate,
                            "host_tables_p50_s": float(np.percentile(tab, 50)),

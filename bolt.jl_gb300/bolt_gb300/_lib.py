@@ -84,6 +84,8 @@ EXPORTS = {
     "bolt_plin": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.POINTER(BoltHier), C.c_double, C.c_double,
                             C.c_double, _dp, _i32p]),
     "bolt_last_stats": (C.c_int, [C.c_void_p, _i64p]),
+    "bolt_adjoint_check": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(BoltHier), C.c_double, C.c_double,
+                                     _dp]),
     "bolt_fp64_peak": (C.c_int, [C.c_int, _dp]),
     "bolt_set_dense_x": (C.c_int, [C.c_void_p, C.c_double]),
     "bolt_source_grid_static": (C.c_int, [C.POINTER(BoltParams), C.POINTER(BoltGrid), C.c_int, _dp, _dp, _dp,

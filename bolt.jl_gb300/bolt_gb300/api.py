@@ -484,6 +484,19 @@ def cl_all(ells, ih, k_grid, lg=8, lnu=8, lmnu=10, nq=None, reltol=1e-11, abstol
     return tt, te, ee, st
 
 
+def adjoint_check(ih: IonizationHistory, k: float, x: float, hstep: float, lg=8, lnu=8, lmnu=10, nq=15) -> np.ndarray:
+    """Residuals of the discrete adjoint's building blocks at one Rosenbrock
+    step (bolt_adjoint_check): [0..4] A^T at the stage abscissae, [5] dA/dx
+    transposed, [6] the transposed solve, [7] the forward solve, [8] the
+    source gradient, [9] the P_lin gradient, [10] the streaming switch,
+    [11] the two solves as each other's transposes."""
+    out = np.zeros(12)
+    c = ih.ctx
+    c.check(c.lib.bolt_adjoint_check(c.h, ih.cosmo_id, float(k), C.byref(_hier(lg, lnu, lmnu, nq)), float(x),
+                                     float(hstep), L.dptr(out)), "bolt_adjoint_check")
+    return out
+
+
 def plin(k, par, bg, ih, n_q=15, lg=50, lnu=50, lmnu=20, x=0.0, reltol=1e-5, abstol=1e-6):
     """plin(k, par, bg, ih, n_q=15, ℓᵧ=50, ℓ_ν=50, ℓ_mν=20, x=0, reltol=1e-5)
     (spectra.jl:163-198); vectorised over k."""

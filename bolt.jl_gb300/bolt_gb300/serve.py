@@ -21,6 +21,9 @@ from . import _lib as L
 from .api import CosmoParams, mass_natural
 
 THETA_NAMES = ("h", "omega_b", "omega_c", "n_s", "A_s", "Sigma_m_nu_eV")
+# Engine grad_scheme values (bolt_engine_cfg.grad_scheme): frozen-step
+# replays, the tangent-linear solver, the discrete adjoint for pullbacks.
+GRAD_SCHEMES = ("replay", "tangent", "adjoint")
 _CL_BITS = {"tt": 1, "te": 2, "ee": 4}
 
 
@@ -133,15 +136,15 @@ class Engine:
     def __init__(self, device: int = 0, lanes: int = 6, host_threads: int = 0, max_batch: int = 0,
                  mem_budget_gb: float = 150.0, warps_per_mode: int = 0, max_steps: int = 0,
                  batch_window_s: float = 0.0, objective: str = "latency", land_stride: int = 1,
-                 grad_scheme: str = "tangent"):
+                 grad_scheme: str = "replay"):
         if objective not in ("latency", "throughput"):
             raise ValueError("objective is 'latency' or 'throughput'")
-        if grad_scheme not in ("tangent", "replay"):
-            raise ValueError("grad_scheme is 'tangent' or 'replay'")
+        if grad_scheme not in GRAD_SCHEMES:
+            raise ValueError("grad_scheme is one of " + ", ".join(GRAD_SCHEMES))
         self.lib = L.load()
         cfg = L.BoltEngineCfg(device, lanes, host_threads, max_batch, mem_budget_gb, warps_per_mode, max_steps,
                               batch_window_s, 1 if objective == "throughput" else 0, land_stride,
-                              0 if grad_scheme == "tangent" else 1)
+                              GRAD_SCHEMES.index(grad_scheme))
         h = C.c_void_p()
         rc = self.lib.bolt_engine_create(C.byref(cfg), C.byref(h))
         if rc != 0:

@@ -56,14 +56,37 @@ struct ModeDev {
   double* tsrc_T[4];  // [nout]
   double* tsrc_E[4];  // [nout]
   double* tplin[4];   // [1]
+  // MODE_CKPT (with MODE_RECORD): the state at the start of every
+  // kCkptEvery-th accepted step, [rec_cap / kCkptEvery + 1][N].
+  // MODE_ADJOINT: the reverse sweep of such a forward mode (same ckpt / rec,
+  // tcos / tinv as a tangent mode): its accepted steps (nfwd, the forward
+  // mode's counters), the cotangents of its outputs (sbar: of S_T at the
+  // nodes [nout], or of P_lin [1]) and where the cotangent's partial
+  // derivatives along the four tangent directions go (tbar [4]).
+  double* ckpt;
+  const int64_t* nfwd;
+  const double* sbar;
+  double* tbar;
 };
+constexpr int kCkptEvery = 32;
 
 // MODE_RECORD stores the end abscissa of every accepted step; MODE_REPLAY
 // takes exactly those steps (no error control), so a mode of perturbed
 // parameters is integrated on the same discretisation as the recorded one.
 // MODE_TANGENT integrates, with the state, its derivatives with respect to
-// four parameters (the tangent-linear solver, tangent.cuh).
-enum ModeFlags { MODE_SOURCES = 1, MODE_TRAJ = 2, MODE_PLIN = 4, MODE_RECORD = 8, MODE_REPLAY = 16, MODE_TANGENT = 32 };
+// four parameters (the tangent-linear solver, tangent.cuh).  MODE_CKPT
+// keeps checkpoints of a recorded forward solve; MODE_ADJOINT runs its
+// discrete adjoint backwards (adjoint.cuh).
+enum ModeFlags {
+  MODE_SOURCES = 1,
+  MODE_TRAJ = 2,
+  MODE_PLIN = 4,
+  MODE_RECORD = 8,
+  MODE_REPLAY = 16,
+  MODE_TANGENT = 32,
+  MODE_CKPT = 64,
+  MODE_ADJOINT = 128
+};
 
 enum StatusBits {
   ST_OK = 0,
@@ -73,7 +96,7 @@ enum StatusBits {
   ST_LU_FAIL = 4,
   ST_BAD_INPUT = 5,
   ST_REPLAY_SHORT = 6,   // MODE_REPLAY ran past the recorded steps
-  ST_TANGENT_RSA = 7,    // MODE_TANGENT: the radiation-streaming overwrite fired (it has no tangent here)
+  ST_TANGENT_RSA = 7,    // MODE_TANGENT / MODE_ADJOINT: the radiation-streaming overwrite fired (no derivative here)
   ST_RSA_FIRED = 256,    // informational, OR-ed into the code
   ST_REC_OVERFLOW = 512  // MODE_RECORD: more accepted steps than rec_cap (record unusable)
 };
@@ -337,6 +360,30 @@ struct LosGradArgs {
   double* tt;           // [nslots]
   double* dtt;          // [6][nslots]
   unsigned long long* terms;  // (l, k, x) terms evaluated, accumulated (null: not counted)
+  // the line of sight's adjoint (dSd null: the derivatives at fixed
+  // sources): 2 w_m Delta_l(k_m) per slot [nslots][nm], and the slot's
+  // zero-skip bound on the Bessel argument [nslots] (null: not written)
+  double* cbar;
+  double* ulo;
+};
+
+// The adjoint of the C_l^TT projection for one cotangent ybar[nslots]:
+// Sbar_d[i][m] = 4 pi sum_l ybar_l cbar[l][m] j_l(k_m y_i) over the terms
+// the forward reduction evaluated, then back through the resampling to the
+// sources' cotangent Sbar[nk][nx] at the nodes i0 .. i0 + nrow - 1.
+struct LosAdjArgs {
+  int nb, nslots, nrow, nm, nk, nx, i0;
+  const double* coef;   // [nslots][nb+2]
+  const double* inv_dg; // [1]
+  const double* yv;     // [nrow]
+  const double* kmid;   // [nm]
+  const double* kgrid;  // [nk]
+  const double* dxs;    // [nrow]
+  const double* ybar;   // [nslots]
+  const double* cbar;   // [nslots][nm]
+  const double* ulo;    // [nslots]
+  double* Sbd;          // [nrow][nm] (zeroed by the launcher)
+  double* Sbar;         // [nk][nx] (zeroed by the launcher)
 };
 
 }  // namespace bolt

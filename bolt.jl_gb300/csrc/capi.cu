@@ -34,6 +34,9 @@ int launch_jl_prefilter(int nb, int nslots, int ncz, const double* d_raw, const 
 int launch_sdense(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_ST, const double* d_SE, int nm,
                   const double* d_kmid, const double* d_dx, double* d_SdT, double* d_SdE, cudaStream_t st);
 int launch_los_cl(const LosArgs& a, int ncz, cudaStream_t st);
+int launch_adjoint_check(const CosmoDev* d_cos, int id, double k, int lg, int lnu, int lmnu, int nq, double x,
+                         double hs, double* d_scr, double* d_out, cudaStream_t st);
+size_t adjoint_check_scratch_bytes(int N);
 }  // namespace bolt
 
 using namespace bolt;
@@ -735,6 +738,28 @@ int bolt_set_dense_x(bolt_ctx* c, double x) {
   if (!c) return -1;
   c->x_dense = x;
   return 0;
+}
+
+int bolt_adjoint_check(bolt_ctx* c, int id, double k, const bolt_hier* h, double x, double hstep, double* out) {
+  return guard(c, [&] {
+    if (!out || !(k > 0.0) || !(hstep > 0.0)) throw Err(-1, "null argument, k <= 0 or hstep <= 0");
+    CosmoEntry& e = get_cosmo(c, id);
+    check_hier(h);
+    const GridSpec& g = e.T.grid;
+    if (!(x >= g.at(0)) || !(x + hstep <= g.at(g.n - 1))) throw Err(-1, "step outside the x grid");
+    const int N = state_len(h);
+    double* d_scr = c->scratch.as<double>(adjoint_check_scratch_bytes(N) / sizeof(double));
+    double* d_out = c->out.as<double>(16);
+    ck(cudaMemsetAsync(d_out, 0, 16 * sizeof(double), c->stream), "out");
+    int rc = launch_adjoint_check(c->d_cos.as<CosmoDev>(c->cos.size()), id, k, h->lg, h->lnu, h->lmnu, h->nq, x,
+                                  hstep, d_scr, d_out, c->stream);
+    if (rc != 0) throw Err(-3, std::string("adjoint check: ") + cudaGetErrorString(cudaError_t(rc)));
+    double o[16];
+    ck(cudaMemcpyAsync(o, d_out, 16 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "out");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    if (o[15] < 0.0) throw Err(-1, "hierarchy does not fit the solver's lane packing");
+    std::copy(o, o + 12, out);
+  });
 }
 
 int bolt_last_stats(bolt_ctx* c, int64_t* out) {

@@ -57,11 +57,11 @@
 
 namespace bolt {
 int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, int* blocks);
-int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, bool tan, int* blocks);
-int rodas_node_params(int wpm, bool tan, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos,
+int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, int kind, int* blocks);
+int rodas_node_params(int wpm, int kind, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos,
                       const SolverCfg& cfg, int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch,
                       RodasNodeArgs* args, cudaKernelNodeParams* p);
-size_t rodas_scratch_per_warp(int maxN, bool tan);
+size_t rodas_scratch_per_warp(int maxN, int kind);
 int rodas_node_params(int wpm, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg,
                       int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch, RodasNodeArgs* args,
                       cudaKernelNodeParams* p);
@@ -77,6 +77,7 @@ int launch_los_cl(const LosArgs& a, int ncz, cudaStream_t st);
 int launch_sdense_diff(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_Sa, const double* d_Sb,
                        double scale, int nm, const double* d_kmid, const double* d_dx, double* d_out, cudaStream_t st);
 int launch_los_tt_grad(const LosGradArgs& a, cudaStream_t st);
+int launch_los_adjoint(const LosAdjArgs& a, cudaStream_t st);
 void fill_cosmo_dev(const CosmoTables& T, double* d_tab, double* h_tab, CosmoDev& d);
 size_t cosmo_table_doubles(const CosmoTables& T);
 }  // namespace bolt
@@ -209,6 +210,13 @@ struct Req {
   int src_from = 0;          // C_l: first x node with sources, findfirst(x_grid .> -8) (spectra.jl:86)
   bool los_tangent = false;  // C_l^TT gradient from the tangent of the LOS integral
   bool tangent = false;      // gradient from tangent-linear modes (sets 1..6 hold derivatives, not perturbed results)
+  // a pullback by the discrete adjoint (bolt_cl_vjp of C_l^TT, bolt_plin_vjp):
+  // the cotangent (C_l: per unique multipole; P_lin: per k) and where the
+  // parameter cotangent goes
+  bool adjoint = false;
+  std::vector<double> ybar;
+  double* vjp_grad = nullptr;
+  size_t o_ckpt = 0, o_sbar = 0, o_tbar = 0, o_ybar = 0, h_tbar = 0;
 };
 
 // The four parameters whose derivatives need a solve (theta indices), in the
@@ -217,7 +225,12 @@ constexpr int kSolvedTheta[kTD] = {0, 1, 2, 5};
 // Whether parameter set s of request r has modes of its own: the perturbed
 // sets of n_s and A_s never do, and those of a tangent request are filled by
 // the base modes' tangents.
-bool set_has_modes(const Req* r, int s) { return !skips_solve(r->nsets, s) && !(r->tangent && s > 0); }
+bool set_has_modes(const Req* r, int s) {
+  return !skips_solve(r->nsets, s) && !((r->tangent || r->adjoint) && s > 0);
+}
+// The kind of a gradient request's second solver phase: 0 frozen-step
+// replays, 1 tangent-linear modes, 2 adjoint modes (rodas_kernel's KIND).
+int grad_kind(const Req* r) { return r->adjoint ? 2 : (r->tangent ? 1 : 0); }
 
 struct Graph {
   cudaGraph_t g = nullptr;
@@ -229,15 +242,15 @@ struct Lane {
   cudaStream_t st = nullptr;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // start, phase 1, phase 2, LOS, done
   int* d_queue = nullptr;  // [2] work-queue counters of the two solver phases
-  Graph graph[4][2];       // [kernel variant: warps per mode 1, 2, 4; tangent][phase]
-  GrowDev scr, los_raw, los_norm, los_coef, los_SdT, los_SdE, los_dSd;
+  Graph graph[5][2];       // [kernel variant: warps per mode 1, 2, 4; tangent; adjoint][phase]
+  GrowDev scr, los_raw, los_norm, los_coef, los_SdT, los_SdE, los_dSd, los_cbar, los_ulo;
   GrowHost up, down;
   bool busy = false;
   std::vector<Req*> batch;
   void* d_block = nullptr;
   size_t block_bytes = 0;
   int wpm[2] = {4, 4};
-  bool tan[2] = {false, false};  // phase runs the tangent-linear kernel
+  int kind[2] = {0, 0};  // rodas_kernel KIND of each phase (0 plain, 1 tangent, 2 adjoint)
   int nmodes[2] = {0, 0};
   int waiting = 0;       // modes of the requests still waiting when the batch was taken
   int key[2] = {0, 0};   // tuner key of each phase (own modes, or the whole load when shared)
@@ -273,7 +286,17 @@ struct bolt_engine {
 namespace {
 
 // --------------------------------------------------------------- validation
-void check_request(const bolt_request* q) {
+// Whether a hierarchy's chains pack into one warp, as build_pack does for
+// 32 threads (at most 24 elements per lane, one lane kept spare): the
+// tangent-linear and adjoint kernels run one warp per mode.
+bool fits_one_warp(const bolt_hier& h) {
+  for (int E = 2; E <= 24; ++E)
+    if (2 * ((h.lg + E) / E) + (h.lnu + E) / E + h.nq * ((h.lmnu + E) / E) <= 31) return true;
+  return false;
+}
+
+// need_jac = false: a pullback, whose Jacobian stays inside the library.
+void check_request(const bolt_request* q, bool need_jac = true) {
   if (!q) throw EngErr(-1, "request is null");
   if (q->kind != BOLT_REQ_PLIN && q->kind != BOLT_REQ_CL) throw EngErr(-1, "request kind must be PLIN or CL");
   const bolt_hier& h = q->hier;
@@ -295,7 +318,7 @@ void check_request(const bolt_request* q) {
   if (!(q->grid.step > 0) || !(q->grid.stop > q->grid.start)) throw EngErr(-1, "invalid x grid");
   if (q->kind == BOLT_REQ_PLIN) {
     if (!q->plin) throw EngErr(-1, "plin output is null");
-    if (q->grad && !q->dplin) throw EngErr(-1, "dplin output is null");
+    if (q->grad && need_jac && !q->dplin) throw EngErr(-1, "dplin output is null");
     if (!(q->plin_x > q->grid.start) || !(q->plin_x <= q->grid.stop)) throw EngErr(-1, "plin_x outside the x grid");
   } else {
     if (q->nk < 2) throw EngErr(-1, "C_l needs at least two source-grid wavenumbers");
@@ -304,10 +327,11 @@ void check_request(const bolt_request* q) {
       if (q->ells[i] < 2 || q->ells[i] > 20000) throw EngErr(-1, "multipoles must be in 2..20000");
     const int w = q->cl_want;
     if (w <= 0 || w > 7) throw EngErr(-1, "cl_want must name TT, TE and/or EE");
-    if (q->plin && q->grad && !q->dplin) throw EngErr(-1, "dplin output is null");
+    if (q->plin && q->grad && need_jac && !q->dplin) throw EngErr(-1, "dplin output is null");
     if (((w & BOLT_CL_TT) && !q->tt) || ((w & BOLT_CL_TE) && !q->te) || ((w & BOLT_CL_EE) && !q->ee))
       throw EngErr(-1, "C_l output is null");
-    if (q->grad && (((w & BOLT_CL_TT) && !q->dtt) || ((w & BOLT_CL_TE) && !q->dte) || ((w & BOLT_CL_EE) && !q->dee)))
+    if (q->grad && need_jac &&
+        (((w & BOLT_CL_TT) && !q->dtt) || ((w & BOLT_CL_TE) && !q->dte) || ((w & BOLT_CL_EE) && !q->dee)))
       throw EngErr(-1, "C_l gradient output is null");
   }
 }
@@ -340,6 +364,16 @@ void layout_request(Req* r, size_t& off) {
   off = align_up(off + size_t(ns) * nk * 16);
   r->o_rec = off;
   if (r->nsets > 1 && !r->tangent) off = align_up(off + size_t(nk) * r->rec_cap * 8);
+  if (r->adjoint) {  // checkpoints, output cotangents, per-mode parameter cotangents, C_l cotangent
+    r->o_ckpt = off;
+    off = align_up(off + size_t(nk) * (r->rec_cap / kCkptEvery + 1) * r->N * 8);
+    r->o_sbar = off;
+    off = align_up(off + size_t(nk) * (r->r.kind == BOLT_REQ_CL ? r->grid.n - r->src_from : 1) * 8);
+    r->o_tbar = off;
+    off = align_up(off + size_t(nk) * kTD * 8);
+    r->o_ybar = off;
+    off = align_up(off + std::max<size_t>(r->ybar.size(), 1) * 8);
+  }
   if (r->r.kind == BOLT_REQ_CL) {
     r->o_src = off;
     off = align_up(off + size_t(ns) * nk * (n - r->src_from) * 8 * (r->wantE ? 2 : 1));
@@ -410,8 +444,8 @@ void set_done(bolt_engine* E, Req* r, int s, const std::string& err) {
   }
 }
 
-Graph& lane_graph(Lane& L, int wpm, bool tan, int phase, const cudaKernelNodeParams& kp) {
-  const int v = tan ? 3 : (wpm == 1 ? 0 : (wpm == 2 ? 1 : 2));
+Graph& lane_graph(Lane& L, int wpm, int kind, int phase, const cudaKernelNodeParams& kp) {
+  const int v = kind ? 2 + kind : (wpm == 1 ? 0 : (wpm == 2 ? 1 : 2));
   Graph& G = L.graph[v][phase];
   if (!G.exec) {
     ck(cudaGraphCreate(&G.g, 0), "cudaGraphCreate");
@@ -440,7 +474,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   cudaStream_t st = L.st;
   // ---- device layout of the batch block (inputs and outputs)
   size_t off = 0;
-  int ncos = 0, m1 = 0, m2 = 0, mt = 0, maxN = 0, maxnq = 1, maxL = 3;
+  int ncos = 0, m1 = 0, m2 = 0, mt = 0, ma = 0, maxN = 0, maxnq = 1, maxL = 3;
   size_t max_sd = 0;
   int max_slots = 0;
   bool anyE = false, anyTangent = false;
@@ -451,6 +485,9 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     ncos += r->nsets;
     if (r->tangent) {
       mt += r->r.nk;
+    } else if (r->adjoint) {
+      m1 += r->r.nk;
+      ma += r->r.nk;
     } else {
       m1 += r->r.nk;
       for (int s = 1; s < r->nsets; ++s) m2 += skips_solve(r->nsets, s) ? 0 : r->r.nk;
@@ -469,17 +506,18 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   const size_t o_cos = off;
   off = align_up(off + size_t(ncos) * sizeof(CosmoDev));
   const size_t o_modes = off;
-  off = align_up(off + size_t(m1 + m2 + mt) * sizeof(ModeDev));
+  off = align_up(off + size_t(m1 + m2 + mt + ma) * sizeof(ModeDev));
   const size_t total = off;
   // ---- solver configurations of both phases (autotuned) and lane buffers
-  // phase 0: plain modes (and recorded ones); phase 1: their frozen-step
-  // replays, or the tangent modes (a batch never holds both, see scheduler)
+  // phase 0: plain modes (and recorded, checkpointed ones); phase 1: their
+  // frozen-step replays, the tangent modes or the adjoint modes (a batch
+  // holds one kind, see scheduler)
   int wpm[2] = {4, 4}, blocks[2] = {0, 0};
-  const bool tan1 = mt > 0;
-  const int nph = (m2 > 0 || mt > 0) ? 2 : 1;
-  const int nmodes[2] = {m1, tan1 ? mt : m2};
-  L.tan[0] = false;
-  L.tan[1] = tan1;
+  const int kind1 = mt > 0 ? 1 : (ma > 0 ? 2 : 0);
+  const int nph = (m2 > 0 || mt > 0 || ma > 0) ? 2 : 1;
+  const int nmodes[2] = {m1, mt > 0 ? mt : (ma > 0 ? ma : m2)};
+  L.kind[0] = 0;
+  L.kind[1] = kind1;
   int other = 0;  // lanes are launched and finished on this (the scheduler) thread
   for (Lane& o : E->lanes)
     if (&o != &L && o.busy) other += o.nmodes[0] + o.nmodes[1];
@@ -487,8 +525,8 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     L.shared[ph] = other > 0 || L.waiting > 0 || E->cfg.objective == 1;
     L.key[ph] = L.shared[ph] ? nmodes[ph] + other + L.waiting : nmodes[ph];
     int w = E->cfg.warps_per_mode;
-    if (L.tan[ph]) {
-      w = 1;  // the tangent-linear kernel runs one warp per mode
+    if (L.kind[ph]) {
+      w = 1;  // the tangent-linear and adjoint kernels run one warp per mode
     } else if (w != 1 && w != 2 && w != 4) {
       std::lock_guard<std::mutex> g(E->mu);
       w = E->tuner.pick(L.shared[ph], L.key[ph], E->nsm);
@@ -498,13 +536,13 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
       wpm[ph] = w;
       continue;
     }
-    int rc = rodas_grid_warps(nmodes[ph], maxN, maxnq, maxL, w, L.tan[ph], &blocks[ph]);
+    int rc = rodas_grid_warps(nmodes[ph], maxN, maxnq, maxL, w, L.kind[ph], &blocks[ph]);
     if (rc != 0) throw EngErr(-3, std::string("solver configuration: ") + cudaGetErrorString(cudaError_t(-rc)));
     wpm[ph] = w;
   }
   double* d_scr = static_cast<double*>(
-      L.scr.get(std::max(size_t(blocks[0]) * rodas_scratch_per_warp(maxN, false),
-                         size_t(blocks[1]) * rodas_scratch_per_warp(maxN, tan1))));
+      L.scr.get(std::max(size_t(blocks[0]) * rodas_scratch_per_warp(maxN, 0),
+                         size_t(blocks[1]) * rodas_scratch_per_warp(maxN, kind1))));
   double *raw = nullptr, *norm = nullptr, *coef = nullptr, *SdT = nullptr, *SdE = nullptr;
   if (max_slots > 0) {
     raw = static_cast<double*>(L.los_raw.get(size_t(max_slots) * kNb * 8));
@@ -514,6 +552,15 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     if (anyE) SdE = static_cast<double*>(L.los_SdE.get(max_sd * 8));
   }
   double* dSd = anyTangent ? static_cast<double*>(L.los_dSd.get(size_t(kTheta) * max_sd * 8)) : nullptr;
+  // adjoint C_l requests: 2 w Delta per slot and midpoint, the slots' skip
+  // bounds, and the resampled sources' cotangent (a batch of them holds no
+  // tangent-LOS request, so dSd's buffer serves)
+  double *cbar = nullptr, *ulo = nullptr, *Sbd = nullptr;
+  if (kind1 == 2 && max_slots > 0) {
+    cbar = static_cast<double*>(L.los_cbar.get(size_t(max_slots) * (kNkd - 1) * 8));
+    ulo = static_cast<double*>(L.los_ulo.get(size_t(max_slots) * 8));
+    Sbd = static_cast<double*>(L.los_dSd.get(max_sd * 8));
+  }
   // ---- host staging (pinned, compact): input segments only
   struct Seg {
     size_t dev, host, bytes;
@@ -525,7 +572,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     hoff = align_up(hoff + bytes);
     return segs.size() - 1;
   };
-  std::vector<size_t> seg_tab(batch.size()), seg_x(batch.size()), seg_los(batch.size());
+  std::vector<size_t> seg_tab(batch.size()), seg_x(batch.size()), seg_los(batch.size()), seg_yb(batch.size());
   size_t req_start = 0;
   std::vector<size_t> starts(batch.size());
   for (size_t b = 0; b < batch.size(); ++b) {
@@ -538,10 +585,12 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
       size_t head = align_up(size_t(r->r.nk + nm + n + 8) * 8 + size_t(r->uniq.back() + 1 + ns) * 4);
       seg_los[b] = seg(r->o_los, head + size_t(r->nsets) * (nm + n) * 8);
     }
+    if (r->adjoint)  // the cotangent: C_l per slot, or P_lin per k (the reverse modes' seeds)
+      seg_yb[b] = r->r.kind == BOLT_REQ_CL ? seg(r->o_ybar, r->ybar.size() * 8) : seg(r->o_sbar, r->ybar.size() * 8);
     req_start += r->bytes;
   }
   const size_t seg_cos = seg(o_cos, size_t(ncos) * sizeof(CosmoDev));
-  const size_t seg_modes = seg(o_modes, size_t(m1 + m2 + mt) * sizeof(ModeDev));
+  const size_t seg_modes = seg(o_modes, size_t(m1 + m2 + mt + ma) * sizeof(ModeDev));
   char* up = static_cast<char*>(L.up.get(std::max<size_t>(hoff, 8)));
   // downloads: status + counters + results per request
   size_t doff = 0;
@@ -559,6 +608,10 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
       r->h_plin = doff;
       doff = align_up(doff + size_t(ns) * nk * 8);
     }
+    if (r->adjoint) {
+      r->h_tbar = doff;
+      doff = align_up(doff + size_t(nk) * kTD * 8);
+    }
   }
   char* down = static_cast<char*>(L.down.get(std::max<size_t>(doff, 8)));
   ck(cudaMallocAsync(&L.d_block, total, st), "cudaMallocAsync batch");
@@ -567,7 +620,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   std::vector<CosmoDev> cos(ncos);
   std::vector<ModeDev> modes, modes2;
   modes.reserve(m1);
-  modes2.reserve(m2 + mt);
+  modes2.reserve(m2 + mt + ma);
   for (size_t b = 0; b < batch.size(); ++b) {
     Req* r = batch[b];
     const int nk = r->r.nk, ns = r->nsets, nsrc = r->grid.n - r->src_from;
@@ -590,6 +643,8 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
     int32_t* dstat = reinterpret_cast<int32_t*>(dev + r->o_stat);
     int64_t* dcnt = reinterpret_cast<int64_t*>(dev + r->o_cnt);
     double* drec = reinterpret_cast<double*>(dev + r->o_rec);
+    if (r->adjoint)
+      std::memcpy(up + segs[seg_yb[b]].host, r->ybar.data(), r->ybar.size() * 8);
     for (int s = 0; s < ns; ++s)
       for (int i = 0; i < nk && set_has_modes(r, s); ++i) {
         ModeDev m;
@@ -631,6 +686,26 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
           m.flags |= s == 0 ? MODE_RECORD : MODE_REPLAY;
           m.rec = drec + size_t(i) * r->rec_cap;
           m.rec_cap = r->rec_cap;
+        }
+        if (r->adjoint) {  // checkpointed forward mode, and its reverse sweep in phase 1
+          m.flags |= MODE_CKPT;
+          m.ckpt = reinterpret_cast<double*>(dev + r->o_ckpt) + size_t(i) * (r->rec_cap / kCkptEvery + 1) * r->N;
+          modes.push_back(m);
+          ModeDev a = m;
+          a.flags = MODE_ADJOINT | (r->r.kind == BOLT_REQ_CL ? MODE_SOURCES : MODE_PLIN);
+          a.src_T = a.src_E = nullptr;
+          a.plin = nullptr;
+          a.nfwd = dcnt + 2 * size_t(i);
+          a.sbar = reinterpret_cast<const double*>(dev + r->o_sbar) + (r->r.kind == BOLT_REQ_CL ? size_t(i) * nsrc : i);
+          a.tbar = reinterpret_cast<double*>(dev + r->o_tbar) + size_t(i) * kTD;
+          for (int d = 0; d < kTD; ++d) {
+            a.tcos[d] = r->cos0 + 1 + kSolvedTheta[d];
+            a.tinv[d] = 1.0 / r->step[kSolvedTheta[d]];
+          }
+          a.status = dstat + size_t(nk) + i;  // the slots of parameter set 1
+          a.counters = dcnt + 2 * (size_t(nk) + i);
+          modes2.push_back(a);
+          continue;
         }
         if (s == 0) modes.push_back(m);
         else modes2.push_back(m);
@@ -701,7 +776,7 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
       for (int m = 0; m < nm; ++m) wts[m] = T.par.A * std::pow(kmid[m] / 0.05, T.par.n - 1.0) * dk[m] / kmid[m];
       for (int i = 0; i < nrow; ++i) yv[i] = T.eta0 - spline_eval(T.coef[T_ETA].data(), n, g.x0, g.h, g.at(i0 + i));
     }
-    if (r->los_tangent)  // sets 1..6 -> derivatives of the weights and of y along theta_j
+    if (r->los_tangent || r->adjoint)  // sets 1..6 -> derivatives of the weights and of y along theta_j
       for (int j = 0; j < kTheta; ++j) {
         double* d = per + size_t(1 + j) * (nm + n);
         if (solve_free(j)) {  // exact: dw/dn = w ln(k/0.05), dw/dA = w/A; y does not depend on them
@@ -729,26 +804,72 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
   cfg.x_dense = -8.5;
   cfg.max_steps = E->cfg.max_steps > 0 ? E->cfg.max_steps : 100000;
   cfg.land_stride = E->cfg.land_stride > 1 ? E->cfg.land_stride : 1;
-  for (int ph = 0; ph < nph; ++ph) {
+  auto run_phase = [&](int ph) {
     L.wpm[ph] = wpm[ph];
     L.nmodes[ph] = nmodes[ph];
     if (nmodes[ph] > 0) {
       RodasNodeArgs args;
       cudaKernelNodeParams kp;
-      rodas_node_params(wpm[ph], L.tan[ph], d_modes + (ph ? m1 : 0), nmodes[ph], d_cos, cfg, L.d_queue + ph, maxN,
+      rodas_node_params(wpm[ph], L.kind[ph], d_modes + (ph ? m1 : 0), nmodes[ph], d_cos, cfg, L.d_queue + ph, maxN,
                         maxnq, maxL, blocks[ph], d_scr, &args, &kp);
-      Graph& G = lane_graph(L, wpm[ph], L.tan[ph], ph, kp);
+      Graph& G = lane_graph(L, wpm[ph], L.kind[ph], ph, kp);
       ck(cudaGraphLaunch(G.exec, st), "cudaGraphLaunch");
       ++launches;
     }
     ck(cudaEventRecord(L.ev[1 + ph], st), "event");
+  };
+  run_phase(0);
+  // adjoint C_l^TT requests: the projection and its adjoint between the
+  // phases -- the reverse modes start from the sources' cotangent
+  for (auto& P : plans) {
+    Req* r = P.r;
+    if (!r->adjoint) continue;
+    const int n = r->grid.n, nk = r->r.nk, nsrc = n - r->src_from, i0s = P.i0 - r->src_from;
+    char* lb = dev + r->o_los;
+    const double* kg = reinterpret_cast<const double*>(lb);
+    const double* kmid = kg + nk;
+    const double* dxs = kmid + P.nm;
+    const double* misc = dxs + n;
+    const int* slot = reinterpret_cast<const int*>(misc + 8);
+    const int* ells = slot + (P.Lmax + 1);
+    const double* per = reinterpret_cast<const double*>(lb + P.head);
+    int rc = launch_jl_raw(kNb, misc, 1, P.Lmax, slot, P.ns, raw, norm, E->d_flags, st);
+    if (rc == 0) rc = launch_jl_prefilter(kNb, P.ns, 1, raw, norm, E->d_w, coef, st);
+    const double* src = reinterpret_cast<const double*>(dev + r->o_src);
+    double* cl = reinterpret_cast<double*>(dev + r->o_cl);
+    if (rc == 0) rc = launch_sdense(nsrc, i0s, P.nrow, nk, kg, src, nullptr, P.nm, kmid, dxs, SdT, nullptr, st);
+    if (rc == 0) {
+      LosGradArgs a;
+      a.nb = kNb; a.nslots = P.ns; a.nrow = P.nrow; a.nm = P.nm;
+      a.ells = ells; a.coef = coef; a.inv_dg = misc + 1;
+      a.wts = per; a.yv = per + P.nm; a.dwts = per + (P.nm + n); a.dyv = per + (P.nm + n) + P.nm; a.dstride = P.nm + n;
+      a.kmid = kmid; a.Sd = SdT; a.dSd = nullptr; a.tt = cl; a.dtt = cl + P.ns;
+      a.terms = nullptr;
+      a.cbar = cbar;
+      a.ulo = ulo;
+      rc = launch_los_tt_grad(a, st);
+    }
+    if (rc == 0) {
+      LosAdjArgs b;
+      b.nb = kNb; b.nslots = P.ns; b.nrow = P.nrow; b.nm = P.nm; b.nk = nk; b.nx = nsrc; b.i0 = i0s;
+      b.coef = coef; b.inv_dg = misc + 1; b.yv = per + P.nm; b.kmid = kmid; b.kgrid = kg; b.dxs = dxs;
+      b.ybar = reinterpret_cast<const double*>(dev + r->o_ybar);
+      b.cbar = cbar; b.ulo = ulo; b.Sbd = Sbd;
+      b.Sbar = reinterpret_cast<double*>(dev + r->o_sbar);
+      rc = launch_los_adjoint(b, st);
+    }
+    if (rc != 0) throw EngErr(-3, std::string("line of sight (adjoint): ") + cudaGetErrorString(cudaError_t(rc)));
+    launches += 6;
   }
-  if (nph == 1) {
+  if (nph == 2) {
+    run_phase(1);
+  } else {
     L.nmodes[1] = 0;
     ck(cudaEventRecord(L.ev[2], st), "event");
   }
   for (auto& P : plans) {
     Req* r = P.r;
+    if (r->adjoint) continue;
     const int n = r->grid.n, nk = r->r.nk, nsrc = n - r->src_from, i0s = P.i0 - r->src_from;
     char* lb = dev + r->o_los;
     const double* kg = reinterpret_cast<const double*>(lb);
@@ -785,6 +906,8 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
       a.wts = per; a.yv = per + P.nm; a.dwts = per + (P.nm + n); a.dyv = per + (P.nm + n) + P.nm; a.dstride = P.nm + n;
       a.kmid = kmid; a.Sd = SdT; a.dSd = dSd; a.tt = cl; a.dtt = cl + P.ns;
       a.terms = nullptr;
+      a.cbar = nullptr;
+      a.ulo = nullptr;
       rc = launch_los_tt_grad(a, st);
       if (rc != 0) throw EngErr(-3, std::string("line of sight (tangent): ") + cudaGetErrorString(cudaError_t(rc)));
       launches += 2 + kTheta;
@@ -819,6 +942,9 @@ void launch_batch(bolt_engine* E, Lane& L, std::vector<Req*>& batch) {
                          st), "C_l");
     if (r->wantP)
       ck(cudaMemcpyAsync(down + r->h_plin, dev + r->o_plin, size_t(ns) * nk * 8, cudaMemcpyDeviceToHost, st), "P_lin");
+    if (r->adjoint)
+      ck(cudaMemcpyAsync(down + r->h_tbar, dev + r->o_tbar, size_t(nk) * kTD * 8, cudaMemcpyDeviceToHost, st),
+         "parameter cotangents");
   }
   ck(cudaFreeAsync(L.d_block, st), "cudaFreeAsync batch");
   L.d_block = nullptr;
@@ -847,6 +973,42 @@ void finalize_request(Lane& L, Req* r) {
         break;
       }
     }
+  if (r->adjoint) {
+    for (int i = 0; i < nk && r->rc == 0; ++i) {  // the reverse sweeps
+      int v = st[size_t(nk) + i];
+      if ((v & 0xFF) != 0) {
+        r->rc = -4;
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "adjoint of mode k=%.6g ended with status %d", r->k[i], v);
+        r->err = buf;
+      }
+    }
+    if (r->rc != 0) return;
+    const double* tb = reinterpret_cast<const double*>(down + r->h_tbar);
+    double g[kTheta] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < nk; ++i)
+      for (int d = 0; d < kTD; ++d) g[kSolvedTheta[d]] += tb[size_t(i) * kTD + d];
+    if (r->r.kind == BOLT_REQ_CL) {  // [0, nsl): C_l^TT, then [6][nsl] its derivatives at fixed sources
+      const double* cl = reinterpret_cast<const double*>(down + r->h_cl);
+      const int nsl = int(r->uniq.size());
+      for (int j = 0; j < kTheta; ++j)
+        for (int sl = 0; sl < nsl; ++sl) g[j] += r->ybar[sl] * cl[size_t(1 + j) * nsl + sl];
+      if (r->r.tt)
+        for (int e = 0; e < r->r.nell; ++e) {
+          int sl = int(std::lower_bound(r->uniq.begin(), r->uniq.end(), r->ells[e]) - r->uniq.begin());
+          r->r.tt[e] = cl[sl];
+        }
+    } else {  // n_s and A_s enter only A (k/0.05)^(n-1) (spectra.jl:195-197)
+      const double* P = reinterpret_cast<const double*>(down + r->h_plin);
+      for (int i = 0; i < nk; ++i) {
+        g[kThetaN] += r->ybar[i] * P[i] * std::log(r->k[i] / 0.05);
+        g[kThetaA] += r->ybar[i] * P[i] / r->T[0].par.A;
+      }
+      if (r->r.plin) std::copy(P, P + nk, r->r.plin);
+    }
+    if (r->vjp_grad) std::copy(g, g + kTheta, r->vjp_grad);
+    return;
+  }
   auto deriv = [&](const double* f, size_t stride, int j, size_t i) -> double {  // set 1 + j: theta_j + h
     if (r->tangent) return f[size_t(1 + j) * stride + i];  // the tangent itself
     return (f[size_t(1 + j) * stride + i] - f[i]) / r->step[j];
@@ -905,9 +1067,16 @@ void finish_lane(bolt_engine* E, Lane& L) {
         r->steps += double(cnt[q] + cnt[q + 1]);
       }
     for (int s = 0; s < r->nsets; ++s) modes += set_has_modes(r, s) ? r->r.nk : 0;
+    if (r->adjoint)  // the reverse sweeps (their accepted steps, in the slots of set 1)
+      for (int i = 0; i < r->r.nk; ++i) {
+        size_t q = 2 * (size_t(r->r.nk) + i);
+        steps[1] += double(cnt[q]);
+        r->steps += double(cnt[q]);
+        ++modes;
+      }
   }
   if (L.nmodes[0] > 0) E->tuner.update(L.shared[0], L.key[0], L.wpm[0], ms1 * 1e-3, steps[0]);
-  if (L.nmodes[1] > 0 && !L.tan[1]) E->tuner.update(L.shared[1], L.key[1], L.wpm[1], ms2 * 1e-3, steps[1]);
+  if (L.nmodes[1] > 0 && L.kind[1] == 0) E->tuner.update(L.shared[1], L.key[1], L.wpm[1], ms2 * 1e-3, steps[1]);
   const double t = now_s(E->t0);
   for (Req* r : L.batch) {
     finalize_request(L, r);
@@ -978,12 +1147,12 @@ void scheduler(bolt_engine* E) {
         size_t bytes = 0;
         const int maxb = E->cfg.max_batch > 0 ? E->cfg.max_batch : 1 << 30;
         const double rt = E->ready.front()->r.reltol, at = E->ready.front()->r.abstol;
-        int gkind = -1;  // gradient requests of one batch: all tangent (0) or all replays (1)
+        int gkind = -1;  // gradient requests of one batch: one kind (replays, tangent or adjoint)
         for (auto it = E->ready.begin(); it != E->ready.end() && int(batch.size()) < maxb;) {
           Req* r = *it;
           if (r->r.reltol != rt || r->r.abstol != at) { ++it; continue; }
           if (r->nsets > 1) {
-            const int kind = r->tangent ? 0 : 1;
+            const int kind = grad_kind(r);
             if (gkind >= 0 && kind != gkind) { ++it; continue; }
             gkind = kind;
           }
@@ -1081,7 +1250,7 @@ int bolt_engine_create(const bolt_engine_cfg* cfg, bolt_engine** out) {
   if (cfg) E->cfg = *cfg;
   if (E->cfg.objective != 0 && E->cfg.objective != 1) return -1;
   if (E->cfg.land_stride < 0 || E->cfg.land_stride > 64) return -1;
-  if (E->cfg.grad_scheme < 0 || E->cfg.grad_scheme > 1) return -1;
+  if (E->cfg.grad_scheme < 0 || E->cfg.grad_scheme > 2) return -1;
   E->device = E->cfg.device;
   if (E->cfg.lanes <= 0) E->cfg.lanes = 6;
   if (E->cfg.lanes > 8) E->cfg.lanes = 8;
@@ -1158,11 +1327,14 @@ void bolt_engine_destroy(bolt_engine* E) {
 
 const char* bolt_engine_last_error(const bolt_engine* E) { return E ? E->err.c_str() : "null engine"; }
 
-int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
+// Submission; with ybar set, a pullback by the discrete adjoint (q->grad is
+// 1; C_l: TT only, ybar per entry of q->ells; P_lin: ybar per k) whose
+// parameter cotangent goes to vjp_grad[6] when the request completes.
+static int submit_impl(bolt_engine* E, const bolt_request* q, const double* ybar, double* vjp_grad, int64_t* ticket) {
   if (!E || !ticket) return -1;
   std::unique_ptr<Req> r(new Req());
   try {
-    check_request(q);
+    check_request(q, ybar == nullptr);
     r->r = *q;
     r->k.assign(q->k, q->k + q->nk);
     r->r.k = r->k.data();
@@ -1180,9 +1352,29 @@ int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
       r->r.ells = nullptr;
       r->r.nell = 0;
     }
-    // P_lin and C_l^TT Jacobians come from tangent-linear modes unless the
-    // engine is set to replays; TE / EE Jacobians difference perturbed C_l
-    r->tangent = q->grad && E->cfg.grad_scheme == 0 && (q->kind == BOLT_REQ_PLIN || r->los_tangent);
+    // P_lin and C_l^TT Jacobians come from tangent-linear modes when the
+    // engine is set to them; otherwise (and for TE / EE) from replays
+    r->tangent = q->grad && E->cfg.grad_scheme == 1 && (q->kind == BOLT_REQ_PLIN || r->los_tangent) &&
+                 fits_one_warp(q->hier);
+    if (ybar) {
+      if (!fits_one_warp(q->hier)) throw EngErr(-1, "hierarchy does not fit the adjoint kernel's one warp");
+      if (!q->grad || (q->kind == BOLT_REQ_CL && (q->cl_want != BOLT_CL_TT || q->plin)))
+        throw EngErr(-1, "an adjoint pullback takes C_l^TT alone or P_lin");
+      r->adjoint = true;
+      r->tangent = false;
+      r->los_tangent = false;
+      r->wantE = false;
+      r->vjp_grad = vjp_grad;
+      if (q->kind == BOLT_REQ_CL) {
+        r->ybar.assign(r->uniq.size(), 0.0);
+        for (int e = 0; e < q->nell; ++e) {
+          int sl = int(std::lower_bound(r->uniq.begin(), r->uniq.end(), q->ells[e]) - r->uniq.begin());
+          r->ybar[sl] += ybar[e];
+        }
+      } else {
+        r->ybar.assign(ybar, ybar + q->nk);
+      }
+    }
     r->grid = make_grid(q->grid.start, q->grid.step, q->grid.stop);
     if (r->grid.n < 4 || r->grid.n > 100000) throw EngErr(-1, "x grid needs 4..100000 nodes");
     if (q->kind == BOLT_REQ_CL) {
@@ -1239,6 +1431,10 @@ int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
   return 0;
 }
 
+int bolt_engine_submit(bolt_engine* E, const bolt_request* q, int64_t* ticket) {
+  return submit_impl(E, q, nullptr, nullptr, ticket);
+}
+
 int bolt_engine_wait(bolt_engine* E, int64_t ticket, double timeout_s, int* rc_out, double* times_out, char* errbuf,
                      int errlen) {
   if (!E) return -1;
@@ -1293,6 +1489,23 @@ static int run_vjp(bolt_engine* E, const bolt_request* q, int kind, const double
   if (q->kind != kind) return fail(kind == BOLT_REQ_CL ? "bolt_cl_vjp needs a C_l request" : "bolt_plin_vjp needs a P_lin request");
   bolt_request r = *q;
   r.grad = 1;
+  const bool adjoint = E->cfg.grad_scheme == 2 && ybar[0] && fits_one_warp(q->hier) &&
+                       (kind == BOLT_REQ_PLIN || (q->cl_want == BOLT_CL_TT && !q->plin && !ybar[1] && !ybar[2]));
+  if (adjoint) {  // one forward and one reverse sweep (csrc/adjoint.cuh)
+    r.dtt = r.dte = r.dee = r.dplin = nullptr;
+    std::vector<double> prim;
+    if (kind == BOLT_REQ_CL && !r.tt && r.nell > 0) { prim.assign(size_t(r.nell), 0.0); r.tt = prim.data(); }
+    if (kind == BOLT_REQ_PLIN && !r.plin && r.nk > 0) { prim.assign(size_t(r.nk), 0.0); r.plin = prim.data(); }
+    int64_t t = 0;
+    int rc = submit_impl(E, &r, ybar[0], grad, &t);
+    if (rc != 0) {
+      std::lock_guard<std::mutex> g(E->mu);
+      return fail(E->err.c_str());
+    }
+    int out = 0;
+    rc = bolt_engine_wait(E, t, -1.0, &out, nullptr, errbuf, errlen);
+    return rc == 1 ? out : rc;
+  }
   const int n = kind == BOLT_REQ_CL ? r.nell : r.nk;
   if (n <= 0) return fail(kind == BOLT_REQ_CL ? "no multipoles" : "no wavenumbers");
   std::vector<double> prim[3], jac[3], jac_p;

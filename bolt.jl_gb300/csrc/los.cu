@@ -350,6 +350,7 @@ __global__ void __launch_bounds__(256) los_tt_grad_kernel(LosGradArgs a) {
   }
   const double ulo = double(reinterpret_cast<int*>(red)[0] - 3);
   __syncthreads();
+  if (a.ulo && threadIdx.x == 0) a.ulo[s] = ulo;
   const double umax = double(a.nb - 2);
   const size_t plane = (size_t)a.nrow * a.nm;
   double stt = 0.0, dstt[kDir];
@@ -388,11 +389,17 @@ __global__ void __launch_bounds__(256) los_tt_grad_kernel(LosGradArgs a) {
       const double S = a.Sd[q];
       th = fma(jv, S, th);
       const double jdS = jd * S * k;
+      if (a.dSd) {
 #pragma unroll
-      for (int j = 0; j < kDir; ++j)
-        dth[j] = fma(jdS, dyl[j * a.nrow + i], fma(jv, a.dSd[j * plane + q], dth[j]));
+        for (int j = 0; j < kDir; ++j)
+          dth[j] = fma(jdS, dyl[j * a.nrow + i], fma(jv, a.dSd[j * plane + q], dth[j]));
+      } else {
+#pragma unroll
+        for (int j = 0; j < kDir; ++j) dth[j] = fma(jdS, dyl[j * a.nrow + i], dth[j]);
+      }
     }
     const double w = a.wts[m];
+    if (a.cbar) a.cbar[(size_t)s * a.nm + m] = 2.0 * w * th;
     stt = fma(th * th, w, stt);
 #pragma unroll
     for (int j = 0; j < kDir; ++j)
@@ -441,6 +448,110 @@ __global__ void sdense_diff_kernel(int nx, int i0, int nrow, int nk, const doubl
   out[(size_t)i * nm + m] = ((1.0 - wk) * d0 + wk * d1) * dxs[i] * scale;
 }
 
+// -------------------------------------------- adjoint of the projection ----
+// Sbar_d[i][m] += 4 pi sum_{l in the block's slots} ybar_l cbar[l][m]
+// j_l(k_m y_i) over the terms with k_m y_i / dg >= ulo_l (the terms the
+// forward reduction kept).  Blocks: (m tile of 256, chunk of kAdjSlots
+// slots whose spline coefficients sit in shared memory); one atomic add per
+// (i, m) and chunk.
+constexpr int kAdjSlots = 2;
+__global__ void __launch_bounds__(256) los_sbar_kernel(LosAdjArgs a) {
+  extern __shared__ double sh[];
+  const int nb2 = a.nb + 2;
+  const int s0 = blockIdx.y * kAdjSlots;
+  const int ns = min(kAdjSlots, a.nslots - s0);
+  double* cs = sh;                        // [kAdjSlots][nb + 2]
+  double* yl = sh + kAdjSlots * nb2;      // [nrow]
+  for (int t = threadIdx.x; t < ns * nb2; t += blockDim.x) cs[t] = a.coef[(size_t)s0 * nb2 + t];
+  const double idg = a.inv_dg[0];
+  for (int j = threadIdx.x; j < a.nrow; j += blockDim.x) yl[j] = a.yv[j] * idg;
+  __syncthreads();
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= a.nm) return;
+  const double k = a.kmid[m];
+  const double umax = double(a.nb - 2);
+  double c[kAdjSlots], ulo[kAdjSlots];
+  int iend[kAdjSlots], imax = 0;
+  for (int q = 0; q < kAdjSlots; ++q) {
+    c[q] = 0.0;
+    ulo[q] = 0.0;
+    iend[q] = 0;
+    if (q >= ns) continue;
+    c[q] = 4.0 * M_PI * a.ybar[s0 + q] * a.cbar[(size_t)(s0 + q) * a.nm + m];
+    ulo[q] = a.ulo[s0 + q];
+    if (c[q] != 0.0 && k * yl[0] >= ulo[q]) {  // kept rows: a prefix (y falls along the rows)
+      int lo = 0, hi = a.nrow;
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (k * yl[mid] >= ulo[q]) lo = mid; else hi = mid;
+      }
+      iend[q] = hi;
+    }
+    imax = max(imax, iend[q]);
+  }
+  for (int i = 0; i < imax; ++i) {
+    const double u = k * yl[i];
+    double f = floor(u);
+    f = fmin(f, umax);
+    const int jj = (int)f;
+    const double t = u - f, sm = 1.0 - t, t2 = t * t, s2 = sm * sm;
+    const double w0 = s2 * sm, w3 = t2 * t;
+    const double w1 = 4.0 - 6.0 * t2 + 3.0 * w3;
+    const double w2 = 4.0 - 6.0 * s2 + 3.0 * w0;
+    double acc = 0.0;
+#pragma unroll
+    for (int q = 0; q < kAdjSlots; ++q) {
+      if (i >= iend[q]) continue;
+      const double* cq = cs + q * nb2;
+      const double jv = (cq[jj] * w0 + cq[jj + 1] * w1 + cq[jj + 2] * w2 + cq[jj + 3] * w3) * (1.0 / 6.0);
+      acc = fma(c[q], jv, acc);
+    }
+    atomicAdd(a.Sbd + (size_t)i * a.nm + m, acc);
+  }
+}
+
+// The transpose of sdense_kernel for S_T: Sbar[j][i0 + i] = dx_i (sum over the
+// midpoints m with lo(m) = j of (1 - w_m) Sbar_d[i][m] + those with
+// lo(m) = j - 1 of w_m Sbar_d[i][m]), lo and w as sdense_kernel computes
+// them.  One thread per (j, i).
+__device__ __forceinline__ int sdense_lo(const double* kgrid, int nk, double k) {
+  int lo = 0, hi = nk - 1;
+  if (k >= kgrid[nk - 1]) lo = nk - 2;
+  else if (k < kgrid[0]) lo = 0;
+  else {
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (kgrid[mid] <= k) lo = mid; else hi = mid;
+    }
+    if (lo > nk - 2) lo = nk - 2;
+  }
+  return lo;
+}
+__global__ void sbar_gather_kernel(LosAdjArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= a.nk || i >= a.nrow) return;
+  // midpoints whose interval is j - 1 or j: lo(m) is non-decreasing in m
+  auto first_m = [&](int jj) {  // first m with lo(m) >= jj
+    int lo = 0, hi = a.nm;
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (sdense_lo(a.kgrid, a.nk, a.kmid[mid]) >= jj) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+  };
+  const int ma = first_m(j - 1), mb = first_m(j), mc = first_m(j + 1);
+  double acc = 0.0;
+  const double* row = a.Sbd + (size_t)i * a.nm;
+  for (int m = ma; m < mc; ++m) {
+    const double k = a.kmid[m];
+    const int lo = m < mb ? j - 1 : j;
+    const double wk = (k - a.kgrid[lo]) / (a.kgrid[lo + 1] - a.kgrid[lo]);
+    acc = fma(lo == j ? 1.0 - wk : wk, row[m], acc);
+  }
+  a.Sbar[(size_t)j * a.nx + a.i0 + i] = acc * a.dxs[i];
+}
+
 // ------------------------------------------------------------ launchers ----
 int launch_jl_raw(int nb, const double* d_dgs, int ncz, int Lmax, const int* d_slot_of_l, int nslots, double* d_raw,
                   double* d_norm, int* d_flags, cudaStream_t st) {
@@ -476,6 +587,23 @@ int launch_los_tt_grad(const LosGradArgs& a, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(los_tt_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return e;
   los_tt_grad_kernel<<<a.nslots, threads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+int launch_los_adjoint(const LosAdjArgs& a, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(a.Sbd, 0, size_t(a.nrow) * a.nm * sizeof(double), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.Sbar, 0, size_t(a.nk) * a.nx * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  const int threads = 256;
+  const size_t smem = (size_t(kAdjSlots) * (a.nb + 2) + a.nrow) * sizeof(double);
+  e = cudaFuncSetAttribute(los_sbar_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return e;
+  dim3 g((a.nm + threads - 1) / threads, (a.nslots + kAdjSlots - 1) / kAdjSlots);
+  los_sbar_kernel<<<g, threads, smem, st>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  dim3 g2((a.nk + 127) / 128, a.nrow);
+  sbar_gather_kernel<<<g2, 128, 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -33,6 +33,9 @@
 // does for every node.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstring>
+
 #include "bolt_dev.cuh"
 
 namespace bolt {
@@ -99,12 +102,22 @@ __host__ __device__ inline int tan_doubles(int N, int nq) {
   return (kStages + 1) * kScal * kTD + 2 * (kStages + 1) * nq * kTD + 5 * nq * kTD + 8 * kTD + 32 * kBorder * kTD +
          2 * kTD * N;
 }
-__host__ __device__ inline int per_mode_doubles(int N, int nq, int Lmax, int threads, bool tan = false) {
+// An adjoint mode (adjoint.cuh) keeps the coefficient tangents but neither
+// the tangent stage vectors nor the tangent solves' partials.
+__host__ __device__ inline int adj_doubles(int N, int nq) { return tan_doubles(N, nq) - 2 * kTD * N - 32 * kBorder * kTD; }
+// Kernel kinds: 0 plain (and recorded / replayed / checkpointed) modes,
+// 1 tangent-linear modes, 2 adjoint (reverse-sweep) modes.
+__host__ __device__ inline int per_mode_doubles(int N, int nq, int Lmax, int threads, int kind = 0) {
   int nch = nq + 5;
   return 5 * N + 4 * nq + 2 * kStages * nq + 2 * nq + 2 * nch * kTail * kBorder + 2 * (Lmax + 1) + kStages * kScal +
-         kScal + kMiscDoubles + (tan ? tan_doubles(N, nq) : 0) + (pack_ints(threads) + 1) / 2;
+         kScal + kMiscDoubles + (kind == 1 ? tan_doubles(N, nq) : (kind == 2 ? adj_doubles(N, nq) : 0)) +
+         (pack_ints(threads) + 1) / 2;
 }
-__host__ __device__ inline int scratch_per_warp(int N, bool tan = false) { return 10 * N + (tan ? 9 * kTD * N : 0); }
+// Global scratch of an adjoint mode after the base slab (adjoint.cuh).
+__host__ __device__ inline int adj_scratch_doubles(int N) { return (15 + 2 * kTD + kCkptEvery) * N; }
+__host__ __device__ inline int scratch_per_warp(int N, int kind = 0) {
+  return 10 * N + (kind == 1 ? 9 * kTD * N : (kind == 2 ? adj_scratch_doubles(N) : 0));
+}
 
 struct Mode {
   const CosmoDev* C;
@@ -772,12 +785,15 @@ __device__ __forceinline__ double block_sum(double v, double* red, int tid) {
   return t;
 }
 
-template <int WPM, bool TAN>
-__device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const SolverCfg& cfg, double* base,
-                          double* gscr, int tid) {
+// Per-mode set-up shared by the solver kinds (0 plain, 1 tangent, 2
+// adjoint): the mode's dimensions and tangent cosmologies, the shared-memory
+// layout per_mode_doubles() sizes, the chain packing, the global slab and
+// the per-mode constants.  All threads; returns false when the chains do
+// not fit the CTA (ends with a barrier).
+template <int WPM, int KIND>
+__device__ bool setup_mode(const ModeDev& md, const CosmoDev* cosmos, double* base, double* gscr, int tid, Mode& m,
+                           Shared& S, Pack& PK, Scratch& G) {
   constexpr int nth = 32 * WPM;
-  const int lane = tid & 31, warp = tid >> 5;
-  Mode m;
   m.C = cosmos + md.cosmo;
   m.k = md.k;
   m.lg = md.lg; m.lnu = md.lnu; m.lmnu = md.lmnu; m.nq = md.nq;
@@ -788,13 +804,12 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   m.iPhi = m.iM + (m.lmnu + 1) * m.nq;
   m.nch = m.nq + 5;
   for (int j = 0; j < kTD; ++j) {
-    m.tc[j] = TAN ? cosmos + md.tcos[j] : m.C;
-    m.tinv[j] = TAN ? md.tinv[j] : 0.0;
+    m.tc[j] = KIND ? cosmos + md.tcos[j] : m.C;
+    m.tinv[j] = KIND ? md.tinv[j] : 0.0;
   }
   const CosmoDev& C = *m.C;
   const int N = m.N, nq = m.nq;
   int Lmax = max(m.lg, max(m.lnu, m.lmnu));
-  Shared S;
   S.sct = S.sct_d = S.qet = S.eqt = S.qet_d = S.eqt_d = S.qpj = S.dq = S.ddf0 = S.dAq = S.dBq = S.cstn = nullptr;
   S.yd = S.bd = S.part4 = nullptr;
   double* p = base;
@@ -819,7 +834,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   S.sc_d = p; p += kScal;
   S.misc = p;                 // [0..8] capacitance inverse, [16..23] block reductions, [24] flags, [32..] partials
   p += kMiscDoubles;
-  if (TAN) {  // the layout tan_doubles() sizes
+  if (KIND) {  // the layout tan_doubles() / adj_doubles() size
     S.sct = p; p += kStages * kScal * kTD;
     S.sct_d = p; p += kScal * kTD;
     S.qet = p; p += kStages * nq * kTD;
@@ -832,12 +847,12 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     S.dAq = p; p += nq * kTD;
     S.dBq = p; p += nq * kTD;
     S.cstn = p; p += 8 * kTD;
-    S.part4 = p; p += 32 * kBorder * kTD;
-    S.yd = p; p += kTD * N;
-    S.bd = p; p += kTD * N;
+    if (KIND == 1) {
+      S.part4 = p; p += 32 * kBorder * kTD;
+      S.yd = p; p += kTD * N;
+      S.bd = p; p += kTD * N;
+    }
   }
-  double* red = S.misc + 16;
-  Pack PK;
   {
     int* ip = reinterpret_cast<int*>(p);
     PK.seg = ip; ip += nth;
@@ -847,17 +862,11 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     PK.E = ip;
     PK.em = kLaneElems / nth;
   }
-  Scratch G;
   G.y = gscr;
   G.fx = gscr + N;
   G.K = gscr + 2 * N;
   G.yp = gscr + 8 * N;
   G.fp = gscr + 9 * N;
-  TanScratch T;
-  T.dy = gscr + 10 * N;
-  T.dK = T.dy + kTD * N;
-  T.fxt = T.dK + 6 * kTD * N;
-  T.tmp = T.fxt + kTD * N;
   // per-mode constants (perturbations.jl:164-166; background.jl:21-30)
   for (int l = tid; l <= Lmax; l += nth) {
     S.cl1[l] = double(l) / (2.0 * l + 1.0);
@@ -866,9 +875,30 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   for (int q = tid; q < nq; q += nth) qconst(C, q, S.q[q], S.df0[q], S.Aq[q], S.Bq[q]);
   if (tid == 0) S.misc[25] = build_pack(m, PK, nth) ? 1.0 : 0.0;
   __syncthreads();
+  return S.misc[25] != 0.0;
+}
+
+template <int WPM, bool TAN>
+__device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const SolverCfg& cfg, double* base,
+                          double* gscr, int tid) {
+  constexpr int nth = 32 * WPM;
+  const int lane = tid & 31, warp = tid >> 5;
+  Mode m;
+  Shared S;
+  Pack PK;
+  Scratch G;
+  const bool packed = setup_mode<WPM, TAN ? 1 : 0>(md, cosmos, base, gscr, tid, m, S, PK, G);
+  const CosmoDev& C = *m.C;
+  const int N = m.N;
+  double* red = S.misc + 16;
+  TanScratch T;
+  T.dy = gscr + 10 * N;
+  T.dK = T.dy + kTD * N;
+  T.fxt = T.dK + 6 * kTD * N;
+  T.tmp = T.fxt + kTD * N;
   double x = C.x0;
   const double xend = md.xout[md.nout - 1];
-  if (S.misc[25] == 0.0) {
+  if (!packed) {
     if (tid == 0) { *md.status = ST_BAD_INPUT; if (md.counters) { md.counters[0] = 0; md.counters[1] = 0; } }
     return;
   }
@@ -878,7 +908,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   __syncthreads();
   if (TAN) {
     tan_setup(m, S, tid, nth);
-    tan_initial(m, S, x, G.y, T.dy, tid, nth);
+    tan_initial(m, S, x, G.y, T.dy, S.bd, tid, nth);
   }
   int status = ST_OK;
   bool rsa_any = false;
@@ -887,7 +917,9 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
   while (jo < md.nout && md.xout[jo] < x) ++jo;
   int jtan = jo;  // next node of the tangent outputs (tangent modes land on every node)
   // nodes below x_dense are produced by dense output (sources only)
-  const bool dense_ok = (md.flags & MODE_SOURCES) && !(md.flags & MODE_TRAJ) && !TAN;
+  const bool ckpt = (md.flags & MODE_CKPT) != 0;  // lands on every node; steps replayable bit for bit
+  const bool dense_ok = (md.flags & MODE_SOURCES) && !(md.flags & MODE_TRAJ) && !TAN && !ckpt;
+  if (ckpt) copy_vec(N, G.y, md.ckpt, tid, nth);
   int jd = 0;
   if (dense_ok)
     while (jd < md.nout - 1 && md.xout[jd] < cfg.x_dense) ++jd;
@@ -971,6 +1003,7 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
     double hs = h;
     if (x + hs >= target - 1e-14 * fabs(target)) { hs = target - x; landing = true; }
     double xn = landing ? target : x + hs;
+    if (ckpt) hs = xn - x;  // the step a replay from the record takes
     if (replay) {
       if (nacc >= md.rec_cap) { status = ST_REPLAY_SHORT; break; }
       xn = md.rec[nacc];
@@ -1092,6 +1125,8 @@ __device__ void solve_one(const ModeDev& md, const CosmoDev* cosmos, const Solve
         if (nacc < md.rec_cap) md.rec[nacc] = xn;
         else rec_over = true;
       }
+      if (ckpt && (nacc + 1) % kCkptEvery == 0 && nacc + 1 <= md.rec_cap)
+        copy_vec(N, G.y, md.ckpt + size_t((nacc + 1) / kCkptEvery) * N, tid, nth);
       __syncthreads();
       if (rsa_switch(m, get_scal<double>(S, 4))) {  // uniform over the CTA
         if (TAN) { status = ST_TANGENT_RSA; break; }
@@ -1178,11 +1213,314 @@ int launch_rsa_post(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos
   return cudaGetLastError();
 }
 
+#include "adjoint.cuh"
+
+// The reverse sweep of one adjoint mode (MODE_ADJOINT, adjoint.cuh): the
+// forward mode's checkpoints and step record, the cotangents of its outputs
+// in md.sbar; writes the parameter cotangent's four partials to md.tbar.
+template <int WPM>
+__device__ void adjoint_one(const ModeDev& md, const CosmoDev* cosmos, double* base, double* gscr, int tid) {
+  constexpr int nth = 32 * WPM;
+  Mode m;
+  Shared S;
+  Pack PK;
+  Scratch G;
+  const bool packed = setup_mode<WPM, 2>(md, cosmos, base, gscr, tid, m, S, PK, G);
+  const CosmoDev& C = *m.C;
+  const int N = m.N;
+  double* red = S.misc + 16;
+  AdjScratch A;
+  {
+    double* p = gscr + 10 * N;
+    A.lam = p; p += N;
+    A.yb = p; p += N;
+    A.Kb = p; p += 6 * N;
+    A.Yb = p; p += N;
+    A.Fb = p; p += N;
+    A.u1 = p; p += N;
+    A.du = p; p += N;
+    A.gu = p; p += N;
+    A.gdu = p; p += N;
+    A.tmp = p; p += N;
+    A.t4 = p; p += kTD * N;
+    A.t4b = p; p += kTD * N;
+    A.seg = p;
+  }
+  double tb[kTD] = {0.0, 0.0, 0.0, 0.0};
+  int status = ST_OK;
+  const long long nf = md.nfwd ? (long long)md.nfwd[0] : 0;
+  if (!packed) status = ST_BAD_INPUT;
+  else if (nf <= 0 || nf > md.rec_cap) status = ST_REPLAY_SHORT;
+  if (status == ST_OK) {
+    tan_setup(m, S, tid, nth);
+    for (int i = tid; i < N; i += nth) A.lam[i] = 0.0;
+    __syncthreads();
+    const bool src = (md.flags & MODE_SOURCES) != 0, plin = (md.flags & MODE_PLIN) != 0;
+    int jo = md.nout - 1;  // the next output node from the top
+    const int nseg = int((nf + kCkptEvery - 1) / kCkptEvery);
+    for (int sg = nseg - 1; sg >= 0 && status == ST_OK; --sg) {
+      const long long n0 = (long long)sg * kCkptEvery, n1 = min(n0 + (long long)kCkptEvery, nf);
+      // replay the segment from its checkpoint, keeping the states y_n0 .. y_{n1-1}
+      copy_vec(N, md.ckpt + size_t(sg) * N, G.y, tid, nth);
+      __syncthreads();
+      double x = n0 == 0 ? C.x0 : md.rec[n0 - 1];
+      for (long long n = n0; n < n1 - 1; ++n) {
+        copy_vec(N, G.y, A.seg + size_t(n - n0) * N, tid, nth);
+        const double xn = md.rec[n];
+        const int rc = replay_stages<WPM>(m, S, PK, G, x, xn - x, xn, tid, nth);
+        if (rc != ST_OK) { status = rc; break; }
+        for (int i = tid; i < N; i += nth) G.y[i] = S.yt[i] + S.b[i];
+        __syncthreads();
+        x = xn;
+      }
+      if (status != ST_OK) break;
+      copy_vec(N, G.y, A.seg + size_t(n1 - 1 - n0) * N, tid, nth);
+      __syncthreads();
+      // backwards through the segment: recompute step n, seed its end node, pull lam back
+      for (long long n = n1 - 1; n >= n0; --n) {
+        const double xs = n == 0 ? C.x0 : md.rec[n - 1], xn = md.rec[n], hs = xn - xs;
+        copy_vec(N, A.seg + size_t(n - n0) * N, G.y, tid, nth);
+        __syncthreads();
+        const int rc = replay_stages<WPM>(m, S, PK, G, xs, hs, xn, tid, nth);
+        if (rc != ST_OK) { status = rc; break; }
+        for (int i = tid; i < N; i += nth) A.u1[i] = S.yt[i] + S.b[i];
+        double xsl[5];
+        xsl[0] = xs;
+        for (int sl = 1; sl < 4; ++sl) xsl[sl] = xs + rodas::kCx[sl] * hs;
+        xsl[4] = xn;
+        tan_prepare(m, S, xsl, 0, 5, tid, nth);  // ends with a barrier
+        bool at_node = false;
+        double sbT = 0.0;
+        if (src && jo >= 0 && md.xout[jo] == xn) {
+          at_node = true;
+          sbT = md.sbar[jo];
+          --jo;
+        }
+        const bool last = (n == nf - 1);
+        const double pb = (plin && last) ? md.sbar[0] : 0.0;
+        if ((at_node && sbT != 0.0) || pb != 0.0)
+          adjoint_seed<WPM>(m, S, A, 4, xn, at_node, sbT, plin && last, pb, tb, tid, nth);
+        adjoint_step<WPM>(m, S, PK, G, A, hs, tb, tid, nth);
+      }
+    }
+    if (status == ST_OK) {
+      copy_vec(N, md.ckpt, A.u1, tid, nth);  // the initial state
+      __syncthreads();
+      if (src && jo >= 0 && md.xout[jo] == C.x0 && md.sbar[jo] != 0.0) {
+        prepare_other(m, S, C.x0, tid, nth);
+        double xsl[kStages];
+        xsl[5] = C.x0;
+        tan_prepare(m, S, xsl, 5, 6, tid, nth);
+        adjoint_seed<WPM>(m, S, A, 5, C.x0, true, md.sbar[jo], false, 0.0, tb, tid, nth);
+      }
+      // the initial conditions' tangents: tb[j] += lam . d y_0 / d theta_j
+      tan_initial(m, S, C.x0, A.u1, A.t4, A.tmp, tid, nth);
+      for (int i = tid; i < N; i += nth)
+#pragma unroll
+        for (int j = 0; j < kTD; ++j) tb[j] = fma(A.lam[i], A.t4[j * N + i], tb[j]);
+    }
+  }
+  for (int j = 0; j < kTD; ++j) {
+    const double v = block_sum<WPM>(tb[j], red, tid);
+    if (tid == 0 && md.tbar) md.tbar[j] = status == ST_OK ? v : 0.0;
+  }
+  if (tid == 0) {
+    *md.status = status;
+    if (md.counters) { md.counters[0] = nf; md.counters[1] = 0; }
+  }
+}
+
+// Self-check of the adjoint's building blocks on one mode at (x, hs), one
+// warp, pseudo-random vectors u, lam, du: out[sl] (sl = 0..4) = |lam.(A u) -
+// (A^T lam).u| over sum |lam_i (A u)_i| at stage slot sl; out[5] the same
+// for A' (d/dx); out[6] = max |M^T z - lam| / max |lam| for z = M^-T lam,
+// M^T z formed as z / (h gamma) - A_0^T z; out[7] = max |M x - u| / max |u|
+// for x = M^-1 u (the forward solve, M x = x / (h gamma) - A_0 x); out[8] =
+// |S_T(u, du) - (g_u.u + g_du.du)| over the sum of the terms' magnitudes
+// (source_grad); out[9] = |(P(u + e v) - P(u - e v)) / 2e - g.v| / |g.v|
+// (plin_grad, P quadratic in u); out[10] = 1 if the streaming switch is on;
+// out[11] = |lam.(M^-1 u) - (M^-T lam).u| / sum |lam_i (M^-1 u)_i|.
+__device__ __forceinline__ double prand(int i, int seed) {
+  unsigned x = unsigned(i) * 2654435761u ^ (unsigned(seed) * 40503u + 12345u);
+  x ^= x >> 13;
+  x *= 0x5bd1e995u;
+  x ^= x >> 15;
+  return double(x & 0xFFFFFFu) / double(0x800000) - 1.0;
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__global__ void __launch_bounds__(32) adjoint_check_kernel(ModeDev md, const CosmoDev* __restrict__ cosmos,
+                                                           double x, double hs, double* __restrict__ gscr,
+                                                           double* __restrict__ out) {
+  extern __shared__ double smem[];
+  const int tid = threadIdx.x, lane = tid, nth = 32;
+  Mode m;
+  Shared S;
+  Pack PK;
+  Scratch G;
+  if (!setup_mode<1, 2>(md, cosmos, smem, gscr, tid, m, S, PK, G)) {
+    if (tid == 0) out[15] = -1.0;
+    return;
+  }
+  const int N = m.N;
+  double* u = gscr + 10 * N;
+  double* lam = u + N;
+  double* du = lam + N;
+  double* w1 = du + N;
+  double* w2 = w1 + N;
+  double* w3 = w2 + N;
+  double* gu = w3 + N;
+  double* gdu = gu + N;
+  for (int i = tid; i < N; i += nth) {
+    u[i] = prand(i, 1);
+    lam[i] = prand(i, 2);
+    du[i] = prand(i, 3);
+  }
+  tan_setup(m, S, tid, nth);
+  prepare_stages(m, S, x, hs, x + hs, tid, nth);
+  const bool fok = factorize_scan(m, S, PK, hs * rodas::kGamma, tid, nth);
+  const double ig = 1.0 / (hs * rodas::kGamma);
+  bool rsa = false;
+  for (int sl = 0; sl < 5; ++sl) {
+    rsa |= rhs_rows<double>(m, S, sl, StP{u}, sink(w1), tid, nth);
+    rhs_cols<double>(m, S, sl, lam, sink(w2), tid, nth);
+    double d1 = 0.0, d2 = 0.0, sc = 0.0;
+    for (int i = tid; i < N; i += nth) {
+      d1 += lam[i] * w1[i];
+      d2 += w2[i] * u[i];
+      sc += fabs(lam[i] * w1[i]);
+    }
+    d1 = warp_sum(d1); d2 = warp_sum(d2); sc = warp_sum(sc);
+    if (tid == 0) out[sl] = fabs(d1 - d2) / sc;
+    __syncthreads();
+  }
+  {
+    rhs_rows<dd>(m, S, 0, StP{u}, sink(w1, w3), tid, nth);          // w3 = A' u
+    rhs_cols<dd>(m, S, 0, lam, sink(w1, w2), tid, nth);             // w2 = A'^T lam
+    double d1 = 0.0, d2 = 0.0, sc = 0.0;
+    for (int i = tid; i < N; i += nth) {
+      d1 += lam[i] * w3[i];
+      d2 += w2[i] * u[i];
+      sc += fabs(lam[i] * w3[i]);
+    }
+    d1 = warp_sum(d1); d2 = warp_sum(d2); sc = warp_sum(sc);
+    if (tid == 0) out[5] = fabs(d1 - d2) / sc;
+    __syncthreads();
+  }
+  {  // transposed solve
+    copy_vec(N, lam, S.b, tid, nth);
+    __syncthreads();
+    wsolve_scan_T(m, S, PK, S.b, tid, nth);
+    copy_vec(N, S.b, w3, tid, nth);
+    __syncthreads();
+    // the two solves are each other's transposes: lam.(M^-1 u) = (M^-T lam).u
+    copy_vec(N, u, S.b, tid, nth);
+    __syncthreads();
+    wsolve_scan(m, S, PK, S.b, tid, nth);
+    {
+      double d1 = 0.0, d2 = 0.0, sc = 0.0;
+      for (int i = tid; i < N; i += nth) {
+        d1 += lam[i] * S.b[i];
+        d2 += w3[i] * u[i];
+        sc += fabs(lam[i] * S.b[i]);
+      }
+      d1 = warp_sum(d1); d2 = warp_sum(d2); sc = warp_sum(sc);
+      if (tid == 0) out[11] = fabs(d1 - d2) / sc;
+    }
+    __syncthreads();
+    rhs_cols<double>(m, S, 0, w3, sink(w2), tid, nth);
+    double e = 0.0, sc = 0.0;
+    for (int i = tid; i < N; i += nth) {
+      e = fmax(e, fabs(ig * w3[i] - w2[i] - lam[i]));
+      sc = fmax(sc, fabs(lam[i]));
+    }
+    e = warp_max(e); sc = warp_max(sc);
+    if (tid == 0) out[6] = fok ? e / sc : -1.0;
+    __syncthreads();
+  }
+  {  // forward solve
+    copy_vec(N, u, S.b, tid, nth);
+    __syncthreads();
+    wsolve_scan(m, S, PK, S.b, tid, nth);
+    copy_vec(N, S.b, w3, tid, nth);
+    __syncthreads();
+    rhs_rows<double>(m, S, 0, StP{w3}, sink(w2), tid, nth);
+    double e = 0.0, sc = 0.0;
+    for (int i = tid; i < N; i += nth) {
+      e = fmax(e, fabs(ig * w3[i] - w2[i] - u[i]));
+      sc = fmax(sc, fabs(u[i]));
+    }
+    e = warp_max(e); sc = warp_max(sc);
+    if (tid == 0) out[7] = fok ? e / sc : -1.0;
+    __syncthreads();
+  }
+  {  // source gradient: S_T is linear in (u, du)
+    for (int i = tid; i < N; i += nth) { gu[i] = 0.0; gdu[i] = 0.0; }
+    __syncthreads();
+    double sT = 0.0, sE = 0.0;
+    emit_sources_t<double>(m, S, x, StP{u}, StP{du}, lane, sT, sE, false);
+    source_grad(m, S, x, 1.0, gu, gdu, lane);
+    __syncwarp();
+    double lin = 0.0, mag = 0.0;
+    for (int i = tid; i < N; i += nth) {
+      lin += gu[i] * u[i] + gdu[i] * du[i];
+      mag += fabs(gu[i] * u[i]) + fabs(gdu[i] * du[i]);
+    }
+    lin = warp_sum(lin); mag = warp_sum(mag);
+    if (tid == 0) out[8] = fabs(sT - lin) / mag;
+    __syncthreads();
+  }
+  {  // P_lin gradient: quadratic in u, so the central difference is exact
+    for (int i = tid; i < N; i += nth) gu[i] = 0.0;
+    __syncthreads();
+    plin_grad(m, S, x, u, 1.0, gu, lane);
+    __syncwarp();
+    const double e = 1e-3;
+    for (int i = tid; i < N; i += nth) { w1[i] = u[i] + e * du[i]; w2[i] = u[i] - e * du[i]; }
+    __syncwarp();
+    double pp = 0.0, pm = 0.0;
+    emit_plin_t<double>(m, S, x, StP{w1}, lane, pp);
+    emit_plin_t<double>(m, S, x, StP{w2}, lane, pm);
+    pp = __shfl_sync(0xffffffffu, pp, 0);
+    pm = __shfl_sync(0xffffffffu, pm, 0);
+    double gv = 0.0;
+    for (int i = tid; i < N; i += nth) gv += gu[i] * du[i];
+    gv = warp_sum(gv);
+    if (tid == 0) {
+      out[9] = fabs((pp - pm) / (2.0 * e) - gv) / fabs(gv);
+      out[10] = rsa ? 1.0 : 0.0;
+      out[15] = N;
+    }
+  }
+}
+
+int launch_adjoint_check(const CosmoDev* d_cos, int id, double k, int lg, int lnu, int lmnu, int nq, double x,
+                         double hs, double* d_scr, double* d_out, cudaStream_t st) {
+  ModeDev md;
+  std::memset(&md, 0, sizeof(md));
+  md.k = k;
+  md.cosmo = id;
+  md.lg = lg; md.lnu = lnu; md.lmnu = lmnu; md.nq = nq;
+  for (int j = 0; j < kTD; ++j) { md.tcos[j] = id; md.tinv[j] = 0.0; }
+  const int N = 2 * (lg + 1) + (lnu + 1) + (lmnu + 1) * nq + 5;
+  const int Lmax = std::max(lg, std::max(lnu, lmnu));
+  const size_t smem = size_t(per_mode_doubles(N, nq, Lmax, 32, 2)) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(adjoint_check_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return e;
+  adjoint_check_kernel<<<1, 32, smem, st>>>(md, d_cos, x, hs, d_scr, d_out);
+  return cudaGetLastError();
+}
+size_t adjoint_check_scratch_bytes(int N) { return size_t(20) * N * sizeof(double); }
+
 // Persistent CTAs: the first wave takes modes blockIdx.x (modes arrive sorted
 // by decreasing cost, and consecutive blocks land on different SMs, so the
 // longest modes spread one per SM); later modes come from a device queue.
-// TAN: every mode of the launch is a tangent mode (MODE_TANGENT).
-template <int WPM, bool TAN>
+// KIND: every mode of the launch is plain (0, including recorded, replayed
+// and checkpointed modes), tangent-linear (1, MODE_TANGENT) or adjoint (2,
+// MODE_ADJOINT).
+template <int WPM, int KIND>
 __global__ void __launch_bounds__(32 * WPM) rodas_kernel(const ModeDev* __restrict__ modes, int nmodes,
                                                          const CosmoDev* __restrict__ cosmos, SolverCfg cfg,
                                                          int* __restrict__ queue, double* __restrict__ scratch,
@@ -1193,7 +1531,8 @@ __global__ void __launch_bounds__(32 * WPM) rodas_kernel(const ModeDev* __restri
   double* gscr = scratch + (size_t)blockIdx.x * scr_per_mode;
   int mi = blockIdx.x;
   while (mi < nmodes) {
-    solve_one<WPM, TAN>(modes[mi], cosmos, cfg, smem, gscr, tid);
+    if (KIND == 2) adjoint_one<WPM>(modes[mi], cosmos, smem, gscr, tid);
+    else solve_one<WPM, KIND == 1>(modes[mi], cosmos, cfg, smem, gscr, tid);
     __syncthreads();
     if (tid == 0) s_mode = gridDim.x + atomicAdd(queue, 1);
     __syncthreads();
@@ -1202,25 +1541,27 @@ __global__ void __launch_bounds__(32 * WPM) rodas_kernel(const ModeDev* __restri
 }
 
 namespace {
-// The kernel variant: warps per mode 1, 2 or 4; tangent modes with one warp.
-const void* kernel_of(int wpm, bool tan) {
-  if (tan) return (const void*)rodas_kernel<1, true>;
-  return wpm == 1 ? (const void*)rodas_kernel<1, false>
-                  : (wpm == 2 ? (const void*)rodas_kernel<2, false> : (const void*)rodas_kernel<4, false>);
+// The kernel variant: warps per mode 1, 2 or 4; tangent and adjoint modes
+// with one warp.
+const void* kernel_of(int wpm, int kind) {
+  if (kind == 1) return (const void*)rodas_kernel<1, 1>;
+  if (kind == 2) return (const void*)rodas_kernel<1, 2>;
+  return wpm == 1 ? (const void*)rodas_kernel<1, 0>
+                  : (wpm == 2 ? (const void*)rodas_kernel<2, 0> : (const void*)rodas_kernel<4, 0>);
 }
-int norm_wpm(int wpm, bool tan) { return tan ? 1 : ((wpm == 1 || wpm == 2) ? wpm : 4); }
-size_t smem_of(int maxN, int maxnq, int maxL, int wpm, bool tan) {
-  return size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * wpm, tan)) * sizeof(double);
+int norm_wpm(int wpm, int kind) { return kind ? 1 : ((wpm == 1 || wpm == 2) ? wpm : 4); }
+size_t smem_of(int maxN, int maxnq, int maxL, int wpm, int kind) {
+  return size_t(per_mode_doubles(maxN, maxnq, maxL, 32 * wpm, kind)) * sizeof(double);
 }
 }  // namespace
 
 // Host helpers.  wpm: warps per mode (1, 2 or 4; anything else means 4;
-// tangent launches use one).  Writes the number of persistent CTAs to
-// launch (one mode each at a time).
-int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, bool tan, int* blocks) {
-  wpm = norm_wpm(wpm, tan);
-  const size_t smem = smem_of(maxN, maxnq, maxL, wpm, tan);
-  const void* f = kernel_of(wpm, tan);
+// tangent and adjoint launches use one); kind as rodas_kernel's KIND.
+// Writes the number of persistent CTAs to launch (one mode each at a time).
+int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, int kind, int* blocks) {
+  wpm = norm_wpm(wpm, kind);
+  const size_t smem = smem_of(maxN, maxnq, maxL, wpm, kind);
+  const void* f = kernel_of(wpm, kind);
   cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return -int(e);
   int dev = 0, nsm = 0;
@@ -1234,46 +1575,48 @@ int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, bool ta
   return 0;
 }
 int rodas_grid_warps(int nmodes, int maxN, int maxnq, int maxL, int wpm, int* blocks) {
-  return rodas_grid_warps(nmodes, maxN, maxnq, maxL, wpm, false, blocks);
+  return rodas_grid_warps(nmodes, maxN, maxnq, maxL, wpm, 0, blocks);
 }
 
 int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
-                 int maxN, int maxnq, int maxL, int wpm, bool tan, int blocks, double* d_scratch, cudaStream_t stream) {
-  wpm = norm_wpm(wpm, tan);
-  const size_t smem = smem_of(maxN, maxnq, maxL, wpm, tan);
+                 int maxN, int maxnq, int maxL, int wpm, int kind, int blocks, double* d_scratch, cudaStream_t stream) {
+  wpm = norm_wpm(wpm, kind);
+  const size_t smem = smem_of(maxN, maxnq, maxL, wpm, kind);
   cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  const int spm = scratch_per_warp(maxN, tan);
-  if (tan)
-    rodas_kernel<1, true><<<blocks, 32, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+  const int spm = scratch_per_warp(maxN, kind);
+  if (kind == 1)
+    rodas_kernel<1, 1><<<blocks, 32, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+  else if (kind == 2)
+    rodas_kernel<1, 2><<<blocks, 32, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
   else if (wpm == 1)
-    rodas_kernel<1, false><<<blocks, 32, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+    rodas_kernel<1, 0><<<blocks, 32, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
   else if (wpm == 2)
-    rodas_kernel<2, false><<<blocks, 64, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+    rodas_kernel<2, 0><<<blocks, 64, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
   else
-    rodas_kernel<4, false><<<blocks, 128, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
+    rodas_kernel<4, 0><<<blocks, 128, smem, stream>>>(d_modes, nmodes, d_cosmos, cfg, d_queue, d_scratch, spm);
   return cudaGetLastError();
 }
 int launch_rodas(const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg, int* d_queue,
                  int maxN, int maxnq, int maxL, int wpm, int blocks, double* d_scratch, cudaStream_t stream) {
-  return launch_rodas(d_modes, nmodes, d_cosmos, cfg, d_queue, maxN, maxnq, maxL, wpm, false, blocks, d_scratch,
+  return launch_rodas(d_modes, nmodes, d_cosmos, cfg, d_queue, maxN, maxnq, maxL, wpm, 0, blocks, d_scratch,
                       stream);
 }
 
 // Kernel-node description of one solver launch, for CUDA graphs whose
 // node parameters are updated per batch.  args must stay alive until the
 // node parameters have been set (the values are copied then).
-int rodas_node_params(int wpm, bool tan, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos,
+int rodas_node_params(int wpm, int kind, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos,
                       const SolverCfg& cfg, int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch,
                       RodasNodeArgs* args, cudaKernelNodeParams* p) {
-  wpm = norm_wpm(wpm, tan);
+  wpm = norm_wpm(wpm, kind);
   args->modes = d_modes;
   args->nmodes = nmodes;
   args->cosmos = d_cosmos;
   args->cfg = cfg;
   args->queue = d_queue;
   args->scratch = d_scratch;
-  args->spm = scratch_per_warp(maxN, tan);
+  args->spm = scratch_per_warp(maxN, kind);
   args->ptrs[0] = &args->modes;
   args->ptrs[1] = &args->nmodes;
   args->ptrs[2] = &args->cosmos;
@@ -1281,10 +1624,10 @@ int rodas_node_params(int wpm, bool tan, const ModeDev* d_modes, int nmodes, con
   args->ptrs[4] = &args->queue;
   args->ptrs[5] = &args->scratch;
   args->ptrs[6] = &args->spm;
-  p->func = const_cast<void*>(kernel_of(wpm, tan));
+  p->func = const_cast<void*>(kernel_of(wpm, kind));
   p->gridDim = dim3(blocks);
   p->blockDim = dim3(32 * wpm);
-  p->sharedMemBytes = unsigned(smem_of(maxN, maxnq, maxL, wpm, tan));
+  p->sharedMemBytes = unsigned(smem_of(maxN, maxnq, maxL, wpm, kind));
   p->kernelParams = args->ptrs;
   p->extra = nullptr;
   return 0;
@@ -1292,19 +1635,19 @@ int rodas_node_params(int wpm, bool tan, const ModeDev* d_modes, int nmodes, con
 int rodas_node_params(int wpm, const ModeDev* d_modes, int nmodes, const CosmoDev* d_cosmos, const SolverCfg& cfg,
                       int* d_queue, int maxN, int maxnq, int maxL, int blocks, double* d_scratch, RodasNodeArgs* args,
                       cudaKernelNodeParams* p) {
-  return rodas_node_params(wpm, false, d_modes, nmodes, d_cosmos, cfg, d_queue, maxN, maxnq, maxL, blocks, d_scratch,
+  return rodas_node_params(wpm, 0, d_modes, nmodes, d_cosmos, cfg, d_queue, maxN, maxnq, maxL, blocks, d_scratch,
                            args, p);
 }
 
-size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm, bool tan) {
-  return smem_of(maxN, maxnq, maxL, norm_wpm(wpm, tan), tan);
+size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm, int kind) {
+  return smem_of(maxN, maxnq, maxL, norm_wpm(wpm, kind), kind);
 }
 size_t rodas_smem_per_mode(int maxN, int maxnq, int maxL, int wpm) {
-  return rodas_smem_per_mode(maxN, maxnq, maxL, wpm, false);
+  return rodas_smem_per_mode(maxN, maxnq, maxL, wpm, 0);
 }
 size_t rodas_smem_per_warp(int maxN, int maxnq, int maxL) { return rodas_smem_per_mode(maxN, maxnq, maxL, 4); }
-size_t rodas_scratch_per_warp(int maxN, bool tan) { return size_t(scratch_per_warp(maxN, tan)) * sizeof(double); }
-size_t rodas_scratch_per_warp(int maxN) { return rodas_scratch_per_warp(maxN, false); }
+size_t rodas_scratch_per_warp(int maxN, int kind) { return size_t(scratch_per_warp(maxN, kind)) * sizeof(double); }
+size_t rodas_scratch_per_warp(int maxN) { return rodas_scratch_per_warp(maxN, 0); }
 
 #ifdef BOLT_PHASE_TIMERS
 int rodas_phase_cycles(unsigned long long* out, bool reset) {

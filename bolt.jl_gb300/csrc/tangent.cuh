@@ -267,12 +267,13 @@ __device__ void tan_prepare(const Mode& m, const Shared& S, const double* xs, in
   __syncthreads();
 }
 
-// Tangent initial state dy[j] = d initial_conditions / d theta_j (G.y holds
-// the base state); S.yt and S.bd serve as scratch.  All threads.
-__device__ void tan_initial(const Mode& m, const Shared& S, double xi, const double* y, double* dy, int tid, int nth) {
+// Tangent initial state dy[j] = d initial_conditions / d theta_j (y the
+// base state); S.yt and qs (nq doubles) serve as scratch.  All threads.
+__device__ void tan_initial(const Mode& m, const Shared& S, double xi, const double* y, double* dy, double* qs,
+                            int tid, int nth) {
   const int N = m.N, nq = m.nq, lane = tid & 31, warp = tid >> 5;
   for (int j = 0; j < kTD; ++j) {
-    double* df0j = S.bd;  // perturbed dlnf0/dlnq
+    double* df0j = qs;  // perturbed dlnf0/dlnq
     for (int q = tid; q < nq; q += nth) {
       double qq, df0, Aq, Bq;
       qconst(*m.tc[j], q, qq, df0, Aq, Bq);

@@ -153,6 +153,27 @@ int bolt_plin(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const bolt_h
  * integrator on every node.  Pass -INFINITY to land on every node. */
 int bolt_set_dense_x(bolt_ctx* ctx, double x_dense);
 
+/* Self-check of the discrete adjoint's building blocks (no counterpart in
+ * the reference; the test suite's probe of the reverse sweep's pieces) on
+ * one mode of cosmology id, wavenumber k and hierarchy h, at the Rosenbrock
+ * step from x of size hstep, with pseudo-random vectors u, lam, du:
+ *   [0..4] |lam.(A u) - (A^T lam).u| / sum |lam_i (A u)_i| at the five
+ *          stage abscissae (A: hierarchy!'s linear map, src/perturbations.jl:196-270;
+ *          A^T: its column form);
+ *   [5]    the same for dA/dx;
+ *   [6]    max |M^T z - lam| / max |lam| for z from the transposed solve
+ *          (M = I/(h gamma) - A, the step matrix);
+ *   [7]    max |M x - u| / max |u| for x from the forward solve;
+ *   [8]    source_function (src/perturbations.jl:343-389) against its
+ *          gradient: |S_T(u, du) - (g_u.u + g_du.du)| / sum of the terms;
+ *   [9]    plin (src/spectra.jl:163-198) against its gradient: relative error
+ *          of a central difference (exact for the quadratic P_lin);
+ *   [10]   1 if the radiation-streaming switch is on at x, else 0;
+ *   [11]   |lam.(M^-1 u) - (M^-T lam).u| / sum |lam_i (M^-1 u)_i|: the two
+ *          solves are each other's transposes.
+ * (12 doubles.)  Returns 0 or a negative code. */
+int bolt_adjoint_check(bolt_ctx* ctx, int id, double k, const bolt_hier* h, double x, double hstep, double* out);
+
 /* Counters of the last call: [0] accepted steps, [1] rejected steps,
  * [2] solver kernel microseconds, [3] LOS kernels microseconds,
  * [4] modes, [5] solver kernel launches, [6] total kernel launches,
@@ -251,10 +272,13 @@ typedef struct {
   int land_stride;       /* source grids: the solver lands on every land_stride-th x node at x >= -8.5
                             (and the last) and takes the others from cubic Hermite dense output, as it
                             does below -8.5 (0 or 1 = lands on every node there; at most 64) */
-  int grad_scheme;       /* Jacobians of P_lin and C_l^TT requests: 0 = the tangent-linear solver (one
-                            solve carries the state and its derivatives along h, omega_b, omega_c and
-                            Sigma m_nu, sharing each step's factorisation), 1 = forward differences of
-                            four frozen-step replays; C_l requests with TE or EE Jacobians always replay */
+  int grad_scheme;       /* derivatives of P_lin and C_l^TT: 0 = forward differences of four frozen-step
+                            replays (the default: the fastest measured); 1 = the tangent-linear solver
+                            (one solve carries the state and its derivatives along h, omega_b, omega_c
+                            and Sigma m_nu, sharing each step's factorisation); 2 = as 0 for Jacobian
+                            requests, and bolt_cl_vjp (C_l^TT cotangents only) / bolt_plin_vjp by the
+                            discrete adjoint (a checkpointed reverse sweep of the solve and of the line
+                            of sight); C_l requests with TE or EE Jacobians always replay */
 } bolt_engine_cfg;
 
 typedef struct bolt_engine bolt_engine;
