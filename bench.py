@@ -69,9 +69,14 @@ import numpy as np  # noqa: E402
 METRIC = "Cℓ+grad spectra/s on 1 GB300 (served vs plain) at ≤1e-4 rel err; p50/p99 latency"
 UNIT = "spectra/s"
 RELTOL, ABSTOL = 1e-8, 3e-7
+# source nodes at x >= -8.5: the solver lands on every LAND_STRIDE-th and
+# takes the others from cubic Hermite dense output (served and plain legs)
+LAND_STRIDE = 2
 ACCURACY = ("at reltol 1e-8 / abstol 3e-7 the oracle's C_l differ from its converged (1e-11) solution by "
             "<= 3.5e-5 (EE), 7.5e-6 (TT), 3.4e-6 (TE) relative; the GPU path matches the oracle at equal "
-            "tolerances to 1e-10; gradients agree with the oracle's central differences within 1e-3")
+            "tolerances to 1e-10; landing on every 2nd source node (dense output between) moves C_l^TT by "
+            "<= 8.5e-6 (EE 1e-6, TE 9e-7 of peak); the hardest served request stays within 1e-4 of the "
+            "converged oracle (GPU test); gradients agree with the oracle's central differences within 1e-3")
 KINDS = ["plin", "cl", "plin", "cl", "plin", "cl", "plin", "cl", "plin", "grad"]  # 5 : 4 : 1
 SEED = 20241204
 RATE = 10.0  # requests per second
@@ -371,7 +376,7 @@ def serve_at_rate(B, local, stream, rate, seed):
     to end, p50 / p99 latency, how many requests waited after their tables
     were ready (lanes or the memory budget busy), host table-build times and
     the largest device footprint in flight."""
-    with B.Engine(device=local, lanes=6, objective="throughput") as eng:
+    with B.Engine(device=local, land_stride=LAND_STRIDE, lanes=6, objective="throughput") as eng:
         warm = make_stream(2, offset=1000)
         for t in [eng.submit(to_request(B, d)) for d in warm]:
             assert eng.wait(t).rc == 0
@@ -417,7 +422,7 @@ def run_serving(args):
     # ---- plain: the drop-in C-ABI, one cosmology per call, nothing else in flight
     plain_lat, plain_solver_s, plain_flops, plain_calls = [], 0.0, 0.0, 0
     plain_los = {"us": 0, "terms": 0, "flops": 0.0}
-    ctx = B.Context(device=local)
+    ctx = B.Context(device=local, land_stride=LAND_STRIDE)
     for d in warm:
         dropin_request(B, ctx, d)
     barrier(dist)
@@ -437,7 +442,7 @@ def run_serving(args):
     plain_wall = max_over_ranks(sum(plain_lat), dist)
 
     # ---- served: Poisson arrivals, continuous batching
-    with B.Engine(device=local, lanes=6, objective="throughput") as eng:
+    with B.Engine(device=local, land_stride=LAND_STRIDE, lanes=6, objective="throughput") as eng:
         ts = [eng.submit(to_request(B, d)) for d in warm]
         for t in ts:
             assert eng.wait(t).rc == 0
@@ -475,19 +480,19 @@ def run_serving(args):
         g_dropin.append(time.perf_counter() - t0)
     ctx.close()
     g_plain = []
-    with B.Engine(device=local, lanes=1, max_batch=1) as eng:
+    with B.Engine(device=local, land_stride=LAND_STRIDE, lanes=1, max_batch=1) as eng:
         eng.run(to_request(B, gwarm))
         for d in gstream:
             t0 = time.perf_counter()
             r = eng.run(to_request(B, d))
             g_plain.append(time.perf_counter() - t0)
             assert r.rc == 0, r.err
-    with B.Engine(device=local, lanes=6, objective="throughput") as eng:
+    with B.Engine(device=local, land_stride=LAND_STRIDE, lanes=6, objective="throughput") as eng:
         eng.run(to_request(B, gwarm))
         gres = [eng.wait(t) for t in [eng.submit(to_request(B, d)) for d in gstream]]
     for r in gres:
         assert r.rc == 0, r.err
-    with B.Engine(device=local, lanes=6, objective="throughput", grad_scheme="tangent") as eng:
+    with B.Engine(device=local, land_stride=LAND_STRIDE, lanes=6, objective="throughput", grad_scheme="tangent") as eng:
         eng.run(to_request(B, gwarm))
         gres_tan = [eng.wait(t) for t in [eng.submit(to_request(B, d)) for d in gstream]]
     for r in gres_tan:
@@ -514,7 +519,7 @@ def run_serving(args):
     ybars = [rng.standard_normal(d["lmax"] - 1) for d in gstream]
     pull, pgrads = {}, {}
     for scheme in ("replay", "adjoint"):
-        with B.Engine(device=local, lanes=6, objective="throughput", grad_scheme=scheme) as eng:
+        with B.Engine(device=local, land_stride=LAND_STRIDE, lanes=6, objective="throughput", grad_scheme=scheme) as eng:
             eng.vjp(to_request(B, gwarm), {"tt": np.ones(gwarm["lmax"] - 1)})
             t0 = time.perf_counter()
             r0, _ = eng.vjp(to_request(B, gstream[0]), {"tt": ybars[0]})
@@ -530,11 +535,13 @@ def run_serving(args):
         pull[scheme] = {"alone_s": alone, "served": len(gstream) / win}
     gr, ga = pgrads["replay"], pgrads["adjoint"]
     pullback = {**pull, "unit": "pullbacks/s (served), s per call (alone)", "requests": len(gstream),
-                "adjoint_vs_replay_max_rel": float(np.max(np.abs(ga - gr)) / np.max(np.abs(gr))),
+                "adjoint_vs_replay_max_rel": float(np.max(np.abs(ga - gr) / np.max(np.abs(gr), axis=0))),
                 "workload": "bolt_cl_vjp of the C_l^TT + Jacobian requests above (random cotangents over l): "
                             "replay = the frozen-step replays' Jacobian contracted in the library; adjoint = one "
                             "checkpointed forward solve, the adjoint of the line of sight and one reverse sweep per "
-                            "mode; alone: one call; served: all calls concurrently from host threads"}
+                            "mode; alone: one call; served: all calls concurrently from host threads; "
+                            "adjoint_vs_replay_max_rel: the largest over the six parameters of the difference "
+                            "over that parameter's largest pullback (the replays' forward differences carry ~1e-6)"}
     # ---- the arrival-rate sweep of the serving configuration (same stream)
     sweep = [serve_at_rate(B, local, stream, rate, SEED + 31 + rank) for rate in SWEEP_RATES] if args.sweep else []
     lat = np.array([r.latency for r in res])
@@ -587,7 +594,7 @@ def run_serving(args):
                                       "in [1e-4,1] h/Mpc, l 50/50/20, nq 15), C_l TT/TE/EE (l_max 1000 or 2500) and "
                                       "C_l^TT l<=2000 + 6-parameter Jacobian (both: 64-1024 log k in [0.1,1000] H0, "
                                       "l_gamma=l_nu in {20,35,50}, l_mnu 10, nq 15); one step = one request",
-                          "requests": counts, "reltol": RELTOL, "abstol": ABSTOL, "accuracy": ACCURACY,
+                          "requests": counts, "reltol": RELTOL, "abstol": ABSTOL, "land_stride": LAND_STRIDE, "accuracy": ACCURACY,
                           "timing": "value: served stream over the GPU window (first batch launch to last "
                                     "completion, 6 lanes, autotuner objective throughput); plain: the drop-in C-ABI one cosmology per call (a "
                                     "gradient request = 7 calls, forward differences), sum of call times",
@@ -641,7 +648,7 @@ def run_reference(args):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": "the serving stream of the GPU arm (bench.py module docstring), CPU oracle, "
                                   "requests one after another", "parallelism": f"{cores} host threads",
-                      "reltol": RELTOL, "abstol": ABSTOL},
+                      "reltol": RELTOL, "abstol": ABSTOL, "land_stride": LAND_STRIDE},
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -703,7 +710,7 @@ def run_batch(args):
     K = args.steps
     reqs = cosmology_requests(args.workload, K, 3000 if args.workload == "batch" else 4000)
     warm = cosmology_requests(args.workload, 1, 9000)
-    ctx = B.Context(device=0)
+    ctx = B.Context(device=0, land_stride=LAND_STRIDE)
     for d in warm:
         batch_dropin(B, ctx, d)
     sampler = clocks_sampler()
@@ -711,7 +718,7 @@ def run_batch(args):
     calls = sum(batch_dropin(B, ctx, d) for d in reqs)
     plain_s = time.perf_counter() - t0
     ctx.close()
-    with B.Engine(device=0, lanes=6, objective="throughput") as eng:
+    with B.Engine(device=0, land_stride=LAND_STRIDE, lanes=6, objective="throughput") as eng:
         for d in warm:
             assert eng.run(batch_request(B, d)).rc == 0
         s0 = eng.stats()
@@ -732,7 +739,7 @@ def run_batch(args):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": what + "; cosmologies from the box h 0.6-0.8, omega_b 0.019-0.025, omega_c 0.10-0.14, n_s 0.92-1.0, ln(1e10 A_s) 2.9-3.2, Sigma m_nu 0-0.3 eV, 64-1024 log k in [0.1,1000] H0, "
                                          "l_gamma = l_nu in {20,35,50}, l_mnu 10, nq 15; all submitted at once",
-                      "reltol": RELTOL, "abstol": ABSTOL},
+                      "reltol": RELTOL, "abstol": ABSTOL, "land_stride": LAND_STRIDE},
            "plain": {"value": K / plain_s, "unit": "cosmologies/s", "calls": calls,
                      "api": "drop-in C-ABI one cosmology per call (bolt_cl_pipeline TT, bolt_plin; Jacobians as "
                             "1 + 6 calls)"},
@@ -756,7 +763,7 @@ def run_pipeline(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     import bolt_gb300 as B
-    ctx = B.Context(device=local, warps_per_block=args.warps_per_mode)
+    ctx = B.Context(device=local, warps_per_block=args.warps_per_mode, land_stride=LAND_STRIDE)
     par = B.CosmoParams(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Y_p=0.24, N_nu=3.046,
                         Sigma_m_nu=0.06 * B.mass_natural())
     bg = B.Background(par)
@@ -798,7 +805,7 @@ def run_pipeline(args):
                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                "config": {"workload": f"full CMB pipeline: fiducial LCDM, {ks.size} log k in "
                                       f"[0.1,{args.kmax_h0:g}]H0, l {args.lg}/{args.lg}/{args.lmnu}, nq 15 (N={N}), "
-                                      f"S_T/S_E on the x nodes > -8, C_l TT/TE/EE l=2..{args.lmax}", "reltol": RELTOL, "abstol": ABSTOL,
+                                      f"S_T/S_E on the x nodes > -8, C_l TT/TE/EE l=2..{args.lmax}", "reltol": RELTOL, "abstol": ABSTOL, "land_stride": LAND_STRIDE,
                           "l2": "flushed (256 MB write) between steps", "parallelism": f"replicas x{ws}"},
                "clocks": clocks, "gpu_launches": launches,
                "roofline": {"bound": "fp64", "achieved": sol, "peak": peak, "unit": "TFLOP/s",

@@ -34,7 +34,7 @@ def _nvcc() -> str:
 def _sources():
     return [os.path.join(CSRC, s) for s in CU_SOURCES + CXX_SOURCES] + [
         os.path.join(CSRC, "bolt_dev.cuh"), os.path.join(CSRC, "host_cosmo.hpp"), os.path.join(CSRC, "tuner.hpp"),
-        os.path.join(CSRC, "chains.cuh"),
+        os.path.join(CSRC, "chains.cuh"), os.path.join(CSRC, "tangent.cuh"), os.path.join(CSRC, "adjoint.cuh"),
         os.path.join(os.path.dirname(ROOT), "include", "bolt_gb300.h")]
 
 

@@ -65,7 +65,7 @@ def _check_status(status, what):
 class Context:
     """One GPU context (device memory, stream, cosmology registry)."""
 
-    def __init__(self, device: int = 0, warps_per_block: int = 0, max_steps: int = 0):
+    def __init__(self, device: int = 0, warps_per_block: int = 0, max_steps: int = 0, land_stride: int = 1):
         self.lib = L.load()
         opts = L.BoltOpts(device, warps_per_block, max_steps)
         h = C.c_void_p()
@@ -73,6 +73,8 @@ class Context:
         if rc != 0 or not h.value:
             raise BoltError(f"bolt_ctx_create failed ({rc}): no usable CUDA device {device}")
         self.h = h
+        if land_stride != 1:
+            self.check(self.lib.bolt_set_land_stride(self.h, int(land_stride)), "bolt_set_land_stride")
 
     def check(self, rc, what):
         if rc != 0:
@@ -489,8 +491,9 @@ def adjoint_check(ih: IonizationHistory, k: float, x: float, hstep: float, lg=8,
     step (bolt_adjoint_check): [0..4] A^T at the stage abscissae, [5] dA/dx
     transposed, [6] the transposed solve, [7] the forward solve, [8] the
     source gradient, [9] the P_lin gradient, [10] the streaming switch,
-    [11] the two solves as each other's transposes."""
-    out = np.zeros(12)
+    [11] the two solves as each other's transposes, [12] the coefficient
+    cotangents against tangent arithmetic."""
+    out = np.zeros(13)
     c = ih.ctx
     c.check(c.lib.bolt_adjoint_check(c.h, ih.cosmo_id, float(k), C.byref(_hier(lg, lnu, lmnu, nq)), float(x),
                                      float(hstep), L.dptr(out)), "bolt_adjoint_check")

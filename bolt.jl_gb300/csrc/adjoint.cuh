@@ -4,9 +4,9 @@
 // abscissa of every accepted step and keeps the state at the start of every
 // kCkptEvery-th one.  The reverse sweep (MODE_ADJOINT) walks the segments
 // between checkpoints from the last to the first: it replays the segment's
-// steps from its checkpoint (states kept in global scratch), then runs
-// through them backwards, recomputing each step's stages and factorisation
-// and pulling the cotangent lambda of the state back through it.  For the
+// steps from its checkpoint (states and stage increments kept in global
+// scratch), then runs through them backwards, refactorising each step and
+// pulling the cotangent lambda of the state back through it.  For the
 // linear ODE u' = A(x) u the step is
 //   M K_i = A_i Y_i + h d_i A'_0 y + (1/h) sum_{j<i} C_ij K_j,
 //   Y_i = y + sum_{j<i} a_ij K_j,  y_new = Y_6 + K_6,  M = I/(h gamma) - A_0,
@@ -399,10 +399,11 @@ __device__ void plin_grad(const Mode& m, const Shared& S, double x, const double
 // Global scratch of an adjoint mode after the base slab: lam, ybar, Kbar
 // [6], Ybar, Fbar, the state at the step's end u1, its derivative du, the
 // output gradients gu / gdu, a vector tmp, two tangent blocks [kTD][N]
-// (t4, t4b) and the segment's states [kCkptEvery][N].
-// (adj_scratch_doubles() in solver.cu sizes it.)
+// (t4, t4b), the segment's states [kCkptEvery + 1][N] and its steps' stage
+// increments [kCkptEvery][6][N].  (adj_scratch_doubles() in solver.cu
+// sizes it.)
 struct AdjScratch {
-  double *lam, *yb, *Kb, *Yb, *Fb, *u1, *du, *gu, *gdu, *tmp, *t4, *t4b, *seg;
+  double *lam, *yb, *Kb, *Yb, *Fb, *u1, *du, *gu, *gdu, *tmp, *t4, *t4b, *seg, *segK;
 };
 
 // rhs_rows in d4 numbers of a constant state u at slot sl: t4[j][i] =
@@ -416,6 +417,181 @@ __device__ __forceinline__ void dA_dot(const Mode& m, const Shared& S, int sl, c
   for (int i = tid; i < m.N; i += nth)
 #pragma unroll
     for (int j = 0; j < kTD; ++j) tb[j] = fma(rb[i], t4[j * m.N + i], tb[j]);
+}
+
+// rb . (dA_sl u) along the kTD tangent directions, added to tb[j], from the
+// cotangents of hierarchy!'s coefficients: the reverse of rhs_rows (and of
+// metric) over its coefficients -- the stage scalars, q/eps and eps/q of
+// slot sl, the momentum-bin constants and the cosmology constants -- each
+// cotangent times its tangents (S.sct, S.qet, S.eqt, S.dq, S.dAq, S.ddf0,
+// S.cstn).  One pass whatever the number of directions; the same products
+// as dA_dot.  Every thread adds its own rows' share (the metric's share on
+// lane 0 and the momentum bins' on their lanes).  One warp.
+__device__ void coef_dot(const Mode& m, const Shared& S, int sl, const double* u, const double* rb, double* tb,
+                         int tid, int nth) {
+  const int lane = tid & 31;
+  const int nq = m.nq, lg = m.lg, lnu = m.lnu, lmnu = m.lmnu;
+  const Scal<double> s = get_scal<double>(S, sl);
+  const bool rsa = rsa_switch(m, s);
+  const double* cl1 = S.cl1;
+  const double* cl2 = S.cl2;
+  const CosmoDev& C = *m.C;
+  const double Omega_nu = C.Omega_nu;
+  const double* qe = S.qe + sl * nq;
+  const double* eq = S.eq + sl * nq;
+  // the metric's values, as metric() forms them
+  double rho = 0.0, sig = 0.0;
+  for (int q = lane; q < nq; q += 32) {
+    rho = rho + (S.Aq[q] * S.q[q]) * eq[q] * u[m.iM + q];
+    sig = sig + (S.Aq[q] * S.q[q]) * qe[q] * u[m.iM + 2 * nq + q];
+  }
+  rho = warp_sum(rho);
+  sig = warp_sum(sig);
+  const double rc0 = cos_const(C, 0), rc1 = cos_const(C, 1), Oc = cos_const(C, 2), Ob = cos_const(C, 3);
+  const double Phi = u[m.iPhi];
+  const double Psi = -Phi - s.cpsi * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig * rc0);
+  const double ia = 1.0 / s.a;
+  const double X1 = Oc * u[m.iPhi + 1] + Ob * u[m.iPhi + 3];
+  const double X2 = 4.0 * C.Omega_r * u[0] + 4.0 * Omega_nu * u[m.iN] + rho * rc1;
+  const double Phip = Psi - s.k2H2 * Phi + s.dphi * (X1 * ia + X2 * (ia * ia));
+  const double Pi = u[2] + u[m.iTp + 2] + u[m.iTp];
+  const double vb = u[m.iPhi + 4];
+  // ---- rows: cotangents of the scalars (this thread's share), of Psi and
+  // Phi', and the momentum-bin ones added at once
+  double bkH = 0.0, btp = 0.0, biHe = 0.0, bcs2 = 0.0, bR = 0.0, bPsi = 0.0, bPhip = 0.0;
+  auto add_q = [&](const double* t, int idx, double bar) {  // tb[j] += bar * t[idx * kTD + j]
+#pragma unroll
+    for (int j = 0; j < kTD; ++j) tb[j] = fma(bar, t[idx * kTD + j], tb[j]);
+  };
+  for (int i = tid; i < m.N; i += nth) {
+    const double r = rb[i];
+    if (i < m.iM) {
+      if (rsa) continue;
+      if (i < m.iN) {  // photon temperature (T) and polarization (P)
+        const bool P = i >= m.iTp;
+        const int b0 = P ? m.iTp : 0, l = i - b0;
+        if (l < lg) {
+          const double lo = l > 0 ? u[b0 + l - 1] : 0.0;
+          bkH += r * (cl1[l] * lo - cl2[l] * u[b0 + l + 1]);
+          if (P || l >= 1) btp += r * u[i];
+          if (!P) {
+            if (l == 0) bPhip -= r;
+            if (l == 1) { bkH += r * (Psi / 3.0); bPsi += r * (s.kH / 3.0); btp += r * (vb / 3.0); }
+            if (l == 2) btp -= r * (Pi / 10.0);
+          } else {
+            if (l == 0) btp -= r * (Pi / 2.0);
+            if (l == 2) btp -= r * (Pi / 10.0);
+          }
+        } else {
+          bkH += r * u[b0 + lg - 1];
+          biHe -= r * (lg + 1.0) * u[i];
+          btp += r * u[i];
+        }
+      } else {  // massless neutrinos
+        const int l = i - m.iN, b0 = m.iN;
+        if (l < lnu) {
+          const double lo = l > 0 ? u[b0 + l - 1] : 0.0;
+          bkH += r * (cl1[l] * lo - cl2[l] * u[b0 + l + 1]);
+          if (l == 0) bPhip -= r;
+          if (l == 1) { bkH += r * (Psi / 3.0); bPsi += r * (s.kH / 3.0); }
+        } else {
+          bkH += r * u[b0 + lnu - 1];
+          biHe -= r * (lnu + 1.0) * u[i];
+        }
+      }
+    } else if (i < m.iPhi) {  // massive neutrinos
+      const int jm = i - m.iM;
+      const int l = jm / nq, q = jm - l * nq;
+      const int iq = sl * nq + q;
+      if (l < lmnu) {
+        const double lo = l > 0 ? u[i - nq] : 0.0;
+        const double B = cl1[l] * lo - cl2[l] * u[i + nq];
+        bkH += r * qe[q] * B;
+        add_q(S.qet, iq, r * s.kH * B);
+        if (l == 0) {
+          bPhip += r * S.df0[q];
+          add_q(S.ddf0, q, r * Phip);
+        }
+        if (l == 1) {
+          const double c = r * (1.0 / 3.0);
+          bkH -= c * eq[q] * Psi * S.df0[q];
+          add_q(S.eqt, iq, -c * s.kH * Psi * S.df0[q]);
+          bPsi -= c * s.kH * eq[q] * S.df0[q];
+          add_q(S.ddf0, q, -c * s.kH * eq[q] * Psi);
+        }
+      } else {
+        const double lo = u[i - nq];
+        add_q(S.qet, iq, r * s.kH * lo);
+        bkH += r * qe[q] * lo;
+        biHe -= r * (lmnu + 1.0) * u[i];
+      }
+    } else {  // metric and matter
+      const int rr = i - m.iPhi;
+      if (rr == 0) bPhip += r;
+      else if (rr == 1) { bkH += r * u[m.iPhi + 2]; bPhip -= 3.0 * r; }
+      else if (rr == 2) { bkH -= r * Psi; bPsi -= r * s.kH; }
+      else if (rr == 3) { bkH += r * vb; bPhip -= 3.0 * r; }
+      else {
+        const double d = u[m.iPhi + 3];
+        bkH -= r * (Psi + s.cs2 * d);
+        bPsi -= r * s.kH;
+        bcs2 -= r * s.kH * d;
+        btp += r * s.R * (3.0 * u[1] + vb);
+        bR += r * s.tp * (3.0 * u[1] + vb);
+      }
+    }
+  }
+  // the scalars' cotangents (this thread's share) times their tangents
+  {
+    const double* st = S.sct + (sl * kScal) * kTD;
+#pragma unroll
+    for (int j = 0; j < kTD; ++j) {
+      double acc = tb[j];
+      acc = fma(bkH, st[5 * kTD + j], acc);
+      acc = fma(btp, st[2 * kTD + j], acc);
+      acc = fma(biHe, st[6 * kTD + j], acc);
+      acc = fma(bcs2, st[3 * kTD + j], acc);
+      acc = fma(bR, st[7 * kTD + j], acc);
+      tb[j] = acc;
+    }
+  }
+  // ---- the metric, backwards: Phi' = Psi - k2H2 Phi + dphi (X1 ia + X2 ia^2),
+  // Psi = -Phi - cpsi (Omega_r Theta_2 + Omega_nu N_2 + sigma rc0)
+  bPhip = warp_sum(bPhip);
+  bPsi = warp_sum(bPsi) + bPhip;
+  const double brho = bPhip * s.dphi * (ia * ia) * rc1;
+  const double bsig = -bPsi * s.cpsi * rc0;
+  if (lane == 0) {
+    const double* st = S.sct + (sl * kScal) * kTD;
+    const double bk2H2 = -bPhip * Phi;
+    const double bdphi = bPhip * (X1 * ia + X2 * (ia * ia));
+    const double bia = bPhip * s.dphi * (X1 + 2.0 * X2 * ia);
+    const double ba = -bia * (ia * ia);
+    const double bcpsi = -bPsi * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig * rc0);
+    const double bOc = bPhip * s.dphi * ia * u[m.iPhi + 1], bOb = bPhip * s.dphi * ia * u[m.iPhi + 3];
+    const double brc1 = bPhip * s.dphi * (ia * ia) * rho, brc0 = -bPsi * s.cpsi * sig;
+#pragma unroll
+    for (int j = 0; j < kTD; ++j) {
+      double acc = tb[j];
+      acc = fma(bk2H2, st[10 * kTD + j], acc);
+      acc = fma(bdphi, st[9 * kTD + j], acc);
+      acc = fma(ba, st[4 * kTD + j], acc);
+      acc = fma(bcpsi, st[8 * kTD + j], acc);
+      acc = fma(brc0, S.cstn[0 * kTD + j], acc);
+      acc = fma(brc1, S.cstn[1 * kTD + j], acc);
+      acc = fma(bOc, S.cstn[2 * kTD + j], acc);
+      acc = fma(bOb, S.cstn[3 * kTD + j], acc);
+      tb[j] = acc;
+    }
+  }
+  for (int q = lane; q < nq; q += 32) {  // rho = sum Aq q eq M_0q, sigma = sum Aq q qe M_2q
+    const double m0 = u[m.iM + q], m2 = u[m.iM + 2 * nq + q];
+    const double Aq = S.Aq[q], qq = S.q[q];
+    add_q(S.dAq, q, brho * qq * eq[q] * m0 + bsig * qq * qe[q] * m2);
+    add_q(S.dq, q, brho * Aq * eq[q] * m0 + bsig * Aq * qe[q] * m2);
+    add_q(S.eqt, sl * nq + q, brho * Aq * qq * m0);
+    add_q(S.qet, sl * nq + q, bsig * Aq * qq * m2);
+  }
 }
 
 // Stages of one replayed step from (x, G.y) with size hs to xn: the
@@ -509,8 +685,8 @@ __device__ void adjoint_step(const Mode& m, const Shared& S, const Pack& PK, con
       }
     }
     __syncthreads();
-    dA_dot(m, S, sl, S.yt, S.b, A.t4, tb, tid, nth);              // rbar . dA_sl Y_st
-    dA_dot(m, S, 0, G.K + st * N, S.b, A.t4, tb, tid, nth);       // rbar . dA_0 K_st (M depends on A_0)
+    coef_dot(m, S, sl, S.yt, S.b, tb, tid, nth);         // rbar . dA_sl Y_st
+    coef_dot(m, S, 0, G.K + st * N, S.b, tb, tid, nth);  // rbar . dA_0 K_st (M depends on A_0)
     const double hd = hs * rodas::kD[st];
     for (int i = tid; i < N; i += nth) {
       const double rb = S.b[i];
@@ -566,15 +742,15 @@ __device__ void adjoint_seed(const Mode& m, const Shared& S, const AdjScratch& A
   if (src && sbT != 0.0) {
     rhs_cols<double>(m, S, sl, A.gdu, sink(A.tmp), tid, nth);  // A^T d S / d(du)
     for (int i = tid; i < N; i += nth) A.gu[i] += A.tmp[i];
-    // partials at fixed state: S_T(u, du) with du = A u, the coefficients' tangents alone
+    // partials at fixed state, S_T(u, du) with du = A u: those of the
+    // source's own coefficients, and (sbT dS/d(du)) . dA u from the
+    // hierarchy's coefficient cotangents
+    coef_dot(m, S, sl, A.u1, A.gdu, tb, tid, nth);
     rhs_rows<double>(m, S, sl, StP{A.u1}, sink(A.du), tid, nth);
-    Sink o;
-    o.v = nullptr; o.d = nullptr; o.t = A.t4; o.td = nullptr; o.N = N;
-    rhs_rows<d4>(m, S, sl, StC{A.u1}, o, tid, nth);
     __syncthreads();
     if (warp == 0) {
       d4 oT = c4(0.0), oE = c4(0.0);
-      emit_sources_t<d4>(m, S, x, StM{A.u1, nullptr, N}, StM{A.du, A.t4, N}, lane, oT, oE, false);
+      emit_sources_t<d4>(m, S, x, StM{A.u1, nullptr, N}, StM{A.du, nullptr, N}, lane, oT, oE, false);
       if (lane == 0)
         for (int j = 0; j < kTD; ++j) tb[j] += sbT * oT.t[j];
     }

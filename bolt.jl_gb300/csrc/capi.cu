@@ -90,6 +90,7 @@ struct bolt_ctx {
   int wpb = 0;
   long long max_steps = 100000;  // OrdinaryDiffEq's default maxiters
   double x_dense = -8.5;
+  int land_stride = 1;
   std::vector<CosmoEntry> cos;
   DBuf d_cos;
   DBuf modes, xout, srcT, srcE, traj, plin, status, counters, queue, flags, scratch;
@@ -222,7 +223,7 @@ void run_solver(bolt_ctx* c, int id, const double* k, int nk, const bolt_hier* h
   cfg.h0 = 1e-3;
   cfg.x_dense = c->x_dense;
   cfg.max_steps = c->max_steps;
-  cfg.land_stride = 1;
+  cfg.land_stride = c->land_stride;
   int Lmax = std::max(h->lg, std::max(h->lnu, h->lmnu));
   // warps per mode: 0 chooses by the launch size alone, one warp per mode
   // from about 20 modes per SM (where the FP64 issue rate, not the longest
@@ -740,6 +741,13 @@ int bolt_set_dense_x(bolt_ctx* c, double x) {
   return 0;
 }
 
+int bolt_set_land_stride(bolt_ctx* c, int stride) {
+  if (!c) return -1;
+  if (stride < 0 || stride > 64) return fail(c, -1, "land stride must be in 0..64");
+  c->land_stride = stride > 1 ? stride : 1;
+  return 0;
+}
+
 int bolt_adjoint_check(bolt_ctx* c, int id, double k, const bolt_hier* h, double x, double hstep, double* out) {
   return guard(c, [&] {
     if (!out || !(k > 0.0) || !(hstep > 0.0)) throw Err(-1, "null argument, k <= 0 or hstep <= 0");
@@ -758,7 +766,7 @@ int bolt_adjoint_check(bolt_ctx* c, int id, double k, const bolt_hier* h, double
     ck(cudaMemcpyAsync(o, d_out, 16 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "out");
     ck(cudaStreamSynchronize(c->stream), "sync");
     if (o[15] < 0.0) throw Err(-1, "hierarchy does not fit the solver's lane packing");
-    std::copy(o, o + 12, out);
+    std::copy(o, o + 13, out);
   });
 }
 

@@ -114,7 +114,7 @@ __host__ __device__ inline int per_mode_doubles(int N, int nq, int Lmax, int thr
          (pack_ints(threads) + 1) / 2;
 }
 // Global scratch of an adjoint mode after the base slab (adjoint.cuh).
-__host__ __device__ inline int adj_scratch_doubles(int N) { return (15 + 2 * kTD + kCkptEvery) * N; }
+__host__ __device__ inline int adj_scratch_doubles(int N) { return (15 + 2 * kTD + 7 * kCkptEvery + 1) * N; }
 __host__ __device__ inline int scratch_per_warp(int N, int kind = 0) {
   return 10 * N + (kind == 1 ? 9 * kTD * N : (kind == 2 ? adj_scratch_doubles(N) : 0));
 }
@@ -1244,7 +1244,8 @@ __device__ void adjoint_one(const ModeDev& md, const CosmoDev* cosmos, double* b
     A.tmp = p; p += N;
     A.t4 = p; p += kTD * N;
     A.t4b = p; p += kTD * N;
-    A.seg = p;
+    A.seg = p; p += size_t(kCkptEvery + 1) * N;
+    A.segK = p;
   }
   double tb[kTD] = {0.0, 0.0, 0.0, 0.0};
   int status = ST_OK;
@@ -1260,30 +1261,39 @@ __device__ void adjoint_one(const ModeDev& md, const CosmoDev* cosmos, double* b
     const int nseg = int((nf + kCkptEvery - 1) / kCkptEvery);
     for (int sg = nseg - 1; sg >= 0 && status == ST_OK; --sg) {
       const long long n0 = (long long)sg * kCkptEvery, n1 = min(n0 + (long long)kCkptEvery, nf);
-      // replay the segment from its checkpoint, keeping the states y_n0 .. y_{n1-1}
+      // replay the segment from its checkpoint, keeping the states y_n0 .. y_n1
+      // and every step's stage increments
       copy_vec(N, md.ckpt + size_t(sg) * N, G.y, tid, nth);
       __syncthreads();
       double x = n0 == 0 ? C.x0 : md.rec[n0 - 1];
-      for (long long n = n0; n < n1 - 1; ++n) {
+      for (long long n = n0; n < n1; ++n) {
         copy_vec(N, G.y, A.seg + size_t(n - n0) * N, tid, nth);
         const double xn = md.rec[n];
         const int rc = replay_stages<WPM>(m, S, PK, G, x, xn - x, xn, tid, nth);
         if (rc != ST_OK) { status = rc; break; }
-        for (int i = tid; i < N; i += nth) G.y[i] = S.yt[i] + S.b[i];
+        double* kk = A.segK + size_t(n - n0) * 6 * N;
+        for (int i = tid; i < N; i += nth) {
+          for (int j = 0; j < 6; ++j) kk[j * N + i] = G.K[j * N + i];
+          G.y[i] = S.yt[i] + S.b[i];
+        }
         __syncthreads();
         x = xn;
       }
       if (status != ST_OK) break;
-      copy_vec(N, G.y, A.seg + size_t(n1 - 1 - n0) * N, tid, nth);
+      copy_vec(N, G.y, A.seg + size_t(n1 - n0) * N, tid, nth);
       __syncthreads();
-      // backwards through the segment: recompute step n, seed its end node, pull lam back
+      // backwards through the segment: step n's factorisation again, its
+      // stored stages, the cotangent of its end node, lam pulled back
       for (long long n = n1 - 1; n >= n0; --n) {
         const double xs = n == 0 ? C.x0 : md.rec[n - 1], xn = md.rec[n], hs = xn - xs;
-        copy_vec(N, A.seg + size_t(n - n0) * N, G.y, tid, nth);
-        __syncthreads();
-        const int rc = replay_stages<WPM>(m, S, PK, G, xs, hs, xn, tid, nth);
-        if (rc != ST_OK) { status = rc; break; }
-        for (int i = tid; i < N; i += nth) A.u1[i] = S.yt[i] + S.b[i];
+        const double* kk = A.segK + size_t(n - n0) * 6 * N;
+        for (int i = tid; i < N; i += nth) {
+          G.y[i] = A.seg[size_t(n - n0) * N + i];
+          A.u1[i] = A.seg[size_t(n + 1 - n0) * N + i];
+          for (int j = 0; j < 6; ++j) G.K[j * N + i] = kk[j * N + i];
+        }
+        prepare_stages(m, S, xs, hs, xn, tid, nth);
+        if (!factorize_scan(m, S, PK, hs * rodas::kGamma, tid, nth)) { status = ST_LU_FAIL; break; }
         double xsl[5];
         xsl[0] = xs;
         for (int sl = 1; sl < 4; ++sl) xsl[sl] = xs + rodas::kCx[sl] * hs;
@@ -1339,7 +1349,9 @@ __device__ void adjoint_one(const ModeDev& md, const CosmoDev* cosmos, double* b
 // |S_T(u, du) - (g_u.u + g_du.du)| over the sum of the terms' magnitudes
 // (source_grad); out[9] = |(P(u + e v) - P(u - e v)) / 2e - g.v| / |g.v|
 // (plin_grad, P quadratic in u); out[10] = 1 if the streaming switch is on;
-// out[11] = |lam.(M^-1 u) - (M^-T lam).u| / sum |lam_i (M^-1 u)_i|.
+// out[11] = |lam.(M^-1 u) - (M^-T lam).u| / sum |lam_i (M^-1 u)_i|;
+// out[12] = the largest over the stage slots and tangent directions of
+// |coef_dot - dA_dot| / sum_i |lam_i (dA u)_i| on pseudo-random tangents.
 __device__ __forceinline__ double prand(int i, int seed) {
   unsigned x = unsigned(i) * 2654435761u ^ (unsigned(seed) * 40503u + 12345u);
   x ^= x >> 13;
@@ -1472,6 +1484,33 @@ __global__ void __launch_bounds__(32) adjoint_check_kernel(ModeDev md, const Cos
     if (tid == 0) out[8] = fabs(sT - lin) / mag;
     __syncthreads();
   }
+  {  // coefficient cotangents against the tangent-number right-hand side, on
+     // pseudo-random tangents of every coefficient
+    double* T1[9] = {S.sct, S.sct_d, S.qet, S.eqt, S.qet_d, S.eqt_d, S.dq, S.ddf0, S.dAq};
+    const int L1[9] = {kStages * kScal * kTD, kScal * kTD, kStages * m.nq * kTD, kStages * m.nq * kTD,
+                       m.nq * kTD, m.nq * kTD, m.nq * kTD, m.nq * kTD, m.nq * kTD};
+    for (int a = 0; a < 9; ++a)
+      for (int t = tid; t < L1[a]; t += nth) T1[a][t] = prand(t, 10 + a);
+    for (int t = tid; t < m.nq * kTD; t += nth) S.dBq[t] = prand(t, 19);
+    for (int t = tid; t < 8 * kTD; t += nth) S.cstn[t] = prand(t, 20);
+    __syncthreads();
+    double worst = 0.0;
+    for (int sl = 0; sl < 5; ++sl) {
+      double t1[kTD] = {0.0, 0.0, 0.0, 0.0}, t2[kTD] = {0.0, 0.0, 0.0, 0.0};
+      double* t4 = gu;  // kTD * N doubles: gu, gdu and the scratch after them
+      dA_dot(m, S, sl, u, lam, t4, t1, tid, nth);
+      coef_dot(m, S, sl, u, lam, t2, tid, nth);
+      for (int j = 0; j < kTD; ++j) {
+        const double a1 = warp_sum(t1[j]), a2 = warp_sum(t2[j]);
+        double mag = 0.0;
+        for (int i = tid; i < N; i += nth) mag += fabs(lam[i] * t4[j * N + i]);
+        mag = warp_sum(mag);
+        worst = fmax(worst, fabs(a1 - a2) / mag);
+      }
+      __syncthreads();
+    }
+    if (tid == 0) out[12] = worst;
+  }
   {  // P_lin gradient: quadratic in u, so the central difference is exact
     for (int i = tid; i < N; i += nth) gu[i] = 0.0;
     __syncthreads();
@@ -1512,7 +1551,7 @@ int launch_adjoint_check(const CosmoDev* d_cos, int id, double k, int lg, int ln
   adjoint_check_kernel<<<1, 32, smem, st>>>(md, d_cos, x, hs, d_scr, d_out);
   return cudaGetLastError();
 }
-size_t adjoint_check_scratch_bytes(int N) { return size_t(20) * N * sizeof(double); }
+size_t adjoint_check_scratch_bytes(int N) { return size_t(24) * N * sizeof(double); }
 
 // Persistent CTAs: the first wave takes modes blockIdx.x (modes arrive sorted
 // by decreasing cost, and consecutive blocks land on different SMs, so the

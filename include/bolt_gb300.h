@@ -153,6 +153,14 @@ int bolt_plin(bolt_ctx* ctx, int cosmo_id, const double* k, int nk, const bolt_h
  * integrator on every node.  Pass -INFINITY to land on every node. */
 int bolt_set_dense_x(bolt_ctx* ctx, double x_dense);
 
+/* Source grids at x >= x_dense: the integrator lands on every stride-th node
+ * (and the last) and takes the others from the same cubic Hermite dense
+ * output (0 or 1, the default: lands on every node; at most 64).  The
+ * reference samples its integrator's interpolant at every node
+ * (src/spectra.jl:6-42); stride 2 moves C_l by below 1e-5 relative at the
+ * served tolerances (the engine's land_stride is the same option). */
+int bolt_set_land_stride(bolt_ctx* ctx, int stride);
+
 /* Self-check of the discrete adjoint's building blocks (no counterpart in
  * the reference; the test suite's probe of the reverse sweep's pieces) on
  * one mode of cosmology id, wavenumber k and hierarchy h, at the Rosenbrock
@@ -170,8 +178,11 @@ int bolt_set_dense_x(bolt_ctx* ctx, double x_dense);
  *          of a central difference (exact for the quadratic P_lin);
  *   [10]   1 if the radiation-streaming switch is on at x, else 0;
  *   [11]   |lam.(M^-1 u) - (M^-T lam).u| / sum |lam_i (M^-1 u)_i|: the two
- *          solves are each other's transposes.
- * (12 doubles.)  Returns 0 or a negative code. */
+ *          solves are each other's transposes;
+ *   [12]   the parameter cotangent lam.(dA/dtheta u) from the coefficients'
+ *          cotangents against tangent-number arithmetic, on pseudo-random
+ *          coefficient tangents (largest relative difference).
+ * (13 doubles.)  Returns 0 or a negative code. */
 int bolt_adjoint_check(bolt_ctx* ctx, int id, double k, const bolt_hier* h, double x, double hstep, double* out);
 
 /* Counters of the last call: [0] accepted steps, [1] rejected steps,

@@ -15,7 +15,10 @@ smallest to the reference plin default (N = 473) and nq = 27:
   loses digits to cancellation in forming M x, whatever the solve);
 * the source and P_lin gradients against the functions at nodes the line of
   sight reads: S_T is linear in (u, du), 1e-13; P_lin is quadratic in u, a
-  central difference, 1e-9.
+  central difference, 1e-9;
+* the parameter cotangent from the coefficients' cotangents (one reverse
+  pass over hierarchy!'s coefficients) against tangent-number arithmetic
+  on pseudo-random coefficient tangents, 1e-12 of the terms' magnitude.
 """
 import numpy as np
 import pytest
@@ -54,6 +57,7 @@ def test_adjoint_building_blocks(ih, hier, k, x, hs):
     assert r[6] < 1e-10 and r[7] < 1e-10, r[6:8]
     assert r[8] < 1e-13, r[8]
     assert r[9] < 1e-9, r[9]
+    assert r[12] < 1e-12, r[12]
 
 
 def _par(h=0.69, wb=0.02254, wc=0.10976, n=0.96, A=2.1e-9, mnu=0.11):

@@ -128,6 +128,30 @@ def test_cl_served_hardest_request_vs_converged_oracle(fid):
     assert np.max(np.abs(te - f["te"])) < 1e-4 * np.max(np.abs(f["te"]))
 
 
+def test_cl_served_hardest_request_land_stride2_vs_converged_oracle(fid):
+    """The served setting of the benchmark: the engine landing on every 2nd
+    source node at x >= -8.5 (cubic Hermite dense output between), and the
+    drop-in with the same option, stay within the serving metric's 1e-4 of
+    the converged oracle on the hardest C_l request."""
+    par, bg, ih, orc = fid
+    f = _fixture("oracle_cl_l50_1024k")
+    ks, ells = f["ks"], f["ells"]
+    with B.Engine(lanes=1, land_stride=2) as eng:
+        r = eng.run(B.Request("cl", par, ks, hier=(50, 50, 10, 15), ells=ells, cl=("tt", "te", "ee"), **SERVED))
+    assert r.rc == 0, r.err
+    ctx = B.Context(land_stride=2)
+    ih2 = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg, ctx=ctx)
+    tt, te, ee, st = B.cl_all(ells, ih2, ks, 50, 50, 10, 15, **SERVED)
+    ih2.close()
+    ctx.close()
+    for c, (a, b) in {"tt": (r.cl["tt"], tt), "te": (r.cl["te"], te), "ee": (r.cl["ee"], ee)}.items():
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * np.max(np.abs(b)), err_msg=c)
+        if c == "te":
+            assert np.max(np.abs(a - f["te"])) < 1e-4 * np.max(np.abs(f["te"]))
+        else:
+            assert np.max(np.abs(a / f[c] - 1)) < 1e-4, c
+
+
 def _per_element(J, Jref, name):
     """Relative error of every element above 1e-3 of its parameter's peak."""
     worst = 0.0
