@@ -714,9 +714,10 @@ def run_batch(args):
     for d in warm:
         batch_dropin(B, ctx, d)
     sampler = clocks_sampler()
+    sample = reqs[:args.plain_sample] if args.plain_sample > 0 else reqs
     t0 = time.perf_counter()
-    calls = sum(batch_dropin(B, ctx, d) for d in reqs)
-    plain_s = time.perf_counter() - t0
+    calls = sum(batch_dropin(B, ctx, d) for d in sample)
+    plain_s = (time.perf_counter() - t0) * len(reqs) / len(sample)  # per-cosmology rate of the sample
     ctx.close()
     with B.Engine(device=0, land_stride=LAND_STRIDE, lanes=6, objective="throughput") as eng:
         for d in warm:
@@ -740,7 +741,7 @@ def run_batch(args):
            "config": {"workload": what + "; cosmologies from the box h 0.6-0.8, omega_b 0.019-0.025, omega_c 0.10-0.14, n_s 0.92-1.0, ln(1e10 A_s) 2.9-3.2, Sigma m_nu 0-0.3 eV, 64-1024 log k in [0.1,1000] H0, "
                                          "l_gamma = l_nu in {20,35,50}, l_mnu 10, nq 15; all submitted at once",
                       "reltol": RELTOL, "abstol": ABSTOL, "land_stride": LAND_STRIDE},
-           "plain": {"value": K / plain_s, "unit": "cosmologies/s", "calls": calls,
+           "plain": {"value": K / plain_s, "unit": "cosmologies/s", "calls": calls, "timed_cosmologies": len(sample),
                      "api": "drop-in C-ABI one cosmology per call (bolt_cl_pipeline TT, bolt_plin; Jacobians as "
                             "1 + 6 calls)"},
            "served_over_plain": plain_s / win,
@@ -821,6 +822,76 @@ def run_pipeline(args):
         dist.destroy_process_group()
 
 
+# ----------------------------------------------------------- trajectories --
+def run_trajectories(args):
+    """Trajectory configuration: perturbation trajectories of 100 log k in
+    [0.1, 1000] H0 on 1000 uniform x in [-20, 0] (l 20/20/10, nq 15, N = 233)
+    and P_lin(k) at z = 0, fiducial LCDM, reltol 1e-8 (abstol the reference's
+    default 1e-6), through the drop-in C ABI (bolt_boltsolve + bolt_plin,
+    the trajectories copied to the host); k-modes per second."""
+    rank, ws, dist = dist_init()
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    import bolt_gb300 as B
+    ctx = B.Context(device=local)
+    par = B.CosmoParams(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Y_p=0.24, N_nu=3.046,
+                        Sigma_m_nu=0.06 * B.mass_natural())
+    bg = B.Background(par)
+    ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg, ctx=ctx)
+    ks = B.log10_k(0.1 * bg.H0, 1000.0 * bg.H0, 100)
+    xo = np.linspace(-20.0, 0.0, 1000)
+    hier = (20, 20, 10, 15)
+    N = B.state_len(*hier)
+    rt, at = 1e-8, 1e-6
+
+    def step():
+        u, st = B.boltsolve_batch(ih, ks, xo, *hier, reltol=rt, abstol=at)
+        s1 = ctx.stats()
+        P = B.plin(ks, par, bg, ih, 15, 20, 20, 10, 0.0, rt, at)
+        s2 = ctx.stats()
+        return u, P, s1, s2
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(dist)
+    sampler = clocks_sampler()
+    t0 = time.perf_counter()
+    dev_us = steps = launches = 0
+    for _ in range(args.steps):
+        u, P, s1, s2 = step()
+        dev_us += s1["solver_us"] + s2["solver_us"]
+        steps += s1["accepted_steps"] + s1["rejected_steps"] + s2["accepted_steps"] + s2["rejected_steps"]
+        launches += s1["kernel_launches"] + s2["kernel_launches"]
+    torch.cuda.synchronize()
+    wall = max_over_ranks(time.perf_counter() - t0, dist)
+    clocks = clocks_summary(sampler)
+    peak = ctypes_peak(B._lib.load(), local)
+    dev_s = max_over_ranks(dev_us / 1e6, dist)
+    sol = steps * solver_flops_per_step(N, 15) / (dev_us / 1e6) / 1e12
+    if rank == 0:
+        out = {"metric": "k-mode trajectories + P_lin per second (drop-in, device time)",
+               "value": ws * args.steps * ks.size / dev_s, "unit": "modes/s", "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": "trajectories: fiducial LCDM, 100 log k in [0.1,1000] H0, 1000 uniform x in "
+                                      "[-20,0], l 20/20/10, nq 15 (N=233), and P_lin(k) at z = 0 on the same k; "
+                                      "one step = bolt_boltsolve + bolt_plin", "reltol": rt, "abstol": at,
+                          "parallelism": f"replicas x{ws}"},
+               "e2e": {"value": ws * args.steps * ks.size / wall, "unit": "modes/s",
+                       "h2d_bytes_per_step": int(ks.size * 8 * 2 + xo.size * 8),
+                       "d2h_bytes_per_step": int(u.nbytes + P.nbytes)},
+               "clocks": clocks, "gpu_launches": launches,
+               "roofline": {"bound": "fp64", "achieved": sol, "peak": peak, "unit": "TFLOP/s",
+                            "frac": sol / peak if peak else None, "traffic": None, "kernel": "rodas_kernel",
+                            "note": "algorithmic solver FLOPs of the accepted + rejected steps / solver "
+                                    "CUDA-event time", "steps_per_step": steps / args.steps}}
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def ctypes_peak(lib, dev):
     import ctypes as C
     v = C.c_double(0.0)
@@ -834,7 +905,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20, help="timed requests (serving) or spectra (pipeline)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="serving", choices=["serving", "pipeline", "batch", "grad"])
+    ap.add_argument("--workload", default="serving", choices=["serving", "pipeline", "batch", "grad", "trajectories"])
+    ap.add_argument("--plain-sample", type=int, default=0,
+                    help="batch / grad: time the plain drop-in on the first N cosmologies only (0: all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweep", dest="sweep", action="store_false", help="serving: skip the arrival-rate sweep")
     ap.add_argument("--grad-requests", type=int, default=6, help="serving: size of the C_l+gradient-only stream")
@@ -852,6 +925,8 @@ def main():
         run_reference(args)
     elif args.workload == "pipeline":
         run_pipeline(args)
+    elif args.workload == "trajectories":
+        run_trajectories(args)
     elif args.workload in ("batch", "grad"):
         run_batch(args)
     else:

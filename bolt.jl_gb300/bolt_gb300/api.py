@@ -492,8 +492,8 @@ def adjoint_check(ih: IonizationHistory, k: float, x: float, hstep: float, lg=8,
     transposed, [6] the transposed solve, [7] the forward solve, [8] the
     source gradient, [9] the P_lin gradient, [10] the streaming switch,
     [11] the two solves as each other's transposes, [12] the coefficient
-    cotangents against tangent arithmetic."""
-    out = np.zeros(13)
+    cotangents against tangent arithmetic, [13] the same for d/dx."""
+    out = np.zeros(14)
     c = ih.ctx
     c.check(c.lib.bolt_adjoint_check(c.h, ih.cosmo_id, float(k), C.byref(_hier(lg, lnu, lmnu, nq)), float(x),
                                      float(hstep), L.dptr(out)), "bolt_adjoint_check")

@@ -425,44 +425,64 @@ __device__ __forceinline__ void dA_dot(const Mode& m, const Shared& S, int sl, c
 // slot sl, the momentum-bin constants and the cosmology constants -- each
 // cotangent times its tangents (S.sct, S.qet, S.eqt, S.dq, S.dAq, S.ddf0,
 // S.cstn).  One pass whatever the number of directions; the same products
-// as dA_dot.  Every thread adds its own rows' share (the metric's share on
-// lane 0 and the momentum bins' on their lanes).  One warp.
+// as dA_dot.  T = dd (slot 0): rb . (dA'_0 u), the tangents of the
+// x-derivative: with coefficients c carrying c' = dc/dx, each cotangent
+// cbar = (d(rb.A u)/dc, its x-derivative) contributes cbar' dc + cbar dc'
+// (dc' the tangents of c', S.sct_d / S.qet_d / S.eqt_d; the momentum-bin
+// and cosmology constants do not depend on x).  Every thread adds its own
+// rows' share (the metric's share on lane 0 and the momentum bins' on their
+// lanes).  One warp.
+template <class T>
+__device__ __forceinline__ void addc(double* tb, const T& bar, const double* t0, const double* td);
+template <>
+__device__ __forceinline__ void addc<double>(double* tb, const double& bar, const double* t0, const double*) {
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) tb[j] = fma(bar, t0[j], tb[j]);
+}
+template <>
+__device__ __forceinline__ void addc<dd>(double* tb, const dd& bar, const double* t0, const double* td) {
+#pragma unroll
+  for (int j = 0; j < kTD; ++j) tb[j] = fma(bar.d, t0[j], td ? fma(bar.v, td[j], tb[j]) : tb[j]);
+}
+
+template <class T>
 __device__ void coef_dot(const Mode& m, const Shared& S, int sl, const double* u, const double* rb, double* tb,
                          int tid, int nth) {
   const int lane = tid & 31;
   const int nq = m.nq, lg = m.lg, lnu = m.lnu, lmnu = m.lmnu;
-  const Scal<double> s = get_scal<double>(S, sl);
+  const bool X = sizeof(T) != sizeof(double);  // the x-derivative variant (slot 0)
+  const Scal<T> s = get_scal<T>(S, sl);
   const bool rsa = rsa_switch(m, s);
   const double* cl1 = S.cl1;
   const double* cl2 = S.cl2;
   const CosmoDev& C = *m.C;
   const double Omega_nu = C.Omega_nu;
-  const double* qe = S.qe + sl * nq;
-  const double* eq = S.eq + sl * nq;
+  const T zero = cst<T>(0.0);
   // the metric's values, as metric() forms them
-  double rho = 0.0, sig = 0.0;
+  T rho = zero, sig = zero;
   for (int q = lane; q < nq; q += 32) {
-    rho = rho + (S.Aq[q] * S.q[q]) * eq[q] * u[m.iM + q];
-    sig = sig + (S.Aq[q] * S.q[q]) * qe[q] * u[m.iM + 2 * nq + q];
+    rho = rho + (S.Aq[q] * S.q[q]) * eq_of<T>(S, sl, nq, q) * u[m.iM + q];
+    sig = sig + (S.Aq[q] * S.q[q]) * qe_of<T>(S, sl, nq, q) * u[m.iM + 2 * nq + q];
   }
-  rho = warp_sum(rho);
-  sig = warp_sum(sig);
+  rho = warp_sum_t<T>(rho);
+  sig = warp_sum_t<T>(sig);
   const double rc0 = cos_const(C, 0), rc1 = cos_const(C, 1), Oc = cos_const(C, 2), Ob = cos_const(C, 3);
   const double Phi = u[m.iPhi];
-  const double Psi = -Phi - s.cpsi * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig * rc0);
-  const double ia = 1.0 / s.a;
+  const T Psi = -Phi - s.cpsi * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig * rc0);
+  const T ia = 1.0 / s.a;
   const double X1 = Oc * u[m.iPhi + 1] + Ob * u[m.iPhi + 3];
-  const double X2 = 4.0 * C.Omega_r * u[0] + 4.0 * Omega_nu * u[m.iN] + rho * rc1;
-  const double Phip = Psi - s.k2H2 * Phi + s.dphi * (X1 * ia + X2 * (ia * ia));
+  const T X2 = 4.0 * C.Omega_r * u[0] + 4.0 * Omega_nu * u[m.iN] + rho * rc1;
+  const T Phip = Psi - s.k2H2 * Phi + s.dphi * (X1 * ia + X2 * (ia * ia));
   const double Pi = u[2] + u[m.iTp + 2] + u[m.iTp];
   const double vb = u[m.iPhi + 4];
+  // tangents of slot sl's scalars and of their x-derivatives (slot 0)
+  const double* st = S.sct + (sl * kScal) * kTD;
+  const double* sd = X ? S.sct_d : nullptr;
+  auto sct = [&](int f) { return st + f * kTD; };
+  auto scd = [&](int f) { return X ? sd + f * kTD : nullptr; };
   // ---- rows: cotangents of the scalars (this thread's share), of Psi and
   // Phi', and the momentum-bin ones added at once
-  double bkH = 0.0, btp = 0.0, biHe = 0.0, bcs2 = 0.0, bR = 0.0, bPsi = 0.0, bPhip = 0.0;
-  auto add_q = [&](const double* t, int idx, double bar) {  // tb[j] += bar * t[idx * kTD + j]
-#pragma unroll
-    for (int j = 0; j < kTD; ++j) tb[j] = fma(bar, t[idx * kTD + j], tb[j]);
-  };
+  T bkH = zero, btp = zero, biHe = zero, bcs2 = zero, bR = zero, bPsi = zero, bPhip = zero;
   for (int i = tid; i < m.N; i += nth) {
     const double r = rb[i];
     if (i < m.iM) {
@@ -472,125 +492,111 @@ __device__ void coef_dot(const Mode& m, const Shared& S, int sl, const double* u
         const int b0 = P ? m.iTp : 0, l = i - b0;
         if (l < lg) {
           const double lo = l > 0 ? u[b0 + l - 1] : 0.0;
-          bkH += r * (cl1[l] * lo - cl2[l] * u[b0 + l + 1]);
-          if (P || l >= 1) btp += r * u[i];
+          bkH = bkH + r * (cl1[l] * lo - cl2[l] * u[b0 + l + 1]);
+          if (P || l >= 1) btp = btp + r * u[i];
           if (!P) {
-            if (l == 0) bPhip -= r;
-            if (l == 1) { bkH += r * (Psi / 3.0); bPsi += r * (s.kH / 3.0); btp += r * (vb / 3.0); }
-            if (l == 2) btp -= r * (Pi / 10.0);
+            if (l == 0) bPhip = bPhip - r;
+            if (l == 1) { bkH = bkH + r * (Psi / 3.0); bPsi = bPsi + r * (s.kH / 3.0); btp = btp + r * (vb / 3.0); }
+            if (l == 2) btp = btp - r * (Pi / 10.0);
           } else {
-            if (l == 0) btp -= r * (Pi / 2.0);
-            if (l == 2) btp -= r * (Pi / 10.0);
+            if (l == 0) btp = btp - r * (Pi / 2.0);
+            if (l == 2) btp = btp - r * (Pi / 10.0);
           }
         } else {
-          bkH += r * u[b0 + lg - 1];
-          biHe -= r * (lg + 1.0) * u[i];
-          btp += r * u[i];
+          bkH = bkH + r * u[b0 + lg - 1];
+          biHe = biHe - r * (lg + 1.0) * u[i];
+          btp = btp + r * u[i];
         }
       } else {  // massless neutrinos
         const int l = i - m.iN, b0 = m.iN;
         if (l < lnu) {
           const double lo = l > 0 ? u[b0 + l - 1] : 0.0;
-          bkH += r * (cl1[l] * lo - cl2[l] * u[b0 + l + 1]);
-          if (l == 0) bPhip -= r;
-          if (l == 1) { bkH += r * (Psi / 3.0); bPsi += r * (s.kH / 3.0); }
+          bkH = bkH + r * (cl1[l] * lo - cl2[l] * u[b0 + l + 1]);
+          if (l == 0) bPhip = bPhip - r;
+          if (l == 1) { bkH = bkH + r * (Psi / 3.0); bPsi = bPsi + r * (s.kH / 3.0); }
         } else {
-          bkH += r * u[b0 + lnu - 1];
-          biHe -= r * (lnu + 1.0) * u[i];
+          bkH = bkH + r * u[b0 + lnu - 1];
+          biHe = biHe - r * (lnu + 1.0) * u[i];
         }
       }
     } else if (i < m.iPhi) {  // massive neutrinos
       const int jm = i - m.iM;
       const int l = jm / nq, q = jm - l * nq;
       const int iq = sl * nq + q;
+      const T qe = qe_of<T>(S, sl, nq, q), eq = eq_of<T>(S, sl, nq, q);
+      const double* qet = S.qet + iq * kTD;
+      const double* qetd = X ? S.qet_d + q * kTD : nullptr;
+      const double* eqt = S.eqt + iq * kTD;
+      const double* eqtd = X ? S.eqt_d + q * kTD : nullptr;
+      const double df0 = S.df0[q];
       if (l < lmnu) {
         const double lo = l > 0 ? u[i - nq] : 0.0;
         const double B = cl1[l] * lo - cl2[l] * u[i + nq];
-        bkH += r * qe[q] * B;
-        add_q(S.qet, iq, r * s.kH * B);
+        bkH = bkH + r * qe * B;
+        addc<T>(tb, r * s.kH * B, qet, qetd);
         if (l == 0) {
-          bPhip += r * S.df0[q];
-          add_q(S.ddf0, q, r * Phip);
+          bPhip = bPhip + r * df0;
+          addc<T>(tb, r * Phip, S.ddf0 + q * kTD, nullptr);
         }
         if (l == 1) {
           const double c = r * (1.0 / 3.0);
-          bkH -= c * eq[q] * Psi * S.df0[q];
-          add_q(S.eqt, iq, -c * s.kH * Psi * S.df0[q]);
-          bPsi -= c * s.kH * eq[q] * S.df0[q];
-          add_q(S.ddf0, q, -c * s.kH * eq[q] * Psi);
+          bkH = bkH - c * eq * Psi * df0;
+          addc<T>(tb, -c * s.kH * Psi * df0, eqt, eqtd);
+          bPsi = bPsi - c * s.kH * eq * df0;
+          addc<T>(tb, -c * s.kH * eq * Psi, S.ddf0 + q * kTD, nullptr);
         }
       } else {
         const double lo = u[i - nq];
-        add_q(S.qet, iq, r * s.kH * lo);
-        bkH += r * qe[q] * lo;
-        biHe -= r * (lmnu + 1.0) * u[i];
+        addc<T>(tb, r * s.kH * lo, qet, qetd);
+        bkH = bkH + r * qe * lo;
+        biHe = biHe - r * (lmnu + 1.0) * u[i];
       }
     } else {  // metric and matter
       const int rr = i - m.iPhi;
-      if (rr == 0) bPhip += r;
-      else if (rr == 1) { bkH += r * u[m.iPhi + 2]; bPhip -= 3.0 * r; }
-      else if (rr == 2) { bkH -= r * Psi; bPsi -= r * s.kH; }
-      else if (rr == 3) { bkH += r * vb; bPhip -= 3.0 * r; }
+      if (rr == 0) bPhip = bPhip + r;
+      else if (rr == 1) { bkH = bkH + r * u[m.iPhi + 2]; bPhip = bPhip - 3.0 * r; }
+      else if (rr == 2) { bkH = bkH - r * Psi; bPsi = bPsi - r * s.kH; }
+      else if (rr == 3) { bkH = bkH + r * vb; bPhip = bPhip - 3.0 * r; }
       else {
         const double d = u[m.iPhi + 3];
-        bkH -= r * (Psi + s.cs2 * d);
-        bPsi -= r * s.kH;
-        bcs2 -= r * s.kH * d;
-        btp += r * s.R * (3.0 * u[1] + vb);
-        bR += r * s.tp * (3.0 * u[1] + vb);
+        bkH = bkH - r * (Psi + s.cs2 * d);
+        bPsi = bPsi - r * s.kH;
+        bcs2 = bcs2 - r * s.kH * d;
+        btp = btp + r * s.R * (3.0 * u[1] + vb);
+        bR = bR + r * s.tp * (3.0 * u[1] + vb);
       }
     }
   }
   // the scalars' cotangents (this thread's share) times their tangents
-  {
-    const double* st = S.sct + (sl * kScal) * kTD;
-#pragma unroll
-    for (int j = 0; j < kTD; ++j) {
-      double acc = tb[j];
-      acc = fma(bkH, st[5 * kTD + j], acc);
-      acc = fma(btp, st[2 * kTD + j], acc);
-      acc = fma(biHe, st[6 * kTD + j], acc);
-      acc = fma(bcs2, st[3 * kTD + j], acc);
-      acc = fma(bR, st[7 * kTD + j], acc);
-      tb[j] = acc;
-    }
-  }
+  addc<T>(tb, bkH, sct(5), scd(5));
+  addc<T>(tb, btp, sct(2), scd(2));
+  addc<T>(tb, biHe, sct(6), scd(6));
+  addc<T>(tb, bcs2, sct(3), scd(3));
+  addc<T>(tb, bR, sct(7), scd(7));
   // ---- the metric, backwards: Phi' = Psi - k2H2 Phi + dphi (X1 ia + X2 ia^2),
   // Psi = -Phi - cpsi (Omega_r Theta_2 + Omega_nu N_2 + sigma rc0)
-  bPhip = warp_sum(bPhip);
-  bPsi = warp_sum(bPsi) + bPhip;
-  const double brho = bPhip * s.dphi * (ia * ia) * rc1;
-  const double bsig = -bPsi * s.cpsi * rc0;
+  bPhip = warp_sum_t<T>(bPhip);
+  bPsi = warp_sum_t<T>(bPsi) + bPhip;
+  const T brho = bPhip * s.dphi * (ia * ia) * rc1;
+  const T bsig = -bPsi * s.cpsi * rc0;
   if (lane == 0) {
-    const double* st = S.sct + (sl * kScal) * kTD;
-    const double bk2H2 = -bPhip * Phi;
-    const double bdphi = bPhip * (X1 * ia + X2 * (ia * ia));
-    const double bia = bPhip * s.dphi * (X1 + 2.0 * X2 * ia);
-    const double ba = -bia * (ia * ia);
-    const double bcpsi = -bPsi * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig * rc0);
-    const double bOc = bPhip * s.dphi * ia * u[m.iPhi + 1], bOb = bPhip * s.dphi * ia * u[m.iPhi + 3];
-    const double brc1 = bPhip * s.dphi * (ia * ia) * rho, brc0 = -bPsi * s.cpsi * sig;
-#pragma unroll
-    for (int j = 0; j < kTD; ++j) {
-      double acc = tb[j];
-      acc = fma(bk2H2, st[10 * kTD + j], acc);
-      acc = fma(bdphi, st[9 * kTD + j], acc);
-      acc = fma(ba, st[4 * kTD + j], acc);
-      acc = fma(bcpsi, st[8 * kTD + j], acc);
-      acc = fma(brc0, S.cstn[0 * kTD + j], acc);
-      acc = fma(brc1, S.cstn[1 * kTD + j], acc);
-      acc = fma(bOc, S.cstn[2 * kTD + j], acc);
-      acc = fma(bOb, S.cstn[3 * kTD + j], acc);
-      tb[j] = acc;
-    }
+    addc<T>(tb, -bPhip * Phi, sct(10), scd(10));                                    // k2H2
+    addc<T>(tb, bPhip * (X1 * ia + X2 * (ia * ia)), sct(9), scd(9));                // dphi
+    addc<T>(tb, -(bPhip * s.dphi * (X1 + 2.0 * X2 * ia)) * (ia * ia), sct(4), scd(4));  // a, through 1/a
+    addc<T>(tb, -bPsi * (C.Omega_r * u[2] + Omega_nu * u[m.iN + 2] + sig * rc0), sct(8), scd(8));  // cpsi
+    addc<T>(tb, -bPsi * s.cpsi * sig, S.cstn + 0 * kTD, nullptr);                  // 0.25 / rho_crit
+    addc<T>(tb, bPhip * s.dphi * (ia * ia) * rho, S.cstn + 1 * kTD, nullptr);       // 1 / rho_crit
+    addc<T>(tb, bPhip * s.dphi * ia * u[m.iPhi + 1], S.cstn + 2 * kTD, nullptr);    // Omega_c
+    addc<T>(tb, bPhip * s.dphi * ia * u[m.iPhi + 3], S.cstn + 3 * kTD, nullptr);    // Omega_b
   }
   for (int q = lane; q < nq; q += 32) {  // rho = sum Aq q eq M_0q, sigma = sum Aq q qe M_2q
     const double m0 = u[m.iM + q], m2 = u[m.iM + 2 * nq + q];
     const double Aq = S.Aq[q], qq = S.q[q];
-    add_q(S.dAq, q, brho * qq * eq[q] * m0 + bsig * qq * qe[q] * m2);
-    add_q(S.dq, q, brho * Aq * eq[q] * m0 + bsig * Aq * qe[q] * m2);
-    add_q(S.eqt, sl * nq + q, brho * Aq * qq * m0);
-    add_q(S.qet, sl * nq + q, bsig * Aq * qq * m2);
+    const T qe = qe_of<T>(S, sl, nq, q), eq = eq_of<T>(S, sl, nq, q);
+    addc<T>(tb, brho * qq * eq * m0 + bsig * qq * qe * m2, S.dAq + q * kTD, nullptr);
+    addc<T>(tb, brho * Aq * eq * m0 + bsig * Aq * qe * m2, S.dq + q * kTD, nullptr);
+    addc<T>(tb, brho * Aq * qq * m0, S.eqt + (sl * nq + q) * kTD, X ? S.eqt_d + q * kTD : nullptr);
+    addc<T>(tb, bsig * Aq * qq * m2, S.qet + (sl * nq + q) * kTD, X ? S.qet_d + q * kTD : nullptr);
   }
 }
 
@@ -685,8 +691,8 @@ __device__ void adjoint_step(const Mode& m, const Shared& S, const Pack& PK, con
       }
     }
     __syncthreads();
-    coef_dot(m, S, sl, S.yt, S.b, tb, tid, nth);         // rbar . dA_sl Y_st
-    coef_dot(m, S, 0, G.K + st * N, S.b, tb, tid, nth);  // rbar . dA_0 K_st (M depends on A_0)
+    coef_dot<double>(m, S, sl, S.yt, S.b, tb, tid, nth);         // rbar . dA_sl Y_st
+    coef_dot<double>(m, S, 0, G.K + st * N, S.b, tb, tid, nth);  // rbar . dA_0 K_st (M depends on A_0)
     const double hd = hs * rodas::kD[st];
     for (int i = tid; i < N; i += nth) {
       const double rb = S.b[i];
@@ -711,14 +717,8 @@ __device__ void adjoint_step(const Mode& m, const Shared& S, const Pack& PK, con
     Sink o;
     o.v = A.tmp; o.d = A.gu; o.t = nullptr; o.td = nullptr; o.N = N;
     rhs_cols<dd>(m, S, 0, A.Fb, o, tid, nth);  // A.gu = A'_0^T Fbar
-    Sink x;
-    x.v = A.tmp; x.d = nullptr; x.t = A.t4; x.td = A.t4b; x.N = N;
-    rhs_rows<x4>(m, S, 0, StC{G.y}, x, tid, nth);  // t4b = dA'_0 y
-    for (int i = tid; i < N; i += nth) {
-      A.lam[i] = A.yb[i] + A.gu[i];
-#pragma unroll
-      for (int j = 0; j < kTD; ++j) tb[j] = fma(A.Fb[i], A.t4b[j * N + i], tb[j]);
-    }
+    coef_dot<dd>(m, S, 0, G.y, A.Fb, tb, tid, nth);  // Fbar . dA'_0 y
+    for (int i = tid; i < N; i += nth) A.lam[i] = A.yb[i] + A.gu[i];
   }
   __syncthreads();
 }
@@ -745,7 +745,7 @@ __device__ void adjoint_seed(const Mode& m, const Shared& S, const AdjScratch& A
     // partials at fixed state, S_T(u, du) with du = A u: those of the
     // source's own coefficients, and (sbT dS/d(du)) . dA u from the
     // hierarchy's coefficient cotangents
-    coef_dot(m, S, sl, A.u1, A.gdu, tb, tid, nth);
+    coef_dot<double>(m, S, sl, A.u1, A.gdu, tb, tid, nth);
     rhs_rows<double>(m, S, sl, StP{A.u1}, sink(A.du), tid, nth);
     __syncthreads();
     if (warp == 0) {

@@ -766,7 +766,7 @@ int bolt_adjoint_check(bolt_ctx* c, int id, double k, const bolt_hier* h, double
     ck(cudaMemcpyAsync(o, d_out, 16 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "out");
     ck(cudaStreamSynchronize(c->stream), "sync");
     if (o[15] < 0.0) throw Err(-1, "hierarchy does not fit the solver's lane packing");
-    std::copy(o, o + 13, out);
+    std::copy(o, o + 14, out);
   });
 }
 

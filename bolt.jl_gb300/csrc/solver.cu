@@ -104,19 +104,27 @@ __host__ __device__ inline int tan_doubles(int N, int nq) {
 }
 // An adjoint mode (adjoint.cuh) keeps the coefficient tangents but neither
 // the tangent stage vectors nor the tangent solves' partials.
-__host__ __device__ inline int adj_doubles(int N, int nq) { return tan_doubles(N, nq) - 2 * kTD * N - 32 * kBorder * kTD; }
+// The coefficient tangents of a tangent or adjoint mode (the first part of
+// tan_doubles()).  An adjoint mode keeps them in its global slab (read
+// through L1), not in shared memory, so that as many adjoint CTAs fit an SM
+// as plain ones; it needs neither the tangent stage vectors nor the tangent
+// solves' partials.
+__host__ __device__ inline int coef_tan_doubles(int nq) {
+  return (kStages + 1) * kScal * kTD + 2 * (kStages + 1) * nq * kTD + 5 * nq * kTD + 8 * kTD;
+}
+constexpr int kCoefTanMax = (kStages + 1) * kScal * kTD + 2 * (kStages + 1) * 27 * kTD + 5 * 27 * kTD + 8 * kTD;
 // Kernel kinds: 0 plain (and recorded / replayed / checkpointed) modes,
 // 1 tangent-linear modes, 2 adjoint (reverse-sweep) modes.
 __host__ __device__ inline int per_mode_doubles(int N, int nq, int Lmax, int threads, int kind = 0) {
   int nch = nq + 5;
   return 5 * N + 4 * nq + 2 * kStages * nq + 2 * nq + 2 * nch * kTail * kBorder + 2 * (Lmax + 1) + kStages * kScal +
-         kScal + kMiscDoubles + (kind == 1 ? tan_doubles(N, nq) : (kind == 2 ? adj_doubles(N, nq) : 0)) +
+         kScal + kMiscDoubles + (kind == 1 ? tan_doubles(N, nq) : 0) +
          (pack_ints(threads) + 1) / 2;
 }
 // Global scratch of an adjoint mode after the base slab (adjoint.cuh).
 __host__ __device__ inline int adj_scratch_doubles(int N) { return (15 + 2 * kTD + 7 * kCkptEvery + 1) * N; }
 __host__ __device__ inline int scratch_per_warp(int N, int kind = 0) {
-  return 10 * N + (kind == 1 ? 9 * kTD * N : (kind == 2 ? adj_scratch_doubles(N) : 0));
+  return 10 * N + (kind == 1 ? 9 * kTD * N : (kind == 2 ? adj_scratch_doubles(N) + kCoefTanMax : 0));
 }
 
 struct Mode {
@@ -834,7 +842,9 @@ __device__ bool setup_mode(const ModeDev& md, const CosmoDev* cosmos, double* ba
   S.sc_d = p; p += kScal;
   S.misc = p;                 // [0..8] capacitance inverse, [16..23] block reductions, [24] flags, [32..] partials
   p += kMiscDoubles;
-  if (KIND) {  // the layout tan_doubles() / adj_doubles() size
+  if (KIND) {  // the layout tan_doubles() sizes (adjoint: in the global slab, after its scratch)
+    double* keep = p;
+    if (KIND == 2) p = gscr + 10 * N + adj_scratch_doubles(N);
     S.sct = p; p += kStages * kScal * kTD;
     S.sct_d = p; p += kScal * kTD;
     S.qet = p; p += kStages * nq * kTD;
@@ -851,6 +861,8 @@ __device__ bool setup_mode(const ModeDev& md, const CosmoDev* cosmos, double* ba
       S.part4 = p; p += 32 * kBorder * kTD;
       S.yd = p; p += kTD * N;
       S.bd = p; p += kTD * N;
+    } else {
+      p = keep;
     }
   }
   {
@@ -1351,7 +1363,8 @@ __device__ void adjoint_one(const ModeDev& md, const CosmoDev* cosmos, double* b
 // (plin_grad, P quadratic in u); out[10] = 1 if the streaming switch is on;
 // out[11] = |lam.(M^-1 u) - (M^-T lam).u| / sum |lam_i (M^-1 u)_i|;
 // out[12] = the largest over the stage slots and tangent directions of
-// |coef_dot - dA_dot| / sum_i |lam_i (dA u)_i| on pseudo-random tangents.
+// |coef_dot - dA_dot| / sum_i |lam_i (dA u)_i| on pseudo-random tangents;
+// out[13] the same for the x-derivative variant against x4 arithmetic.
 __device__ __forceinline__ double prand(int i, int seed) {
   unsigned x = unsigned(i) * 2654435761u ^ (unsigned(seed) * 40503u + 12345u);
   x ^= x >> 13;
@@ -1499,7 +1512,7 @@ __global__ void __launch_bounds__(32) adjoint_check_kernel(ModeDev md, const Cos
       double t1[kTD] = {0.0, 0.0, 0.0, 0.0}, t2[kTD] = {0.0, 0.0, 0.0, 0.0};
       double* t4 = gu;  // kTD * N doubles: gu, gdu and the scratch after them
       dA_dot(m, S, sl, u, lam, t4, t1, tid, nth);
-      coef_dot(m, S, sl, u, lam, t2, tid, nth);
+      coef_dot<double>(m, S, sl, u, lam, t2, tid, nth);
       for (int j = 0; j < kTD; ++j) {
         const double a1 = warp_sum(t1[j]), a2 = warp_sum(t2[j]);
         double mag = 0.0;
@@ -1510,6 +1523,27 @@ __global__ void __launch_bounds__(32) adjoint_check_kernel(ModeDev md, const Cos
       __syncthreads();
     }
     if (tid == 0) out[12] = worst;
+    // the x-derivative variant against x4 arithmetic: lam . (dA'_0 u)
+    {
+      double t2[kTD] = {0.0, 0.0, 0.0, 0.0};
+      Sink o;
+      o.v = w1; o.d = nullptr; o.t = gu; o.td = gu + kTD * N; o.N = N;
+      rhs_rows<x4>(m, S, 0, StC{u}, o, tid, nth);
+      coef_dot<dd>(m, S, 0, u, lam, t2, tid, nth);
+      double wx = 0.0;
+      for (int j = 0; j < kTD; ++j) {
+        double a1 = 0.0, mag = 0.0;
+        for (int i = tid; i < N; i += nth) {
+          a1 += lam[i] * o.td[j * N + i];
+          mag += fabs(lam[i] * o.td[j * N + i]);
+        }
+        a1 = warp_sum(a1);
+        mag = warp_sum(mag);
+        wx = fmax(wx, fabs(a1 - warp_sum(t2[j])) / mag);
+      }
+      if (tid == 0) out[13] = wx;
+    }
+    __syncthreads();
   }
   {  // P_lin gradient: quadratic in u, so the central difference is exact
     for (int i = tid; i < N; i += nth) gu[i] = 0.0;
@@ -1551,7 +1585,7 @@ int launch_adjoint_check(const CosmoDev* d_cos, int id, double k, int lg, int ln
   adjoint_check_kernel<<<1, 32, smem, st>>>(md, d_cos, x, hs, d_scr, d_out);
   return cudaGetLastError();
 }
-size_t adjoint_check_scratch_bytes(int N) { return size_t(24) * N * sizeof(double); }
+size_t adjoint_check_scratch_bytes(int N) { return size_t(scratch_per_warp(N, 2) + 8 * N) * sizeof(double); }
 
 // Persistent CTAs: the first wave takes modes blockIdx.x (modes arrive sorted
 // by decreasing cost, and consecutive blocks land on different SMs, so the

@@ -181,8 +181,9 @@ int bolt_set_land_stride(bolt_ctx* ctx, int stride);
  *          solves are each other's transposes;
  *   [12]   the parameter cotangent lam.(dA/dtheta u) from the coefficients'
  *          cotangents against tangent-number arithmetic, on pseudo-random
- *          coefficient tangents (largest relative difference).
- * (13 doubles.)  Returns 0 or a negative code. */
+ *          coefficient tangents (largest relative difference);
+ *   [13]   the same for lam.(d(dA/dx)/dtheta u).
+ * (14 doubles.)  Returns 0 or a negative code. */
 int bolt_adjoint_check(bolt_ctx* ctx, int id, double k, const bolt_hier* h, double x, double hstep, double* out);
 
 /* Counters of the last call: [0] accepted steps, [1] rejected steps,

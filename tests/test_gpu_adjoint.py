@@ -57,7 +57,7 @@ def test_adjoint_building_blocks(ih, hier, k, x, hs):
     assert r[6] < 1e-10 and r[7] < 1e-10, r[6:8]
     assert r[8] < 1e-13, r[8]
     assert r[9] < 1e-9, r[9]
-    assert r[12] < 1e-12, r[12]
+    assert r[12] < 1e-12 and r[13] < 1e-12, r[12:14]
 
 
 def _par(h=0.69, wb=0.02254, wc=0.10976, n=0.96, A=2.1e-9, mnu=0.11):
