@@ -157,7 +157,7 @@ __device__ void wsolve_scan_T(const Mode& m, const Shared& S, const Pack& P, dou
   const int own_c = (tid == P.E[1]) ? 3 + m.nq : ((c >= 0 && P.owner[c] == tid) ? c : -1);
   const int own_c2 = (tid == P.E[1]) ? 4 + m.nq : -1;
   const int idb = m.iPhi + 3, ivb = m.iPhi + 4;
-  const int* idx = P.idx + tid * P.em;
+  const LaneIdx idx = lane_idx(P, tid);
   int cnt = 0;
   if (c >= 0)
     for (int e = 0; e < E; ++e) {
@@ -171,8 +171,8 @@ __device__ void wsolve_scan_T(const Mode& m, const Shared& S, const Pack& P, dou
     segend = l2;
   }
   // fc of the element before this lane's first, fl of the one after its last
-  const double fc_in = (c >= 0 && lane > seg) ? S.fc[P.idx[(tid - 1) * P.em + E - 1]] : 0.0;
-  const double fl_out = (c >= 0 && lane < segend) ? S.fl[P.idx[(tid + 1) * P.em]] : 0.0;
+  const double fc_in = (c >= 0 && lane > seg) ? S.fc[P.idx[(E - 1) * P.nt + tid - 1]] : 0.0;
+  const double fl_out = (c >= 0 && lane < segend) ? S.fl[P.idx[tid + 1]] : 0.0;
   // ---- forward (U^T): v_j = b_j - fc_{j-1} v_{j-1}; the baryon pair (delta_b,
   // v_b, eliminated before Theta_1) folds into Theta_1's right-hand side
   double A = 1.0, B = 0.0;

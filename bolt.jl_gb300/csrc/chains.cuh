@@ -27,11 +27,22 @@ constexpr int kMaxChains = 32;
 struct Pack {
   int* seg;      // [threads] segment start lane within the warp, -1 = idle lane
   int* chain;    // [threads] chain id of the lane
-  int* idx;      // [threads][em] state indices in elimination order, -1 = pad (at the end)
+  int* idx;      // [em][threads] state indices in elimination order, -1 = pad (at the end); element e of
+                 // thread t at idx[e * nt + t], so a warp reading its lanes' e-th elements touches 32
+                 // consecutive words (no bank conflicts)
   int* owner;    // [kMaxChains] thread holding the chain's l = 0 element
   int* E;        // [0] elements per lane, [1] thread for the CDM pair + Phi, [2] lanes of the longest segment
   int em;        // largest elements per lane (kLaneElems / threads)
+  int nt;        // threads
 };
+
+// Thread tid's element list, read as idx[e].
+struct LaneIdx {
+  const int* p;
+  int s;
+  __device__ __forceinline__ int operator[](int e) const { return p[e * s]; }
+};
+__device__ __forceinline__ LaneIdx lane_idx(const Pack& P, int tid) { return LaneIdx{P.idx + tid, P.nt}; }
 
 struct ChainDesc {
   int L, base, stride;  // top multipole, state index of l = 0, index stride
@@ -71,7 +82,7 @@ __device__ bool build_pack(const Mode& m, const Pack& P, int nthreads) {
     for (int t = 0; t < nthreads; ++t) {
       P.seg[t] = -1;
       P.chain[t] = -1;
-      for (int e = 0; e < P.em; ++e) P.idx[t * P.em + e] = -1;
+      for (int e = 0; e < P.em; ++e) P.idx[e * nthreads + t] = -1;
     }
     for (int c = 0; c < nc; ++c) {
       ChainDesc d = chain_desc(m, c);
@@ -82,7 +93,7 @@ __device__ bool build_pack(const Mode& m, const Pack& P, int nthreads) {
         P.chain[t] = c;
         for (int e = 0; e < E; ++e) {
           int j = g * E + e;
-          if (j < len) P.idx[t * P.em + e] = d.base + (d.L - j) * d.stride;
+          if (j < len) P.idx[e * nthreads + t] = d.base + (d.L - j) * d.stride;
         }
       }
       P.owner[c] = t0 + (len - 1) / E;
@@ -273,7 +284,7 @@ __device__ bool factorize_scan(const Mode& m, const Shared& S, const Pack& P, do
   const int own_c = (tid == P.E[1]) ? 3 + m.nq : ((c >= 0 && P.owner[c] == tid) ? c : -1);
   const int own_c2 = (tid == P.E[1]) ? 4 + m.nq : -1;
   bool ok = true;
-  const int* idx = P.idx + tid * P.em;
+  const LaneIdx idx = lane_idx(P, tid);
   // ---- local Moebius products; the per-element factors wait in fl / fi
   // (multipliers) and yt / b (couplings), which are free during the
   // factorisation
@@ -376,7 +387,7 @@ __device__ void wsolve_scan(const Mode& m, const Shared& S, const Pack& P, doubl
   const int own_c = (tid == P.E[1]) ? 3 + m.nq : ((c >= 0 && P.owner[c] == tid) ? c : -1);
   const int own_c2 = (tid == P.E[1]) ? 4 + m.nq : -1;
   // ---- forward: b'_j = b_j - fl_j b'_{j-1}
-  const int* idx = P.idx + tid * P.em;
+  const LaneIdx idx = lane_idx(P, tid);
   double A = 1.0, B = 0.0;
   int cnt = 0;  // valid elements of this lane
   if (c >= 0) {

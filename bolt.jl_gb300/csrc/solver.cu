@@ -873,6 +873,7 @@ __device__ bool setup_mode(const ModeDev& md, const CosmoDev* cosmos, double* ba
     PK.owner = ip; ip += 32;
     PK.E = ip;
     PK.em = kLaneElems / nth;
+    PK.nt = nth;
   }
   G.y = gscr;
   G.fx = gscr + N;

@@ -34,7 +34,7 @@ __device__ void wsolve_scan4(const Mode& m, const Shared& S, const Pack& P, doub
   const int own_c2 = (tid == P.E[1]) ? 4 + m.nq : -1;
   const int idb = m.iPhi + 3, ivb = m.iPhi + 4;
   // ---- forward: b'_j = b_j - fl_j b'_{j-1}
-  const int* idx = P.idx + tid * P.em;
+  const LaneIdx idx = lane_idx(P, tid);
   double A = 1.0, B[kTD];
 #pragma unroll
   for (int d = 0; d < kTD; ++d) B[d] = 0.0;
