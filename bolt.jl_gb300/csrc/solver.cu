@@ -93,26 +93,23 @@ constexpr int kMiscDoubles = 32 + 9 * 32;  // capacitance, reductions, per-chain
 // element lists (768 ints for every variant), owners and three counters.
 __host__ __device__ inline int pack_ints(int threads) { return 2 * threads + 768 + 32 + 4; }
 
-// Shared-memory doubles of the tangent part of a tangent mode (tangent.cuh):
-// stage-scalar tangents (6 slots and d/dx), q/eps and eps/q tangents,
-// perturbed q and q-constant tangents, the cosmology-constant tangents, the
-// tangent solves' border partials (32 chains x 3) and the tangent stage
-// states and right-hand sides.
-__host__ __device__ inline int tan_doubles(int N, int nq) {
-  return (kStages + 1) * kScal * kTD + 2 * (kStages + 1) * nq * kTD + 5 * nq * kTD + 8 * kTD + 32 * kBorder * kTD +
-         2 * kTD * N;
-}
-// An adjoint mode (adjoint.cuh) keeps the coefficient tangents but neither
-// the tangent stage vectors nor the tangent solves' partials.
-// The coefficient tangents of a tangent or adjoint mode (the first part of
-// tan_doubles()).  An adjoint mode keeps them in its global slab (read
-// through L1), not in shared memory, so that as many adjoint CTAs fit an SM
-// as plain ones; it needs neither the tangent stage vectors nor the tangent
-// solves' partials.
+// The coefficient tangents of a tangent or adjoint mode: stage-scalar
+// tangents (6 slots and d/dx), q/eps and eps/q tangents, the perturbed sets'
+// momenta and the momentum-bin constants' tangents, the cosmology
+// constants' tangents -- at most kCoefTanMax doubles (nq <= 27).
 __host__ __device__ inline int coef_tan_doubles(int nq) {
   return (kStages + 1) * kScal * kTD + 2 * (kStages + 1) * nq * kTD + 5 * nq * kTD + 8 * kTD;
 }
 constexpr int kCoefTanMax = (kStages + 1) * kScal * kTD + 2 * (kStages + 1) * 27 * kTD + 5 * 27 * kTD + 8 * kTD;
+// A tangent mode keeps them in shared memory with the tangent solves' border
+// partials and its tangent stage state and right-hand sides (kTD x N each);
+// an adjoint mode keeps them in its global slab (read through L1), so that
+// as many adjoint CTAs fit an SM as plain ones.  (Measured: the tangent
+// kernel with its stage vectors in the global slab instead runs 0.27 vs
+// 0.33 served spectra/s -- its solves then read global memory.)
+__host__ __device__ inline int tan_doubles(int N, int nq) {
+  return coef_tan_doubles(nq) + 32 * kBorder * kTD + 2 * kTD * N;
+}
 // Kernel kinds: 0 plain (and recorded / replayed / checkpointed) modes,
 // 1 tangent-linear modes, 2 adjoint (reverse-sweep) modes.
 __host__ __device__ inline int per_mode_doubles(int N, int nq, int Lmax, int threads, int kind = 0) {
@@ -842,7 +839,8 @@ __device__ bool setup_mode(const ModeDev& md, const CosmoDev* cosmos, double* ba
   S.sc_d = p; p += kScal;
   S.misc = p;                 // [0..8] capacitance inverse, [16..23] block reductions, [24] flags, [32..] partials
   p += kMiscDoubles;
-  if (KIND) {  // the layout tan_doubles() sizes (adjoint: in the global slab, after its scratch)
+  if (KIND) {  // tangent: tan_doubles() of shared memory; adjoint: the coefficient tangents in the
+              // global slab after its scratch
     double* keep = p;
     if (KIND == 2) p = gscr + 10 * N + adj_scratch_doubles(N);
     S.sct = p; p += kStages * kScal * kTD;
