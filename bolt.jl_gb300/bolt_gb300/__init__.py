@@ -2,7 +2,7 @@
 served requests in serve.py)."""
 from .api import (BasicNewtonian, Background, BoltError, Context, CosmoParams, GPUNewtonian, Hierarchy,
                   adjoint_check,
-                  IonizationHistory, Perturbation, RECFAST, SourceGrid, boltsolve, boltsolve_batch, boltsolve_rsa,
+                  IonizationHistory, Peebles, Perturbation, RECFAST, SourceGrid, boltsolve, boltsolve_batch, boltsolve_rsa,
                   boltsolve_rsa_batch, cl_all, clee,
                   clte, cltt, default_context, host_tables, km_s_Mpc_100, log10_k, mass_natural, plin,
                   quadratic_k, source_grid, source_grid_P, state_len)
@@ -10,7 +10,7 @@ from .serve import GRAD_SCHEMES, THETA_NAMES, Engine, Request, Result, params_of
 
 __all__ = ["BasicNewtonian", "Background", "BoltError", "Context", "CosmoParams", "Engine", "GPUNewtonian",
            "GRAD_SCHEMES", "adjoint_check",
-           "Hierarchy", "IonizationHistory", "Perturbation", "RECFAST", "Request", "Result", "SourceGrid",
+           "Hierarchy", "IonizationHistory", "Peebles", "Perturbation", "RECFAST", "Request", "Result", "SourceGrid",
            "THETA_NAMES", "boltsolve", "boltsolve_batch", "boltsolve_rsa", "boltsolve_rsa_batch", "cl_all", "clee", "clte", "cltt", "default_context",
            "host_tables", "km_s_Mpc_100", "log10_k", "mass_natural", "params_of", "plin", "quadratic_k",
            "source_grid", "source_grid_P", "state_len", "theta_of"]

@@ -28,7 +28,7 @@ class BoltGrid(C.Structure):
 
 class BoltRecfast(C.Structure):
     _fields_ = [("Yp", C.c_double), ("OmegaB", C.c_double), ("OmegaG", C.c_double), ("Tnow", C.c_double),
-                ("tol", C.c_double)]
+                ("tol", C.c_double), ("ionization", C.c_int)]
 
 
 class BoltHier(C.Structure):

@@ -206,11 +206,31 @@ def _host_tables(par, x_grid, nq, rf):
 
 
 def host_tables(par: CosmoParams, x_grid=(-20.0, 0.01, 0.0), nq: int = 15, Yp=None, OmegaB=None, OmegaG=None,
-                Tnow=-1.0, tol=1e-8):
-    """Node values of all 16 background/ionization tables, host-built."""
+                Tnow=-1.0, tol=1e-8, ionization: str = "recfast"):
+    """Node values of all 16 background/ionization tables, host-built
+    (ionization "recfast", or "peebles" for Saha-Peebles, see Peebles)."""
     rf = L.BoltRecfast(par.Y_p if Yp is None else Yp, par.Omega_b if OmegaB is None else OmegaB,
-                       par.Omega_r if OmegaG is None else OmegaG, -1.0 if Tnow is None else Tnow, tol)
+                       par.Omega_r if OmegaG is None else OmegaG, -1.0 if Tnow is None else Tnow, tol,
+                       _ION[ionization])
     return _host_tables(par, tuple(x_grid), nq, rf)
+
+
+_ION = {"recfast": 0, "peebles": 1}
+
+
+@dataclass
+class Peebles:
+    """Peebles() -- exported by Bolt.jl (Bolt.jl:6) but never defined there.
+    Here: the reference's Saha-Peebles X_e (saha_peebles_recombination,
+    ionization.jl:83-93: Saha until z = 1587.4, then the Peebles equation by
+    Tsit5 at 1e-11) made an IonizationHistory as customion does
+    (ionization.jl:141-164), with T_mat = 2.725 K (1 + z) (the T_b of its
+    Saha and Peebles equations) and RECFAST's sound-speed formula on it
+    (recfast.jl:709-712) for the two functions customion takes from its
+    caller."""
+    Yp: float = 0.24
+    OmegaB: float = 0.046
+    OmegaG: float = 5.0469e-5
 
 
 @dataclass
@@ -229,10 +249,14 @@ class IonizationHistory:
     """IonizationHistory(RECFAST, par, bg) (recfast.jl:674-726): host-built,
     then resident in HBM for the solver; ``cosmo_id`` names it there."""
 
-    def __init__(self, rf: RECFAST, par: CosmoParams, bg: Background, ctx: Context | None = None):
+    def __init__(self, rf, par: CosmoParams, bg: Background, ctx: Context | None = None):
         self.ctx = ctx or default_context()
         self.par, self.bg, self.rf = par, bg, rf
-        r = L.BoltRecfast(rf.Yp, rf.OmegaB, rf.OmegaG, -1.0 if rf.Tnow is None else rf.Tnow, rf.tol)
+        if isinstance(rf, Peebles):
+            r = L.BoltRecfast(rf.Yp, rf.OmegaB, rf.OmegaG, -1.0, 1e-8, _ION["peebles"])
+        else:
+            r = L.BoltRecfast(rf.Yp, rf.OmegaB, rf.OmegaG, -1.0 if rf.Tnow is None else rf.Tnow, rf.tol,
+                              _ION["recfast"])
         cid = C.c_int(-1)
         g = L.BoltGrid(*bg.x_grid_spec)
         self.ctx.check(self.ctx.lib.bolt_cosmo_build(self.ctx.h, C.byref(par.c()), C.byref(g), bg.nq, C.byref(r),

@@ -418,7 +418,8 @@ int bolt_host_tables(const bolt_params* par, const bolt_grid* grid, int nq, cons
     if (!par || !grid || !rf || !nodes || !scalars) throw Err(-1, "null argument");
     if (!(grid->step > 0) || !(grid->stop > grid->start)) throw Err(-1, "bad x grid");
     CosmoTables T;
-    RecfastOpts ro{rf->Yp, rf->OmegaB, rf->OmegaG, rf->Tnow, rf->tol > 0 ? rf->tol : 1e-8};
+    RecfastOpts ro{rf->Yp, rf->OmegaB, rf->OmegaG, rf->Tnow, rf->tol > 0 ? rf->tol : 1e-8, rf->ionization};
+    if (ro.ionization != 0 && ro.ionization != 1) throw Err(-1, "ionization must be 0 (RECFAST) or 1 (Saha-Peebles)");
     build_cosmo_tables(to_h(par), make_grid(grid->start, grid->step, grid->stop), nq, ro, T);
     const int n = T.grid.n;
     for (int t = 0; t < T_COUNT; ++t) std::copy(T.nodes[t].begin(), T.nodes[t].end(), nodes + size_t(t) * n);
@@ -447,7 +448,8 @@ int bolt_host_tables_frozen(const bolt_params* base, const bolt_params* par, con
     CosmoTables T0, T;
     RecfastOpts r0{rf_base->Yp, rf_base->OmegaB, rf_base->OmegaG, rf_base->Tnow, rf_base->tol > 0 ? rf_base->tol : 1e-8};
     build_cosmo_tables(to_h(base), g, nq, r0, T0, &fz);  // records
-    RecfastOpts ro{rf->Yp, rf->OmegaB, rf->OmegaG, rf->Tnow, rf->tol > 0 ? rf->tol : 1e-8};
+    RecfastOpts ro{rf->Yp, rf->OmegaB, rf->OmegaG, rf->Tnow, rf->tol > 0 ? rf->tol : 1e-8, rf->ionization};
+    if (ro.ionization != 0 && ro.ionization != 1) throw Err(-1, "ionization must be 0 (RECFAST) or 1 (Saha-Peebles)");
     build_cosmo_tables(to_h(par), g, nq, ro, T, &fz);    // replays
     const int n = T.grid.n;
     for (int t = 0; t < T_COUNT; ++t) std::copy(T.nodes[t].begin(), T.nodes[t].end(), nodes + size_t(t) * n);
@@ -507,7 +509,8 @@ int bolt_cosmo_build(bolt_ctx* c, const bolt_params* par, const bolt_grid* grid,
     if (!par || !grid || !rf || !cosmo_id) throw Err(-1, "null argument");
     if (!(grid->step > 0) || !(grid->stop > grid->start)) throw Err(-1, "bad x grid");
     CosmoEntry e;
-    RecfastOpts ro{rf->Yp, rf->OmegaB, rf->OmegaG, rf->Tnow, rf->tol > 0 ? rf->tol : 1e-8};
+    RecfastOpts ro{rf->Yp, rf->OmegaB, rf->OmegaG, rf->Tnow, rf->tol > 0 ? rf->tol : 1e-8, rf->ionization};
+    if (ro.ionization != 0 && ro.ionization != 1) throw Err(-1, "ionization must be 0 (RECFAST) or 1 (Saha-Peebles)");
     build_cosmo_tables(to_h(par), make_grid(grid->start, grid->step, grid->stop), nq, ro, e.T);
     *cosmo_id = add_cosmo(c, std::move(e));
   });

@@ -20,6 +20,8 @@ const double kMpc = 3.0856775814913673e22;
 const double kG = 6.67430e-11;
 const double kMp = 1.67262192369e-27;
 const double kSigmaT = 6.6524587321e-29;
+const double kMe = 9.1093837015e-31;
+const double kAlphaFS = 7.2973525693e-3;
 const double kZeta3 = 1.2020569;  // background.jl:3
 
 double nat_G() { return kG * kHbar / (kC * kC * kC) / (kMpc * kMpc); }
@@ -502,6 +504,50 @@ struct Rf {
   }
 };
 
+// ----------------------------------------------------------- Saha-Peebles
+// The Saha equation for hydrogen and the Peebles equation (ionization.jl:1-93)
+// in Bolt's natural units (Mpc^-1), T_b = 2.725 K / a.  The Saha root is
+// taken without cancellation, 2r / (sqrt(r^2 + 4r) + r), the same number as
+// the reference's (sqrt(r^2 + 4r) - r) / 2; beta2 = beta exp(3 eps0 / 4T) is
+// formed as one exponential, exp(-eps0 / 4T), which the reference reaches in
+// BigFloat (its ODE right-hand side, ionization.jl:61-66).
+struct SahaPeebles {
+  const Bg* bg;
+  double T0, eps0, me, mH, alpha, L2s;
+  void init(const Bg* b) {
+    bg = b;
+    T0 = 2.725 / kelvin_per_nat();                  // ionization.jl:5
+    eps0 = 13.605698 * units_mass_eV();             // ionization.jl:26
+    me = kMe * kC / kHbar * kMpc;
+    mH = nat_mH();
+    alpha = kAlphaFS;
+    L2s = 8.227 * sec_per_nat();                    // ionization.jl:25
+  }
+  double nH(double a) const { return bg->p.Omega_b * bg->rc / (mH * a * a * a) * (1 - bg->p.Y_p); }
+  double xe_saha(double x) const {                 // ionization.jl:12-16
+    double a = std::exp(x), Tb = T0 / a;
+    double r = std::pow(me * Tb / (2 * M_PI), 1.5) / nH(a) * std::exp(-eps0 / Tb);
+    return 2 * r / (std::sqrt(r * r + 4 * r) + r);
+  }
+  double Hold(double a) const {                    // background.jl:51-55
+    const CosmoParamsH& p = bg->p;
+    return bg->H0 * std::sqrt((p.Omega_c + p.Omega_b) * std::pow(a, -3) +
+                              p.Omega_r * (1 + (2.0 / 3.0) * (7 * p.N_nu / 8) * std::pow(4.0 / 11.0, 4.0 / 3.0)) *
+                                  std::pow(a, -4) +
+                              bg->OL);
+  }
+  double dxe_dx(double x, double xe) const {       // ionization.jl:36-66
+    double a = std::exp(x), Tb = T0 / a, H = Hold(a), n = nH(a);
+    double a2 = (64 * M_PI / std::sqrt(27 * M_PI)) * (alpha * alpha / (me * me)) * std::sqrt(eps0 / Tb) *
+                (0.448 * std::log(eps0 / Tb));
+    double pre = a2 * std::pow(me * Tb / (2 * M_PI), 1.5);
+    double beta = pre * std::exp(-eps0 / Tb), beta2 = pre * std::exp(-eps0 / (4 * Tb));
+    double La = H * std::pow(3 * eps0, 3) / (std::pow(8 * M_PI, 2) * (1 - xe) * n);
+    double Cr = (L2s + La) / (L2s + La + beta2);
+    return Cr / H * (beta * (1 - xe) - n * a2 * xe * xe);
+  }
+};
+
 // Bracketing root of f on [a, b]: regula falsi then bisection, to floating
 // point resolution (the NonlinearSolve Falsi call at recfast.jl:451-459).
 double bracket_root(const std::function<double(double)>& f, double a, double b) {
@@ -574,99 +620,119 @@ void build_cosmo_tables(const CosmoParamsH& p, const GridSpec& g, int nq, const 
   Rf rf;
   rf.init(&bg, &sH, &sHp, ro);
   T.Tnow = rf.Tnow;
-  const double zini = 10000.0, zfin = 0.0, zre_ini = 50.0;
-  double zHe = replay ? fz->zHe
-                      : bracket_root([&](double z) { return (rf.xtot_He1_saha(z) - 1.0) / rf.fHe - 0.99; },
-                                     std::min(zini, 3500.0), zfin);
-  double zHH = replay ? fz->zHH : bracket_root([&](double z) { return rf.xH_saha(z) - 0.985; }, zHe, zfin);
-  T.z_He_evo_start = zHe;
-  T.z_H_He_evo_start = zHH;
-  std::vector<double> zland;
-  for (int j = 0; j < n; ++j) {
-    double z = 1.0 / std::exp(g.at(j)) - 1.0;
-    if (z < zini) zland.push_back(z);
-  }
-  BranchLog logHe, logHHe;
-  if (fz) {
-    logHe.bits = &fz->bHe;
-    logHHe.bits = &fz->bHHe;
-    logHe.replay = logHHe.replay = replay;
-    if (!replay) { fz->bHe.clear(); fz->bHHe.clear(); }
-  }
-  double y2[2] = {(rf.xtot_He1_saha(zHe) - 1.0) / rf.fHe, rf.Tnow * (1 + zHe)};
-  rf.blog = fz ? &logHe : nullptr;
-  Traj He = tsit5_integrate(
-      [&](double z, const double* u, double* du) {
-        double yy[3] = {rf.xH_saha(z), u[0], u[1]}, d[3];
-        rf.rhs(z, yy, d);
-        du[0] = d[1];
-        du[1] = d[2];
-      },
-      2, y2, zHe, zHH, rf.tol, 1e-6, zland, replay ? &fz->tHe : nullptr, replay ? &fz->hHe : nullptr,
-      fz ? &logHe : nullptr);
-  rf.blog = fz ? &logHHe : nullptr;
-  double y3[3] = {rf.xH_saha(zHH), He.last()[0], He.last()[1]};
-  std::vector<double> land3 = zland;
-  land3.push_back(zre_ini);
-  Traj HHe = tsit5_integrate([&](double z, const double* u, double* du) { rf.rhs(z, u, du); }, 3, y3, zHH, zfin, rf.tol,
-                             1e-6, land3, replay ? &fz->tHHe : nullptr, replay ? &fz->hHHe : nullptr,
-                             fz ? &logHHe : nullptr);
-  rf.blog = nullptr;
-  auto xe_recfast = [&](double z) -> double {  // recfast.jl:413-433
-    if (z > 8000.) return 1 + 2 * rf.fHe;
-    if (z > 5000.) {
-      double r = rf.saha(z, rf.CB1_He2);
-      return Rf::quad_root(r - 1 - rf.fHe, (1 + 2 * rf.fHe) * r);
+  if (ro.ionization == 1) {
+    // Saha-Peebles (ionization.jl:83-93) through customion (ionization.jl:141-164)
+    if (fz) throw std::runtime_error("gradients of a Saha-Peebles ionization history are not available");
+    SahaPeebles sp;
+    sp.init(&bg);
+    const double xtr = std::log(1.0 / (1.0 + 1587.4));  // z2x(1587.4)
+    std::vector<double> land;
+    for (int j = 0; j < n; ++j)
+      if (g.at(j) > xtr) land.push_back(g.at(j));
+    double x0 = sp.xe_saha(xtr);
+    Traj Pe = tsit5_integrate([&](double x, const double* u, double* du) { du[0] = sp.dxe_dx(x, u[0]); }, 1, &x0, xtr,
+                              0.0, 1e-11, 1e-11, land);
+    T.z_He_evo_start = T.z_H_He_evo_start = 0.0;
+    for (int j = 0; j < n; ++j) {
+      double x = g.at(j), z = 1.0 / std::exp(x) - 1.0;
+      T.nodes[T_XE][j] = x < xtr ? sp.xe_saha(x) : Pe.eval1(x, 0);
+      T.nodes[T_TMAT][j] = 2.725 * (1 + z);  // saha_T_b (ionization.jl:8)
     }
-    if (z > 3500.) return 1 + rf.fHe;
-    if (z > zHe) return rf.xtot_He1_saha(z);
-    if (z > zHH) return rf.xH_saha(z) + rf.fHe * He.eval1(z, 0);
-    double b[3];
-    HHe.eval(z, b);
-    return b[0] + rf.fHe * b[1];
-  };
-  auto tmat_recfast = [&](double z) -> double {  // recfast.jl:435-444
-    if (z > zHe) return rf.Tnow * (1 + z);
-    if (z > zHH) return He.eval1(z, 1);
-    return HHe.eval1(z, 2);
-  };
-  const double Xfin = 1 + rf.Yp / (rf.not4 * (1 - rf.Yp));
-  auto xe_reio = [&](double z) -> double {  // recfast.jl:478-488
-    const double zre = 7.6711, al = 1.5, dH = 0.5, zHe2 = 3.5, dHe = 0.5;
-    double xo = xe_recfast(z);
-    double xH = (Xfin - xo) / 2 * (1 + std::tanh((std::pow(1 + zre, al) - std::pow(1 + z, al)) / (al * std::pow(1 + zre, al - 1)) / dH)) + xo;
-    return xH + (Xfin - 1) / 2 * (1 + std::tanh((zHe2 - z) / dHe));
-  };
-  double T50 = tmat_recfast(zre_ini);
-  Traj Re = tsit5_integrate(
-      [&](double z, const double* u, double* du) {  // recfast.jl:491-502
-        double xr = xe_reio(z), a = 1.0 / (1 + z);
-        double Hz = sH(std::log(a)) / a / sec_per_nat(), Trad = rf.Tnow * (1 + z);
-        du[0] = rf.CT * std::pow(Trad, 4) * xr / (1 + xr + rf.fHe) * (u[0] - Trad) / (Hz * (1 + z)) + 2 * u[0] / (1 + z);
-      },
-      1, &T50, zre_ini, zfin, rf.tol, 1e-6, zland, replay ? &fz->tRe : nullptr, replay ? &fz->hRe : nullptr);
-  if (fz && !replay) {
-    fz->zHe = zHe;
-    fz->zHH = zHH;
-    fz->tHe = He.t;
-    fz->tHHe = HHe.t;
-    fz->tRe = Re.t;
-    fz->hHe = He.h;
-    fz->hHHe = HHe.h;
-    fz->hRe = Re.h;
-    fz->have = true;
-  }
+  } else {
+    const double zini = 10000.0, zfin = 0.0, zre_ini = 50.0;
+    double zHe = replay ? fz->zHe
+                        : bracket_root([&](double z) { return (rf.xtot_He1_saha(z) - 1.0) / rf.fHe - 0.99; },
+                                       std::min(zini, 3500.0), zfin);
+    double zHH = replay ? fz->zHH : bracket_root([&](double z) { return rf.xH_saha(z) - 0.985; }, zHe, zfin);
+    T.z_He_evo_start = zHe;
+    T.z_H_He_evo_start = zHH;
+    std::vector<double> zland;
+    for (int j = 0; j < n; ++j) {
+      double z = 1.0 / std::exp(g.at(j)) - 1.0;
+      if (z < zini) zland.push_back(z);
+    }
+    BranchLog logHe, logHHe;
+    if (fz) {
+      logHe.bits = &fz->bHe;
+      logHHe.bits = &fz->bHHe;
+      logHe.replay = logHHe.replay = replay;
+      if (!replay) { fz->bHe.clear(); fz->bHHe.clear(); }
+    }
+    double y2[2] = {(rf.xtot_He1_saha(zHe) - 1.0) / rf.fHe, rf.Tnow * (1 + zHe)};
+    rf.blog = fz ? &logHe : nullptr;
+    Traj He = tsit5_integrate(
+        [&](double z, const double* u, double* du) {
+          double yy[3] = {rf.xH_saha(z), u[0], u[1]}, d[3];
+          rf.rhs(z, yy, d);
+          du[0] = d[1];
+          du[1] = d[2];
+        },
+        2, y2, zHe, zHH, rf.tol, 1e-6, zland, replay ? &fz->tHe : nullptr, replay ? &fz->hHe : nullptr,
+        fz ? &logHe : nullptr);
+    rf.blog = fz ? &logHHe : nullptr;
+    double y3[3] = {rf.xH_saha(zHH), He.last()[0], He.last()[1]};
+    std::vector<double> land3 = zland;
+    land3.push_back(zre_ini);
+    Traj HHe = tsit5_integrate([&](double z, const double* u, double* du) { rf.rhs(z, u, du); }, 3, y3, zHH, zfin, rf.tol,
+                               1e-6, land3, replay ? &fz->tHHe : nullptr, replay ? &fz->hHHe : nullptr,
+                               fz ? &logHHe : nullptr);
+    rf.blog = nullptr;
+    auto xe_recfast = [&](double z) -> double {  // recfast.jl:413-433
+      if (z > 8000.) return 1 + 2 * rf.fHe;
+      if (z > 5000.) {
+        double r = rf.saha(z, rf.CB1_He2);
+        return Rf::quad_root(r - 1 - rf.fHe, (1 + 2 * rf.fHe) * r);
+      }
+      if (z > 3500.) return 1 + rf.fHe;
+      if (z > zHe) return rf.xtot_He1_saha(z);
+      if (z > zHH) return rf.xH_saha(z) + rf.fHe * He.eval1(z, 0);
+      double b[3];
+      HHe.eval(z, b);
+      return b[0] + rf.fHe * b[1];
+    };
+    auto tmat_recfast = [&](double z) -> double {  // recfast.jl:435-444
+      if (z > zHe) return rf.Tnow * (1 + z);
+      if (z > zHH) return He.eval1(z, 1);
+      return HHe.eval1(z, 2);
+    };
+    const double Xfin = 1 + rf.Yp / (rf.not4 * (1 - rf.Yp));
+    auto xe_reio = [&](double z) -> double {  // recfast.jl:478-488
+      const double zre = 7.6711, al = 1.5, dH = 0.5, zHe2 = 3.5, dHe = 0.5;
+      double xo = xe_recfast(z);
+      double xH = (Xfin - xo) / 2 * (1 + std::tanh((std::pow(1 + zre, al) - std::pow(1 + z, al)) / (al * std::pow(1 + zre, al - 1)) / dH)) + xo;
+      return xH + (Xfin - 1) / 2 * (1 + std::tanh((zHe2 - z) / dHe));
+    };
+    double T50 = tmat_recfast(zre_ini);
+    Traj Re = tsit5_integrate(
+        [&](double z, const double* u, double* du) {  // recfast.jl:491-502
+          double xr = xe_reio(z), a = 1.0 / (1 + z);
+          double Hz = sH(std::log(a)) / a / sec_per_nat(), Trad = rf.Tnow * (1 + z);
+          du[0] = rf.CT * std::pow(Trad, 4) * xr / (1 + xr + rf.fHe) * (u[0] - Trad) / (Hz * (1 + z)) + 2 * u[0] / (1 + z);
+        },
+        1, &T50, zre_ini, zfin, rf.tol, 1e-6, zland, replay ? &fz->tRe : nullptr, replay ? &fz->hRe : nullptr);
+    if (fz && !replay) {
+      fz->zHe = zHe;
+      fz->zHH = zHH;
+      fz->tHe = He.t;
+      fz->tHHe = HHe.t;
+      fz->tRe = Re.t;
+      fz->hHe = He.h;
+      fz->hHHe = HHe.h;
+      fz->hRe = Re.h;
+      fz->have = true;
+    }
 
-  // --- node values (recfast.jl:689-708)
-  double xini = std::log(1.0 / (zini + 1.0));
-  for (int j = 0; j < n; ++j) {
-    double x = g.at(j), z = 1.0 / std::exp(x) - 1.0;
-    if (x < xini) {
-      T.nodes[T_XE][j] = 1 + 2 * rf.fHe;
-      T.nodes[T_TMAT][j] = rf.Tnow * (1 + z);
-    } else {
-      T.nodes[T_XE][j] = z > zre_ini ? xe_recfast(z) : xe_reio(z);
-      T.nodes[T_TMAT][j] = z > zre_ini ? tmat_recfast(z) : Re.eval1(z, 0);
+    // --- node values (recfast.jl:689-708)
+    double xini = std::log(1.0 / (zini + 1.0));
+    for (int j = 0; j < n; ++j) {
+      double x = g.at(j), z = 1.0 / std::exp(x) - 1.0;
+      if (x < xini) {
+        T.nodes[T_XE][j] = 1 + 2 * rf.fHe;
+        T.nodes[T_TMAT][j] = rf.Tnow * (1 + z);
+      } else {
+        T.nodes[T_XE][j] = z > zre_ini ? xe_recfast(z) : xe_reio(z);
+        T.nodes[T_TMAT][j] = z > zre_ini ? tmat_recfast(z) : Re.eval1(z, 0);
+      }
     }
   }
   // tau' and its reverse cumulative trapezoid (ionization.jl:105-127)

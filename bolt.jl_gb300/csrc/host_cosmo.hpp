@@ -42,6 +42,11 @@ struct RecfastOpts {
   double Yp, OmegaB, OmegaG;
   double Tnow;  // <= 0: derived from OmegaG and the background
   double tol;
+  // 0: RECFAST (recfast.jl:446-536, 674-726); 1: Saha until z = 1587.4, then
+  // the Peebles equation (ionization.jl:1-93, saha_peebles_recombination),
+  // with T_mat = 2.725 K (1 + z) and the RECFAST path's sound speed formula
+  // on it (customion, ionization.jl:141-164, takes both from its caller)
+  int ionization = 0;
 };
 
 struct GridSpec {

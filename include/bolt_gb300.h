@@ -39,6 +39,10 @@ typedef struct {
  * Tnow <= 0 derives the CMB temperature from OmegaG (recfast.jl:108). */
 typedef struct {
   double Yp, OmegaB, OmegaG, Tnow, tol;
+  int ionization; /* 0 = RECFAST (src/ionization/recfast.jl:674-726); 1 = Saha until z = 1587.4, then the
+                     Peebles equation (saha_peebles_recombination, src/ionization/ionization.jl:83-93) through
+                     customion (ionization.jl:141-164) with T_mat = 2.725 K (1 + z) and RECFAST's sound-speed
+                     formula on it; OmegaG, Tnow and tol then apply to that formula only */
 } bolt_recfast;
 
 /* Hierarchy truncation (src/perturbations.jl:7-21). */

@@ -96,6 +96,9 @@ def lib():
                                 C.c_int, _dp, _dp, _dp, C.c_int]
         L.oracle_cl_frozen.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, _ip, C.c_int, C.c_double,
                                        C.c_double, C.c_int, C.c_double, _dp, _dp, _dp, C.c_int]
+        L.oracle_cosmo_new_peebles.restype = C.c_void_p
+        L.oracle_cosmo_new_peebles.argtypes = [C.POINTER(_Params), C.c_double, C.c_double, C.c_double, C.c_int,
+                                               C.c_double, C.c_double, C.c_double]
         L.oracle_cosmo_new_atol.restype = C.c_void_p
         L.oracle_cosmo_new_atol.argtypes = [C.POINTER(_Params), C.c_double, C.c_double, C.c_double, C.c_int,
                                             C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -147,14 +150,18 @@ def state_len(lg, lnu, lmnu, nq):
 
 
 class Cosmo:
-    """Background + RECFAST IonizationHistory for one parameter set."""
+    """Background + IonizationHistory (RECFAST, or with ionization="peebles"
+    the Saha-Peebles history through customion) for one parameter set."""
 
     def __init__(self, p: Params, x_grid=(-20.0, 0.01, 0.0), nq=15, OmegaG=None, Tnow=-1.0,
-                 recfast_tol=1e-8, recfast_atol=None):
+                 recfast_tol=1e-8, recfast_atol=None, ionization="recfast"):
         self.p = p
         self._pc = p.c()
         og = p.Omega_r if OmegaG is None else OmegaG
-        if recfast_atol is None:
+        if ionization == "peebles":
+            self.h = lib().oracle_cosmo_new_peebles(C.byref(self._pc), x_grid[0], x_grid[1], x_grid[2], nq,
+                                                    p.Y_p, p.Omega_b, og)
+        elif recfast_atol is None:
             self.h = lib().oracle_cosmo_new(C.byref(self._pc), x_grid[0], x_grid[1], x_grid[2], nq,
                                             p.Y_p, p.Omega_b, og, Tnow, recfast_tol)
         else:

@@ -20,6 +20,7 @@ struct OCosmo {
   Cosmo C;
   std::unique_ptr<Background> bg;
   std::unique_ptr<Recfast> rf;
+  std::unique_ptr<SahaPeebles> sp;
   std::unique_ptr<Ionization> ih;
 };
 
@@ -68,6 +69,29 @@ void* oracle_cosmo_new_atol(const oracle_params* p, double x_start, double x_ste
     return o;
   } catch (const std::exception& e) {
     std::fprintf(stderr, "oracle_cosmo_new_atol: %s\n", e.what());
+    return nullptr;
+  }
+}
+
+// Background + the Saha-Peebles ionization history (saha_peebles_recombination
+// through customion, ionization.jl:83-93, 141-164; T_mat = 2.725 K (1 + z),
+// the sound speed by RECFAST's formula with Yp, OmegaB, OmegaG).
+void* oracle_cosmo_new_peebles(const oracle_params* p, double x_start, double x_step, double x_stop, int nq,
+                               double Yp, double OmegaB, double OmegaG) {
+  try {
+    OCosmo* o = new OCosmo();
+    o->C.par = to_params(p);
+    o->bg.reset(new Background(o->C.par, Grid::range(x_start, x_step, x_stop), nq));
+    o->rf.reset(new Recfast(o->bg.get(), Yp, OmegaB, OmegaG, -1.0, 1e-8));
+    std::vector<double> xs(o->bg->xg.n);
+    for (int j = 0; j < o->bg->xg.n; ++j) xs[j] = o->bg->xg.at(j);
+    o->sp.reset(new SahaPeebles(o->bg.get(), xs));
+    o->ih.reset(new Ionization(*o->sp, *o->rf, o->C.par, *o->bg));
+    o->C.bg = o->bg.get();
+    o->C.ih = o->ih.get();
+    return o;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_cosmo_new_peebles: %s\n", e.what());
     return nullptr;
   }
 }

@@ -35,6 +35,7 @@ constexpr double G = 6.67430e-11;             // CODATA 2018
 constexpr double m_e = 9.1093837015e-31;      // CODATA 2018
 constexpr double m_p = 1.67262192369e-27;     // CODATA 2018 (ProtonMass)
 constexpr double sigma_T = 6.6524587321e-29;  // CODATA 2018
+constexpr double alpha = 7.2973525693e-3;      // CODATA 2018 fine-structure constant
 }  // namespace si
 
 struct Units {

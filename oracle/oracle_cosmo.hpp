@@ -417,13 +417,81 @@ struct RecfastHistoryT {
 };
 using RecfastHistory = RecfastHistoryT<double>;
 
-// IonizationHistory(RECFAST, par, bg) (recfast.jl:674-726, ionization.jl:107-137)
+// saha_peebles_recombination (ionization.jl:1-93): X_e from the Saha
+// equation for hydrogen until z = 1587.4, then the Peebles equation by Tsit5
+// at reltol = abstol = 1e-11, in Bolt's natural units (Mpc^-1), with
+// T_b = 2.725 K / a.  (The Saha root as (sqrt(r^2 + 4r) - r) / 2 rounded
+// without cancellation; beta2 = beta exp(3 eps0 / 4T) as exp(-eps0 / 4T),
+// which the reference evaluates in BigFloat.)
+struct SahaPeebles {
+  const BackgroundT<double>* bg;
+  double T0, eps0, me, mH, L2s, xtr;
+  Tsit5Sol late;
+  SahaPeebles(const BackgroundT<double>* b, const std::vector<double>& xout) : bg(b) {
+    const Units& U = units();
+    T0 = 2.725 / U.K_conv;                                      // ionization.jl:5 (PeeblesT0)
+    eps0 = 13.605698 * U.mass_natural;                          // ionization.jl:26
+    me = si::m_e * si::c / si::hbar * si::Mpc;                  // ionization.jl:27
+    mH = U.m_H;                                                 // ionization.jl:28
+    L2s = 8.227 * U.H0_conv;                                    // ionization.jl:25
+    xtr = log(1.0 / (1.0 + 1587.4));                            // ionization.jl:83-84
+    double x0 = saha(xtr);
+    Rhs f = [&](double x, const double* y, double* dy) { dy[0] = peebles(x, y[0]); };
+    std::vector<double> stops;
+    for (double x : xout)
+      if (x > xtr) stops.push_back(x);
+    late = tsit5(f, 1, &x0, xtr, 0.0, 1e-11, 1e-11, stops);   // ionization.jl:70-74
+  }
+  double nH(double a) const {                                   // ionization.jl:6-7
+    const ParamsT<double>& p = bg->par;
+    return p.Omega_b * bg->rho_crit / (mH * a * a * a) * (1 - p.Y_p);
+  }
+  double saha(double x) const {                                 // ionization.jl:9-16
+    double a = exp(x), Tb = T0 / a;
+    double r = pow(me * Tb / (2 * M_PI), 1.5) / nH(a) * exp(-eps0 / Tb);
+    return 2 * r / (sqrt(r * r + 4 * r) + r);
+  }
+  double oldH(double a) const {                                 // background.jl:51-55
+    const ParamsT<double>& p = bg->par;
+    return bg->H0 * sqrt((p.Omega_c + p.Omega_b) * pow(a, -3) +
+                         p.Omega_r * (1 + (2.0 / 3.0) * (7 * p.N_nu / 8) * pow(4.0 / 11.0, 4.0 / 3.0)) * pow(a, -4) +
+                         bg->Omega_Lambda);
+  }
+  double peebles(double x, double Xe) const {                   // ionization.jl:32-66
+    double a = exp(x), Tb = T0 / a, H = oldH(a), n = nH(a);
+    double phi2 = 0.448 * log(eps0 / Tb);
+    double alpha2 = (64 * M_PI / sqrt(27 * M_PI)) * (si::alpha * si::alpha / (me * me)) * sqrt(eps0 / Tb) * phi2;
+    double beta = alpha2 * pow(me * Tb / (2 * M_PI), 1.5) * exp(-eps0 / Tb);
+    double beta2 = alpha2 * pow(me * Tb / (2 * M_PI), 1.5) * exp(-eps0 / (4 * Tb));
+    double Lalpha = H * pow(3 * eps0, 3) / (pow(8 * M_PI, 2) * ((1 - Xe) * n));
+    double Cr = (L2s + Lalpha) / (L2s + Lalpha + beta2);
+    return Cr / H * (beta * (1 - Xe) - n * alpha2 * Xe * Xe);
+  }
+  double Xe(double x) const { return x < xtr ? saha(x) : late.at(x, 0); }  // ionization.jl:90-92
+};
+
+// IonizationHistory(RECFAST, par, bg) (recfast.jl:674-726, ionization.jl:107-137),
+// or, with a SahaPeebles X_e, customion (ionization.jl:141-164) with
+// T_mat = 2.725 K (1 + z) and RECFAST's sound-speed formula on it.
 template <class T>
 struct IonizationT {
   T tau0 = 0.0;
   SplineT<T> Xe, tau, taup, taupp, g, gp, gpp, Tmat, csb2;
   std::vector<T> Xe_nodes, Tmat_nodes;
   double z_He_evo_start = 0, z_H_He_evo_start = 0;
+
+  IonizationT(const SahaPeebles& sp, const RecfastT<T>& r, const ParamsT<T>& par, const BackgroundT<T>& bg) {
+    const Grid& g_ = bg.xg;
+    int n = g_.n;
+    Xe_nodes.resize(n);
+    Tmat_nodes.resize(n);
+    for (int j = 0; j < n; ++j) {
+      double x = g_.at(j);
+      Xe_nodes[j] = sp.Xe(x);
+      Tmat_nodes[j] = 2.725 * (1 + (1.0 / exp(x) - 1.0));
+    }
+    finish(r, par, bg);
+  }
 
   IonizationT(const RecfastT<T>& r, const ParamsT<T>& par, const BackgroundT<T>& bg) {
     const Grid& g_ = bg.xg;
@@ -447,6 +515,13 @@ struct IonizationT {
       Xe_nodes[j] = (x < xinit) ? Xe_initial : rh.Xe_TanhReio(z);
       Tmat_nodes[j] = (x < xinit) ? r.Tnow * (1 + z) : rh.Tmat_TanhReio(z);
     }
+    finish(r, par, bg);
+  }
+
+  // tau, g, their splines and the sound speed from the X_e and T_mat nodes
+  void finish(const RecfastT<T>& r, const ParamsT<T>& par, const BackgroundT<T>& bg) {
+    const Grid& g_ = bg.xg;
+    int n = g_.n;
     // tau' (ionization.jl:122-127) and reverse cumulative trapezoid (ionization.jl:105-115)
     const Units& U = units();
     T rc = BackgroundT<T>::rho_crit_of(par);
