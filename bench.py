@@ -838,7 +838,11 @@ def run_trajectories(args):
     par = B.CosmoParams(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Y_p=0.24, N_nu=3.046,
                         Sigma_m_nu=0.06 * B.mass_natural())
     bg = B.Background(par)
-    ih = B.IonizationHistory(B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg, ctx=ctx)
+    if args.ionization == "peebles":
+        rf = B.Peebles(Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r)
+    else:
+        rf = B.RECFAST(bg, Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r)
+    ih = B.IonizationHistory(rf, par, bg, ctx=ctx)
     ks = B.log10_k(0.1 * bg.H0, 1000.0 * bg.H0, 100)
     xo = np.linspace(-20.0, 0.0, 1000)
     hier = (20, 20, 10, 15)
@@ -878,6 +882,7 @@ def run_trajectories(args):
                "config": {"workload": "trajectories: fiducial LCDM, 100 log k in [0.1,1000] H0, 1000 uniform x in "
                                       "[-20,0], l 20/20/10, nq 15 (N=233), and P_lin(k) at z = 0 on the same k; "
                                       "one step = bolt_boltsolve + bolt_plin", "reltol": rt, "abstol": at,
+                          "ionization": {"peebles": "Saha-Peebles", "recfast": "RECFAST"}[args.ionization],
                           "parallelism": f"replicas x{ws}"},
                "e2e": {"value": ws * args.steps * ks.size / wall, "unit": "modes/s",
                        "h2d_bytes_per_step": int(ks.size * 8 * 2 + xo.size * 8),
@@ -919,6 +924,8 @@ def main():
                     help="pipeline: solver warps per mode (0: by launch size)")
     ap.add_argument("--lg", type=int, default=50, help="pipeline: l_gamma = l_nu of the hierarchy")
     ap.add_argument("--lmnu", type=int, default=20, help="pipeline: l_mnu of the hierarchy")
+    ap.add_argument("--ionization", default="peebles", choices=["peebles", "recfast"],
+                    help="trajectories: the ionization history (the configuration names Peebles recombination)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

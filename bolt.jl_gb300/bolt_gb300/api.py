@@ -246,8 +246,10 @@ class RECFAST:
 
 
 class IonizationHistory:
-    """IonizationHistory(RECFAST, par, bg) (recfast.jl:674-726): host-built,
-    then resident in HBM for the solver; ``cosmo_id`` names it there."""
+    """IonizationHistory(RECFAST, par, bg) (recfast.jl:674-726), or from
+    ``Peebles()`` (the Saha-Peebles history, ionization.jl:83-93,141-164):
+    host-built, then resident in HBM for the solver; ``cosmo_id`` names it
+    there."""
 
     def __init__(self, rf, par: CosmoParams, bg: Background, ctx: Context | None = None):
         self.ctx = ctx or default_context()

@@ -4,7 +4,8 @@ ABI) against the CPU oracle.
 * Trajectories at the reference plin default hierarchy l 50/50/20, nq 15
   (N = 473, the largest shared-memory layout) and at the trajectory
   configuration (100 log k in [0.1, 1000] H0, l 20/20/10, 1000 uniform x in
-  [-20, 0], N = 233) with its P_lin(k) at z = 0: both sides at
+  [-20, 0], N = 233) with its P_lin(k) at z = 0, under the RECFAST and the
+  Saha-Peebles histories: both sides at
   reltol = abstol = 1e-10, every component within 1e-6 of its peak over x,
   P_lin within 1e-6.
 * P_lin on 200 log k in [1e-4, 1] h/Mpc at N = 473 against the oracle at
@@ -76,10 +77,16 @@ def test_trajectories_n473(fid):
         assert err < 1e-6, (k, err)
 
 
-def test_trajectories_and_plin_config1(fid):
+@pytest.mark.parametrize("ion", ["recfast", "peebles"])
+def test_trajectories_and_plin_config1(fid, ion):
     """100 log k in [0.1, 1000] H0 on 1000 uniform x in [-20, 0], l 20/20/10,
-    nq 15, and P_lin(k) at z = 0 on the same k."""
+    nq 15, and P_lin(k) at z = 0 on the same k; with the RECFAST history and
+    with the Saha-Peebles one the configuration names."""
     par, bg, ih, orc = fid
+    if ion == "peebles":
+        ih = B.IonizationHistory(B.Peebles(Yp=par.Y_p, OmegaB=par.Omega_b, OmegaG=par.Omega_r), par, bg)
+        orc = O.Cosmo(O.Params(h=0.7, Omega_b=0.046, Omega_c=0.224, n=0.96, A=2.1e-9, Sigma_m_nu_eV=0.06),
+                      ionization="peebles")
     hier = (20, 20, 10, 15)
     assert B.state_len(*hier) == 233
     ks = B.log10_k(0.1 * bg.H0, 1000.0 * bg.H0, 100)
@@ -96,6 +103,8 @@ def test_trajectories_and_plin_config1(fid):
     with ThreadPoolExecutor(CORES) as ex:
         Po = np.array(list(ex.map(lambda k: orc.plin(k, 15, 20, 20, 10, 0.0, 1e-10, 1e-10), ks)))
     assert np.max(np.abs(P / Po - 1)) < 1e-6
+    if ion == "peebles":
+        ih.close()
 
 
 @pytest.mark.parametrize("tol,bound", [((1e-10, 1e-10), 1e-6), ((1e-8, 3e-7), 1e-4)], ids=["tight", "served"])
