@@ -897,6 +897,108 @@ def run_trajectories(args):
         dist.destroy_process_group()
 
 
+FILON_FLOPS_PER_PAIR = 53  # one (k, node) term: spline locate + weights, 3 x 4-term B-spline sums, 3 accumulations
+
+
+def filon_workload():
+    """The Filon workload: f(t) = exp(-((t - 1400)/80)^2) (1 + 0.3 sin(t/50))
+    sampled with its exact derivatives on 2001 nodes of [0, 2000], integrated
+    against j_3(k t) for 5000 k in [1e-3, 8] (k t <= 1.6e4) over the
+    reference's test table (nu 3, order 3, [0, 1.6e4], 2e6 nodes)."""
+    t = np.linspace(0.0, 2000.0, 2001)
+    z = (t - 1400.0) / 80.0
+    g = np.exp(-z * z)
+    gp = -2.0 * z / 80.0 * g
+    gpp = (4.0 * z * z - 2.0) / 6400.0 * g
+    sn, cs = np.sin(t / 50.0), np.cos(t / 50.0)
+    sv, svp, svpp = 1.0 + 0.3 * sn, 0.3 / 50.0 * cs, -0.3 / 2500.0 * sn
+    f, fp, fpp = g * sv, gp * sv + g * svp, gpp * sv + 2.0 * gp * svp + g * svpp
+    k = np.linspace(1e-3, 8.0, 5000)
+    return t, f, fp, fpp, k
+
+
+def run_filon(args):
+    """Bessel-moment table build and piecewise Filon integrals (Bolt.jl
+    src/bessel/) through the C ABI; (k, segment) terms per second."""
+    t, f, fp, fpp, k = filon_workload()
+    pairs = k.size * (t.size - 1)
+    cores = os.cpu_count() or 1
+    if args.impl == "reference":
+        O = _oracle()
+        ot = O.MomentTable(3, 3, 0.0, 1.6e4, 2_000_000)
+        ks = k[:: max(1, k.size // 200)]
+        ot.filon_piecewise(t, f, fp, fpp, ks[:4], nthreads=cores)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ot.filon_piecewise(t, f, fp, fpp, ks, nthreads=cores)
+        sec = (time.perf_counter() - t0) / args.steps
+        v = ks.size * (t.size - 1) / sec
+        print(json.dumps({"impl": "reference", "metric": "Filon (k, segment) terms per second", "value": v,
+                          "unit": "terms/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1000.0 * sec * pairs / (ks.size * (t.size - 1)), "higher_is_better": True,
+                          "config": {"workload": "filon"}, "e2e": {"value": v, "unit": "terms/s",
+                                                                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                          "cpu_baseline": {"value": v, "unit": "terms/s", "cores": cores, "kind": "port",
+                                           "sample": f"{ks.size} of the {k.size} k, all nodes"}}))
+        return
+    import torch
+    torch.cuda.set_device(0)
+    import bolt_gb300 as B
+    ctx = B.Context(device=0)
+    build_s = []
+    for _ in range(3):
+        tab = B.MomentTable(3, 3, 0.0, 1.6e4, 2_000_000, ctx=ctx)
+        build_s.append(ctx.stats()["los_us"] / 1e6)
+        tab.close()
+    tab = B.MomentTable(3, 3, 0.0, 1.6e4, 2_000_000, ctx=ctx)
+    for _ in range(args.warmup):
+        B.integrate_sph_bessel_filon_piecewise(t, f, fp, fpp, k, tab)
+    sampler = clocks_sampler()
+    dev_s, launches = 0.0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = B.integrate_sph_bessel_filon_piecewise(t, f, fp, fpp, k, tab)
+        st = ctx.stats()
+        dev_s += st["los_us"] / 1e6
+        launches += st["kernel_launches"]
+    wall = time.perf_counter() - t0
+    clocks = clocks_summary(sampler)
+    peak = ctypes_peak(B._lib.load(), 0)
+    per = dev_s / args.steps
+    achieved = pairs * FILON_FLOPS_PER_PAIR / per / 1e12
+    cpu = None
+    if not args.no_cpu_baseline:
+        O = _oracle()
+        ot = O.MomentTable(3, 3, 0.0, 1.6e4, 2_000_000)
+        ks = k[:: max(1, k.size // 200)]
+        c0 = time.perf_counter()
+        ref = ot.filon_piecewise(t, f, fp, fpp, ks, nthreads=cores)
+        csec = time.perf_counter() - c0
+        got = out[:: max(1, k.size // 200)]
+        cpu = {"value": ks.size * (t.size - 1) / csec, "unit": "terms/s", "cores": cores, "kind": "port",
+               "sample": f"{ks.size} of the {k.size} k, all {t.size - 1} segments",
+               "max_abs_diff_vs_gpu": float(np.max(np.abs(got - ref))), "scale": float(np.max(np.abs(ref)))}
+    print(json.dumps({
+        "metric": "Filon (k, segment) terms per second", "value": pairs / per, "unit": "terms/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * per, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "filon: int_0^2000 f(t) j_3(k t) dt, f a smooth bump sampled on 2001 nodes with "
+                               "exact derivatives, 5000 k in [1e-3, 8]; moment table nu 3, order 3, [0, 1.6e4], "
+                               "2e6 nodes (48 MB, L2-resident); one step = bolt_filon_piecewise",
+                   "parallelism": "1 GPU"},
+        "e2e": {"value": pairs * args.steps / wall, "unit": "terms/s",
+                "h2d_bytes_per_step": int(8 * (4 * t.size + k.size)), "d2h_bytes_per_step": int(8 * k.size)},
+        "table_build": {"seconds": min(build_s), "nodes_per_s": 2_000_000 / min(build_s)},
+        "clocks": clocks, "gpu_launches": launches,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": None, "kernel": "filon_piecewise_kernel",
+                     "note": f"{FILON_FLOPS_PER_PAIR} FP64 flops per (k, node) term / CUDA-event time of the call's "
+                             "two kernels; FP64 peak measured in this run (bolt_fp64_peak)"},
+        "cpu_baseline": cpu}))
+    tab.close()
+    ctx.close()
+
+
 def ctypes_peak(lib, dev):
     import ctypes as C
     v = C.c_double(0.0)
@@ -910,7 +1012,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20, help="timed requests (serving) or spectra (pipeline)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="serving", choices=["serving", "pipeline", "batch", "grad", "trajectories"])
+    ap.add_argument("--workload", default="serving",
+                    choices=["serving", "pipeline", "batch", "grad", "trajectories", "filon"])
     ap.add_argument("--plain-sample", type=int, default=0,
                     help="batch / grad: time the plain drop-in on the first N cosmologies only (0: all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -928,7 +1031,9 @@ def main():
                     help="trajectories: the ionization history (the configuration names Peebles recombination)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.impl == "reference":
+    if args.workload == "filon":
+        run_filon(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "pipeline":
         run_pipeline(args)

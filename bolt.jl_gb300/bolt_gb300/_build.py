@@ -20,7 +20,7 @@ OBJ_DIR = os.path.join(ROOT, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-diag-suppress", "177"]
-CU_SOURCES = ["solver.cu", "los.cu", "capi.cu", "probe.cu", "noalloc.cu", "engine.cu"]
+CU_SOURCES = ["solver.cu", "los.cu", "capi.cu", "probe.cu", "noalloc.cu", "engine.cu", "moments.cu"]
 CXX_SOURCES = ["host_cosmo.cpp"]
 
 

@@ -89,6 +89,12 @@ EXPORTS = {
     "bolt_fp64_peak": (C.c_int, [C.c_int, _dp]),
     "bolt_set_dense_x": (C.c_int, [C.c_void_p, C.c_double]),
     "bolt_set_land_stride": (C.c_int, [C.c_void_p, C.c_int]),
+    "bolt_sph_j_moment": (C.c_int, [C.c_void_p, C.c_int, C.c_double, _dp, C.c_int, _dp]),
+    "bolt_moment_table_build": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, _ip]),
+    "bolt_moment_table_eval": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, _dp]),
+    "bolt_moment_table_free": (C.c_int, [C.c_void_p, C.c_int]),
+    "bolt_filon": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "bolt_filon_piecewise": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp]),
     "bolt_source_grid_static": (C.c_int, [C.POINTER(BoltParams), C.POINTER(BoltGrid), C.c_int, _dp, _dp, _dp,
                                           C.c_int, C.POINTER(BoltHier), C.c_double, C.c_double, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]),

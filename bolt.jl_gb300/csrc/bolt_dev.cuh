@@ -386,4 +386,19 @@ struct LosAdjArgs {
   double* Sbar;         // [nk][nx] (zeroed by the launcher)
 };
 
+// 8-point Gauss-Legendre rule on [-1, 1] (nodes ascending).
+struct GL8 {
+  double x[8], w[8];
+};
+
+// A spherical-Bessel moment table (order moments m = 0..order-1 of j_n on N
+// uniform nodes of [kmin, kmax], step h) and its B-spline coefficients
+// coef[(N + 2) * order] in HBM.
+struct MomTabDev {
+  double* coef;
+  int n, order, N;
+  double kmin, kmax, h;
+  GL8 g;
+};
+
 }  // namespace bolt

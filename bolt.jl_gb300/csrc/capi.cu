@@ -34,6 +34,15 @@ int launch_jl_prefilter(int nb, int nslots, int ncz, const double* d_raw, const 
 int launch_sdense(int nx, int i0, int nrow, int nk, const double* d_kgrid, const double* d_ST, const double* d_SE, int nm,
                   const double* d_kmid, const double* d_dx, double* d_SdT, double* d_SdE, cudaStream_t st);
 int launch_los_cl(const LosArgs& a, int ncz, cudaStream_t st);
+int launch_moment_direct(int n, double m, const double* d_x, int nx, double* d_out, const GL8& g, cudaStream_t st);
+int launch_moment_table(const MomTabDev& T, double* d_y, double* d_seg, const double* d_w, double* d_work,
+                        cudaStream_t st);
+int launch_moment_eval(const MomTabDev& T, const double* d_x, int nx, double* d_out, cudaStream_t st);
+int launch_filon(const MomTabDev& T, int n, const double* f, const double* fp, const double* fpp, const double* k,
+                 const double* a, const double* b, double* out, cudaStream_t st);
+int launch_filon_piecewise(const MomTabDev& T, int nt, const double* t, const double* f, const double* fp,
+                           const double* fpp, double* D, int nk, const double* k, double* out, int nblocks,
+                           cudaStream_t st);
 int launch_adjoint_check(const CosmoDev* d_cos, int id, double k, int lg, int lnu, int lmnu, int nq, double x,
                          double hs, double* d_scr, double* d_out, cudaStream_t st);
 size_t adjoint_check_scratch_bytes(int N);
@@ -83,6 +92,12 @@ struct CosmoEntry {
 
 }  // namespace
 
+struct MomEntry {
+  bool live = false;
+  MomTabDev T{};
+  DBuf coef;
+};
+
 struct bolt_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -95,6 +110,8 @@ struct bolt_ctx {
   DBuf d_cos;
   DBuf modes, xout, srcT, srcE, traj, plin, status, counters, queue, flags, scratch;
   DBuf kgrid, raw, norm, coef, w, slot_of_l, ells, SdT, SdE, kmid, wts, yv, dx, dgs, idg, out, terms;
+  std::vector<MomEntry> mtab;
+  DBuf m0, m1, m2, m3, m4, m5, m6, m7, m8;  // Bessel-moment and Filon arguments
   std::string err;
   int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
@@ -494,7 +511,9 @@ void bolt_ctx_destroy(bolt_ctx* c) {
     if (e.d_tab) cudaFree(e.d_tab);
   DBuf* bufs[] = {&c->d_cos, &c->modes, &c->xout, &c->srcT, &c->srcE, &c->traj, &c->plin, &c->status, &c->counters,
                   &c->queue, &c->flags, &c->scratch, &c->kgrid, &c->raw, &c->norm, &c->coef, &c->w, &c->slot_of_l, &c->ells,
-                  &c->SdT, &c->SdE, &c->kmid, &c->wts, &c->yv, &c->dx, &c->dgs, &c->idg, &c->out};
+                  &c->SdT, &c->SdE, &c->kmid, &c->wts, &c->yv, &c->dx, &c->dgs, &c->idg, &c->out, &c->terms,
+                  &c->m0, &c->m1, &c->m2, &c->m3, &c->m4, &c->m5, &c->m6, &c->m7, &c->m8};
+  for (auto& e : c->mtab) e.coef.release();
   for (DBuf* b : bufs) b->release();
   for (int i = 0; i < 4; ++i) cudaEventDestroy(c->ev[i]);
   cudaStreamDestroy(c->stream);
@@ -770,6 +789,215 @@ int bolt_adjoint_check(bolt_ctx* c, int id, double k, const bolt_hier* h, double
     ck(cudaStreamSynchronize(c->stream), "sync");
     if (o[15] < 0.0) throw Err(-1, "hierarchy does not fit the solver's lane packing");
     std::copy(o, o + 14, out);
+  });
+}
+
+}  // extern "C"
+
+// ------------------------------------------- Bessel moments and Filon ---
+namespace {
+
+// 8-point Gauss-Legendre nodes and weights (Newton on the Legendre
+// recurrence), computed once.
+const GL8& gl8() {
+  static const GL8 g = [] {
+    GL8 r;
+    const int n = 8;
+    for (int i = 0; i < n; ++i) {
+      double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+      for (int it = 0; it < 100; ++it) {
+        double p0 = 1.0, p1 = z;
+        for (int k = 2; k <= n; ++k) {
+          double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+          p0 = p1;
+          p1 = p2;
+        }
+        dp = n * (z * p1 - p0) / (z * z - 1.0);
+        double dz = p1 / dp;
+        z -= dz;
+        if (std::fabs(dz) < 1e-17) break;
+      }
+      r.x[n - 1 - i] = z;
+      r.w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+    return r;
+  }();
+  return g;
+}
+
+MomEntry& get_mtab(bolt_ctx* c, int id) {
+  if (id < 0 || id >= int(c->mtab.size()) || !c->mtab[id].live) throw Err(-1, "no such moment table");
+  return c->mtab[id];
+}
+
+template <class T>
+T* upload(bolt_ctx* c, DBuf& b, const T* h, size_t n, const char* what) {
+  T* d = b.as<T>(std::max<size_t>(n, 1));
+  ck(cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream), what);
+  return d;
+}
+
+void time_kernels(bolt_ctx* c, int launches) {
+  ck(cudaEventRecord(c->ev[1], c->stream), "event");
+  ck(cudaEventSynchronize(c->ev[1]), "sync");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+  c->stats[3] += int64_t(ms * 1000.0);
+  c->stats[6] += launches;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bolt_sph_j_moment(bolt_ctx* c, int nu, double m, const double* x, int nx, double* out) {
+  return guard(c, [&] {
+    if (!x || !out || nx < 0) throw Err(-1, "null argument or nx < 0");
+    if (nu < 0 || nu > 100000 || !(m + nu > -1.0) || !std::isfinite(m)) throw Err(-1, "need 0 <= nu, m + nu > -1");
+    for (int i = 0; i < nx; ++i)
+      if (!(x[i] >= 0.0) || !std::isfinite(x[i])) throw Err(-1, "x must be finite and >= 0");
+    if (nx == 0) return;
+    const double* dx = upload(c, c->m0, x, nx, "x");
+    double* d_out = c->m1.as<double>(nx);
+    ck(cudaEventRecord(c->ev[0], c->stream), "event");
+    int rc = launch_moment_direct(nu, m, dx, nx, d_out, gl8(), c->stream);
+    if (rc != 0) throw Err(-3, std::string("moment launch: ") + cudaGetErrorString(cudaError_t(rc)));
+    time_kernels(c, 1);
+    ck(cudaMemcpyAsync(out, d_out, nx * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "out");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+  });
+}
+
+int bolt_moment_table_build(bolt_ctx* c, int nu, int order, double kmin, double kmax, int N, int* table_id) {
+  return guard(c, [&] {
+    if (!table_id) throw Err(-1, "null argument");
+    *table_id = -1;
+    if (nu < 0 || nu > 100000) throw Err(-1, "nu must be in 0..100000");
+    if (order < 1 || order > 4) throw Err(-1, "order must be 1..4");
+    if (N < 2 || N > (1 << 28)) throw Err(-1, "N must be in 2..2^28");
+    if (!(kmin >= 0.0) || !(kmax > kmin) || !std::isfinite(kmax)) throw Err(-1, "need 0 <= kmin < kmax");
+    int id = -1;
+    for (int i = 0; i < int(c->mtab.size()); ++i)
+      if (!c->mtab[i].live) { id = i; break; }
+    if (id < 0) { id = int(c->mtab.size()); c->mtab.emplace_back(); }
+    MomEntry& e = c->mtab[id];
+    MomTabDev& T = e.T;
+    T.n = nu;
+    T.order = order;
+    T.N = N;
+    T.kmin = kmin;
+    T.kmax = kmax;
+    T.h = (kmax - kmin) / (N - 1);
+    T.g = gl8();
+    T.coef = e.coef.as<double>(size_t(N + 2) * order);
+    const double r = 2.0 - std::sqrt(3.0);
+    double w[33];
+    for (int d = 0; d <= 32; ++d) w[d] = std::sqrt(3.0) * std::pow(-r, d);
+    const double* d_w = upload(c, c->m2, w, 33, "weights");
+    double* d_y = c->m3.as<double>(size_t(N) * order);
+    double* d_seg = c->m4.as<double>(size_t(N) * order);
+    double* d_work = c->m5.as<double>(size_t(4) * 70);
+    ck(cudaEventRecord(c->ev[0], c->stream), "event");
+    int rc = launch_moment_table(T, d_y, d_seg, d_w, d_work, c->stream);
+    if (rc != 0) throw Err(-3, std::string("moment table launch: ") + cudaGetErrorString(cudaError_t(rc)));
+    time_kernels(c, 4);
+    e.live = true;
+    *table_id = id;
+  });
+}
+
+int bolt_moment_table_eval(bolt_ctx* c, int id, const double* x, int nx, double* out) {
+  return guard(c, [&] {
+    if (!x || !out || nx < 0) throw Err(-1, "null argument or nx < 0");
+    MomEntry& e = get_mtab(c, id);
+    for (int i = 0; i < nx; ++i)
+      if (!(x[i] >= 0.0) || !std::isfinite(x[i])) throw Err(-1, "x must be finite and >= 0");
+    if (nx == 0) return;
+    const double* dx = upload(c, c->m0, x, nx, "x");
+    double* d_out = c->m1.as<double>(size_t(nx) * e.T.order);
+    ck(cudaEventRecord(c->ev[0], c->stream), "event");
+    int rc = launch_moment_eval(e.T, dx, nx, d_out, c->stream);
+    if (rc != 0) throw Err(-3, std::string("moment eval launch: ") + cudaGetErrorString(cudaError_t(rc)));
+    time_kernels(c, 1);
+    ck(cudaMemcpyAsync(out, d_out, size_t(nx) * e.T.order * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+       "out");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+  });
+}
+
+int bolt_moment_table_free(bolt_ctx* c, int id) {
+  return guard(c, [&] {
+    MomEntry& e = get_mtab(c, id);
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    e.coef.release();
+    e.live = false;
+  });
+}
+
+int bolt_filon(bolt_ctx* c, int id, int n, const double* f, const double* fp, const double* fpp, const double* k,
+               const double* a, const double* b, double* out) {
+  return guard(c, [&] {
+    if (!f || !fp || !fpp || !k || !a || !b || !out || n < 0) throw Err(-1, "null argument or n < 0");
+    MomEntry& e = get_mtab(c, id);
+    if (e.T.order < 3) throw Err(-1, "the Filon integral needs a table of order >= 3");
+    for (int i = 0; i < n; ++i)
+      if (!(k[i] > 0.0) || !(a[i] >= 0.0) || !(b[i] >= 0.0) || !std::isfinite(k[i] * a[i]) ||
+          !std::isfinite(k[i] * b[i]))
+        throw Err(-1, "need k > 0 and finite a, b >= 0");
+    if (n == 0) return;
+    const double* df = upload(c, c->m0, f, n, "f");
+    const double* dfp = upload(c, c->m1, fp, n, "fp");
+    const double* dfpp = upload(c, c->m2, fpp, n, "fpp");
+    const double* dk = upload(c, c->m3, k, n, "k");
+    const double* da = upload(c, c->m4, a, n, "a");
+    const double* db = upload(c, c->m5, b, n, "b");
+    double* d_out = c->m6.as<double>(n);
+    ck(cudaEventRecord(c->ev[0], c->stream), "event");
+    int rc = launch_filon(e.T, n, df, dfp, dfpp, dk, da, db, d_out, c->stream);
+    if (rc != 0) throw Err(-3, std::string("filon launch: ") + cudaGetErrorString(cudaError_t(rc)));
+    time_kernels(c, 1);
+    ck(cudaMemcpyAsync(out, d_out, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "out");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+  });
+}
+
+int bolt_filon_piecewise(bolt_ctx* c, int id, int nt, const double* t, const double* f, const double* fp,
+                         const double* fpp, int nk, const double* k, double* out) {
+  return guard(c, [&] {
+    if (!t || !f || !fp || !fpp || !k || !out || nt < 0 || nk < 0) throw Err(-1, "null argument or negative size");
+    MomEntry& e = get_mtab(c, id);
+    if (e.T.order < 3) throw Err(-1, "the Filon integral needs a table of order >= 3");
+    double kmax = 0.0, tmax = 0.0;
+    for (int i = 0; i < nk; ++i) {
+      if (!(k[i] > 0.0) || !std::isfinite(k[i])) throw Err(-1, "need finite k > 0");
+      kmax = std::max(kmax, k[i]);
+    }
+    for (int i = 0; i < nt; ++i) {
+      if (!(t[i] >= 0.0) || !std::isfinite(t[i])) throw Err(-1, "need finite t >= 0");
+      tmax = std::max(tmax, t[i]);
+    }
+    if (!std::isfinite(kmax * tmax)) throw Err(-1, "k t overflows");
+    if (nk == 0) return;
+    if (nt < 2) {
+      std::fill(out, out + nk, 0.0);
+      return;
+    }
+    const double* dt = upload(c, c->m0, t, nt, "t");
+    const double* df = upload(c, c->m1, f, nt, "f");
+    const double* dfp = upload(c, c->m2, fp, nt, "fp");
+    const double* dfpp = upload(c, c->m3, fpp, nt, "fpp");
+    const double* dk = upload(c, c->m4, k, nk, "k");
+    double* dD = c->m5.as<double>(size_t(nt) * 4);
+    double* d_out = c->m6.as<double>(nk);
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+    const int nblocks = std::min(nk, std::max(nsm, 1) * 8);
+    ck(cudaEventRecord(c->ev[0], c->stream), "event");
+    int rc = launch_filon_piecewise(e.T, nt, dt, df, dfp, dfpp, dD, nk, dk, d_out, nblocks, c->stream);
+    if (rc != 0) throw Err(-3, std::string("filon launch: ") + cudaGetErrorString(cudaError_t(rc)));
+    time_kernels(c, 2);
+    ck(cudaMemcpyAsync(out, d_out, nk * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "out");
+    ck(cudaStreamSynchronize(c->stream), "sync");
   });
 }
 

@@ -190,8 +190,53 @@ int bolt_set_land_stride(bolt_ctx* ctx, int stride);
  * (14 doubles.)  Returns 0 or a negative code. */
 int bolt_adjoint_check(bolt_ctx* ctx, int id, double k, const bolt_hier* h, double x, double hstep, double* out);
 
+/* ---------------------------------------------------------------------
+ * Moments of spherical Bessel functions and the Filon-type integrator
+ * (src/bessel/).  I_m(x) = int_0^x t^m j_nu(t) dt.
+ * --------------------------------------------------------------------- */
+
+/* sph_j_moment_maclaurin_1F2 / sph_j_moment_asymp / sph_j_moment_weniger_1F2
+ * (src/bessel/moments.jl:56-92; each returns I_m(x), by its own method):
+ * out[i] = I_m(x[i]) for integer 0 <= nu <= 100000, real m with m + nu > -1,
+ * x[i] >= 0, evaluated on the device (series below x = 2, quadrature up to
+ * max(50, 4 nu), the Lommel-function form above).  J_moment_* of
+ * half-integer order nu + 1/2 and power alpha is sqrt(2/pi) times this
+ * with m = alpha + 1/2. */
+int bolt_sph_j_moment(bolt_ctx* ctx, int nu, double m, const double* x, int nx, double* out);
+
+/* sph_bessel_interpolator(nu, order, kmin, kmax, N)
+ * (src/bessel/interpolator.jl:81-94): the moments m = 0..order-1
+ * (order 1..4) on N uniform nodes of [kmin, kmax] (0 <= kmin < kmax,
+ * 2 <= N <= 2^28), one cubic B-spline per order (Cubic(Line(OnGrid()))),
+ * built and kept on the device; *table_id names the table in this
+ * context. */
+int bolt_moment_table_build(bolt_ctx* ctx, int nu, int order, double kmin, double kmax, int N, int* table_id);
+
+/* The table's call (src/bessel/interpolator.jl:67-75): out[i][m] = I_m(x[i])
+ * from the splines inside [kmin, kmax], the Lommel form above, the
+ * Maclaurin series below.  out[nx][order]. */
+int bolt_moment_table_eval(bolt_ctx* ctx, int table_id, const double* x, int nx, double* out);
+int bolt_moment_table_free(bolt_ctx* ctx, int table_id);
+
+/* integrate_sph_bessel_filon(f, f', f'', k, a, b, itp)
+ * (src/bessel/integrator.jl:7-19), n independent segments:
+ * out[i] = int_{a_i}^{b_i} p_i(t) j_nu(k_i t) dt, p_i the quadratic with
+ * p(a_i) = f_i, p'(a_i) = fp_i, p'' = fpp_i.  Table order >= 3; k > 0,
+ * a, b >= 0. */
+int bolt_filon(bolt_ctx* ctx, int table_id, int n, const double* f, const double* fp, const double* fpp,
+               const double* k, const double* a, const double* b, double* out);
+
+/* The piecewise integrator that _loop_integrate_sph_bessel_filon
+ * (src/bessel/integrator.jl:25-38) serves: for every k,
+ * out[ik] = sum_{i < nt-1} int_{t_i}^{t_{i+1}} p_i(t) j_nu(k t) dt with the
+ * quadratic p_i at t_i (f, fp, fpp sampled on the nodes t[nt] >= 0), each
+ * node's moments evaluated once.  Device time in bolt_last_stats [3]. */
+int bolt_filon_piecewise(bolt_ctx* ctx, int table_id, int nt, const double* t, const double* f, const double* fp,
+                         const double* fpp, int nk, const double* k, double* out);
+
 /* Counters of the last call: [0] accepted steps, [1] rejected steps,
- * [2] solver kernel microseconds, [3] LOS kernels microseconds,
+ * [2] solver kernel microseconds, [3] LOS kernels microseconds (the
+ * Bessel-moment and Filon calls: their kernels' microseconds),
  * [4] modes, [5] solver kernel launches, [6] total kernel launches,
  * [7] (l, k, x) terms the line-of-sight reduction evaluated (those below
  * the Bessel turning point are skipped).  out[8]. */

@@ -107,6 +107,16 @@ def lib():
         L.oracle_plin.restype = C.c_double
         L.oracle_plin.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                   C.c_double, C.c_double, _ip]
+        L.oracle_sphj.restype = C.c_double
+        L.oracle_sphj.argtypes = [C.c_int, C.c_double]
+        L.oracle_sphj_moment.restype = C.c_double
+        L.oracle_sphj_moment.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int]
+        L.oracle_moment_table_new.restype = C.c_void_p
+        L.oracle_moment_table_new.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]
+        L.oracle_moment_table_free.argtypes = [C.c_void_p]
+        L.oracle_moment_table_eval.argtypes = [C.c_void_p, _dp, C.c_int, _dp]
+        L.oracle_filon.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oracle_filon_piecewise.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp, C.c_int]
         _lib = L
     return _lib
 
@@ -359,3 +369,68 @@ def sph_bessel_all(L, x):
     out = np.zeros(L + 1)
     lib().oracle_sph_bessel(L, x, _d(out))
     return out
+
+
+# ------------------------------------------------- Bessel moments, Filon ---
+_MOMENT_METHODS = {"auto": 0, "maclaurin": 1, "asymp": 2, "quad": 3}
+
+
+def sphj(n, t):
+    """j_n(t) of one order (n = -1: cos t / t)."""
+    return lib().oracle_sphj(int(n), float(t))
+
+
+def sph_j_moment(x, nu, m, method="auto"):
+    """int_0^x t^m j_nu(t) dt (moments.jl: sph_j_moment_asymp /
+    sph_j_moment_weniger_1F2 / sph_j_moment_maclaurin_1F2 all return this)."""
+    return lib().oracle_sphj_moment(int(nu), float(m), float(x), _MOMENT_METHODS[method])
+
+
+def J_moment(x, nu, alpha, method="auto"):
+    """int_0^x t^alpha J_nu(t) dt for half-integer nu = n + 1/2 (moments.jl:
+    J_moment_asymp / J_moment_weniger_1F2): sqrt(2/pi) times the spherical
+    moment of order alpha + 1/2."""
+    n = int(round(nu - 0.5))
+    assert abs(n + 0.5 - nu) < 1e-12, "half-integer orders only"
+    return np.sqrt(2.0 / np.pi) * sph_j_moment(x, n, alpha + 0.5, method)
+
+
+class MomentTable:
+    """sph_bessel_interpolator(nu, order, kmin, kmax, N) (interpolator.jl:81-94);
+    calling it evaluates the moments m = 0..order-1 (interpolator.jl:67-75)."""
+
+    def __init__(self, nu, order, kmin, kmax, N):
+        self.nu, self.order = int(nu), int(order)
+        self.h = lib().oracle_moment_table_new(self.nu, self.order, float(kmin), float(kmax), int(N))
+        if not self.h:
+            raise ValueError("bad moment table arguments")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_moment_table_free(self.h)
+            self.h = None
+
+    def __call__(self, x):
+        xa = np.ascontiguousarray(np.atleast_1d(np.asarray(x, dtype=np.float64)))
+        out = np.zeros((xa.size, self.order))
+        lib().oracle_moment_table_eval(self.h, _d(xa), xa.size, _d(out))
+        return out[0] if np.ndim(x) == 0 else out
+
+    def filon(self, f, fp, fpp, k, a, b):
+        """integrate_sph_bessel_filon (integrator.jl:7-19), elementwise."""
+        arr = [np.ascontiguousarray(np.atleast_1d(np.asarray(v, dtype=np.float64))) for v in (f, fp, fpp, k, a, b)]
+        n = max(v.size for v in arr)
+        arr = [np.ascontiguousarray(np.broadcast_to(v, (n,))) for v in arr]
+        out = np.zeros(n)
+        lib().oracle_filon(self.h, n, *[_d(v) for v in arr], _d(out))
+        return out[0] if all(np.ndim(v) == 0 for v in (f, fp, fpp, k, a, b)) else out
+
+    def filon_piecewise(self, t, f, fp, fpp, k, nthreads=0):
+        """sum over segments [t_i, t_{i+1}] of the Filon integral of the
+        quadratic at t_i (integrator.jl:25-38), for every k."""
+        t, f, fp, fpp = (np.ascontiguousarray(v, dtype=np.float64) for v in (t, f, fp, fpp))
+        k = np.ascontiguousarray(np.atleast_1d(k), dtype=np.float64)
+        out = np.zeros(k.size)
+        lib().oracle_filon_piecewise(self.h, t.size, _d(t), _d(f), _d(fp), _d(fpp), k.size, _d(k), _d(out),
+                                     int(nthreads))
+        return out

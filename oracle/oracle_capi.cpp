@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <memory>
 
+#include "oracle_bessel.hpp"
 #include "oracle_grad.hpp"
 
 using namespace orc;
@@ -423,6 +424,39 @@ int oracle_dual_cltt(void* h, const double* kg, int nk, int lg, int lnu, int lmn
   cl_of<G6>(o->C, ST.data(), nullptr, kg, nk, ells, nell, kd, argmax, tt.data(), nullptr, nullptr);
   for (int i = 0; i < nell; ++i) put7(tt[i], out + 7 * size_t(i));
   return st;
+}
+
+// ------------------------------------------- Bessel moments and Filon ---
+// src/bessel/moments.jl, interpolator.jl, integrator.jl.
+double oracle_sphj(int n, double t) { return sphj1(n, t); }
+
+// int_0^x t^m j_n(t) dt; method 0 by range, 1 series, 2 large-argument form, 3 quadrature.
+double oracle_sphj_moment(int n, double m, double x, int method) { return sphj_moment(n, m, x, method); }
+
+void* oracle_moment_table_new(int n, int order, double kmin, double kmax, int N) {
+  if (order < 1 || order > 4 || N < 2 || !(kmax > kmin) || n < 0) return nullptr;
+  return new MomentTableO(n, order, kmin, kmax, N);
+}
+void oracle_moment_table_free(void* h) { delete static_cast<MomentTableO*>(h); }
+
+// out[i * order + m] = I_m(x_i)
+void oracle_moment_table_eval(void* h, const double* x, int nx, double* out) {
+  const MomentTableO* T = static_cast<MomentTableO*>(h);
+  for (int i = 0; i < nx; ++i) T->eval(x[i], out + size_t(i) * T->order);
+}
+
+void oracle_filon(void* h, int n, const double* f, const double* fp, const double* fpp, const double* k,
+                  const double* a, const double* b, double* out) {
+  const MomentTableO* T = static_cast<MomentTableO*>(h);
+  for (int i = 0; i < n; ++i) out[i] = filon_segment(*T, f[i], fp[i], fpp[i], k[i], a[i], b[i]);
+}
+
+void oracle_filon_piecewise(void* h, int nt, const double* t, const double* f, const double* fp, const double* fpp,
+                            int nk, const double* k, double* out, int nthreads) {
+  const MomentTableO* T = static_cast<MomentTableO*>(h);
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int i = 0; i < nk; ++i) out[i] = filon_piecewise(*T, nt, t, f, fp, fpp, k[i]);
 }
 
 }  // extern "C"

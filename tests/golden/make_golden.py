@@ -1,5 +1,6 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference's own
-test data (Bolt.jl test/data/*.dat) and from mpmath.
+test data (Bolt.jl test/data/*.dat, the known answers of test/testbessel.jl)
+and from mpmath.
 
 Run in a checkout that has the reference mounted:
     python tests/golden/make_golden.py /path/to/Bolt.jl
@@ -36,6 +37,7 @@ def main(ref):
     np.savez_compressed(os.path.join(HERE, "camb_rough.npz"), ell=camb[0][:2600], tt=camb[1][:2600],
                         te=camb[2][:2600], ee=camb[3][:2600])
     camb_pk(data)
+    bessel_moment_refs(ref)
     # spherical Bessel j_l(x) known answers from mpmath (50 digits)
     import mpmath as mp
     mp.mp.dps = 50
@@ -48,6 +50,30 @@ def main(ref):
             v = mp.sqrt(mp.pi / (2 * mp.mpf(x))) * mp.besselj(int(l) + mp.mpf(1) / 2, mp.mpf(x))
             vals[i, j] = float(v) if abs(v) > mp.mpf("1e-300") else 0.0
     np.savez_compressed(os.path.join(HERE, "sph_bessel_mpmath.npz"), ell=ls, x=xs, j=vals)
+
+
+def bessel_moment_refs(ref):
+    """Known answers of the Bessel-moment and Filon tests (test/testbessel.jl):
+    every testset's reference values, in the order they appear, as decimal
+    strings (the big"..." literals keep their 30+ digits)."""
+    import json
+    import re
+    src = open(os.path.join(ref, "test", "testbessel.jl")).read()
+    parts = re.split(r'@testset\s+"([^"]+)"', src)
+    out = {}
+    num = r'[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?'
+    for name, body in zip(parts[1::2], parts[2::2]):
+        vals = []
+        for m in re.finditer(r'big"(' + num + r')"|refs\s*=\s*\(([^)]*)\)', body):
+            if m.group(1) is not None:
+                vals.append(m.group(1))
+            elif "big" in m.group(2):
+                vals.extend(re.findall(r'big"(' + num + r')"', m.group(2)))
+            else:
+                vals.extend(v.strip() for v in m.group(2).split(",") if v.strip())
+        out[name] = vals
+    with open(os.path.join(HERE, "bessel_moment_refs.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
 
 
 def camb_pk(data):
