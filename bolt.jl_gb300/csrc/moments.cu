@@ -339,11 +339,11 @@ __host__ __device__ __forceinline__ void mom_eval(const MomTabDev& T, double x, 
     double u = (x - T.kmin) / T.h;
     double fl = floor(u);
     fl = fmin(fmax(fl, 0.0), (double)(T.N - 2));
-    const double t = u - fl, s = 1.0 - t;
-    const double w0 = s * s * s * (1.0 / 6.0);
-    const double w1 = 2.0 / 3.0 - t * t + 0.5 * t * t * t;
-    const double w2 = 2.0 / 3.0 - s * s + 0.5 * s * s * s;
-    const double w3 = t * t * t * (1.0 / 6.0);
+    const double t = u - fl, s = 1.0 - t, t2 = t * t, s2 = s * s;
+    const double w0 = s2 * s * (1.0 / 6.0);
+    const double w3 = t2 * t * (1.0 / 6.0);
+    const double w1 = fma(t2, fma(0.5, t, -1.0), 2.0 / 3.0);  // 2/3 - t^2 + t^3/2
+    const double w2 = fma(s2, fma(0.5, s, -1.0), 2.0 / 3.0);  // 2/3 - s^2 + s^3/2
     const double* c = T.coef + (size_t)fl * T.order;
     for (int m = 0; m < T.order; ++m)
       out[m] = c[m] * w0 + c[T.order + m] * w1 + c[2 * T.order + m] * w2 + c[3 * T.order + m] * w3;
@@ -420,16 +420,17 @@ __global__ void __launch_bounds__(256) filon_piecewise_kernel(MomTabDev T, int n
   __shared__ double red[32];
   for (int ik = blockIdx.x; ik < nk; ik += gridDim.x) {
     const double kk = k[ik], i1 = 1.0 / kk, i2 = i1 * i1, i3 = i2 * i1;
-    double acc = 0.0;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;  // sum_i D_j(i) I_j(k t_i), scaled by k^{-j-1} once
     for (int i = threadIdx.x; i < nt; i += blockDim.x) {
       const double2 d01 = reinterpret_cast<const double2*>(D)[2 * i];
       const double2 d23 = reinterpret_cast<const double2*>(D)[2 * i + 1];
       double v[4];
       mom_eval(T, kk * d23.y, v);
-      acc = fma(d01.x * i1, v[0], acc);
-      acc = fma(d01.y * i2, v[1], acc);
-      acc = fma(d23.x * i3, v[2], acc);
+      a0 = fma(d01.x, v[0], a0);
+      a1 = fma(d01.y, v[1], a1);
+      a2 = fma(d23.x, v[2], a2);
     }
+    double acc = fma(a0, i1, fma(a1, i2, a2 * i3));
     acc = mom_warp_sum(acc);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) red[wid] = acc;
