@@ -281,9 +281,11 @@ __global__ void bspline_fir_kernel(MomTabDev T, const double* __restrict__ y, co
 }
 
 // The coefficients next to the ends (or all of them for short tables): the
-// (1, 4, 1) system between c[1] = y[0] and c[P + 1] (left), c[N - P] and
-// c[N] = y[N - 1] (right), by a sequential sweep; then the padding c[0],
-// c[N + 1].  Thread (side, order); side 2 = the whole table.
+// (1, 4, 1) system between c[1] = y[0] and the convolved c[kFir + 1] (left
+// side), and between the convolved c[N - kFir] and c[N] = y[N - 1] (right
+// side), by a sequential sweep; then the padding c[0], c[N + 1].  Thread
+// t = side * order + m; below 2 kFir + 4 nodes one thread per order sweeps
+// the whole table.
 __host__ __device__ __forceinline__ void ends_thread(const MomTabDev& T, const double* y, double* coef, double* work,
                                                     int t) {
   const bool whole = T.N < 2 * kFir + 4;
