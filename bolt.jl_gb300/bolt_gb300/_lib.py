@@ -95,6 +95,7 @@ EXPORTS = {
     "bolt_moment_table_free": (C.c_int, [C.c_void_p, C.c_int]),
     "bolt_filon": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "bolt_filon_piecewise": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp]),
+    "bolt_filon_batched": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp]),
     "bolt_source_grid_static": (C.c_int, [C.POINTER(BoltParams), C.POINTER(BoltGrid), C.c_int, _dp, _dp, _dp,
                                           C.c_int, C.POINTER(BoltHier), C.c_double, C.c_double, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]),

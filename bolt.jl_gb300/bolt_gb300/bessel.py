@@ -7,6 +7,7 @@ C ABI (bolt_sph_j_moment, bolt_moment_table_*, bolt_filon*).
     sph_bessel_interpolator(nu, order, kmin, kmax, N)  interpolator.jl:81-94 -> MomentTable
     integrate_sph_bessel_filon(f, f', f'', k, a, b, itp)  integrator.jl:7-19 -> integrate_sph_bessel_filon
     _loop_integrate_sph_bessel_filon (summed)          integrator.jl:25-38 -> integrate_sph_bessel_filon_piecewise
+    (one integrand per k on shared nodes, the line-of-sight shape)          -> integrate_sph_bessel_filon_batched
 """
 from __future__ import annotations
 
@@ -104,3 +105,18 @@ def integrate_sph_bessel_filon_piecewise(t, f, fp, fpp, k, itp: MomentTable):
     c.check(c.lib.bolt_filon_piecewise(c.h, itp.id, t.size, L.dptr(t), L.dptr(f), L.dptr(fp), L.dptr(fpp), ka.size,
                                        L.dptr(ka), L.dptr(out)), "bolt_filon_piecewise")
     return float(out[0]) if np.ndim(k) == 0 else out
+
+
+def integrate_sph_bessel_filon_batched(t, f, fp, fpp, k, itp: MomentTable):
+    """One integrand per k: f, fp, fpp of shape (nk, nt) on the shared nodes
+    t; returns, for every k, the sum over segments of the Filon integral of
+    that k's quadratic at t_i."""
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    ka = _arr(k)
+    f, fp, fpp = (np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (ka.size, t.size)))
+                  for v in (f, fp, fpp))
+    out = np.zeros(ka.size)
+    c = itp.ctx
+    c.check(c.lib.bolt_filon_batched(c.h, itp.id, t.size, L.dptr(t), L.dptr(f), L.dptr(fp), L.dptr(fpp), ka.size,
+                                     L.dptr(ka), L.dptr(out)), "bolt_filon_batched")
+    return out

@@ -43,6 +43,8 @@ int launch_filon(const MomTabDev& T, int n, const double* f, const double* fp, c
 int launch_filon_piecewise(const MomTabDev& T, int nt, const double* t, const double* f, const double* fp,
                            const double* fpp, double* D, int nk, const double* k, double* out, int nblocks,
                            cudaStream_t st);
+int launch_filon_batched(const MomTabDev& T, int nt, const double* t, const double* f, const double* fp,
+                         const double* fpp, int nk, const double* k, double* out, int nblocks, cudaStream_t st);
 int launch_adjoint_check(const CosmoDev* d_cos, int id, double k, int lg, int lnu, int lmnu, int nq, double x,
                          double hs, double* d_scr, double* d_out, cudaStream_t st);
 size_t adjoint_check_scratch_bytes(int N);
@@ -996,6 +998,46 @@ int bolt_filon_piecewise(bolt_ctx* c, int id, int nt, const double* t, const dou
     int rc = launch_filon_piecewise(e.T, nt, dt, df, dfp, dfpp, dD, nk, dk, d_out, nblocks, c->stream);
     if (rc != 0) throw Err(-3, std::string("filon launch: ") + cudaGetErrorString(cudaError_t(rc)));
     time_kernels(c, 2);
+    ck(cudaMemcpyAsync(out, d_out, nk * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "out");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+  });
+}
+
+int bolt_filon_batched(bolt_ctx* c, int id, int nt, const double* t, const double* f, const double* fp,
+                       const double* fpp, int nk, const double* k, double* out) {
+  return guard(c, [&] {
+    if (!t || !f || !fp || !fpp || !k || !out || nt < 0 || nk < 0) throw Err(-1, "null argument or negative size");
+    MomEntry& e = get_mtab(c, id);
+    if (e.T.order < 3) throw Err(-1, "the Filon integral needs a table of order >= 3");
+    double kmax = 0.0, tmax = 0.0;
+    for (int i = 0; i < nk; ++i) {
+      if (!(k[i] > 0.0) || !std::isfinite(k[i])) throw Err(-1, "need finite k > 0");
+      kmax = std::max(kmax, k[i]);
+    }
+    for (int i = 0; i < nt; ++i) {
+      if (!(t[i] >= 0.0) || !std::isfinite(t[i])) throw Err(-1, "need finite t >= 0");
+      tmax = std::max(tmax, t[i]);
+    }
+    if (!std::isfinite(kmax * tmax)) throw Err(-1, "k t overflows");
+    if (nk == 0) return;
+    if (nt < 2) {
+      std::fill(out, out + nk, 0.0);
+      return;
+    }
+    const size_t nf = size_t(nk) * nt;
+    const double* dt = upload(c, c->m0, t, nt, "t");
+    const double* df = upload(c, c->m1, f, nf, "f");
+    const double* dfp = upload(c, c->m2, fp, nf, "fp");
+    const double* dfpp = upload(c, c->m3, fpp, nf, "fpp");
+    const double* dk = upload(c, c->m4, k, nk, "k");
+    double* d_out = c->m6.as<double>(nk);
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+    const int nblocks = std::min(nk, std::max(nsm, 1) * 8);
+    ck(cudaEventRecord(c->ev[0], c->stream), "event");
+    int rc = launch_filon_batched(e.T, nt, dt, df, dfp, dfpp, nk, dk, d_out, nblocks, c->stream);
+    if (rc != 0) throw Err(-3, std::string("filon launch: ") + cudaGetErrorString(cudaError_t(rc)));
+    time_kernels(c, 1);
     ck(cudaMemcpyAsync(out, d_out, nk * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "out");
     ck(cudaStreamSynchronize(c->stream), "sync");
   });

@@ -8,6 +8,7 @@
 //   MomentTable call (x)                                interpolator.jl:67-75 -> moment_eval_kernel
 //   integrate_sph_bessel_filon                          integrator.jl:7-19    -> filon_kernel
 //   _loop_integrate_sph_bessel_filon, summed            integrator.jl:25-38   -> filon_piecewise_kernel
+//     (one integrand per k, the line-of-sight shape)                          -> filon_batched_kernel
 //
 // Methods.  The Maclaurin series of the moment below x = 2 (and below the
 // table), the Lommel-function form above x_c = max(50, 4n) (and above the
@@ -446,6 +447,46 @@ __global__ void __launch_bounds__(256) filon_piecewise_kernel(MomTabDev T, int n
   }
 }
 
+// The line-of-sight shape of the same sum: one integrand per k (f, f', f''
+// [nk][nt] on shared nodes t), out[ik] = sum_i int_{t_i}^{t_{i+1}} p_{ik,i}(t)
+// j_nu(k t) dt.  One block per k (grid-stride), threads over nodes; each
+// node forms its weights from the quadratics of the segments on either side.
+__global__ void __launch_bounds__(256) filon_batched_kernel(MomTabDev T, int nt, const double* __restrict__ t,
+                                                            const double* __restrict__ f,
+                                                            const double* __restrict__ fp,
+                                                            const double* __restrict__ fpp, int nk,
+                                                            const double* __restrict__ k, double* __restrict__ out) {
+  __shared__ double red[32];
+  for (int ik = blockIdx.x; ik < nk; ik += gridDim.x) {
+    const double kk = k[ik], i1 = 1.0 / kk, i2 = i1 * i1, i3 = i2 * i1;
+    const double* fk = f + (size_t)ik * nt;
+    const double* fpk = fp + (size_t)ik * nt;
+    const double* fppk = fpp + (size_t)ik * nt;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+      double l0 = 0.0, l1 = 0.0, l2 = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0;
+      if (i > 0) quad_coefs(fk[i - 1], fpk[i - 1], fppk[i - 1], t[i - 1], l0, l1, l2);
+      if (i < nt - 1) quad_coefs(fk[i], fpk[i], fppk[i], t[i], r0, r1, r2);
+      double v[4];
+      mom_eval(T, kk * t[i], v);
+      a0 = fma(l0 - r0, v[0], a0);
+      a1 = fma(l1 - r1, v[1], a1);
+      a2 = fma(l2 - r2, v[2], a2);
+    }
+    double acc = fma(a0, i1, fma(a1, i2, a2 * i3));
+    acc = mom_warp_sum(acc);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = acc;
+    __syncthreads();
+    if (wid == 0) {
+      double s = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+      s = mom_warp_sum(s);
+      if (lane == 0) out[ik] = s;
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------- launchers ---
 int launch_moment_direct(int n, double m, const double* d_x, int nx, double* d_out, const GL8& g, cudaStream_t st) {
   if (nx <= 0) return 0;
@@ -494,6 +535,13 @@ int launch_filon_piecewise(const MomTabDev& T, int nt, const double* t, const do
   if (nt <= 0 || nk <= 0) return 0;
   filon_weights_kernel<<<(nt + 255) / 256, 256, 0, st>>>(nt, t, f, fp, fpp, D);
   filon_piecewise_kernel<<<nblocks > 0 ? nblocks : nk, 256, 0, st>>>(T, nt, D, nk, k, out);
+  return (int)cudaGetLastError();
+}
+
+int launch_filon_batched(const MomTabDev& T, int nt, const double* t, const double* f, const double* fp,
+                         const double* fpp, int nk, const double* k, double* out, int nblocks, cudaStream_t st) {
+  if (nt <= 0 || nk <= 0) return 0;
+  filon_batched_kernel<<<nblocks > 0 ? nblocks : nk, 256, 0, st>>>(T, nt, t, f, fp, fpp, nk, k, out);
   return (int)cudaGetLastError();
 }
 

@@ -234,6 +234,13 @@ int bolt_filon(bolt_ctx* ctx, int table_id, int n, const double* f, const double
 int bolt_filon_piecewise(bolt_ctx* ctx, int table_id, int nt, const double* t, const double* f, const double* fp,
                          const double* fpp, int nk, const double* k, double* out);
 
+/* The line-of-sight shape: one integrand per k on shared nodes t[nt],
+ * f, fp, fpp [nk][nt]; out[ik] = sum_{i < nt-1} int_{t_i}^{t_{i+1}}
+ * p_{ik,i}(t) j_nu(k_ik t) dt (Tl's sum over x with j_nu taken exactly
+ * through the moments and the integrand quadratic per segment). */
+int bolt_filon_batched(bolt_ctx* ctx, int table_id, int nt, const double* t, const double* f, const double* fp,
+                       const double* fpp, int nk, const double* k, double* out);
+
 /* Counters of the last call: [0] accepted steps, [1] rejected steps,
  * [2] solver kernel microseconds, [3] LOS kernels microseconds (the
  * Bessel-moment and Filon calls: their kernels' microseconds),
