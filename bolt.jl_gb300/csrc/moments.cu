@@ -26,9 +26,10 @@
 // coefficient adjacent (one evaluation reads 4 * order consecutive-ish
 // doubles).  The prefilter of the constant (1, 4, 1) system is the
 // convolution c_j = sqrt(3) sum_d (-r)^|d| y_{j+d}, r = 2 - sqrt(3),
-// truncated at |d| <= 32 (r^33 < 1e-18), one thread per coefficient; the 33
-// coefficients next to each end are solved exactly by a short sequential
-// sweep between the known end value and the first convolved coefficient.
+// truncated at |d| <= 32 (r^33 < 1e-18), one thread per coefficient; the
+// coefficients within 32 of each end are solved exactly by a short
+// sequential sweep between the known end value and the first convolved
+// coefficient.
 #include <cuda_runtime.h>
 
 #include "bolt_dev.cuh"
