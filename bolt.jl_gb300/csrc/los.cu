@@ -297,6 +297,153 @@ __global__ void __launch_bounds__(256) los_cl_kernel(LosArgs a) {
   }
 }
 
+// The same reduction for kLB multipoles per block: the spline abscissa
+// k y_i, its cell and the four B-spline weights depend on (k, x) alone (all
+// multipoles share the Bessel grid), so they are formed once and serve kLB
+// coefficient tables held side by side in shared memory (4 x 40 KB on the
+// reference's 5001-point grid).  Each multipole keeps its own turning-point
+// cut; per term the arithmetic is the single-multipole kernel's, so every
+// (l, k, x) term is bitwise the same.
+constexpr int kLB = 4;
+constexpr int kLosMultiThreads = 512;
+
+__global__ void __launch_bounds__(kLosMultiThreads) los_cl_multi_kernel(LosArgs a) {
+  extern __shared__ double sh[];
+  const int s0 = blockIdx.x * kLB, cz = blockIdx.y;
+  const int nb2 = a.nb + 2;
+  const int nl = min(kLB, a.nslots - s0);
+  double* yl = sh + (size_t)kLB * nb2;  // nrow scaled arguments
+  double* red = yl + a.nrow;            // 3 * blockDim
+  for (int b = 0; b < nl; ++b) {
+    const double* src = a.coef + ((size_t)cz * a.nslots + s0 + b) * nb2;
+    for (int j = threadIdx.x; j < nb2; j += blockDim.x) sh[(size_t)b * nb2 + j] = src[j];
+  }
+  const double idg = a.inv_dg[cz];
+  for (int j = threadIdx.x; j < a.nrow; j += blockDim.x) yl[j] = a.yv[(size_t)cz * a.nrow + j] * idg;
+  __syncthreads();
+  // per multipole: the first coefficient above kSkipRel of its largest
+  double ulo[kLB];
+  for (int b = 0; b < kLB; ++b) {
+    ulo[b] = 1e300;  // empty slot: no terms
+    if (b >= nl) continue;
+    const double* cs = sh + (size_t)b * nb2;
+    double cmax = 0.0;
+    for (int j = threadIdx.x; j < nb2; j += blockDim.x) cmax = fmax(cmax, fabs(cs[j]));
+    red[threadIdx.x] = cmax;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+      __syncthreads();
+    }
+    const double thr = kSkipRel * red[0];
+    __syncthreads();
+    int jfirst = nb2;
+    for (int j = threadIdx.x; j < nb2; j += blockDim.x)
+      if (fabs(cs[j]) > thr) { jfirst = j; break; }
+    reinterpret_cast<int*>(red)[threadIdx.x] = jfirst;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) {
+        int* ir = reinterpret_cast<int*>(red);
+        ir[threadIdx.x] = min(ir[threadIdx.x], ir[threadIdx.x + o]);
+      }
+      __syncthreads();
+    }
+    ulo[b] = double(reinterpret_cast<int*>(red)[0] - 3);
+    __syncthreads();
+  }
+  double lfac[kLB];
+#pragma unroll
+  for (int b = 0; b < kLB; ++b) {
+    const int l = b < nl ? a.ells[s0 + b] : 2;
+    lfac[b] = sqrt(double((long long)(l + 2) * (l + 1) * (long long)l * (l - 1)));
+  }
+  const double* SdT = a.SdT + (size_t)cz * a.nrow * a.nm;
+  const double* SdE = a.SdE ? a.SdE + (size_t)cz * a.nrow * a.nm : nullptr;
+  const double* km = a.kmid + (size_t)cz * a.nm;
+  const double* wm = a.wts + (size_t)cz * a.nm;
+  const double umax = double(a.nb - 2);
+  double stt[kLB], ste[kLB], see[kLB];
+#pragma unroll
+  for (int b = 0; b < kLB; ++b) { stt[b] = 0.0; ste[b] = 0.0; see[b] = 0.0; }
+  unsigned long long nterm = 0;
+  for (int m = threadIdx.x; m < a.nm; m += blockDim.x) {
+    const double k = km[m];
+    int iend[kLB];
+    int imax = 0;
+#pragma unroll
+    for (int b = 0; b < kLB; ++b) {
+      int ie = 0;
+      if (k * yl[0] >= ulo[b]) {
+        int lo = 0, hi = a.nrow;
+        while (hi - lo > 1) {
+          int mid = (lo + hi) >> 1;
+          if (k * yl[mid] >= ulo[b]) lo = mid; else hi = mid;
+        }
+        ie = hi;
+      }
+      iend[b] = ie;
+      imax = max(imax, ie);
+      nterm += ie;
+    }
+    double th[kLB], ep[kLB];
+#pragma unroll
+    for (int b = 0; b < kLB; ++b) { th[b] = 0.0; ep[b] = 0.0; }
+    for (int i = 0; i < imax; ++i) {
+      double u = k * yl[i];
+      double f = floor(u);
+      f = fmin(f, umax);
+      int j = (int)f;
+      double t = u - f, sm = 1.0 - t, t2 = t * t, s2 = sm * sm;
+      double w0 = s2 * sm, w3 = t2 * t;
+      double w1 = 4.0 - 6.0 * t2 + 3.0 * w3;
+      double w2 = 4.0 - 6.0 * s2 + 3.0 * w0;
+      const double sT = SdT[(size_t)i * a.nm + m];
+      const double sE = SdE ? SdE[(size_t)i * a.nm + m] : 0.0;
+#pragma unroll
+      for (int b = 0; b < kLB; ++b) {
+        if (i < iend[b]) {
+          const double* cs = sh + (size_t)b * nb2;
+          double jv = (cs[j] * w0 + cs[j + 1] * w1 + cs[j + 2] * w2 + cs[j + 3] * w3) * (1.0 / 6.0);
+          th[b] = fma(jv, sT, th[b]);
+          if (SdE) ep[b] = fma(jv, sE, ep[b]);
+        }
+      }
+    }
+    const double w = wm[m];
+#pragma unroll
+    for (int b = 0; b < kLB; ++b) {
+      const double e = ep[b] * lfac[b];
+      stt[b] = fma(th[b] * th[b], w, stt[b]);
+      ste[b] = fma(th[b] * e, w, ste[b]);
+      see[b] = fma(e * e, w, see[b]);
+    }
+  }
+  count_terms(a.terms, nterm);
+  for (int b = 0; b < nl; ++b) {
+    red[threadIdx.x] = stt[b];
+    red[blockDim.x + threadIdx.x] = ste[b];
+    red[2 * blockDim.x + threadIdx.x] = see[b];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) {
+        red[threadIdx.x] += red[threadIdx.x + o];
+        red[blockDim.x + threadIdx.x] += red[blockDim.x + threadIdx.x + o];
+        red[2 * blockDim.x + threadIdx.x] += red[2 * blockDim.x + threadIdx.x + o];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const double fp = 4.0 * M_PI;
+      const size_t o = (size_t)cz * a.nslots + s0 + b;
+      if (a.tt) a.tt[o] = fp * red[0];
+      if (a.te) a.te[o] = fp * red[blockDim.x];
+      if (a.ee) a.ee[o] = fp * red[2 * blockDim.x];
+    }
+    __syncthreads();
+  }
+}
+
 // -------------------------------------------------- C_l^TT and its tangent
 // Derivatives of C_l^TT along six parameter directions j at a frozen Bessel
 // grid and frozen k grids (the derivative the reference's ForwardDiff
@@ -607,7 +754,17 @@ int launch_los_adjoint(const LosAdjArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// kLB multipoles per block where their tables fit in shared memory (the
+// reference's 5001-point Bessel grid: 190 KB), else one per block.
 int launch_los_cl(const LosArgs& a, int ncz, cudaStream_t st) {
+  const size_t multi = (size_t(kLB) * (a.nb + 2) + a.nrow + 3 * kLosMultiThreads) * sizeof(double);
+  if (a.nslots >= 2 && multi <= 227 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(los_cl_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(multi));
+    if (e != cudaSuccess) return e;
+    dim3 g((a.nslots + kLB - 1) / kLB, ncz);
+    los_cl_multi_kernel<<<g, kLosMultiThreads, multi, st>>>(a);
+    return cudaGetLastError();
+  }
   const int threads = 256;
   size_t smem = (size_t(a.nb + 2) + a.nrow + 3 * threads) * sizeof(double);
   cudaError_t e = cudaFuncSetAttribute(los_cl_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
