@@ -569,6 +569,166 @@ __global__ void __launch_bounds__(256) los_tt_grad_kernel(LosGradArgs a) {
   }
 }
 
+// los_tt_grad_kernel for kLB multipoles per block: the spline cell and
+// weights, the source plane values S and dS_j and the argument derivatives
+// of a (k, x) term are read and formed once and serve all kLB multipoles;
+// per multipole the arithmetic is the single-multipole kernel's.  The block
+// reduction reuses the coefficient tables' shared memory.
+__global__ void __launch_bounds__(256) los_tt_grad_multi_kernel(LosGradArgs a) {
+  extern __shared__ double sh[];
+  const int s0 = blockIdx.x * kLB;
+  const int nb2 = a.nb + 2;
+  const int nl = min(kLB, a.nslots - s0);
+  double* yl = sh + (size_t)kLB * nb2;  // nrow scaled arguments
+  double* dyl = yl + a.nrow;            // kDir * nrow scaled argument derivatives
+  double* red = sh;                     // reductions: over the tables (bounds) or after the sum
+  double* redb = dyl + kDir * a.nrow;   // blockDim scratch for the bounds
+  for (int b = 0; b < nl; ++b) {
+    const double* src = a.coef + (size_t)(s0 + b) * nb2;
+    for (int j = threadIdx.x; j < nb2; j += blockDim.x) sh[(size_t)b * nb2 + j] = src[j];
+  }
+  const double idg = a.inv_dg[0];
+  for (int j = threadIdx.x; j < a.nrow; j += blockDim.x) yl[j] = a.yv[j] * idg;
+  for (int j = threadIdx.x; j < kDir * a.nrow; j += blockDim.x)
+    dyl[j] = a.dyv[(size_t)(j / a.nrow) * a.dstride + j % a.nrow] * idg;
+  __syncthreads();
+  double ulo[kLB];
+  for (int b = 0; b < kLB; ++b) {
+    ulo[b] = 1e300;
+    if (b >= nl) continue;
+    const double* cs = sh + (size_t)b * nb2;
+    double cmax = 0.0;
+    for (int j = threadIdx.x; j < nb2; j += blockDim.x) cmax = fmax(cmax, fabs(cs[j]));
+    redb[threadIdx.x] = cmax;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) redb[threadIdx.x] = fmax(redb[threadIdx.x], redb[threadIdx.x + o]);
+      __syncthreads();
+    }
+    const double thr = kSkipRel * redb[0];
+    __syncthreads();
+    int jfirst = nb2;
+    for (int j = threadIdx.x; j < nb2; j += blockDim.x)
+      if (fabs(cs[j]) > thr) { jfirst = j; break; }
+    reinterpret_cast<int*>(redb)[threadIdx.x] = jfirst;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) {
+        int* ir = reinterpret_cast<int*>(redb);
+        ir[threadIdx.x] = min(ir[threadIdx.x], ir[threadIdx.x + o]);
+      }
+      __syncthreads();
+    }
+    ulo[b] = double(reinterpret_cast<int*>(redb)[0] - 3);
+    if (a.ulo && threadIdx.x == 0) a.ulo[s0 + b] = ulo[b];
+    __syncthreads();
+  }
+  const double umax = double(a.nb - 2);
+  const size_t plane = (size_t)a.nrow * a.nm;
+  double stt[kLB], dstt[kLB][kDir];
+  unsigned long long nterm = 0;
+#pragma unroll
+  for (int b = 0; b < kLB; ++b) {
+    stt[b] = 0.0;
+#pragma unroll
+    for (int j = 0; j < kDir; ++j) dstt[b][j] = 0.0;
+  }
+  for (int m = threadIdx.x; m < a.nm; m += blockDim.x) {
+    const double k = a.kmid[m];
+    int iend[kLB];
+    int imax = 0;
+#pragma unroll
+    for (int b = 0; b < kLB; ++b) {
+      int ie = 0;
+      if (k * yl[0] >= ulo[b]) {
+        int lo = 0, hi = a.nrow;
+        while (hi - lo > 1) {
+          int mid = (lo + hi) >> 1;
+          if (k * yl[mid] >= ulo[b]) lo = mid; else hi = mid;
+        }
+        ie = hi;
+      }
+      iend[b] = ie;
+      imax = max(imax, ie);
+      nterm += ie;
+    }
+    double th[kLB], dth[kLB][kDir];
+#pragma unroll
+    for (int b = 0; b < kLB; ++b) {
+      th[b] = 0.0;
+#pragma unroll
+      for (int j = 0; j < kDir; ++j) dth[b][j] = 0.0;
+    }
+    for (int i = 0; i < imax; ++i) {
+      double u = k * yl[i];
+      double f = floor(u);
+      f = fmin(f, umax);
+      int jj = (int)f;
+      double t = u - f, sm = 1.0 - t, t2 = t * t, s2 = sm * sm;
+      double w0 = s2 * sm, w3 = t2 * t;
+      double w1 = 4.0 - 6.0 * t2 + 3.0 * w3;
+      double w2 = 4.0 - 6.0 * s2 + 3.0 * w0;
+      const double d0 = -0.5 * s2, d1 = -2.0 * t + 1.5 * t2, d2 = 2.0 * sm - 1.5 * s2, d3 = 0.5 * t2;
+      const size_t q = (size_t)i * a.nm + m;
+      const double S = a.Sd[q];
+      double dy[kDir], dS[kDir];
+#pragma unroll
+      for (int j = 0; j < kDir; ++j) {
+        dy[j] = dyl[j * a.nrow + i];
+        dS[j] = a.dSd ? a.dSd[j * plane + q] : 0.0;
+      }
+#pragma unroll
+      for (int b = 0; b < kLB; ++b) {
+        if (i < iend[b]) {
+          const double* cs = sh + (size_t)b * nb2;
+          const double c0 = cs[jj], c1 = cs[jj + 1], c2 = cs[jj + 2], c3 = cs[jj + 3];
+          double jv = (c0 * w0 + c1 * w1 + c2 * w2 + c3 * w3) * (1.0 / 6.0);
+          double jd = d0 * c0 + d1 * c1 + d2 * c2 + d3 * c3;
+          th[b] = fma(jv, S, th[b]);
+          const double jdS = jd * S * k;
+          if (a.dSd) {
+#pragma unroll
+            for (int j = 0; j < kDir; ++j) dth[b][j] = fma(jdS, dy[j], fma(jv, dS[j], dth[b][j]));
+          } else {
+#pragma unroll
+            for (int j = 0; j < kDir; ++j) dth[b][j] = fma(jdS, dy[j], dth[b][j]);
+          }
+        }
+      }
+    }
+    const double w = a.wts[m];
+    double dw[kDir];
+#pragma unroll
+    for (int j = 0; j < kDir; ++j) dw[j] = a.dwts[(size_t)j * a.dstride + m];
+#pragma unroll
+    for (int b = 0; b < kLB; ++b) {
+      if (b < nl && a.cbar) a.cbar[(size_t)(s0 + b) * a.nm + m] = 2.0 * w * th[b];
+      stt[b] = fma(th[b] * th[b], w, stt[b]);
+#pragma unroll
+      for (int j = 0; j < kDir; ++j) dstt[b][j] = fma(2.0 * w * th[b], dth[b][j], fma(dw[j], th[b] * th[b], dstt[b][j]));
+    }
+  }
+  count_terms(a.terms, nterm);
+  __syncthreads();  // the tables are done: their memory holds the reductions
+  for (int b = 0; b < nl; ++b) {
+    red[threadIdx.x] = stt[b];
+#pragma unroll
+    for (int j = 0; j < kDir; ++j) red[(1 + j) * blockDim.x + threadIdx.x] = dstt[b][j];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o)
+        for (int j = 0; j <= kDir; ++j) red[j * blockDim.x + threadIdx.x] += red[j * blockDim.x + threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const double fp = 4.0 * M_PI;
+      a.tt[s0 + b] = fp * red[0];
+      for (int j = 0; j < kDir; ++j) a.dtt[(size_t)j * a.nslots + s0 + b] = fp * red[(1 + j) * blockDim.x];
+    }
+    __syncthreads();
+  }
+}
+
 // (S_a - S_b) * scale resampled like sdense_kernel (dx folded in).
 __global__ void sdense_diff_kernel(int nx, int i0, int nrow, int nk, const double* __restrict__ kgrid,
                                    const double* __restrict__ Sa, const double* __restrict__ Sb, double scale, int nm,
@@ -730,6 +890,16 @@ int launch_sdense_diff(int nx, int i0, int nrow, int nk, const double* d_kgrid, 
 
 int launch_los_tt_grad(const LosGradArgs& a, cudaStream_t st) {
   const int threads = 256;
+  // kLB multipoles per block where their tables, the arguments and their
+  // derivatives fit (the reduction space aliases the tables)
+  const size_t multi = (size_t(kLB) * (a.nb + 2) + size_t(1 + kDir) * a.nrow + threads) * sizeof(double);
+  if (a.nslots >= 2 && multi <= 227 * 1024 && size_t(kLB) * (a.nb + 2) >= size_t(1 + kDir) * threads) {
+    cudaError_t e =
+        cudaFuncSetAttribute(los_tt_grad_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(multi));
+    if (e != cudaSuccess) return e;
+    los_tt_grad_multi_kernel<<<(a.nslots + kLB - 1) / kLB, threads, multi, st>>>(a);
+    return cudaGetLastError();
+  }
   size_t smem = (size_t(a.nb + 2) + size_t(1 + kDir) * a.nrow + size_t(1 + kDir) * threads) * sizeof(double);
   cudaError_t e = cudaFuncSetAttribute(los_tt_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return e;
