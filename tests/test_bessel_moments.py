@@ -3,7 +3,10 @@ Filon-type integrator (Bolt.jl src/bessel/): the oracle against the
 reference's own known answers (test/testbessel.jl, read into
 tests/golden/bessel_moment_refs.json by tests/golden/make_golden.py), at the
 reference's tolerances: TOL = 1e-13 relative for moments (1e-15 where
-testbessel.jl asks it), 1e-12 for table values, TOL on Filon integrals.
+testbessel.jl asks it), 1e-12 for table values, TOL on Filon integrals;
+and, at orders 7-150 above the reference's tests, against the moments'
+Maclaurin series summed exactly by mpmath
+(tests/golden/make_moment_fixtures.py), 1e-12 relative.
 
 Cylindrical moments int_0^x t^alpha J_nu(t) dt with nu = n + 1/2 (the
 reference's J_moment_* tests) are sqrt(2/pi) times the spherical moment of
@@ -146,3 +149,11 @@ def test_filon_piecewise_converges_to_the_integral():
                       mp.besselj(3.5, k * s), mp.linspace(0, 20, 60))
         # a quadratic per segment of width 0.05: error ~ h^3 f''' / 24 per unit length
         assert abs(g - float(ref)) < 2e-6 * 20, (k, g, float(ref))
+
+
+def test_high_order_moments_vs_exact_series():
+    d = np.load(os.path.join(GOLDEN, "sph_moment_mpmath.npz"))
+    got = np.array([O.sph_j_moment(x, int(n), m) for n, m, x in zip(d["n"], d["m"], d["x"])])
+    ref = d["moment"]
+    big = ref != 0.0
+    assert np.max(np.abs(got[big] / ref[big] - 1)) < 1e-12

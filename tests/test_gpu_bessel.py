@@ -52,6 +52,19 @@ def test_direct_moments_known_answers():
     assert np.all(rel(got, r) < TOL)
 
 
+def test_high_order_moments_vs_exact_series():
+    """Orders 7-150 against the Maclaurin series summed exactly (fixture),
+    1e-12 relative, through the series, quadrature and Lommel ranges."""
+    d = np.load(os.path.join(GOLDEN, "sph_moment_mpmath.npz"))
+    for n in np.unique(d["n"]):
+        for m in np.unique(d["m"]):
+            sel = (d["n"] == n) & (d["m"] == m)
+            got = B.sph_j_moment(d["x"][sel], int(n), float(m))
+            ref = d["moment"][sel]
+            big = ref != 0.0
+            assert np.max(np.abs(got[big] / ref[big] - 1)) < 1e-12, (n, m)
+
+
 def test_direct_moments_vs_oracle():
     rng = np.random.default_rng(7)
     for nu in (0, 1, 2, 5, 40, 300):
