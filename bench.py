@@ -90,7 +90,7 @@ def solver_flops_per_step(N, nq):
     return 159 * N + 560 * (nq + 5) + 66 * nq + 650
 
 
-LOS_FLOPS_TE = 27  # FLOPs per evaluated (l, k, x) term of los_cl_kernel with T and E (FMA = 2)
+LOS_FLOPS_TE = 27  # FLOPs per evaluated (l, k, x) term of the C_l projection with T and E (FMA = 2)
 LOS_FLOPS_T = 25   # the same with T alone
 
 
@@ -569,7 +569,7 @@ def run_serving(args):
                     "(per-CTA state slab L2-resident), see profiles/"}
     ach_los = plain_los["flops"] / (plain_los["us"] / 1e6) / 1e12 if plain_los["us"] > 0 else None
     roof_los = {"bound": "fp64", "achieved": ach_los, "peak": peak, "unit": "TFLOP/s",
-                "frac": ach_los / peak if (peak and ach_los) else None, "kernel": "los_cl_kernel (+ j_l tables)",
+                "frac": ach_los / peak if (peak and ach_los) else None, "kernel": "los_cl_multi_kernel (+ j_l tables)",
                 "terms": plain_los["terms"],
                 "note": "plain leg: FLOPs of the (l, k, x) terms the kernel evaluated (its counter; 27 per term with "
                         "T and E, 25 with T alone) / CUDA-event time of the projection launches (Bessel tables, "

@@ -2,8 +2,8 @@
 // the C_l^TT / TE / EE reduction (Bolt.jl src/spectra.jl:49-160).
 //
 //   bessel_interpolator(l, kmax*eta0)  spectra.jl:49-58  -> jl_raw_kernel + jl_prefilter_kernel
-//   Tl / _Tl_integrand                 spectra.jl:70-82  -> los_cl_kernel (inner x loop)
-//   cltt / clte / clee                 spectra.jl:84-160 -> los_cl_kernel (k sum, fused)
+//   Tl / _Tl_integrand                 spectra.jl:70-82  -> los_cl_multi_kernel / los_cl_kernel (inner x loop)
+//   cltt / clte / clee                 spectra.jl:84-160 -> los_cl_multi_kernel / los_cl_kernel (k sum, fused)
 //
 // The reference tabulates j_l on 5001 uniform points of [0, kmax*eta0],
 // splines it (cubic B-spline, natural ends) and evaluates
