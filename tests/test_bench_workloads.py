@@ -84,3 +84,16 @@ def test_los_flops_from_terms():
     assert bench.los_flops(1000) == 27000.0
     assert bench.los_flops(1000, with_e=False) == 25000.0
     assert bench.SWEEP_RATES == (1.0, 10.0, 100.0, 500.0, 2000.0)
+
+
+def test_filon_workload():
+    """The Filon workload's integrand carries its exact derivatives, and its
+    (k, t) products stay inside the moment table's range [0, 1.6e4]."""
+    t, f, fp, fpp, k = bench.filon_workload()
+    assert t.size == 2001 and k.size == 5000
+    assert np.max(k) * np.max(t) <= 1.6e4
+    h = 1e-4
+    z = lambda s: np.exp(-((s - 1400.0) / 80.0) ** 2) * (1.0 + 0.3 * np.sin(s / 50.0))
+    np.testing.assert_allclose(f, z(t), rtol=0, atol=1e-15)
+    np.testing.assert_allclose(fp, (z(t + h) - z(t - h)) / (2 * h), rtol=0, atol=1e-9)
+    np.testing.assert_allclose(fpp, (z(t + h) - 2 * z(t) + z(t - h)) / h ** 2, rtol=0, atol=1e-6)
